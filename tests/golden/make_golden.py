@@ -1,0 +1,349 @@
+"""Generate golden vectors by running the unmodified PETITE reference.
+
+Runs only in the development container (the reference is not present on the
+GPU machine); the outputs are committed as ``tests/golden/*.npz``.
+
+The reference draws from numpy's and Python's global generators.  Here every
+call site on the SM shower path is redirected to the per-particle Philox
+stream of the particle being processed (``oracle/philox.py``):
+
+* ``PETITE.shower.draw_U``      (accept/reject uniform, shower.py:30,457)
+* ``numpy.random.uniform``      (shower.py:540,561-562,583; kinematics.py azimuths)
+* ``numpy.random.choice``       (process choice, shower.py:671-697): cumsum,
+                                  normalise by the last entry, searchsorted right
+* ``random.choice/gauss/uniform`` (moliere.py:284,382); gauss is Box-Muller with
+                                  the second value cached exactly as CPython does
+* ``vegas.UNIFORM``             (the map-sampling shim's y draws)
+
+The particle being processed is tracked by wrapping the Shower instance's
+``propagate_particle`` and ``sample_scattering``; daughters get the keys of
+``oracle.philox.daughter_key``.
+
+Usage: python tests/golden/make_golden.py DICT_DIR   (DICT_DIR from rebuild_maps.py)
+"""
+import copy
+import math
+import os
+import random
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+import refimport  # noqa: E402
+from oracle.philox import Stream, daughter_key, primary_key  # noqa: E402
+
+SEED = 0x5EED
+
+
+class StreamRouter:
+    def __init__(self, seed):
+        self.seed = seed
+        self.streams = {}
+        self.cur = None
+        self.gauss_next = None
+
+    def stream(self, pkey):
+        if pkey not in self.streams:
+            self.streams[pkey] = Stream(self.seed, pkey)
+        return self.streams[pkey]
+
+    def set_current(self, pkey):
+        if self.gauss_next is not None:
+            raise RuntimeError("gauss cache not empty on particle switch")
+        self.cur = self.stream(pkey)
+
+    def u(self):
+        return self.cur.next()
+
+
+def install(router):
+    import vegas
+    import PETITE.shower as sh
+    saved = dict(draw_U=sh.draw_U, uniform=np.random.uniform, choice=np.random.choice,
+                 rgauss=random.gauss, rchoice=random.choice, runiform=random.uniform,
+                 vu=vegas.UNIFORM)
+
+    def draw_U():
+        return router.u()
+
+    def np_uniform(low=0.0, high=1.0, size=None):
+        if size is not None:
+            raise RuntimeError("sized uniform not on the shower path")
+        return low + (high - low) * router.u()
+
+    def np_choice(a, size=None, replace=True, p=None):
+        p = np.asarray(p, dtype=float)
+        cdf = p.cumsum()
+        cdf /= cdf[-1]
+        idx = int(cdf.searchsorted(router.u(), side="right"))
+        return a[idx]
+
+    def r_gauss(mu=0.0, sigma=1.0):
+        z = router.gauss_next
+        router.gauss_next = None
+        if z is None:
+            x2pi = router.u() * (2 * math.pi)
+            g2rad = math.sqrt(-2.0 * math.log(1.0 - router.u()))
+            z = math.cos(x2pi) * g2rad
+            router.gauss_next = math.sin(x2pi) * g2rad
+        return mu + z * sigma
+
+    def r_choice(seq):
+        return seq[int(router.u() * len(seq))]
+
+    def r_uniform(a, b):
+        return a + (b - a) * router.u()
+
+    sh.draw_U = draw_U
+    np.random.uniform = np_uniform
+    np.random.choice = np_choice
+    random.gauss = r_gauss
+    random.choice = r_choice
+    random.uniform = r_uniform
+    vegas.UNIFORM = lambda n: np.array([router.u() for _ in range(n)])
+    return saved
+
+
+def uninstall(saved):
+    import vegas
+    import PETITE.shower as sh
+    sh.draw_U = saved["draw_U"]
+    np.random.uniform = saved["uniform"]
+    np.random.choice = saved["choice"]
+    random.gauss, random.choice, random.uniform = saved["rgauss"], saved["rchoice"], saved["runiform"]
+    vegas.UNIFORM = saved["vu"]
+
+
+def wrap_shower(shower, router):
+    orig_prop = shower.propagate_particle
+    orig_ss = shower.sample_scattering
+
+    def prop(ap, *a, **k):
+        router.set_current(ap._pkey)
+        return orig_prop(ap, *a, **k)
+
+    def ss(ap, process, VB=False):
+        router.set_current(ap._pkey)
+        out = orig_ss(ap, process, VB=VB)
+        if out is not None:
+            for bit, d in enumerate(out):
+                d._pkey = daughter_key(ap._pkey, bit)
+        return out
+
+    shower.propagate_particle = prop
+    shower.sample_scattering = ss
+
+
+PROC_CODE = {"Input": -1, "Brem": 0, "Ann": 1, "PairProd": 2, "Comp": 3, "Moller": 4,
+             "Bhabha": 5, "MuonE": 6, "MuonBrem": 7}
+
+
+def shower_arrays(parts, router, primary):
+    n = len(parts)
+    f = np.zeros((n, 16))
+    i = np.zeros((n, 6), np.int64)
+    ids = []
+    keys = np.zeros(n, np.uint64)
+    draws = np.zeros(n, np.int64)
+    for k, p in enumerate(parts):
+        d = p.get_ids()
+        f[k, 0:4] = p.get_p0()
+        f[k, 4:7] = p.get_r0()
+        f[k, 7:11] = p.get_pf()
+        f[k, 11:14] = p.get_rf()
+        f[k, 14] = d["weight"]
+        f[k, 15] = d["mass"]
+        i[k] = [d["PID"], d["parent_PID"], d["generation_number"], PROC_CODE[d["generation_process"]],
+                int(p.get_ended()), primary]
+        ids.append((d["ID"], d["parent_ID"]))
+        keys[k] = p._pkey
+        s = router.streams.get(p._pkey)
+        draws[k] = s.n if s is not None else 0
+    return f, i, ids, keys, draws
+
+
+def gen_showers(dict_dir, out_path, cases):
+    refimport.setup()
+    from PETITE.shower import Shower
+    from PETITE.particle import Particle
+    result = {}
+    for name, target, cut, pid, E0, n, mass in cases:
+        t0 = time.time()
+        router = StreamRouter(SEED)
+        shower = Shower(dict_dir, target, cut)
+        wrap_shower(shower, router)
+        saved = install(router)
+        F, I, IDS, K, D = [], [], [], [], []
+        try:
+            for j in range(n):
+                m = 0.0 if pid == 22 else mass
+                p = math.sqrt(E0 * E0 - m * m)
+                ids = {"PID": pid}
+                part = Particle([E0, 0.0, 0.0, p], [0.0, 0.0, 0.0], ids)
+                part._pkey = primary_key(j)
+                parts = shower.generate_shower(part)
+                f, i, ids_, k, d = shower_arrays(parts, router, j)
+                F.append(f); I.append(i); K.append(k); D.append(d)
+                IDS.extend(ids_)
+        finally:
+            uninstall(saved)
+        F, I, K, D = np.concatenate(F), np.concatenate(I), np.concatenate(K), np.concatenate(D)
+        result[f"{name}/f64"] = F
+        result[f"{name}/i64"] = I
+        result[f"{name}/pkey"] = K
+        result[f"{name}/draws"] = D
+        result[f"{name}/id_str"] = np.array([f"{a}:{b}" for a, b in IDS])
+        result[f"{name}/meta"] = np.array([SEED, pid, n], np.int64)
+        result[f"{name}/params"] = np.array([E0, cut, mass])
+        result[f"{name}/target"] = np.array(target)
+        print(f"{name}: {n} primaries, {len(F)} particles, {time.time() - t0:.1f} s")
+    np.savez_compressed(out_path, **result)
+
+
+def gen_units(dict_dir, out_path):
+    """Known-answer vectors for the per-interaction functions."""
+    refimport.setup()
+    import PETITE.all_processes as proc
+    from PETITE import kinematics as kin
+    from PETITE import moliere
+    from PETITE.particle import Particle
+    from PETITE.shower import Shower
+    from PETITE.physical_constants import m_electron, m_muon, alpha_em
+    rng = np.random.default_rng(12345)
+    out = {}
+    # ---- differential cross sections at mapped points of the shipped maps
+    sh = {t: Shower(dict_dir, t, 0.010) for t in ("graphite", "lead")}
+    for t, s in sh.items():
+        for pname in ("Brem", "PairProd", "Comp", "Ann", "Moller", "Bhabha", "MuonE", "MuonBrem"):
+            rows = s._loaded_samples[pname]
+            X, E, V, ROW = [], [], [], []
+            for r in rng.choice(len(rows), size=12, replace=False):
+                Erow, info = rows[r]
+                amap = info["adaptive_map"]
+                d = len(amap.grid)
+                for _ in range(8):
+                    Einc = float(Erow) * float(rng.uniform(0.9, 1.1))
+                    x, _ = amap.map_one(rng.random(d))
+                    ev = {'E_inc': Einc, 'm_e': m_electron, 'Z_T': s._ZTarget, 'A_T': s._ATarget,
+                          'mT': s._ATarget, 'alpha_FS': alpha_em, 'mV': 0, 'Eg_min': s._Egamma_min,
+                          'Ee_min': s._Ee_min}
+                    if pname == "Brem":
+                        ev["m_lepton"] = m_electron
+                    if pname == "MuonBrem":
+                        ev["m_lepton"] = m_muon
+                    f = proc.__dict__[{"Brem": "dsigma_brem_dimensionless", "MuonBrem": "dsigma_brem_dimensionless",
+                                       "PairProd": "dsigma_pairprod_dimensionless", "Comp": "dsigma_compton_dCT",
+                                       "Ann": "dsigma_annihilation_dCT", "Moller": "dsigma_moller_dCT",
+                                       "Bhabha": "dsigma_bhabha_dCT", "MuonE": "dsigma_muonelectron_dCT"}[pname]](ev, d)
+                    with np.errstate(all="ignore"):
+                        v = float(f(np.asarray(x)))
+                    X.append(np.pad(x, (0, 4 - d))); E.append(Einc); V.append(v); ROW.append(r)
+            out[f"dsigma/{t}/{pname}/x"] = np.array(X)
+            out[f"dsigma/{t}/{pname}/E"] = np.array(E)
+            out[f"dsigma/{t}/{pname}/value"] = np.array(V)
+        # ---- mean free paths and branching inputs on a log grid
+        Es = np.geomspace(1e-3, 120.0, 400)
+        mf = np.array([[s.get_mfp([pid, e]) for e in Es] for pid in (11, -11, 22, 13)])
+        out[f"mfp/{t}/E"] = Es
+        out[f"mfp/{t}/value"] = mf
+        ns = np.array([[float(fn(e)) for e in Es] for fn in (s._NSigmaBrem, s._NSigmaPP, s._NSigmaAnn, s._NSigmaComp,
+                                                               s._NSigmaMoller, s._NSigmaBhabha, s._NSigmaMuonE,
+                                                               s._NSigmaMuonBrem)])
+        out[f"nsigma/{t}/value"] = ns
+    # ---- kinematics with a fixed azimuth uniform
+    router = StreamRouter(SEED)
+    saved = install(router)
+    try:
+        K = []
+        for case in range(200):
+            kind = case % 6
+            E = float(10 ** rng.uniform(-1.5, 2))
+            router.set_current(10_000 + case)
+            if kind == 0:
+                part = Particle([E, 0, 0, math.sqrt(E * E - m_electron ** 2)], [0, 0, 0], {"PID": 11, "mass": m_electron})
+                x = [rng.uniform(0, 0.999), rng.uniform(0, 0.01), rng.uniform(-0.01, 0.01), rng.uniform(0, 1)]
+                a, b = kin.e_to_egamma_fourvecs(part, x)
+            elif kind == 1:
+                part = Particle([E, 0, 0, E], [0, 0, 0], {"PID": 22, "mass": 0.0})
+                x = [rng.uniform(0.001, 0.999), rng.uniform(0, 0.01), rng.uniform(-0.01, 0.01), rng.uniform(0, 1)]
+                a, b = kin.gamma_to_epem_fourvecs(part, x)
+            elif kind == 2:
+                part = Particle([E, 0, 0, E], [0, 0, 0], {"PID": 22, "mass": 0.0})
+                x = [rng.uniform(-1, 1), 0, 0, 0]
+                a, b = kin.compton_fourvecs(part, x)
+            elif kind == 3:
+                part = Particle([E, 0, 0, math.sqrt(E * E - m_electron ** 2)], [0, 0, 0], {"PID": -11, "mass": m_electron})
+                x = [rng.uniform(-1, 0.99), 0, 0, 0]
+                a, b = kin.annihilation_fourvecs(part, x)
+            elif kind == 4:
+                part = Particle([E, 0, 0, math.sqrt(E * E - m_electron ** 2)], [0, 0, 0], {"PID": 11, "mass": m_electron})
+                x = [rng.uniform(-0.99, 0.99), 0, 0, 0]
+                a, b = kin.ee_to_ee_fourvecs(part, x)
+            else:
+                E = E + 0.2
+                part = Particle([E, 0, 0, math.sqrt(E * E - m_muon ** 2)], [0, 0, 0], {"PID": 13, "mass": m_muon})
+                x = [rng.uniform(-1, 0.999), 0, 0, 0]
+                a, b = kin.mue_to_mue_fourvecs(part, x)
+            K.append(np.concatenate([[kind, E], x, a, b]))
+        out["kin/rows"] = np.array(K)
+        # ---- multiple scattering (moliere.py:350-400) with routed draws
+        M = []
+        for case in range(300):
+            E = float(10 ** rng.uniform(-2, 2))
+            m = m_muon if case % 5 == 4 else m_electron
+            E = max(E, 1.5 * m)
+            th, ph = rng.uniform(0, 0.5), rng.uniform(-math.pi, math.pi)
+            pn = math.sqrt(E * E - m * m)
+            p4 = np.array([E, pn * math.sin(th) * math.cos(ph), pn * math.sin(th) * math.sin(ph), pn * math.cos(th)])
+            if case % 7 == 3:
+                p4[1] = 0.0
+            tt = float(10 ** rng.uniform(-4, 0))
+            A, Z = (12, 6) if case % 2 else (207, 82)
+            router.set_current(20_000 + case)
+            r = moliere.get_scattered_momentum_fast(p4, tt, A, Z, 1, m_lepton=m)
+            M.append(np.concatenate([[E, tt, A, Z, m], p4, r]))
+        out["mcs/rows"] = np.array(M)
+        # ---- Particle.rotation_matrix
+        R = []
+        for case in range(100):
+            v = rng.normal(size=3)
+            part = Particle([10.0, *v], [0, 0, 0], {"PID": 22, "mass": 0.0})
+            R.append(np.concatenate([v, np.array(part.rotation_matrix()).ravel()]))
+        out["rot/rows"] = np.array(R)
+        # ---- draw_sample: returned x and proposal counts for a fixed stream
+        s = sh["graphite"]
+        D = []
+        for case, (pname, E) in enumerate([(p, e) for p in ("Brem", "PairProd", "Comp", "Ann", "Moller", "Bhabha", "MuonE")
+                                           for e in (0.05, 0.3, 1.0, 7.0, 60.0)]):
+            if pname == "MuonE" and E < 0.3:
+                continue
+            router.set_current(30_000 + case)
+            x = s.draw_sample(E, process=pname, VB=True)
+            D.append(np.concatenate([[case, list(("Brem", "PairProd", "Comp", "Ann", "Moller", "Bhabha", "MuonE")).index(pname), E],
+                                     np.pad(x[:-1], (0, 4 - (len(x) - 1))), [x[-1]]]))
+        out["draw/rows"] = np.array(D)
+    finally:
+        uninstall(saved)
+    np.savez_compressed(out_path, **out)
+    print("units written", out_path)
+
+
+CASES = [
+    # name, target, cut, pid, E0, n primaries, primary mass for the momentum
+    ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 12, 0.000511),
+    ("gamma10_lead", "lead", 0.010, 22, 10.0, 2, 0.0),
+    ("pos3_lead", "lead", 0.010, -11, 3.0, 4, 0.000511),
+    ("mu5_graphite", "graphite", 0.010, 13, 5.0, 4, 0.1056583755),
+]
+
+if __name__ == "__main__":
+    d = sys.argv[1].rstrip("/") + "/"
+    which = sys.argv[2] if len(sys.argv) > 2 else "all"
+    if which in ("all", "units"):
+        gen_units(d, os.path.join(HERE, "units.npz"))
+    if which in ("all", "showers"):
+        gen_showers(d, os.path.join(HERE, "showers.npz"), CASES)

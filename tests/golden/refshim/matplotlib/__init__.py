@@ -1,0 +1,1 @@
+"""Empty stand-in so PETITE's plot-only import succeeds (see README.txt)."""
