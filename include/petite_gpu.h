@@ -1,0 +1,148 @@
+/*
+ * petite_gpu.h -- C ABI of the GB300 electromagnetic-shower engine.
+ *
+ * PETITE (kjkellyphys/PETITE) is pure Python and has no FFI; these entry
+ * points replace the Python functions named in each comment (paths are
+ * inside PETITE's src/PETITE/).  The ctypes layer in petite_gb300/_lib.py
+ * binds exactly these symbols.
+ *
+ * Conventions
+ *  - Every pointer inside a struct below is a DEVICE pointer (cudaMalloc'd or
+ *    a torch tensor's data_ptr()); the caller owns all memory and the library
+ *    never frees it.  Handles own only a small device copy of the scalar
+ *    table description.
+ *  - Functions return a pt_status; no exception or C++ type crosses the ABI.
+ *  - Work is enqueued on the given stream (0 = legacy default stream); calls
+ *    that must report a count or an error synchronise that stream.
+ *  - Handles are not thread-safe; use one per host thread.
+ */
+#ifndef PETITE_GPU_H
+#define PETITE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pt_status {
+  PT_OK = 0,
+  PT_NO_SAMPLE = 1,   /* rejection sampler exhausted max_n_integrators*neval proposals
+                         ("No Sample Found", shower.py:460-461) */
+  PT_TIMEOUT = 2,     /* a bounded device loop hit its iteration limit */
+  PT_BAD_TABLE = 3,   /* inconsistent table description */
+  PT_OOM = 4,         /* output/queue capacity too small: retry with more rows */
+  PT_CUDA_ERR = 5,    /* a CUDA runtime call failed */
+  PT_BAD_ARG = 6      /* invalid argument (null pointer, unsupported PID, ...) */
+} pt_status;
+
+enum { PT_N_PROCESSES = 8, PT_N_NSIGMA = 8, PT_MAX_DIM = 4 };
+
+/* Process codes follow shower.py:36. */
+enum { PT_BREM = 0, PT_ANN = 1, PT_PAIRPROD = 2, PT_COMP = 3, PT_MOLLER = 4,
+       PT_BHABHA = 5, PT_MUONE = 6, PT_MUONBREM = 7 };
+
+/* Tables for one target material: the content of sm_maps.pkl/sm_xsec.pkl
+ * after Shower.__init__ (shower.py:100-142,210-320).  Map rows of all
+ * processes are concatenated; process p owns rows [map_base[p], map_base[p]+map_rows[p]). */
+typedef struct pt_tables {
+  int32_t map_base[PT_N_PROCESSES];
+  int32_t map_rows[PT_N_PROCESSES];
+  int32_t n_rows;                 /* total map rows */
+  const double* map_energy;       /* [n_rows] incoming energy of each trained map */
+  const double* map_maxF;         /* [n_rows] max_F[target] * maxF_fudge_global */
+  const double* map_neval;        /* [n_rows] neval of each map */
+  const int64_t* grid_offset;     /* [n_rows*4] first node of dimension d of row r */
+  const int32_t* grid_ninc;       /* [n_rows*4] increments (nodes - 1) */
+  const double* grid_nodes;       /* [n_nodes] all grid nodes, float64 */
+  const float* grid_nodes_f32;    /* [n_nodes] same nodes rounded to float32 (mixed form) */
+  int64_t n_nodes;
+  /* n*sigma(E) interpolation tables in 1/cm, slots: Brem, PairProd, Ann, Comp,
+   * Moller, Bhabha, MuonE, MuonBrem (shower.py:280-295) */
+  int32_t ns_base[PT_N_NSIGMA];
+  int32_t ns_len[PT_N_NSIGMA];
+  const double* ns_x;
+  const double* ns_y;
+  /* target and thresholds */
+  double Z, A, rho;               /* physical_constants.py:49-55 */
+  double dEdx_GeV_per_m;          /* 0.1 * dEdx[MeV/cm] (shower.py:649) */
+  double Eg_min, Ee_min;          /* shower.py:214-215 */
+  double min_calc_electron, min_calc_positron, min_calc_muon, min_calc_photon; /* shower.py:242-246 */
+  /* form-factor and multiple-scattering constants, evaluated on the host with
+   * the reference's expressions: a0 = aa(Z, m_e) (all_processes.py:92-94) */
+  double a0sq;                    /* a0**2 */
+  double Z2a04;                   /* Z**2 * a0**4  (g2_elastic, all_processes.py:99-103) */
+  double Z23;                     /* Z**(2/3)      (moliere.py:219) */
+} pt_tables;
+
+typedef struct pt_handle pt_handle;
+
+/* Shower.__init__ (shower.py:100-142): validates and keeps the table description. */
+pt_status pt_create(const pt_tables* tables, pt_handle** out);
+/* Releases the handle (not the caller's device buffers). */
+void pt_destroy(pt_handle* h);
+/* Text for a status code. */
+const char* pt_strerror(int status);
+/* Details of the last PT_NO_SAMPLE/PT_TIMEOUT: process code, energy, LU_Key. */
+pt_status pt_last_error_info(pt_handle* h, int32_t* process, double* energy, int32_t* lu_key);
+
+/* Particle list in structure-of-arrays form; one row per Particle
+ * (particle.py:50-131).  Vectors are component-major: p0[c*capacity + row]. */
+typedef struct pt_particles {
+  double* p0;        /* [4][capacity] initial four-momentum (E, px, py, pz) */
+  double* r0;        /* [3][capacity] initial position (m) */
+  double* pf;        /* [4][capacity] four-momentum after propagation */
+  double* rf;        /* [3][capacity] position after propagation */
+  double* weight;    /* [capacity] */
+  double* mass;      /* [capacity] */
+  int32_t* pid;      /* [capacity] PDG id */
+  int32_t* gen;      /* [capacity] generation_number */
+  int32_t* proc;     /* [capacity] generation_process code, -1 = "Input" */
+  int32_t* bit;      /* [capacity] 0/1: first or second daughter (ID = 2*parent_ID + bit) */
+  int32_t* primary;  /* [capacity] index of the primary the row belongs to */
+  int32_t* draws;    /* [capacity] uniforms consumed by this particle (diagnostic) */
+  int64_t* parent;   /* [capacity] parent row, -1 for a primary */
+  uint64_t* pkey;    /* [capacity] random-stream key of the particle */
+  int64_t capacity;
+} pt_particles;
+
+typedef struct pt_opts {
+  double min_energy;             /* Shower(min_energy) */
+  int64_t max_n_integrators;     /* Shower(max_n_integrators): proposals <= this * neval */
+  double rescale_MCS;            /* Shower(rescale_MCS) */
+  int32_t multiple_scattering;   /* generate_shower(GlobalMS) */
+  int32_t precision;             /* 0 = float64 throughout, 1 = float32 sampling + float64 kinematics */
+  uint64_t seed;                 /* Philox key */
+  int64_t primary_offset;        /* primary i draws from the stream of index primary_offset + i */
+} pt_opts;
+
+/* Shower.generate_shower (shower.py:603-708) for n_primaries independent
+ * primaries at once.  Rows [0, n_primaries) of `out` must hold the primaries
+ * (p0, r0, pid, mass, weight; the remaining fields are filled here).  The
+ * call transports every particle, appends daughters with E > min_energy,
+ * and returns the number of rows used in *n_rows.  Row order is not the
+ * reference's list order; parent/bit give the tree (the Python layer
+ * restores list order).  Returns PT_OOM if capacity is too small. */
+pt_status pt_run_sm(pt_handle* h, pt_particles* out, int64_t n_primaries,
+                    const pt_opts* opts, int64_t* n_rows, void* stream);
+
+/* Counters of the last pt_run_sm on this handle: kernel launches and waves
+ * (transport iterations).  Diagnostic; no reference counterpart. */
+pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* waves);
+
+/* Shower.draw_sample (shower.py:401-465) for a batch: for each i, draws the
+ * final-state variables of `process` at energy energy[i] from stream key
+ * pkey[i] starting at draw 0.  Writes x[i*4 + d], proposals[i], lu_key[i]. */
+pt_status pt_sample_only(pt_handle* h, int32_t process, const double* energy,
+                         const uint64_t* pkey, int64_t n, const pt_opts* opts,
+                         double* x, int64_t* proposals, int32_t* lu_key, void* stream);
+
+/* Differential cross section of `process` (all_processes.py, the dsigma_*
+ * classes) at n points x[i*4 + d] and energies energy[i]: value[i]. */
+pt_status pt_dsigma(pt_handle* h, int32_t process, const double* x, const double* energy,
+                    int64_t n, int32_t precision, double* value, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PETITE_GPU_H */

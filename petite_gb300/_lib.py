@@ -1,0 +1,98 @@
+"""ctypes binding of include/petite_gpu.h.
+
+The engine has no CPU fallback: if the library is missing or a CUDA device
+is absent, the calls that need it raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+N_PROC = 8
+N_NS = 8
+
+STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE", 4: "PT_OOM",
+                5: "PT_CUDA_ERR", 6: "PT_BAD_ARG"}
+PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
+
+EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats", "pt_run_sm",
+           "pt_sample_only", "pt_dsigma")
+
+
+class PtTables(C.Structure):
+    _fields_ = [
+        ("map_base", C.c_int32 * N_PROC), ("map_rows", C.c_int32 * N_PROC), ("n_rows", C.c_int32),
+        ("map_energy", C.c_void_p), ("map_maxF", C.c_void_p), ("map_neval", C.c_void_p),
+        ("grid_offset", C.c_void_p), ("grid_ninc", C.c_void_p), ("grid_nodes", C.c_void_p),
+        ("grid_nodes_f32", C.c_void_p), ("n_nodes", C.c_int64),
+        ("ns_base", C.c_int32 * N_NS), ("ns_len", C.c_int32 * N_NS), ("ns_x", C.c_void_p), ("ns_y", C.c_void_p),
+        ("Z", C.c_double), ("A", C.c_double), ("rho", C.c_double), ("dEdx_GeV_per_m", C.c_double),
+        ("Eg_min", C.c_double), ("Ee_min", C.c_double),
+        ("min_calc_electron", C.c_double), ("min_calc_positron", C.c_double),
+        ("min_calc_muon", C.c_double), ("min_calc_photon", C.c_double),
+        ("a0sq", C.c_double), ("Z2a04", C.c_double), ("Z23", C.c_double),
+    ]
+
+
+class PtParticles(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("p0", "r0", "pf", "rf", "weight", "mass", "pid", "gen", "proc",
+                                          "bit", "primary", "draws", "parent", "pkey")] + [("capacity", C.c_int64)]
+
+
+class PtOpts(C.Structure):
+    _fields_ = [("min_energy", C.c_double), ("max_n_integrators", C.c_int64), ("rescale_MCS", C.c_double),
+                ("multiple_scattering", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64),
+                ("primary_offset", C.c_int64)]
+
+
+class PetiteGPUError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return os.path.join(_build.LIBDIR, _build.LIBNAME)
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Loads (building first if needed) the CUDA library; raises if impossible."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if build_if_missing and not _build.up_to_date(path):
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"petite_gb300 CUDA library not built: {path}")
+    lib = C.CDLL(path)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    lib.pt_create.argtypes = [C.POINTER(PtTables), C.POINTER(vp)]
+    lib.pt_create.restype = C.c_int
+    lib.pt_destroy.argtypes = [vp]
+    lib.pt_destroy.restype = None
+    lib.pt_strerror.argtypes = [C.c_int]
+    lib.pt_strerror.restype = C.c_char_p
+    lib.pt_last_error_info.argtypes = [vp, C.POINTER(i32), C.POINTER(C.c_double), C.POINTER(i32)]
+    lib.pt_last_error_info.restype = C.c_int
+    lib.pt_last_run_stats.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
+    lib.pt_last_run_stats.restype = C.c_int
+    lib.pt_run_sm.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
+    lib.pt_run_sm.restype = C.c_int
+    lib.pt_sample_only.argtypes = [vp, i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp, vp]
+    lib.pt_sample_only.restype = C.c_int
+    lib.pt_dsigma.argtypes = [vp, i32, vp, vp, i64, i32, vp, vp]
+    lib.pt_dsigma.restype = C.c_int
+    _LIB = lib
+    return lib
+
+
+def check(status: int, what: str = ""):
+    if status != PT_OK:
+        msg = load().pt_strerror(status).decode()
+        raise PetiteGPUError(status, f"{what}: {msg}" if what else msg)

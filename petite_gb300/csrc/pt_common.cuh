@@ -1,0 +1,115 @@
+// pt_common.cuh -- constants, random streams and arithmetic helpers shared by
+// the shower kernels.  sm_103a only.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pt {
+
+// ---------------------------------------------------------------- constants
+// Same expressions as PETITE's physical_constants.py:11-38, so every value
+// rounds exactly as the Python module's does.
+constexpr double kPi = 3.141592653589793;
+constexpr double kMeV = 1e-3;
+constexpr double kkeV = 1e-6;
+constexpr double kAlpha = 1 / 137.035999;
+constexpr double kMe = 510.998950 * kkeV;
+constexpr double kMmu = 105.6583755 * kMeV;
+constexpr double kCmToM = 0.01;
+
+// ------------------------------------------------------------ random stream
+// Philox4x32-10 (Salmon et al., SC'11).  Counter = (draw block lo, hi,
+// particle key lo, hi), key = 64-bit seed.  Draw n of a particle uses block
+// n>>1 and 64-bit half n&1; uniform double = (u64 >> 11) * 2^-53 in [0,1).
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {   // SplitMix64 finaliser
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t primary_key(uint64_t i) { return mix64(i + 1); }
+__host__ __device__ __forceinline__ uint64_t daughter_key(uint64_t parent, int bit) {
+  return mix64(parent + 0x9E3779B97F4A7C15ull * (uint64_t)(1 + bit));
+}
+
+struct Rng {
+  uint32_t s0, s1, k0, k1;   // seed lo/hi, particle key lo/hi
+  uint64_t n;                // next draw index
+  uint64_t spare;            // odd half of the current block
+  __device__ __forceinline__ void init(uint64_t seed, uint64_t key) {
+    s0 = (uint32_t)seed; s1 = (uint32_t)(seed >> 32);
+    k0 = (uint32_t)key;  k1 = (uint32_t)(key >> 32);
+    n = 0; spare = 0;
+  }
+  __device__ __forceinline__ uint64_t next_u64() {
+    if (n & 1ull) { ++n; return spare; }
+    const uint64_t blk = n >> 1;
+    const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+    spare = (uint64_t)o.z | ((uint64_t)o.w << 32);
+    ++n;
+    return (uint64_t)o.x | ((uint64_t)o.y << 32);
+  }
+  __device__ __forceinline__ double u() { return (double)(next_u64() >> 11) * 0x1p-53; }
+  // float form of the same draw (its top 24 bits); used by the float32 sampler
+  __device__ __forceinline__ float uf() { return (float)(next_u64() >> 40) * 0x1p-24f; }
+};
+
+// --------------------------------------------------- non-contracting float64
+// The reference evaluates expressions one rounding per operation (numpy
+// scalars).  Where a formula is ill-conditioned (1 - beta^2, arccos near 1,
+// sqrt(1 - c^2)) a fused multiply-add changes the result far beyond the last
+// place, so those code paths use S, whose operators never fuse.
+struct S {
+  double v;
+  __device__ __forceinline__ S() : v(0) {}
+  __device__ __forceinline__ S(double x) : v(x) {}
+  __device__ __forceinline__ operator double() const { return v; }
+};
+__device__ __forceinline__ S operator+(S a, S b) { return S(__dadd_rn(a.v, b.v)); }
+__device__ __forceinline__ S operator-(S a, S b) { return S(__dsub_rn(a.v, b.v)); }
+__device__ __forceinline__ S operator*(S a, S b) { return S(__dmul_rn(a.v, b.v)); }
+__device__ __forceinline__ S operator/(S a, S b) { return S(__ddiv_rn(a.v, b.v)); }
+__device__ __forceinline__ S operator-(S a) { return S(-a.v); }
+__device__ __forceinline__ S sq(S a) { return a * a; }
+__device__ __forceinline__ S ssqrt(S a) { return S(__dsqrt_rn(a.v)); }
+
+// numpy.linalg.norm of a 3-vector: sqrt of a sequential fused dot product.
+__device__ __forceinline__ double norm3_np(double x, double y, double z) {
+  return __dsqrt_rn(__fma_rn(z, z, __fma_rn(y, y, __dmul_rn(x, x))));
+}
+
+// ------------------------------------------------------------ warp helpers
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Each lane of the currently converged group asks for `want` in {0,1,2}
+// slots of `counter`; one atomic per group.  Returns this lane's first slot.
+__device__ __forceinline__ unsigned long long warp_reserve(unsigned long long* counter, int want) {
+  const unsigned mask = __activemask();
+  const unsigned b1 = __ballot_sync(mask, want >= 1);
+  const unsigned b2 = __ballot_sync(mask, want >= 2);
+  const unsigned lt = lanemask_lt();
+  const unsigned prefix = __popc(b1 & lt) + __popc(b2 & lt);
+  const unsigned total = __popc(b1) + __popc(b2);
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if ((int)(threadIdx.x & 31) == leader && total) base = atomicAdd(counter, (unsigned long long)total);
+  base = __shfl_sync(mask, base, leader);
+  return base + prefix;
+}
+
+}  // namespace pt

@@ -1,0 +1,226 @@
+"""Device side of the SM shower: tables in HBM and the calls into the C ABI.
+
+Torch owns every device buffer; the library only reads and writes them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from .tables import M_ELECTRON, SMTables
+
+U64 = (1 << 64) - 1
+
+
+def mix64(z: int) -> int:
+    """SplitMix64 finaliser; same as the device's (pt_common.cuh)."""
+    z &= U64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & U64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & U64
+    return z ^ (z >> 31)
+
+
+def primary_key(i: int) -> int:
+    """Random-stream key of primary number i."""
+    return mix64(i + 1)
+
+
+def daughter_key(parent: int, bit: int) -> int:
+    """Random-stream key of daughter `bit` (0 or 1) of a particle."""
+    return mix64(parent + 0x9E3779B97F4A7C15 * (1 + bit))
+
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+class ParticleStore:
+    """SoA particle rows on the device (layout of ``pt_particles``)."""
+
+    FIELDS_F64 = {"p0": 4, "r0": 3, "pf": 4, "rf": 3, "weight": 1, "mass": 1}
+    FIELDS_I32 = ("pid", "gen", "proc", "bit", "primary", "draws")
+
+    def __init__(self, capacity: int, device):
+        torch = _torch()
+        self.capacity = int(capacity)
+        self.t = {}
+        for k, n in self.FIELDS_F64.items():
+            self.t[k] = torch.zeros((n, self.capacity) if n > 1 else (self.capacity,), dtype=torch.float64, device=device)
+        for k in self.FIELDS_I32:
+            self.t[k] = torch.zeros(self.capacity, dtype=torch.int32, device=device)
+        self.t["parent"] = torch.zeros(self.capacity, dtype=torch.int64, device=device)
+        self.t["pkey"] = torch.zeros(self.capacity, dtype=torch.int64, device=device)   # uint64 bits
+
+    def abi(self) -> _lib.PtParticles:
+        s = _lib.PtParticles()
+        for k in ("p0", "r0", "pf", "rf", "weight", "mass", "pid", "gen", "proc", "bit", "primary", "draws",
+                  "parent", "pkey"):
+            setattr(s, k, self.t[k].data_ptr())
+        s.capacity = self.capacity
+        return s
+
+    def to_numpy(self, n: int) -> dict:
+        out = {}
+        for k, v in self.t.items():
+            a = v[..., :n].cpu().numpy()
+            out[k] = a.T.copy() if a.ndim == 2 else a
+        out["pkey"] = out["pkey"].view(np.uint64)
+        return out
+
+
+class SMEngine:
+    """Uploads one target's tables and exposes the C-ABI entry points."""
+
+    def __init__(self, tables: SMTables, device="cuda"):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("petite_gb300 needs a CUDA device (GB300); there is no CPU fallback")
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.tables = tables
+        dev = self.device
+        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float64), device=dev)
+        self._keep = {
+            "map_energy": f64(tables.map_energy),
+            "map_maxF": f64(tables.map_maxF),
+            "map_neval": f64(tables.map_neval),
+            "grid_offset": torch.as_tensor(np.ascontiguousarray(tables.grid_offset.reshape(-1), np.int64), device=dev),
+            "grid_ninc": torch.as_tensor(np.ascontiguousarray(tables.grid_ninc.reshape(-1), np.int32), device=dev),
+            "grid_nodes": f64(tables.grid_nodes),
+            "grid_nodes_f32": torch.as_tensor(tables.grid_nodes.astype(np.float32), device=dev),
+        }
+        ns_x = np.concatenate([x for x, _ in tables.nsigma])
+        ns_y = np.concatenate([y for _, y in tables.nsigma])
+        self._keep["ns_x"] = f64(ns_x)
+        self._keep["ns_y"] = f64(ns_y)
+        pt = _lib.PtTables()
+        for p in range(_lib.N_PROC):
+            pt.map_base[p] = int(tables.map_base[p])
+            pt.map_rows[p] = int(tables.map_rows[p])
+        pt.n_rows = int(len(tables.map_energy))
+        for k in ("map_energy", "map_maxF", "map_neval", "grid_offset", "grid_ninc", "grid_nodes", "grid_nodes_f32"):
+            setattr(pt, k, self._keep[k].data_ptr())
+        pt.n_nodes = int(len(tables.grid_nodes))
+        base = 0
+        for s, (x, _) in enumerate(tables.nsigma):
+            pt.ns_base[s] = base
+            pt.ns_len[s] = len(x)
+            base += len(x)
+        pt.ns_x = self._keep["ns_x"].data_ptr()
+        pt.ns_y = self._keep["ns_y"].data_ptr()
+        pt.Z, pt.A, pt.rho = tables.Z, tables.A, tables.rho
+        pt.dEdx_GeV_per_m = tables.dEdx * 0.1
+        pt.Eg_min, pt.Ee_min = tables.Eg_min, tables.Ee_min
+        mc = tables.min_calc
+        pt.min_calc_electron, pt.min_calc_positron = mc[11], mc[-11]
+        pt.min_calc_muon, pt.min_calc_photon = mc[13], mc[22]
+        # all_processes.py:92-103 and moliere.py:219, same expressions as the reference
+        Z = tables.Z_int
+        a0 = 184.15 * (2.718) ** -0.5 * Z ** (-1.0 / 3.0) / M_ELECTRON
+        pt.a0sq = a0 ** 2
+        pt.Z2a04 = Z ** 2 * a0 ** 4
+        pt.Z23 = Z ** (2. / 3.)
+        self._pt = pt
+        h = C.c_void_p()
+        _lib.check(self.lib.pt_create(C.byref(pt), C.byref(h)), "pt_create")
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _stream(self):
+        return C.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
+
+    def _raise(self, status, what):
+        if status == _lib.PT_NO_SAMPLE:
+            proc, E, key = C.c_int32(), C.c_double(), C.c_int32()
+            self.lib.pt_last_error_info(self.handle, C.byref(proc), C.byref(E), C.byref(key))
+            from .tables import PROCESSES
+            raise Exception("No Sample Found", PROCESSES[proc.value], E.value, key.value)
+        _lib.check(status, what)
+
+    @staticmethod
+    def opts(min_energy, max_n_integrators=10000, rescale_MCS=1.0, ms=True, precision="fp64", seed=0,
+             primary_offset=0):
+        o = _lib.PtOpts()
+        o.min_energy = float(min_energy)
+        o.max_n_integrators = int(max_n_integrators)
+        o.rescale_MCS = float(rescale_MCS)
+        o.multiple_scattering = 1 if ms else 0
+        o.precision = PRECISIONS[precision]
+        o.seed = int(seed) & ((1 << 64) - 1)
+        o.primary_offset = int(primary_offset)
+        return o
+
+    def run_sm(self, p0, r0, pid, mass, weight, opts: _lib.PtOpts, capacity: int | None = None):
+        """Transports primaries (host arrays); returns (store, n_rows)."""
+        torch = _torch()
+        p0 = np.asarray(p0, np.float64).reshape(-1, 4)
+        n = len(p0)
+        r0 = np.asarray(r0, np.float64).reshape(n, 3)
+        if capacity is None:
+            est = np.sum(2.0 * p0[:, 0] / max(opts.min_energy, 1e-3)) + 16 * n
+            capacity = int(min(max(est, 1024), 2 ** 31 - 1))
+        while True:
+            st = ParticleStore(capacity, self.device)
+            st.t["p0"][:, :n] = torch.as_tensor(p0.T, device=self.device)
+            st.t["r0"][:, :n] = torch.as_tensor(r0.T, device=self.device)
+            st.t["pid"][:n] = torch.as_tensor(np.asarray(pid, np.int32), device=self.device)
+            st.t["mass"][:n] = torch.as_tensor(np.asarray(mass, np.float64), device=self.device)
+            st.t["weight"][:n] = torch.as_tensor(np.asarray(weight, np.float64), device=self.device)
+            abi = st.abi()
+            nrows = C.c_int64()
+            s = self.lib.pt_run_sm(self.handle, C.byref(abi), n, C.byref(opts), C.byref(nrows), self._stream())
+            if s == _lib.PT_OOM:
+                capacity *= 2
+                del st
+                continue
+            self._raise(s, "pt_run_sm")
+            return st, int(nrows.value)
+
+    def last_run_stats(self):
+        l, w = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.pt_last_run_stats(self.handle, C.byref(l), C.byref(w)), "pt_last_run_stats")
+        return int(l.value), int(w.value)
+
+    def sample_only(self, process: int, energy, pkey, opts: _lib.PtOpts):
+        torch = _torch()
+        E = torch.as_tensor(np.asarray(energy, np.float64), device=self.device)
+        K = torch.as_tensor(np.asarray(pkey, np.uint64).view(np.int64), device=self.device)
+        n = E.numel()
+        x = torch.zeros(n * 4, dtype=torch.float64, device=self.device)
+        props = torch.zeros(n, dtype=torch.int64, device=self.device)
+        lu = torch.zeros(n, dtype=torch.int32, device=self.device)
+        s = self.lib.pt_sample_only(self.handle, int(process), _ptr(E), _ptr(K), n, C.byref(opts), _ptr(x),
+                                    _ptr(props), _ptr(lu), self._stream())
+        self._raise(s, "pt_sample_only")
+        return x.view(n, 4).cpu().numpy(), props.cpu().numpy(), lu.cpu().numpy()
+
+    def dsigma(self, process: int, x, energy, precision="fp64"):
+        torch = _torch()
+        x = np.asarray(x, np.float64).reshape(-1, 4)
+        X = torch.as_tensor(x, device=self.device).contiguous()
+        E = torch.as_tensor(np.asarray(energy, np.float64), device=self.device)
+        out = torch.zeros(len(x), dtype=torch.float64, device=self.device)
+        s = self.lib.pt_dsigma(self.handle, int(process), _ptr(X), _ptr(E), len(x), PRECISIONS[precision],
+                               _ptr(out), self._stream())
+        _lib.check(s, "pt_dsigma")
+        return out.cpu().numpy()

@@ -1,0 +1,225 @@
+"""Drop-in ``Shower`` for PETITE's SM shower path (shower.py:98-708).
+
+Same constructor and ``generate_shower`` signature as PETITE; the transport
+runs in the CUDA engine.  ``generate_showers`` is the batched form (many
+primaries per launch, structure-of-arrays output).
+
+Random numbers: PETITE draws from process-global generators in list order.
+Here each particle has its own Philox stream, keyed by ``seed`` and by its
+lineage (primary index, then the daughter bit at every generation), so a
+shower does not depend on how the engine schedules particles.
+"""
+from __future__ import annotations
+
+import copy
+import os
+
+import numpy as np
+
+from . import tables as T
+from ._lib import PetiteGPUError
+from .engine import SMEngine
+from .particle import MASS, Particle
+
+SUPPORTED_PIDS = (11, -11, 22, 13, -13)
+
+
+class ShowerBatch:
+    """Output of :meth:`Shower.generate_showers`: one row per particle.
+
+    Arrays (numpy): p0 (n,4), r0 (n,3), pf (n,4), rf (n,3), weight, mass,
+    pid, gen, proc (-1 = "Input"), bit, primary, parent (row, -1 for
+    primaries), pkey, draws.  ``order`` lists rows in PETITE's list order
+    (primary by primary, breadth first).
+    """
+
+    def __init__(self, arrays: dict, n_primaries: int):
+        self.__dict__.update(arrays)
+        self.n_primaries = n_primaries
+        self.n = len(self.pid)
+        self._order = None
+
+    @property
+    def order(self):
+        if self._order is None:
+            self._order = list_order(self.primary, self.gen, self.parent, self.bit)
+        return self._order
+
+
+def list_order(primary, gen, parent, bit):
+    """Row order of PETITE's ``all_particles`` list (shower.py:634-706):
+    per primary, generation by generation, children in the order of their
+    parents' positions, first daughter before second."""
+    n = len(primary)
+    pos = np.full(n, -1, np.int64)
+    roots = np.where(parent < 0)[0]
+    roots = roots[np.argsort(primary[roots], kind="stable")]
+    pos[roots] = np.arange(len(roots))          # provisional, per-generation
+    order_by_gen = [roots]
+    g = 1
+    while True:
+        rows = np.where(gen == g)[0]
+        if len(rows) == 0:
+            break
+        keys = np.lexsort((bit[rows], pos[parent[rows]]))
+        rows = rows[keys]
+        pos[rows] = np.arange(len(rows))
+        order_by_gen.append(rows)
+        g += 1
+    allrows = np.concatenate(order_by_gen)
+    # stable sort by primary keeps the breadth-first order inside each shower
+    return allrows[np.argsort(primary[allrows], kind="stable")]
+
+
+class Shower:
+    """Representation of a shower (shower.py:98-142)."""
+
+    def __init__(self, dict_dir, target_material, min_energy, maxF_fudge_global=1,
+                 max_n_integrators=int(1e4), fast_MCS_mode=True, seed=None, rescale_MCS=1,
+                 precision="fp64", device="cuda"):
+        if not fast_MCS_mode:
+            raise NotImplementedError("fast_MCS_mode=False (Bethe-Moliere scattering) is not implemented")
+        if dict_dir is None:
+            dict_dir = T.BUNDLED_DIR
+        self._dict_dir = dict_dir
+        self._target_material = target_material
+        self.min_energy = min_energy
+        self._raw = T.read_dict_dir(dict_dir)
+        self.tables = T.SMTables(self._raw, target_material, maxF_fudge_global)
+        self._ZTarget, self._ATarget = T.TARGET_INFORMATION[target_material]["Z_T"], T.TARGET_INFORMATION[target_material]["A_T"]
+        self._rhoTarget, self._dEdx = self.tables.rho, self.tables.dEdx
+        self._maxF_fudge_global = maxF_fudge_global
+        self._max_n_integrators = max_n_integrators
+        self._MCS_rescale_factor = rescale_MCS
+        self._precision = precision
+        if seed is None:
+            seed = int.from_bytes(os.urandom(8), "little")
+        self._seed = int(seed)
+        self._next_primary = 0          # successive showers use fresh streams
+        self._engine = SMEngine(self.tables, device)
+
+    # ------------------------------------------------------------- accessors
+    def get_dict_dir(self):
+        return self._dict_dir
+
+    def get_target_material(self):
+        return self._target_material
+
+    def get_material_properties(self):
+        return self._ZTarget, self._ATarget, self._rhoTarget, self._dEdx
+
+    def get_n_targets(self):
+        return self.tables.n_target, self.tables.n_elec
+
+    def _opts(self, GlobalMS=True, precision=None):
+        return SMEngine.opts(self.min_energy, self._max_n_integrators, self._MCS_rescale_factor,
+                             ms=GlobalMS, precision=precision or self._precision, seed=self._seed)
+
+    # ------------------------------------------------------------- n*sigma
+    def _ns(self, slot, E):
+        x, y = self.tables.nsigma[slot]
+        E = np.asarray(E, dtype=np.float64)
+        return np.where((E < x[0]) | (E > x[-1]), 0.0, np.interp(E, x, y))
+
+    def get_mfp(self, particle):
+        """Mean free path in metres (shower.py:370-389)."""
+        if isinstance(particle, (list, tuple, np.ndarray)):
+            PID, E = particle
+        else:
+            PID, E = particle.get_ids()["PID"], particle.get_pf()[0]
+        slots = {22: (T.NS_PP, T.NS_COMP), 11: (T.NS_BREM, T.NS_MOLLER),
+                 -11: (T.NS_BREM, T.NS_BHABHA, T.NS_ANN)}.get(PID, (T.NS_MUONBREM, T.NS_MUONE))
+        ns = sum(self._ns(s, E) for s in slots)
+        if ns <= 0.0:
+            return 1.0e12
+        return T.CMTOM / ns
+
+    # ------------------------------------------------------------- sampling
+    def draw_sample(self, Einc, LU_Key=-1, process="PairProd", VB=False, pkey=None):
+        """Draws final-state variables from the trained map (shower.py:401-465).
+
+        ``pkey`` selects the random stream (default: a fresh one per call)."""
+        if process not in T.PROCESS_CODE:
+            raise Exception("Your process is not in the list")
+        if pkey is None:
+            pkey = np.uint64(_stream_key(self._next_primary))
+            self._next_primary += 1
+        x, props, _ = self._engine.sample_only(T.PROCESS_CODE[process], [Einc], [pkey], self._opts())
+        x = x[0, :T.DIMENSIONS[process]]
+        if VB:
+            return np.concatenate([x, [props[0]]])
+        return x
+
+    # ------------------------------------------------------------- showers
+    def generate_showers(self, p0, r0=None, pid=11, mass=None, weight=1.0, GlobalMS=True,
+                         precision=None, first_primary=None) -> ShowerBatch:
+        """Batched generate_shower: p0 (n,4) four-momenta, r0 (n,3) positions,
+        pid (n,) or scalar.  Returns every particle of every shower."""
+        p0 = np.atleast_2d(np.asarray(p0, np.float64))
+        n = len(p0)
+        r0 = np.zeros((n, 3)) if r0 is None else np.asarray(r0, np.float64).reshape(n, 3)
+        pid = np.broadcast_to(np.asarray(pid, np.int32), (n,)).copy()
+        for q in np.unique(pid):
+            if int(q) not in SUPPORTED_PIDS:
+                raise ValueError(f"PID {int(q)} is not transported by the shower path")
+        if mass is None:
+            mass = np.array([MASS[int(q)] for q in pid])
+        mass = np.broadcast_to(np.asarray(mass, np.float64), (n,)).copy()
+        weight = np.broadcast_to(np.asarray(weight, np.float64), (n,)).copy()
+        if first_primary is None:
+            first_primary = self._next_primary
+            self._next_primary += n
+        opts = self._opts(GlobalMS, precision)
+        opts.primary_offset = int(first_primary)      # primary i uses stream first_primary + i
+        st, rows = self._engine.run_sm(p0, r0, pid, mass, weight, opts)
+        return ShowerBatch(st.to_numpy(rows), n)
+
+    def generate_shower(self, p0, VB=False, GlobalMS=True):
+        """Generates a particle shower from an initial particle (shower.py:603-708)."""
+        ids = p0.get_ids()
+        if ids.get("stability", "stable") != "stable":
+            raise NotImplementedError("decays of unstable primaries are outside the shower path")
+        p0.set_ended(False)
+        p0copy = copy.deepcopy(p0)
+        if p0.get_p0()[0] < self.min_energy:
+            p0.set_ended(True)
+            return [p0copy]
+        mass = ids["mass"]
+        b = self.generate_showers(np.asarray(p0.get_p0(), np.float64)[None], np.asarray(p0.get_r0(), np.float64)[None],
+                                  pid=ids["PID"], mass=mass, weight=ids["weight"], GlobalMS=GlobalMS)
+        return batch_to_particles(b, [p0copy])[0]
+
+
+def _stream_key(i):
+    from .engine import primary_key
+    return primary_key(i)   # host copy of the device's key derivation
+
+
+def batch_to_particles(b: ShowerBatch, primaries):
+    """Builds PETITE Particle lists (one per primary) from a ShowerBatch."""
+    order = b.order
+    out = [[] for _ in range(b.n_primaries)]
+    ids_of = {}
+    for r in order:
+        k = int(b.primary[r])
+        if b.parent[r] < 0:
+            part = primaries[k]
+            part.set_pf(b.pf[r].copy())
+            part.set_rf(b.rf[r].copy())
+            part.set_ended(True)
+            ids_of[r] = (part.get_ids()["ID"], part.get_ids()["generation_number"], part.get_ids()["PID"])
+            out[k].append(part)
+            continue
+        pr = int(b.parent[r])
+        pid_parent, gen_parent, pdg_parent = ids_of[pr]
+        my_id = 2 * pid_parent + int(b.bit[r])
+        d = {"PID": int(b.pid[r]), "parent_PID": pdg_parent, "ID": my_id, "parent_ID": pid_parent,
+             "generation_number": gen_parent + 1, "generation_process": T.PROCESSES[int(b.proc[r])],
+             "weight": float(b.weight[r]), "mass": float(b.mass[r])}
+        part = Particle(b.p0[r].copy(), b.r0[r].copy(), d)
+        part.set_pf(b.pf[r].copy())
+        part.set_rf(b.rf[r].copy())
+        part.set_ended(True)
+        ids_of[r] = (my_id, gen_parent + 1, int(b.pid[r]))
+        out[k].append(part)
+    return out

@@ -34,8 +34,8 @@ DIMENSIONS = {"PairProd": 4, "Comp": 1, "Brem": 4, "MuonBrem": 4, "Ann": 1,
 
 # physical_constants.py:11-38
 ALPHA_EM = 1 / 137.035999
-M_ELECTRON = 510.998950e-6
-M_MUON = 105.6583755e-3
+M_ELECTRON = 510.998950 * 1e-6           # 510.998950*keV
+M_MUON = 105.6583755 * 1e-3             # 105.6583755*MeV
 M_PROTON_GRAMS = 1.67262192369e-24
 HBARC = 0.1973269804e-13
 GEVSQCM2 = HBARC ** 2
@@ -234,6 +234,7 @@ class SMTables:
         ti = TARGET_INFORMATION[target_material]
         self.target = target_material
         self.Z, self.A, self.rho, self.dEdx = float(ti["Z_T"]), float(ti["A_T"]), float(ti["rho"]), float(ti["dEdx"])
+        self.Z_int = ti["Z_T"]
         self.n_target = self.rho / M_PROTON_GRAMS / self.A                # shower.py:202-208
         self.n_elec = self.n_target * self.Z
         xs = {p: raw.xsec[p][target_material] for p in PROCESSES}
