@@ -55,7 +55,8 @@ typedef struct pt_tables {
   const int64_t* grid_offset;     /* [n_rows*4] first node of dimension d of row r */
   const int32_t* grid_ninc;       /* [n_rows*4] increments (nodes - 1) */
   const double* grid_nodes;       /* [n_nodes] all grid nodes, float64 */
-  const float* grid_nodes_f32;    /* [n_nodes] same nodes rounded to float32 (mixed form) */
+  const float* grid_f32x4;        /* [n_nodes][4] float32 (node, increment to next node, 1-node, 1+node),
+                                     each rounded once from float64 (mixed-precision form) */
   int64_t n_nodes;
   /* n*sigma(E) interpolation tables in 1/cm, slots: Brem, PairProd, Ann, Comp,
    * Moller, Bhabha, MuonE, MuonBrem (shower.py:280-295) */
@@ -63,6 +64,8 @@ typedef struct pt_tables {
   int32_t ns_len[PT_N_NSIGMA];
   const double* ns_x;
   const double* ns_y;
+  const float* ns_x32;            /* float32 copies (mixed-precision form) */
+  const float* ns_y32;
   /* target and thresholds */
   double Z, A, rho;               /* physical_constants.py:49-55 */
   double dEdx_GeV_per_m;          /* 0.1 * dEdx[MeV/cm] (shower.py:649) */
@@ -125,6 +128,35 @@ typedef struct pt_opts {
  * restores list order).  Returns PT_OOM if capacity is too small. */
 pt_status pt_run_sm(pt_handle* h, pt_particles* out, int64_t n_primaries,
                     const pt_opts* opts, int64_t* n_rows, void* stream);
+
+/* Tallies of a batched run (all device pointers; accumulated, never cleared
+ * by the library).  Histograms: [kind][species][PT_HIST_BINS] with kinds
+ * 0 = log10(E0/GeV) at creation in [-2, 2], 1 = log10(polar angle of p0 / rad)
+ * in [-6, 0.5], 2 = depth z of the interaction point in [0, z_max] m;
+ * species 0 = photon, 1 = electron, 2 = positron, 3 = muon. */
+enum { PT_HIST_BINS = 100, PT_N_COUNTS = 16, PT_N_ESUM = 8 };
+enum { PT_C_STEPS = 0, PT_C_PROPOSALS = 1, PT_C_SUBSTEPS = 2, PT_C_ENDED = 3, PT_C_PUSHED = 4,
+       PT_C_BELOW_CUT = 5, PT_C_WAVES = 6, PT_C_SAMPLED = 7, PT_C_SPECIES = 8 /* ..11 */ };
+enum { PT_E_CONTINUOUS = 0, PT_E_BELOW_CUT = 1, PT_E_ENDED = 2, PT_E_PRIMARY = 3 };
+typedef struct pt_tally {
+  unsigned long long* counts;   /* [PT_N_COUNTS] */
+  double* energy;               /* [PT_N_ESUM] GeV: continuous dE/dx loss, daughters below the cut,
+                                   particles that end without an interaction, primaries */
+  unsigned int* hist;           /* [3][4][PT_HIST_BINS] */
+  unsigned int* primary_count;  /* [n_primaries] particles per shower (rows of its list) */
+  double* primary_edep;         /* [n_primaries] deposited energy per shower */
+  double z_max;                 /* depth histogram range (m) */
+} pt_tally;
+
+/* Shower.generate_shower (shower.py:603-708) for many primaries without
+ * materialising the particle list: every particle-step is tallied instead.
+ * Primaries: p0 [4][n] and r0 [3][n] component-major, pid/mass [n].  Uses
+ * the same per-particle random streams as pt_run_sm, so opts->precision = 0
+ * reproduces pt_run_sm's showers exactly.  queue_capacity bounds the live
+ * particles per wave (0 = library default); primaries are fed in chunks. */
+pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const int32_t* pid, const double* mass,
+                       int64_t n_primaries, const pt_opts* opts, pt_tally* tally, int64_t queue_capacity,
+                       void* stream);
 
 /* Counters of the last pt_run_sm on this handle: kernel launches and waves
  * (transport iterations).  Diagnostic; no reference counterpart. */

@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE
 PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats", "pt_run_sm",
-           "pt_sample_only", "pt_dsigma")
+           "pt_run_batch", "pt_sample_only", "pt_dsigma")
 
 
 class PtTables(C.Structure):
@@ -26,8 +26,9 @@ class PtTables(C.Structure):
         ("map_base", C.c_int32 * N_PROC), ("map_rows", C.c_int32 * N_PROC), ("n_rows", C.c_int32),
         ("map_energy", C.c_void_p), ("map_maxF", C.c_void_p), ("map_neval", C.c_void_p),
         ("grid_offset", C.c_void_p), ("grid_ninc", C.c_void_p), ("grid_nodes", C.c_void_p),
-        ("grid_nodes_f32", C.c_void_p), ("n_nodes", C.c_int64),
+        ("grid_f32x4", C.c_void_p), ("n_nodes", C.c_int64),
         ("ns_base", C.c_int32 * N_NS), ("ns_len", C.c_int32 * N_NS), ("ns_x", C.c_void_p), ("ns_y", C.c_void_p),
+        ("ns_x32", C.c_void_p), ("ns_y32", C.c_void_p),
         ("Z", C.c_double), ("A", C.c_double), ("rho", C.c_double), ("dEdx_GeV_per_m", C.c_double),
         ("Eg_min", C.c_double), ("Ee_min", C.c_double),
         ("min_calc_electron", C.c_double), ("min_calc_positron", C.c_double),
@@ -39,6 +40,16 @@ class PtTables(C.Structure):
 class PtParticles(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("p0", "r0", "pf", "rf", "weight", "mass", "pid", "gen", "proc",
                                           "bit", "primary", "draws", "parent", "pkey")] + [("capacity", C.c_int64)]
+
+
+HIST_BINS = 100
+N_COUNTS = 16
+N_ESUM = 8
+
+
+class PtTally(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("energy", C.c_void_p), ("hist", C.c_void_p),
+                ("primary_count", C.c_void_p), ("primary_edep", C.c_void_p), ("z_max", C.c_double)]
 
 
 class PtOpts(C.Structure):
@@ -84,6 +95,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_last_run_stats.restype = C.c_int
     lib.pt_run_sm.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
     lib.pt_run_sm.restype = C.c_int
+    lib.pt_run_batch.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp]
+    lib.pt_run_batch.restype = C.c_int
     lib.pt_sample_only.argtypes = [vp, i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp, vp]
     lib.pt_sample_only.restype = C.c_int
     lib.pt_dsigma.argtypes = [vp, i32, vp, vp, i64, i32, vp, vp]

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <new>
 
+#include "pt_internal.cuh"
 #include "pt_physics.cuh"
 
 using namespace pt;
@@ -278,8 +279,19 @@ struct pt_handle {
   unsigned long long* h_counters = nullptr; // pinned
   int* h_status = nullptr;
   double last_info[3] = {0, 0, 0};
-  int64_t last_launches = 0, last_waves = 0;
+  int64_t launches[2] = {0, 0};   // kernel launches, waves of the last run
+  BatchScratch* batch = nullptr;
 };
+
+pt_status batch_scratch_get(pt_handle* h, BatchScratch** out, int64_t ring_capacity) {
+  pt_status s = batch_scratch_alloc(&h->batch, ring_capacity);
+  *out = h->batch;
+  return s;
+}
+
+HandleParts handle_parts(pt_handle* h) {
+  return HandleParts{&h->T, h->status, h->err_info, h->last_info, h->launches};
+}
 
 static const char* kMessages[] = {
     "ok", "No Sample Found", "device loop limit reached", "inconsistent tables",
@@ -328,6 +340,7 @@ extern "C" pt_status pt_create(const pt_tables* t, pt_handle** out) {
 
 extern "C" void pt_destroy(pt_handle* h) {
   if (!h) return;
+  batch_scratch_free(h->batch);
   cudaFree(h->live[0]);
   cudaFree(h->live[1]);
   cudaFree(h->counters);
@@ -399,11 +412,11 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
   int cur = 0;
   int64_t n_in = n_primaries;
   const int tbt = 128;
-  h->last_launches = 2;
-  h->last_waves = 0;
+  h->launches[0] = 2;
+  h->launches[1] = 0;
   while (n_in > 0) {
-    ++h->last_launches;
-    ++h->last_waves;
+    ++h->launches[0];
+    ++h->launches[1];
     PT_CUDA(cudaMemsetAsync(h->counters + 0, 0, sizeof(unsigned long long), st));
     c.live_in = h->live[cur];
     c.n_in = n_in;
@@ -426,8 +439,8 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
 
 extern "C" pt_status pt_last_run_stats(pt_handle* h, int64_t* launches, int64_t* waves) {
   if (!h) return PT_BAD_ARG;
-  if (launches) *launches = h->last_launches;
-  if (waves) *waves = h->last_waves;
+  if (launches) *launches = h->launches[0];
+  if (waves) *waves = h->launches[1];
   return PT_OK;
 }
 

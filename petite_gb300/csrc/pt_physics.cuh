@@ -102,7 +102,7 @@ __device__ __forceinline__ double map_dim(const double* g, int ninc, double y, d
 
 // ------------------------------------------------- differential cross sections
 // dsigma_brem_dimensionless.__call__ (all_processes.py:153-206); also MuonBrem.
-__device__ double dsig_brem(const Tabs& T, const double* x, double ep, double m) {
+static __device__ double dsig_brem(const Tabs& T, const double* x, double ep, double m) {
   const double Eg = T.t.Eg_min;
   const double w = Eg + x[0] * (ep - m - Eg);
   const double k = ep / (2 * m);
@@ -129,7 +129,7 @@ __device__ double dsig_brem(const Tabs& T, const double* x, double ep, double m)
 }
 
 // dsigma_pairprod_dimensionless.__call__ (all_processes.py:546-622)
-__device__ double dsig_pairprod(const Tabs& T, const double* x, double w) {
+static __device__ double dsig_pairprod(const Tabs& T, const double* x, double w) {
   const double me = kMe;
   const double epp = me + x[0] * (w - 2 * me);
   const double k = w / (2 * me);
@@ -156,7 +156,7 @@ __device__ double dsig_pairprod(const Tabs& T, const double* x, double w) {
 }
 
 // dsigma_compton_dCT.__call__ (all_processes.py:639-742), mV = 0
-__device__ double dsig_compton(double ct, double Eg) {
+static __device__ double dsig_compton(double ct, double Eg) {
   const double me = kMe, me2 = me * me, me4 = me2 * me2;
   const double s = me2 + 2 * Eg * me;
   if (s < me2) return 0.0;
@@ -172,7 +172,7 @@ __device__ double dsig_compton(double ct, double Eg) {
 }
 
 // dsigma_annihilation_dCT.__call__ (all_processes.py:475-529), mV = 0
-__device__ double dsig_annihilation(const Tabs& T, double ct, double Ee) {
+static __device__ double dsig_annihilation(const Tabs& T, double ct, double Ee) {
   const double me = kMe;
   const double s = 2.0 * me * (Ee + me);
   const double ctMax = sqrt((Ee + me) / (Ee - me)) * (2 * me * (Ee - 2 * T.t.Eg_min + me)) / (2 * me * (Ee + me));
@@ -182,7 +182,7 @@ __device__ double dsig_annihilation(const Tabs& T, double ct, double Ee) {
 }
 
 // dsigma_moller_dCT.__call__ (all_processes.py:799-840)
-__device__ double dsig_moller(const Tabs& T, double ct, double Ee) {
+static __device__ double dsig_moller(const Tabs& T, double ct, double Ee) {
   const double me = kMe;
   const double lim = 2.0 * T.t.Ee_min / (Ee - me);
   if (!((ct > -1 + lim) && (ct < 1.0 - lim))) return 0.0;
@@ -194,7 +194,7 @@ __device__ double dsig_moller(const Tabs& T, double ct, double Ee) {
 }
 
 // dsigma_bhabha_dCT.__call__ (all_processes.py:960-1007)
-__device__ double dsig_bhabha(const Tabs& T, double ct, double Ee) {
+static __device__ double dsig_bhabha(const Tabs& T, double ct, double Ee) {
   const double me = kMe;
   const double lim = 2.0 * T.t.Ee_min / (Ee - me);
   if (!((ct > -1 + lim) && (ct < 1.0 - lim))) return 0.0;
@@ -211,7 +211,7 @@ __device__ double dsig_bhabha(const Tabs& T, double ct, double Ee) {
 }
 
 // dsigma_muonelectron_dCT.__call__ (all_processes.py:855-886)
-__device__ double dsig_muone(const Tabs& T, double ct, double Emu) {
+static __device__ double dsig_muone(const Tabs& T, double ct, double Emu) {
   const double me = kMe, mm = kMmu, me2 = me * me, mm2 = mm * mm;
   const double s = me2 + mm2 + 2 * me * Emu;
   const double t_limit = 2.0 * me * (me - T.t.Ee_min);
@@ -242,7 +242,7 @@ __device__ __forceinline__ double dsigma_any(const Tabs& T, int process, const d
 struct V4 { double e, x, y, z; };
 
 // e_to_egamma_fourvecs, kinematics.py:10-41 (Egamma_min = 0.001, :9)
-__device__ void kin_brem(double ep_, double m_, const double* xs, double al_, V4& lep, V4& gam) {
+static __device__ void kin_brem(double ep_, double m_, const double* xs, double al_, V4& lep, V4& gam) {
   const S ep(ep_), m(m_), Egmin(0.001), x1(xs[0]), x2(xs[1]), x3(xs[2]), x4(xs[3]), al(al_);
   const S w = Egmin + x1 * (ep - m - Egmin);
   const S ct = S(cos(((x2 + x3) / S(2.0)).v));
@@ -260,7 +260,7 @@ __device__ void kin_brem(double ep_, double m_, const double* xs, double al_, V4
 }
 
 // gamma_to_epem_fourvecs, kinematics.py:70-102 -> (positron, electron)
-__device__ void kin_pairprod(double w_, const double* xs, double al_, V4& pos, V4& ele) {
+static __device__ void kin_pairprod(double w_, const double* xs, double al_, V4& pos, V4& ele) {
   const S w(w_), me(kMe), x1(xs[0]), x2(xs[1]), x3(xs[2]), x4(xs[3]), al(al_);
   const S epp = me + x1 * (w - S(2.0) * me);
   const S ctp = S(cos((w * (x2 + x3) / (S(2.0) * epp)).v));
@@ -280,7 +280,7 @@ __device__ void kin_pairprod(double w_, const double* xs, double al_, V4& pos, V
 // the signs of kinematics.py:129-130 (compton), 234-235 (ee), 262-263 (mue),
 // 331-332 (annihilation).
 // compton_fourvecs, kinematics.py:104-132, mV = 0 -> (electron, photon)
-__device__ void kin_compton(double Eg_, double ct_, double ph_, V4& e, V4& g) {
+static __device__ void kin_compton(double Eg_, double ct_, double ph_, V4& e, V4& g) {
   const S Eg(Eg_), ct(ct_), ph(ph_), me(kMe);
   const S s = sq(me) + S(2.0) * Eg * me;
   const S rs = ssqrt(s);
@@ -297,7 +297,7 @@ __device__ void kin_compton(double Eg_, double ct_, double ph_, V4& e, V4& g) {
 }
 
 // ee_to_ee_fourvecs, kinematics.py:213-237 -> (scattered lepton, new electron)
-__device__ void kin_ee(double Einc_, double ct_, double ph_, V4& a, V4& b) {
+static __device__ void kin_ee(double Einc_, double ct_, double ph_, V4& a, V4& b) {
   const S E(Einc_), ct(ct_), ph(ph_), me(kMe);
   const S s = S(2.0) * sq(me) + S(2.0) * E * me;
   const S Ee0 = ssqrt(s) / S(2.0);
@@ -311,7 +311,7 @@ __device__ void kin_ee(double Einc_, double ct_, double ph_, V4& a, V4& b) {
 }
 
 // mue_to_mue_fourvecs, kinematics.py:239-265 -> (muon, electron)
-__device__ void kin_mue(double Einc_, double ct_, double ph_, V4& mu, V4& el) {
+static __device__ void kin_mue(double Einc_, double ct_, double ph_, V4& mu, V4& el) {
   const S E(Einc_), ct(ct_), ph(ph_), me(kMe), mm(kMmu);
   const S s = sq(me) + sq(mm) + S(2.0) * E * me;
   const S rs = ssqrt(s);
@@ -328,7 +328,7 @@ __device__ void kin_mue(double Einc_, double ct_, double ph_, V4& mu, V4& el) {
 }
 
 // annihilation_fourvecs, kinematics.py:301-334, mV = 0 -> (photon, photon)
-__device__ void kin_ann(double Ee_, double ct_, double ph_, V4& a, V4& b) {
+static __device__ void kin_ann(double Ee_, double ct_, double ph_, V4& a, V4& b) {
   const S E(Ee_), ct(ct_), ph(ph_), me(kMe);
   const S s = S(2.0) * me * (E + me);
   const S rs = ssqrt(s);
@@ -373,7 +373,7 @@ __device__ __forceinline__ V4 to_lab(const Rot& R, const V4& v) {
 // get_scattered_momentum_fast (moliere.py:350-400) with the Lynch-Dahl width
 // of moliere.py:196-219,265-284.  Draw order: sign, Gaussian pair (angle,
 // radius; the pair shares one Box-Muller evaluation), phi.
-__device__ void mcs_fast(double* p4, double t_, double A_, double Z_, double Z23, double rescale, double m_lep,
+static __device__ void mcs_fast(double* p4, double t_, double A_, double Z_, double Z23, double rescale, double m_lep,
                          Rng& rng) {
   const double pn = norm3_np(p4[1], p4[2], p4[3]);
   if (!(pn > 0)) return;

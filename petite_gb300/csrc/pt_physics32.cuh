@@ -1,0 +1,263 @@
+// pt_physics32.cuh -- float32 forms used by the mixed-precision engine.
+//
+// Same physics as pt_physics.cuh (PETITE's all_processes.py / moliere.py /
+// kinematics.py), rearranged so float32 keeps its accuracy:
+//  * every sampled variable comes with its complements (1-x, 1+x) read from
+//    a node table built in float64, so 1-cos(theta) never cancels;
+//  * the Brem and pair-production angular factors T1+T2+T3+T4 are rewritten
+//    as sums of non-negative terms (they cancel near the peak otherwise):
+//      Brem:  T*D = ((a-b)(1-ab))^2/D + 4ab s2 + W((a-b)^2/2 + 2ab s2),
+//             a=delta, b=delta', s2=sin^2(phi/2), D=(1+a^2)(1+b^2), W=w^2/(E E')
+//      pair:  T*D = (a-b)^2 (1 + (a+b)^2/D + K) + 4ab c2 (1+K),
+//             a=delta+, b=delta-, c2=cos^2(phi/2), K=(E+ - E-)^2/(2 E+ E-)
+//  * the form factor and prefactors are grouped so no intermediate leaves
+//    the float32 range, and the result is the acceptance ratio
+//    wgt*f/max_F directly.
+// Energies, positions and the final daughter four-momenta stay float64.
+#pragma once
+#include "pt_physics.cuh"
+
+namespace pt {
+
+// One map node in float32: value, increment to the next node, 1-value, 1+value.
+struct Node32 { float g, inc, cm, cp; };
+
+struct MapPt32 { float x, omx, opx; };   // x, 1-x, 1+x
+
+__device__ __forceinline__ MapPt32 map_dim32(const float4* nodes, int ninc, float y, float& jac) {
+  const float t = y * (float)ninc;
+  int i = (int)t;
+  if (i > ninc - 1) i = ninc - 1;
+  const float f = t - (float)i;
+  const float4 n = __ldg(nodes + i);     // (g, inc, 1-g, 1+g)
+  jac *= (float)ninc * n.y;
+  MapPt32 r;
+  r.x = fmaf(n.y, f, n.x);
+  r.omx = fmaf(-n.y, f, n.z);
+  r.opx = fmaf(n.y, f, n.w);
+  return r;
+}
+
+// Per-task constants of the float32 sampler (computed once per particle).
+struct Samp32 {
+  float E, m, k, span, Eg, C;      // C folds prefactors and 1/(max_F*neval)
+  float b;                         // form-factor scale (a0*m)^2
+  float aux0, aux1, aux2;          // process-specific
+};
+
+// ---- Brem / MuonBrem: dsigma_brem_dimensionless (all_processes.py:153-206)
+__device__ __forceinline__ void brem32_setup(Samp32& S, double E, double m, double Eg, double a0sq_me2_ratio,
+                                             double Z2, double inv_norm) {
+  // b = (a0 m)^2 with a0 = aa(Z, m_e); a0sq_me2_ratio = a0^2 (float64 on host)
+  const double b = a0sq_me2_ratio * m * m;
+  const double m2 = m * m;
+  const double C1 = 8.0 * kAlpha * kAlpha * kAlpha * Z2 * (b / m2) * (b / m2);   // 8 a^3 Z^2 b^2 / m^4
+  S.E = (float)E; S.m = (float)m; S.k = (float)(E / (2 * m)); S.span = (float)(E - m - Eg); S.Eg = (float)Eg;
+  S.b = (float)b;
+  S.C = (float)(C1 * inv_norm);
+  S.aux0 = (float)(E * (E - m - Eg));     // E * span (float64 product)
+}
+__device__ __forceinline__ float brem32_ratio(const Samp32& S, const MapPt32* x, float jac) {
+  const float w = fmaf(x[0].x, S.span, S.Eg);
+  const float epp = fmaf(S.span, x[0].omx, S.m);
+  const float d = S.k * (x[1].x + x[2].x);
+  const float dp = S.k * (x[1].x - x[2].x);
+  if (!((S.Eg < w) && (w < S.E - S.m) && (S.m < epp) && (epp < S.E) && (d > 0.f) && (dp > 0.f))) return 0.f;
+  const float sp = sinpif(x[3].x - 0.5f);      // sin(phi/2), phi = (x4-1/2)*2pi
+  const float s2 = sp * sp;
+  const float amb = 2.f * S.k * x[2].x;        // d - dp
+  const float ab = d * dp;
+  const float d2 = d * d;
+  const float Anum = 4.f * S.k * S.k * x[1].x * x[2].x * S.E - (1.f + d2) * w;
+  const float mA = S.m * Anum / (2.f * S.E * epp);
+  const float qh = amb * amb + 4.f * ab * s2 + mA * mA;     // qsq / m^2
+  const float D = (1.f + d2) * (1.f + dp * dp);
+  const float iD = 1.f / D;
+  const float t1 = amb * (1.f - ab) * iD;
+  const float W = (w / S.E) * (w / epp);
+  const float T = t1 * t1 + 4.f * ab * s2 * iD + W * (0.5f * amb * amb + 2.f * ab * s2) * iD;
+  const float u = 1.f / fmaf(S.b, qh, 1.f);
+  const float Q = S.aux0 * (epp / w);          // E' E (E - m - Eg) / w
+  return ((S.C * jac) * Q) * ((ab * T) * (u * u));
+}
+
+// ---- PairProd: dsigma_pairprod_dimensionless (all_processes.py:546-622)
+__device__ __forceinline__ void pair32_setup(Samp32& S, double w, double a0sq, double Z2, double inv_norm) {
+  const double me = kMe, b = a0sq * me * me, m2 = me * me;
+  const double C1 = 8.0 * kAlpha * kAlpha * kAlpha * Z2 * (b / m2) * (b / m2);
+  S.E = (float)w; S.m = (float)me; S.k = (float)(w / (2 * me)); S.span = (float)(w - 2 * me);
+  S.b = (float)b;
+  S.C = (float)(C1 * inv_norm);
+  S.aux0 = (float)((w - 2 * me) / w);
+}
+__device__ __forceinline__ float pair32_ratio(const Samp32& S, const MapPt32* x, float jac) {
+  const float epp = fmaf(x[0].x, S.span, S.m);
+  const float epm = fmaf(x[0].omx, S.span, S.m);
+  const float dp = S.k * (x[1].x + x[2].x);
+  const float dm = S.k * (x[1].x - x[2].x);
+  if (!((S.m < epm) && (epm < S.E) && (S.m < epp) && (epp < S.E) && (dm > 0.f) && (dp > 0.f))) return 0.f;
+  const float cp = cospif(x[3].x);             // cos(phi/2), phi = 2 pi x4
+  const float c2 = cp * cp;
+  const float dd = 2.f * S.k * x[2].x;         // dp - dm
+  const float ab = dp * dm;
+  const float B = (1.f + dp * dp) / (2.f * epp) + (1.f + dm * dm) / (2.f * epm);
+  const float q = dd * dd + 4.f * ab * c2 + (S.m * B) * (S.m * B);
+  const float D = (1.f + dp * dp) * (1.f + dm * dm);
+  const float iD = 1.f / D;
+  const float dE = S.span * (x[0].x - x[0].omx);          // E+ - E-
+  const float K = 0.5f * (dE / epp) * (dE / epm);
+  const float spm = dp + dm;
+  const float T = (dd * dd * (1.f + spm * spm * iD + K) + 4.f * ab * c2 * (1.f + K)) * iD;
+  const float u = 1.f / fmaf(S.b, q, 1.f);
+  const float Q = (epp * epm) * S.aux0;        // E+ E- (w - 2 me) / w
+  return ((S.C * jac) * Q) * ((ab * T) * (u * u));
+}
+
+// ---- Compton (mV = 0): dsigma_compton_dCT (all_processes.py:639-742),
+// with s - m^2 = D = 2 E m, t = -D^2 (1+c)/(2s), s + t - m^2 = D (2m^2 + D(1-c))/(2s).
+__device__ __forceinline__ void comp32_setup(Samp32& S, double Eg, double inv_norm) {
+  const double me2 = kMe * kMe, D = 2 * Eg * kMe, s = me2 + D;
+  S.E = (float)D; S.m = (float)me2; S.span = (float)s;
+  S.C = (float)(kPi * kAlpha * kAlpha / s * inv_norm);   // PF * jac = pi a^2 / s
+}
+__device__ __forceinline__ float comp32_ratio(const Samp32& S, const MapPt32& c, float jac) {
+  const float D = S.E, m2 = S.m, s = S.span;
+  const float t = -D * D * c.opx / (2.f * s);
+  const float u = D * fmaf(D, c.omx, 2.f * m2) / (2.f * s);
+  const float T1 = (6.f * m2 * s + 3.f * m2 * m2 - s * s) / (-D * u);
+  const float T2 = 4.f * m2 * m2 / (u * u);
+  const float sp = s + m2;
+  const float T3 = (t * D + sp * sp) / (D * D);
+  return (S.C * jac) * (T1 + T2 + T3);
+}
+
+// ---- Annihilation (mV = 0): dsigma_annihilation_dCT (all_processes.py:475-529)
+__device__ __forceinline__ void ann32_setup(Samp32& S, double Ee, double Eg_min, double inv_norm) {
+  const double me = kMe, s = 2.0 * me * (Ee + me);
+  const double ctMax = sqrt((Ee + me) / (Ee - me)) * (2 * me * (Ee - 2 * Eg_min + me)) / (2 * me * (Ee + me));
+  S.E = (float)s;
+  S.aux0 = (float)(4.0 * me * me / s);                 // 1 - b^2
+  S.aux1 = (float)(1.0 - ctMax);                       // ct > ctMax <=> 1-ct < 1-ctMax
+  S.C = (float)(4.0 * kPi * kAlpha * kAlpha / s * 0.5 * inv_norm);
+}
+__device__ __forceinline__ float ann32_ratio(const Samp32& S, const MapPt32& c, float jac) {
+  if (c.omx < S.aux1) return 0.f;
+  const float den = fmaf(S.aux0 * c.x, c.x, c.omx * c.opx);   // 1 - b^2 c^2
+  return (S.C * jac) * fmaf(c.x, c.x, 1.f) / den;
+}
+
+// ---- Moller: dsigma_moller_dCT (all_processes.py:799-840)
+__device__ __forceinline__ void moller32_setup(Samp32& S, double Ee, double Ee_min, double inv_norm) {
+  const double me = kMe, s = me * me + 2 * Ee * me, v = s - 4 * me * me;
+  S.E = (float)s; S.m = (float)(me * me);
+  S.aux0 = (float)(2.0 * Ee_min / (Ee - me));          // delta_ct_limit
+  S.C = (float)(16 * kPi * kPi * kAlpha * kAlpha / (8 * kPi * s * v * v) * inv_norm);
+}
+__device__ __forceinline__ float moller32_ratio(const Samp32& S, const MapPt32& c, float jac) {
+  if (!(c.opx > S.aux0 && c.omx > S.aux0)) return 0.f;
+  const float s = S.E, m2 = S.m, c2 = c.x * c.x, a = 3.f + c2;
+  const float num = s * s * a * a - 8.f * m2 * s * (7.f + c2 * c2) + 16.f * m2 * m2 * (6.f - 3.f * c2 + c2 * c2);
+  const float den = (c.omx * c.opx) * (c.omx * c.opx);
+  return (S.C * jac) * (num / den);
+}
+
+// ---- Bhabha: dsigma_bhabha_dCT (all_processes.py:960-1007)
+__device__ __forceinline__ void bhabha32_setup(Samp32& S, double Ee, double Ee_min, double inv_norm) {
+  const double me = kMe, s = me * me + 2 * Ee * me, v = s - 4 * me * me;
+  S.E = (float)s; S.m = (float)(me * me);
+  S.aux0 = (float)(2.0 * Ee_min / (Ee - me));
+  S.C = (float)(kAlpha * kAlpha * kPi / (2.0 * s * s * s * v * v) * inv_norm);
+}
+__device__ __forceinline__ float bhabha32_ratio(const Samp32& S, const MapPt32& c, float jac) {
+  if (!(c.opx > S.aux0 && c.omx > S.aux0)) return 0.f;
+  const float s = S.E, m2 = S.m, ct = c.x, cm1 = -c.omx;
+  const float m4 = m2 * m2, m6 = m4 * m2, m8 = m4 * m4, a = 3.f + ct * ct;
+  const float num = 256.f * (cm1 * cm1) * (ct * ct) * m8
+                  - 128.f * cm1 * (1.f + ct * (1.f + ct) * (-3.f + 2.f * ct)) * m6 * s
+                  + 16.f * (7.f + ct * (2.f + ct * (-5.f + 6.f * cm1 * ct))) * m4 * (s * s)
+                  - 8.f * (7.f + ct * (-3.f + ct * (3.f + ct * (-1.f + 2.f * ct)))) * m2 * (s * s * s)
+                  + (a * a) * ((s * s) * (s * s));
+  return (S.C * jac) * (num / (cm1 * cm1));
+}
+
+// ---- mu e -> mu e: dsigma_muonelectron_dCT (all_processes.py:855-886),
+// with p_cm^2 = m_e^2 (E^2 - m_mu^2)/s so t = -2(1-c) p_cm^2 does not cancel.
+__device__ __forceinline__ void muone32_setup(Samp32& S, double Emu, double Ee_min, double inv_norm) {
+  const double me = kMe, mm = kMmu, s = me * me + mm * mm + 2 * me * Emu;
+  const double pcm2 = me * me * (Emu - mm) * (Emu + mm) / s;
+  S.E = (float)s; S.m = (float)(me * me); S.span = (float)pcm2;
+  S.aux0 = (float)(me * (Ee_min - me) / pcm2);         // t < t_limit <=> 1-c > this
+  S.aux1 = (float)(mm * mm);
+  S.C = (float)(16 * kPi * kPi * kAlpha * kAlpha / (16 * kPi * s) * inv_norm);
+}
+__device__ __forceinline__ float muone32_ratio(const Samp32& S, const MapPt32& c, float jac) {
+  if (!(c.omx > S.aux0)) return 0.f;
+  const float s = S.E, m2 = S.m, mm2 = S.aux1;
+  const float t = -2.f * c.omx * S.span;
+  const float v = s + t - 4.f * m2;
+  const float num = s * s + 2.f * (m2 + mm2) * (2.f * t + mm2 - 3.f * m2) + v * v;
+  return (S.C * jac) * (num / (t * t));
+}
+
+// -------------------------------------------- multiple scattering, float32
+// Lynch-Dahl width (moliere.py:196-219,265-284) with the momentum taken as
+// |p| directly (the reference's m*beta/sqrt(1-beta^2) is the same quantity),
+// same four draws as the float64 form, frame rotation of moliere.py:287-348
+// written algebraically (its branches reduce to ca = vx/rho, sa = -vy/rho,
+// cb = vz/r, sb = -rho/r).
+__device__ __forceinline__ float lynch_dahl_g(float v) {
+  // (1+v) ln(1+v)/v - 1 without cancellation at small v
+  if (v < 1e-2f) return v * (0.5f + v * (-1.f / 6.f + v * (1.f / 12.f - v * 0.05f)));
+  return (1.f + v) * log1pf(v) / v - 1.f;
+}
+
+__device__ __forceinline__ void mcs32(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
+                                      float rescale, Rng& rng) {
+  if (!(pmag > 0.f)) return;             // a particle at rest draws nothing (moliere.py:359-363)
+  const float u_sign = rng.uf(), u_ang = rng.uf(), u_rad = rng.uf(), u_phi = rng.uf();
+  (void)u_ang;   // the Gaussian pair's angle cancels in the space angle
+  const float beta = pmag / E;
+  const float p = pmag * 1000.f;                         // MeV
+  const float pb = p * beta;
+  const float chic2 = 0.157f * Z * (Z + 1.f) * (t / A) / (pb * pb);
+  const float zab = Z * (float)kAlpha / beta;
+  const float chia2 = 2.007e-5f * Z23 * (1.f + 3.34f * zab * zab) / (p * p);
+  const float v = 0.5f * (chic2 / chia2) / (1.f - 0.98f);
+  const float th0 = sqrtf(chic2 * lynch_dahl_g(v) / (1.f + 0.98f * 0.98f));
+  const float r = sqrtf(-2.f * __logf(1.f - u_rad));
+  float theta = th0 * r * rescale;
+  if (u_sign < 0.5f) theta = -theta;
+  float sth, cth, sph, cph;
+  sincosf(theta, &sth, &cth);
+  sincospif(2.f * u_phi, &sph, &cph);
+  const float n0 = sph * sth, n1 = -cph * sth, n2 = cth;
+  const float vx = dir.x, vy = dir.y, vz = dir.z;
+  const float rho = sqrtf(vx * vx + vy * vy);
+  float ca = 1.f, sa = 0.f, cb = 1.f, sb = 0.f;
+  if (rho > 0.f) { ca = vx / rho; sa = -vy / rho; }
+  const float rr = sqrtf(rho * rho + vz * vz);
+  if (rho > 0.f) { cb = vz / rr; sb = -rho / rr; }
+  // lab = Ra^T Rb^T n
+  const float w0 = cb * n0 - sb * n2, w1 = n1, w2 = sb * n0 + cb * n2;
+  float3 o = make_float3(ca * w0 + sa * w1, -sa * w0 + ca * w1, w2);
+  const float inv = rsqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+  dir = make_float3(o.x * inv, o.y * inv, o.z * inv);
+}
+
+// Lab frame from the parent's unit direction: Particle.rotation_matrix
+// (particle.py:176-185) with cos/sin of ThZ, PhiZ taken from the direction.
+struct Rot32 { float cT, sT, cP, sP; };
+__device__ __forceinline__ Rot32 rot32_from(float3 d) {
+  Rot32 R;
+  const float rho = sqrtf(d.x * d.x + d.y * d.y);
+  R.cT = d.z; R.sT = rho;
+  if (rho > 0.f) { R.cP = d.x / rho; R.sP = d.y / rho; } else { R.cP = 1.f; R.sP = 0.f; }
+  return R;
+}
+__device__ __forceinline__ float3 rot32_apply(const Rot32& R, float3 v) {
+  return make_float3(R.cT * R.cP * v.x - R.sP * v.y + R.sT * R.cP * v.z,
+                     R.cT * R.sP * v.x + R.cP * v.y + R.sT * R.sP * v.z,
+                     -R.sT * v.x + R.cT * v.z);
+}
+
+}  // namespace pt

@@ -78,6 +78,41 @@ class ParticleStore:
         return out
 
 
+class Tally:
+    """Device tallies of pt_run_batch (layout of ``pt_tally``)."""
+
+    COUNT_NAMES = {0: "steps", 1: "proposals", 2: "substeps", 3: "ended", 4: "pushed", 5: "below_cut",
+                   7: "sampled", 8: "photon_steps", 9: "electron_steps", 10: "positron_steps", 11: "muon_steps"}
+
+    def __init__(self, n_primaries: int, device, z_max: float = 1.0):
+        torch = _torch()
+        self.counts = torch.zeros(_lib.N_COUNTS, dtype=torch.int64, device=device)
+        self.energy = torch.zeros(_lib.N_ESUM, dtype=torch.float64, device=device)
+        self.hist = torch.zeros((3, 4, _lib.HIST_BINS), dtype=torch.int32, device=device)
+        self.primary_count = torch.zeros(max(n_primaries, 1), dtype=torch.int32, device=device)
+        self.primary_edep = torch.zeros(max(n_primaries, 1), dtype=torch.float64, device=device)
+        self.z_max = float(z_max)
+
+    def abi(self) -> _lib.PtTally:
+        t = _lib.PtTally()
+        t.counts = self.counts.data_ptr()
+        t.energy = self.energy.data_ptr()
+        t.hist = self.hist.data_ptr()
+        t.primary_count = self.primary_count.data_ptr()
+        t.primary_edep = self.primary_edep.data_ptr()
+        t.z_max = self.z_max
+        self._abi = t
+        return t
+
+    def summary(self) -> dict:
+        c = self.counts.cpu().numpy()
+        e = self.energy.cpu().numpy()
+        out = {name: int(c[k]) for k, name in self.COUNT_NAMES.items()}
+        out.update(E_continuous=float(e[0]), E_below_cut=float(e[1]), E_ended=float(e[2]), E_primaries=float(e[3]))
+        out["E_deposited"] = float(e[0] + e[1] + e[2])
+        return out
+
+
 class SMEngine:
     """Uploads one target's tables and exposes the C-ABI entry points."""
 
@@ -97,18 +132,20 @@ class SMEngine:
             "grid_offset": torch.as_tensor(np.ascontiguousarray(tables.grid_offset.reshape(-1), np.int64), device=dev),
             "grid_ninc": torch.as_tensor(np.ascontiguousarray(tables.grid_ninc.reshape(-1), np.int32), device=dev),
             "grid_nodes": f64(tables.grid_nodes),
-            "grid_nodes_f32": torch.as_tensor(tables.grid_nodes.astype(np.float32), device=dev),
+            "grid_f32x4": torch.as_tensor(tables.grid_f32x4(), device=dev),
         }
         ns_x = np.concatenate([x for x, _ in tables.nsigma])
         ns_y = np.concatenate([y for _, y in tables.nsigma])
         self._keep["ns_x"] = f64(ns_x)
         self._keep["ns_y"] = f64(ns_y)
+        self._keep["ns_x32"] = torch.as_tensor(ns_x.astype(np.float32), device=dev)
+        self._keep["ns_y32"] = torch.as_tensor(ns_y.astype(np.float32), device=dev)
         pt = _lib.PtTables()
         for p in range(_lib.N_PROC):
             pt.map_base[p] = int(tables.map_base[p])
             pt.map_rows[p] = int(tables.map_rows[p])
         pt.n_rows = int(len(tables.map_energy))
-        for k in ("map_energy", "map_maxF", "map_neval", "grid_offset", "grid_ninc", "grid_nodes", "grid_nodes_f32"):
+        for k in ("map_energy", "map_maxF", "map_neval", "grid_offset", "grid_ninc", "grid_nodes", "grid_f32x4"):
             setattr(pt, k, self._keep[k].data_ptr())
         pt.n_nodes = int(len(tables.grid_nodes))
         base = 0
@@ -118,6 +155,8 @@ class SMEngine:
             base += len(x)
         pt.ns_x = self._keep["ns_x"].data_ptr()
         pt.ns_y = self._keep["ns_y"].data_ptr()
+        pt.ns_x32 = self._keep["ns_x32"].data_ptr()
+        pt.ns_y32 = self._keep["ns_y32"].data_ptr()
         pt.Z, pt.A, pt.rho = tables.Z, tables.A, tables.rho
         pt.dEdx_GeV_per_m = tables.dEdx * 0.1
         pt.Eg_min, pt.Ee_min = tables.Eg_min, tables.Ee_min
@@ -200,6 +239,32 @@ class SMEngine:
         l, w = C.c_int64(), C.c_int64()
         _lib.check(self.lib.pt_last_run_stats(self.handle, C.byref(l), C.byref(w)), "pt_last_run_stats")
         return int(l.value), int(w.value)
+
+    def new_tally(self, n_primaries: int, z_max: float = 1.0) -> "Tally":
+        return Tally(n_primaries, self.device, z_max)
+
+    def run_batch(self, p0, r0, pid, mass, opts: _lib.PtOpts, tally: "Tally", queue_capacity: int = 0,
+                  device_inputs=None):
+        """Transports primaries without storing particle lists; accumulates into `tally`.
+
+        p0 (n,4), r0 (n,3), pid (n,), mass (n,) host arrays, or device tensors in
+        `device_inputs` = (p0 [4,n], r0 [3,n], pid [n], mass [n]) already resident."""
+        torch = _torch()
+        if device_inputs is None:
+            p0 = np.asarray(p0, np.float64).reshape(-1, 4)
+            n = len(p0)
+            dev = self.device
+            P0 = torch.as_tensor(np.ascontiguousarray(p0.T), device=dev)
+            R0 = torch.as_tensor(np.ascontiguousarray(np.asarray(r0, np.float64).reshape(n, 3).T), device=dev)
+            PID = torch.as_tensor(np.asarray(pid, np.int32), device=dev)
+            M = torch.as_tensor(np.asarray(mass, np.float64), device=dev)
+        else:
+            P0, R0, PID, M = device_inputs
+            n = P0.shape[1]
+        s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
+                                  C.byref(tally.abi()), int(queue_capacity), self._stream())
+        self._raise(s, "pt_run_batch")
+        return tally
 
     def sample_only(self, process: int, energy, pkey, opts: _lib.PtOpts):
         torch = _torch()

@@ -309,3 +309,18 @@ class SMTables:
         self.grid_nodes = np.concatenate(nodes)
         self.map_rows = np.array(self.map_rows, np.int32)
         self.map_base = np.array(self.map_base, np.int32)
+        self._node_is_last = np.zeros(len(self.grid_nodes), bool)
+        for o4, n4 in zip(offs, nincs):
+            for o, n in zip(o4, n4):
+                if n:
+                    self._node_is_last[o + n] = True
+
+    def grid_f32x4(self) -> np.ndarray:
+        """Float32 node table for the mixed-precision sampler: per node
+        (value, increment to the next node, 1 - value, 1 + value), each
+        computed in float64 and rounded once."""
+        g = self.grid_nodes
+        inc = np.zeros_like(g)
+        inc[:-1] = g[1:] - g[:-1]
+        inc[self._node_is_last] = 0.0
+        return np.ascontiguousarray(np.stack([g, inc, 1.0 - g, 1.0 + g], axis=1).astype(np.float32))

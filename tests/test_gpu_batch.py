@@ -1,0 +1,88 @@
+"""Batched (tally) engine: float64 form vs the record engine, ring-capacity
+independence, and the mixed-precision form vs float64."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 1
+
+
+def primaries(n, seed=7, emin=0.1, emax=10.0, species=(11, -11, 22)):
+    rng = np.random.default_rng(seed)
+    pid = np.asarray(species)[rng.integers(0, len(species), n)]
+    E = 10 ** rng.uniform(math.log10(emin), math.log10(emax), n)
+    m = np.where(np.abs(pid) == 11, 0.000511, np.where(np.abs(pid) == 13, 0.1056583755, 0.0))
+    p0 = np.c_[E, np.zeros(n), np.zeros(n), np.sqrt(E * E - m * m)]
+    return p0, pid.astype(np.int32), m
+
+
+@pytest.fixture(scope="module")
+def lead():
+    from petite_gb300 import Shower
+    return Shower(None, "lead", 0.010, seed=SEED)
+
+
+def run_batch(sh, p0, pid, m, precision, cap=0, offset=0):
+    eng = sh._engine
+    opts = sh._opts(True, precision)
+    opts.primary_offset = offset
+    t = eng.new_tally(len(p0), z_max=0.3)
+    eng.run_batch(p0, np.zeros((len(p0), 3)), pid, m, opts, t, queue_capacity=cap)
+    return t
+
+
+def test_fp64_batch_equals_record_engine(lead):
+    p0, pid, m = primaries(300)
+    b = lead.generate_showers(p0, pid=pid, mass=m, first_primary=0)
+    rows_per_primary = np.bincount(b.primary, minlength=len(p0))
+    t = run_batch(lead, p0, pid, m, "fp64")
+    s = t.summary()
+    assert np.array_equal(t.primary_count.cpu().numpy(), rows_per_primary)
+    assert s["steps"] == b.n
+    sp = [int((b.pid == q).sum()) for q in (22, 11, -11)]
+    assert [s["photon_steps"], s["electron_steps"], s["positron_steps"]] == sp
+    # continuous dE/dx loss summed over the records
+    np.testing.assert_allclose(s["E_continuous"], float(np.sum(b.p0[:, 0] - b.pf[:, 0])), rtol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_capacity_does_not_change_results(lead, precision):
+    p0, pid, m = primaries(400, seed=3)
+    big = run_batch(lead, p0, pid, m, precision, cap=1 << 22)
+    small = run_batch(lead, p0, pid, m, precision, cap=1 << 12)
+    assert np.array_equal(big.primary_count.cpu().numpy(), small.primary_count.cpu().numpy())
+    assert np.array_equal(big.hist.cpu().numpy(), small.hist.cpu().numpy())
+    np.testing.assert_allclose(big.primary_edep.cpu().numpy(), small.primary_edep.cpu().numpy(), rtol=1e-9)
+
+
+def test_mixed_matches_fp64(lead):
+    """Same random streams: the float32 sampler changes a decision only when a
+    uniform falls within float32 rounding of the acceptance boundary."""
+    p0, pid, m = primaries(3000, seed=11, emax=100.0)
+    f = run_batch(lead, p0, pid, m, "fp64")
+    x = run_batch(lead, p0, pid, m, "mixed")
+    sf, sx = f.summary(), x.summary()
+    cf, cx = f.primary_count.cpu().numpy(), x.primary_count.cpu().numpy()
+    same = float(np.mean(cf == cx))
+    print("identical showers:", same, "steps", sf["steps"], sx["steps"])
+    assert same > 0.9
+    assert abs(sx["steps"] - sf["steps"]) / sf["steps"] < 2e-3
+    assert abs(sx["E_deposited"] - sf["E_deposited"]) / sf["E_deposited"] < 1e-3
+    # binned spectra: chi2 per bin of creation energies and depths
+    hf, hx = f.hist.cpu().numpy().astype(float), x.hist.cpu().numpy().astype(float)
+    for kind in (0, 2):
+        a, b = hf[kind].ravel(), hx[kind].ravel()
+        mask = (a + b) > 20
+        chi2 = np.sum((a[mask] - b[mask]) ** 2 / (a[mask] + b[mask]))
+        assert chi2 / mask.sum() < 2.0, (kind, chi2 / mask.sum())
+
+
+def test_batch_no_sample_reports():
+    from petite_gb300 import Shower
+    sh = Shower(None, "graphite", 0.010, seed=1, max_n_integrators=1, maxF_fudge_global=1e300)
+    p0, pid, m = primaries(4, species=(22,))
+    with pytest.raises(Exception, match="No Sample Found"):
+        run_batch(sh, p0, pid, m, "mixed")
