@@ -64,8 +64,18 @@ typedef struct pt_tables {
   int32_t ns_len[PT_N_NSIGMA];
   const double* ns_x;
   const double* ns_y;
-  const float* ns_x32;            /* float32 copies (mixed-precision form) */
+  /* float32 forms for the mixed-precision engine: nodes, values and slopes
+   * (y[j+1]-y[j])/(x[j+1]-x[j]) computed in float64; first-guess index
+   * j ~ (ln E - ns_lnx0) * ns_invdlog (exact for the geometric grids PETITE
+   * uses, corrected by one step otherwise) */
+  const float* ns_x32;
   const float* ns_y32;
+  const float* ns_s32;
+  float ns_lnx0[PT_N_NSIGMA];
+  float ns_invdlog[PT_N_NSIGMA];
+  const float* map_energy32;      /* [n_rows] */
+  float map_lnE0[PT_N_PROCESSES];
+  float map_invdlog[PT_N_PROCESSES];
   /* target and thresholds */
   double Z, A, rho;               /* physical_constants.py:49-55 */
   double dEdx_GeV_per_m;          /* 0.1 * dEdx[MeV/cm] (shower.py:649) */

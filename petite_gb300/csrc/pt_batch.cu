@@ -2,20 +2,24 @@
 //
 // Live particles sit in a power-of-two ring buffer in HBM (structure of
 // arrays).  Primaries stream in while there is room; each wave takes up to
-// (capacity - live)/2 entries from the head, so the at most two daughters
-// per entry always fit behind the tail.  A wave is two kernels:
+// (capacity - live)/2 entries from the head, so the at most two daughters per
+// entry always fit behind the tail.  A wave is two kernels:
 //  1. k_propagate: propagate_particle (shower.py:509-601) and the process
-//     choice (shower.py:665-698).  Lanes refill themselves from the wave and
-//     advance one charged-particle substep per iteration, so a long track does
-//     not hold its warp.  Interacting particles are parked in place and listed
-//     by process; the others are tallied and retired.
+//     choice (shower.py:665-698).  Lanes refill themselves and advance one
+//     charged-particle substep per iteration, so a long track does not hold
+//     its warp.  Interacting particles are parked in place and listed by
+//     process; the others are tallied and retired.
 //  2. k_sample: draw_sample's accept/reject loop (shower.py:401-465) over the
 //     task list ordered by process, one proposal per lane per iteration with
 //     refill, then the final-state kinematics and lab rotation
 //     (shower.py:467-507); daughters above min_energy are appended at the tail.
+// Both kernels run warp-convergent loops: refills come from a warp-private
+// pool of work indices fetched CHUNK at a time (one atomic per chunk), and
+// sampling tasks are gathered per warp and process and published 32 at a
+// time, so no counter is hit once per particle.
 // PREC = 0 is the float64 engine (same device functions and operation order
-// as pt_run_sm, hence the same showers); PREC = 1 samples and scatters in
-// float32 and keeps energies, positions and daughter energies in float64.
+// as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
+// builds directions in float32 and keeps energies in float64.
 #include <cstdio>
 
 #include "pt_internal.cuh"
@@ -26,8 +30,11 @@ using namespace pt;
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
+constexpr unsigned kFull = 0xffffffffu;
 constexpr int kHB = PT_HIST_BINS;
 constexpr int kHist = 3 * 4 * kHB;
+constexpr int kBuf = 64;        // per-warp, per-process task buffer (published at >= 32)
 
 struct Ring {
   double *E, *px, *py, *pz, *x, *y, *z, *mass;
@@ -69,17 +76,40 @@ __device__ void raise_status(int* status, double* info, int code, int process, d
   }
 }
 
-// Warp-aggregated pop: each requesting lane gets one index of [0, n) or -1.
-__device__ __forceinline__ int64_t warp_pop(unsigned long long* head, int64_t n, bool need) {
-  const unsigned mask = __activemask();
-  const unsigned b = __ballot_sync(mask, need);
-  const int leader = __ffs(mask) - 1;
-  unsigned long long base = 0;
-  if ((int)(threadIdx.x & 31) == leader && b) base = atomicAdd(head, (unsigned long long)__popc(b));
-  base = __shfl_sync(mask, base, leader);
+// ------------------------------------------------------- warp work pools
+// Warp-uniform range [next, end) of work indices, refilled `chunk` at a time.
+struct WarpPool {
+  int64_t next = 0, end = 0;
+  bool exhausted = false;
+};
+
+// Called by all 32 lanes.  Returns the lane's new index in [0, n) or -1.
+__device__ __forceinline__ int64_t pool_take(WarpPool& P, unsigned long long* head, int64_t n, bool need,
+                                             int chunk) {
+  const unsigned b = __ballot_sync(kFull, need);
+  if (!b) return -1;
+  const int cnt = __popc(b);
+  const int rank = __popc(b & lanemask_lt());
+  const int64_t avail = P.end - P.next;
+  int64_t got;
+  if (avail >= cnt) {
+    got = P.next + rank;
+    P.next += cnt;
+  } else {
+    int64_t base = n;
+    if (!P.exhausted) {
+      unsigned long long bb = 0;
+      if ((threadIdx.x & 31) == 0) bb = atomicAdd(head, (unsigned long long)chunk);
+      base = (int64_t)__shfl_sync(kFull, bb, 0);
+      if (base >= n) { P.exhausted = true; base = n; }
+    }
+    got = rank < avail ? P.next + rank : base + (rank - avail);
+    P.next = base + (cnt - avail);
+    P.end = P.exhausted ? base : base + chunk;
+    if (P.next > P.end) P.next = P.end;
+  }
   if (!need) return -1;
-  const unsigned long long mine = base + __popc(b & lanemask_lt());
-  return (int64_t)mine < n ? (int64_t)mine : -1;
+  return got < n ? got : -1;
 }
 
 __device__ __forceinline__ int species_of(int pid) {
@@ -99,14 +129,13 @@ struct LocalTally {
 
 __device__ void flush_tally(const Tally& T, LocalTally& L, const unsigned int* sh_hist) {
   auto red = [](unsigned long long v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;
   };
   auto redd = [](double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
     return v;
   };
-  __syncwarp();
   const unsigned long long c[7] = {red(L.steps), red(L.props), red(L.substeps), red(L.ended), red(L.pushed),
                                    red(L.below), red(L.sampled)};
   const unsigned long long sp[4] = {red(L.species[0]), red(L.species[1]), red(L.species[2]), red(L.species[3])};
@@ -127,7 +156,103 @@ __device__ void flush_tally(const Tally& T, LocalTally& L, const unsigned int* s
   }
 }
 
-// Process choice (shower.py:665-698), float64 in both engines.
+// Per-primary tallies: one count atomic per distinct primary among the
+// finishing lanes of the warp; energy deposits per lane.
+__device__ __forceinline__ void primary_tally(const Tally& T, bool on, int prim, double edep) {
+  if (!__any_sync(kFull, on)) return;
+  const unsigned grp = __match_any_sync(kFull, on ? prim : -1 - (int)(threadIdx.x & 31));
+  if (on && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(T.prim_count + prim, (unsigned)__popc(grp));
+  if (on && edep != 0.0) atomicAdd(T.prim_edep + prim, edep);
+}
+
+// Output slots at the ring tail, reserved 64 at a time per warp.  Slots of a
+// chunk left over when the kernel ends are written as dead entries (pid 0).
+struct OutPool {
+  uint64_t next = 0, end = 0;   // offsets from the wave's tail
+};
+constexpr int kOutChunk = 64;
+
+// All lanes call.  Writes this lane's slot offsets (want of them) to slot[].
+__device__ __forceinline__ void out_take(OutPool& P, unsigned long long* ctr, int want, uint64_t* slot) {
+  const unsigned b1 = __ballot_sync(kFull, want >= 1), b2 = __ballot_sync(kFull, want >= 2);
+  const unsigned total = __popc(b1) + __popc(b2);
+  if (!total) return;
+  const unsigned lt = lanemask_lt();
+  const uint64_t prefix = __popc(b1 & lt) + __popc(b2 & lt);
+  const uint64_t avail = P.end - P.next;
+  uint64_t base = 0;
+  if (avail < total) {
+    unsigned long long bb = 0;
+    if ((threadIdx.x & 31) == 0) bb = atomicAdd(ctr, (unsigned long long)kOutChunk);
+    base = __shfl_sync(kFull, bb, 0);
+  }
+  for (int j = 0; j < want; ++j) {
+    const uint64_t r = prefix + j;
+    slot[j] = r < avail ? P.next + r : base + (r - avail);
+  }
+  if (avail < total) { P.next = base + (total - avail); P.end = base + kOutChunk; }
+  else P.next += total;
+}
+
+// ---------------------------------------------- float32 table lookups
+__device__ __forceinline__ int geo_index(const float* x, int n, float lnx0, float idl, float E) {
+  int j = (int)((__logf(E) - lnx0) * idl);
+  j = j < 0 ? 0 : (j > n - 2 ? n - 2 : j);
+  while (j > 0 && __ldg(x + j) > E) --j;
+  while (j < n - 2 && __ldg(x + j + 1) <= E) ++j;
+  return j;
+}
+
+// interp1d(kind='linear', fill_value=0) in float32 (shower.py:280-295)
+__device__ __forceinline__ float nsig32(const Tabs& T, int slot, float E) {
+  const int b = T.t.ns_base[slot], n = T.t.ns_len[slot];
+  const float* x = T.t.ns_x32 + b;
+  if (!(E >= __ldg(x)) || E > __ldg(x + n - 1)) return 0.f;
+  const int j = geo_index(x, n, T.t.ns_lnx0[slot], T.t.ns_invdlog[slot], E);
+  return fmaf(E - __ldg(x + j), __ldg(T.t.ns_s32 + b + j), __ldg(T.t.ns_y32 + b + j));
+}
+
+__device__ __forceinline__ float mfp32(const Tabs& T, int pid, float E) {
+  float ns;
+  if (pid == 22) ns = nsig32(T, 1, E) + nsig32(T, 3, E);
+  else if (pid == 11) ns = nsig32(T, 0, E) + nsig32(T, 4, E);
+  else if (pid == -11) ns = nsig32(T, 0, E) + nsig32(T, 5, E) + nsig32(T, 2, E);
+  else ns = nsig32(T, 7, E) + nsig32(T, 6, E);
+  return ns > 0.f ? (float)kCmToM / ns : 1.0e12f;
+}
+
+// Process choice in float32 (shower.py:665-698)
+__device__ __forceinline__ int choose32(const Tabs& T, int pid, float E, float u) {
+  float c0, c1, c2 = 0.f;
+  int n0, n1, n2 = -1;
+  if (pid == 11) { n0 = PT_BREM; n1 = PT_MOLLER; c0 = nsig32(T, 0, E); c1 = nsig32(T, 4, E); }
+  else if (pid == -11) { n0 = PT_BREM; n1 = PT_ANN; n2 = PT_BHABHA; c0 = nsig32(T, 0, E); c1 = nsig32(T, 2, E); c2 = nsig32(T, 5, E); }
+  else if (pid == 22) { n0 = PT_PAIRPROD; n1 = PT_COMP; c0 = nsig32(T, 1, E); c1 = nsig32(T, 3, E); }
+  else { n0 = PT_MUONE; n1 = PT_MUONBREM; c0 = nsig32(T, 6, E); c1 = nsig32(T, 7, E); }
+  const float sum = c0 + c1 + c2;
+  if (!(sum > 0.f)) return -1;
+  const float t = u * sum;
+  if (c0 > t) return n0;
+  if (c0 + c1 > t || n2 < 0) return n1;
+  return n2;
+}
+
+// LU_Key (shower.py:416-426) in float32: argmin |E_i - E| + 1, clipped.
+__device__ __forceinline__ int lu_key32(const Tabs& T, int process, float E) {
+  const float* Ei = T.t.map_energy32 + T.t.map_base[process];
+  const int n = T.t.map_rows[process];
+  int best;
+  if (!(E > __ldg(Ei))) best = 0;
+  else if (E >= __ldg(Ei + n - 1)) best = n - 1;
+  else {
+    const int j = geo_index(Ei, n, T.t.map_lnE0[process], T.t.map_invdlog[process], E);  // Ei[j] <= E < Ei[j+1]
+    best = (E - __ldg(Ei + j) <= __ldg(Ei + j + 1) - E) ? j : j + 1;
+  }
+  const int key = best + 1;
+  return key >= n ? n - 1 : key;
+}
+
+// Process choice (shower.py:665-698), float64 (the float64 engine).
 __device__ int choose_process_b(const Tabs& T, int pid, double E, Rng& rng) {
   int names[3];
   double c[3];
@@ -156,34 +281,88 @@ __device__ int choose_process_b(const Tabs& T, int pid, double E, Rng& rng) {
   return names[idx];
 }
 
+// Publishes this iteration's sampling tasks: lanes with `emit` append ring
+// index `i` to the warp's buffer for `process`; full buffers go to the global
+// per-process lists 32 at a time.  All 32 lanes call it.
+__device__ __forceinline__ void publish_tasks(const WaveCtx& c, int32_t (*buf)[kBuf], int* cnt, bool emit,
+                                              int process, int32_t i) {
+  unsigned left = __ballot_sync(kFull, emit);
+  const int lane = threadIdx.x & 31;
+  while (left) {
+    const int leader = __ffs(left) - 1;
+    const int p = __shfl_sync(kFull, process, leader);
+    const unsigned m = __ballot_sync(kFull, emit && process == p);
+    if (emit && process == p) buf[p][cnt[p] + __popc(m & lanemask_lt())] = i;
+    cnt[p] += __popc(m);
+    left &= ~m;
+    __syncwarp();
+    if (cnt[p] >= 32) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(c.ctr + 8 + p, 32ull);
+      base = __shfl_sync(kFull, base, 0);
+      c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
+      __syncwarp();
+      const int rest = cnt[p] - 32;
+      int32_t carry = lane < rest ? buf[p][32 + lane] : 0;
+      __syncwarp();
+      if (lane < rest) buf[p][lane] = carry;
+      cnt[p] = rest;
+      __syncwarp();
+    }
+  }
+}
+
+__device__ __forceinline__ void publish_rest(const WaveCtx& c, int32_t (*buf)[kBuf], int* cnt) {
+  const int lane = threadIdx.x & 31;
+  for (int p = 0; p < 8; ++p) {
+    if (!cnt[p]) continue;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(c.ctr + 8 + p, (unsigned long long)cnt[p]);
+    base = __shfl_sync(kFull, base, 0);
+    if (lane < cnt[p]) c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
+    cnt[p] = 0;
+  }
+  __syncwarp();
+}
+
 // ------------------------------------------------------------ phase 1
 template <int PREC>
 __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
   __shared__ unsigned int sh_hist[kHist];
+  __shared__ int32_t sh_buf[kWarps][8][kBuf];
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
   __syncthreads();
+  int32_t (*buf)[kBuf] = sh_buf[threadIdx.x / 32];
+  int bcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const Tabs& T = c.T;
   LocalTally L;
+  WarpPool pool;
   bool active = false;
   uint64_t i = 0;
   double E0 = 0, E = 0, px = 0, py = 0, pz = 0, x = 0, y = 0, z = 0, mass = 0, pme = 0, dz = 0;
   float3 dir = make_float3(0.f, 0.f, 1.f), disp = make_float3(0.f, 0.f, 0.f);
-  float pmag = 0.f;
+  float Ef = 0.f, lossf = 0.f, dzf = 0.f, pmef = 0.f;
   int pid = 0, prim = 0;
   Rng rng;
   const double losses = T.t.dEdx_GeV_per_m;
+  const float lossesf = (float)losses;
   const float zmax = c.tally.z_max;
 
   for (;;) {
+    __syncwarp();
     const bool need = !active;
-    const int64_t got = warp_pop(c.ctr + 0, c.n_in, need);
+    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, 128);
+    const bool fresh = need && got >= 0;
+    if (__all_sync(kFull, !active && !fresh)) break;
     bool finish = false;
-    if (need) {
-      if (got < 0) break;
+    if (fresh) {
       i = (c.head + (uint64_t)got) & c.mask;
       E0 = c.q.E[i]; px = c.q.px[i]; py = c.q.py[i]; pz = c.q.pz[i];
       x = c.q.x[i]; y = c.q.y[i]; z = c.q.z[i];
       mass = c.q.mass[i]; pid = c.q.pid[i]; prim = c.q.prim[i];
+    }
+    // a dead entry (pid 0, left by the sampler's slot pool) is consumed without work
+    if (fresh && pid != 0) {
       rng.init(c.seed, c.q.key[i]);
       E = E0;
       pme = fmax(fmax(min_calc(T, pid), c.min_energy), mass);
@@ -191,38 +370,45 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
       const int sp = species_of(pid);
       ++L.species[sp];
       atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f((float)E0), -2.f, 2.f)], 1u);
-      const float th = atan2f((float)sqrt(px * px + py * py), (float)pz);
+      const float th = atan2f(sqrtf((float)px * (float)px + (float)py * (float)py), (float)pz);
       atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(th > 0.f ? log10f(th) : -6.f, -6.f, 0.5f)], 1u);
+      if (PREC == 1) {
+        const float pn = sqrtf((float)px * (float)px + (float)py * (float)py + (float)pz * (float)pz);
+        dir = pn > 0.f ? make_float3((float)px / pn, (float)py / pn, (float)pz / pn) : make_float3(0.f, 0.f, 1.f);
+        disp = make_float3(0.f, 0.f, 0.f);
+        Ef = (float)E0; lossf = 0.f; pmef = (float)pme;
+      }
       if (E0 < pme) {
         finish = true;
       } else if (pid == 22) {               // shower.py:538-553
-        const double mfp = mfp_of(T, pid, E);
-        const double distC = rng.u();
-        const double dist = (S(mfp) * S(log((S(1.0) / (S(1.0) - S(distC))).v))).v;
-        const double n = norm3_np(px, py, pz);
-        x = (S(x) + S(px) / S(n) * S(dist)).v;
-        y = (S(y) + S(py) / S(n) * S(dist)).v;
-        z = (S(z) + S(pz) / S(n) * S(dist)).v;
+        if (PREC == 0) {
+          const double mfp = mfp_of(T, pid, E);
+          const double distC = rng.u();
+          const double dist = (S(mfp) * S(log((S(1.0) / (S(1.0) - S(distC))).v))).v;
+          const double n = norm3_np(px, py, pz);
+          x = (S(x) + S(px) / S(n) * S(dist)).v;
+          y = (S(y) + S(py) / S(n) * S(dist)).v;
+          z = (S(z) + S(pz) / S(n) * S(dist)).v;
+        } else {
+          const float dist = -mfp32(T, pid, Ef) * log1pf(-rng.uf());
+          x += (double)(dir.x * dist); y += (double)(dir.y * dist); z += (double)(dir.z * dist);
+        }
         finish = true;
       } else {
         active = true;
         dz = 0.0;
-        if (PREC == 1) {
-          const double pn = sqrt(px * px + py * py + pz * pz);
-          pmag = (float)pn;
-          dir = pn > 0 ? make_float3((float)(px / pn), (float)(py / pn), (float)(pz / pn)) : make_float3(0.f, 0.f, 1.f);
-          disp = make_float3(0.f, 0.f, 0.f);
-        }
+        dzf = 0.f;
       }
     }
     if (active) {
       // one iteration of the substep loop (shower.py:559-581)
-      bool stop = !(E >= pme);
-      if (!stop) {
-        ++L.substeps;
-        const double mfp = mfp_of(T, pid, E);
-        const double u_hard = rng.u();
-        if (PREC == 0) {
+      bool stop;
+      if (PREC == 0) {
+        stop = !(E >= pme);
+        if (!stop) {
+          ++L.substeps;
+          const double mfp = mfp_of(T, pid, E);
+          const double u_hard = rng.u();
           dz = (S(mfp) / (S(6.0) + S(14.0) * S(rng.u()))).v;
           if (u_hard > exp(-dz / mfp)) {
             stop = true;
@@ -234,128 +420,145 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
                                table_mass(pid), rng);
             E = pf[0]; px = pf[1]; py = pf[2]; pz = pf[3]; x = rf[0]; y = rf[1]; z = rf[2];
           }
-        } else {
-          const float q = fmaf(14.f, rng.uf(), 6.f);
-          dz = mfp / (double)q;
-          if ((float)u_hard > __expf(-1.f / q)) {
-            stop = true;
-          } else {
-            // lose_energy (particle.py:143-153): E in float64, |p| from (E-m)(E+m)
-            double En = E - losses * dz;
-            if (En <= mass) En = mass;
-            E = En;
-            pmag = sqrtf((float)((En - mass) * (En + mass)));
-            if (pmag > 0.f) {
-              const float dzf = (float)dz;
-              disp.x = fmaf(dir.x, dzf, disp.x); disp.y = fmaf(dir.y, dzf, disp.y); disp.z = fmaf(dir.z, dzf, disp.z);
-            }
-            if (c.ms)
-              mcs32(dir, pmag, (float)E, (float)(T.t.rho * (dz / kCmToM)), (float)T.t.A, (float)T.t.Z,
-                    (float)T.t.Z23, (float)c.rescale, rng);
+        }
+        if (stop) {
+          // final partial increment (shower.py:583-598)
+          const double distC = rng.u();
+          double last;
+          if (E < pme) last = (S(distC) * S(dz)).v;
+          else {
+            const double mfp = mfp_of(T, pid, E);
+            const S e = S(exp(-dz / mfp));
+            last = (S(mfp) * S(log((S(1.0) / (S(1.0) + (e - S(1.0)) * S(distC))).v))).v;
           }
-        }
-      }
-      if (stop) {
-        // final partial increment (shower.py:583-598)
-        const double distC = rng.u();
-        double last;
-        if (E < pme) last = (S(distC) * S(dz)).v;
-        else {
-          const double mfp = mfp_of(T, pid, E);
-          const S e = S(exp(-dz / mfp));
-          last = (S(mfp) * S(log((S(1.0) / (S(1.0) + (e - S(1.0)) * S(distC))).v))).v;
-        }
-        if (PREC == 0) {
           double pf[4] = {E, px, py, pz}, rf[3] = {x, y, z};
           lose_energy(pf, mass, (S(losses) * S(last)).v);
           move_along(pf, rf, last);
           if (c.ms) mcs_fast(pf, (S(T.t.rho) * (S(last) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, c.rescale, kMe, rng);
           E = pf[0]; px = pf[1]; py = pf[2]; pz = pf[3]; x = rf[0]; y = rf[1]; z = rf[2];
-        } else {
-          double En = E - losses * last;
-          if (En <= mass) En = mass;
-          E = En;
-          pmag = sqrtf((float)((En - mass) * (En + mass)));
-          if (pmag > 0.f) {
-            const float lf = (float)last;
-            disp.x = fmaf(dir.x, lf, disp.x); disp.y = fmaf(dir.y, lf, disp.y); disp.z = fmaf(dir.z, lf, disp.z);
-          }
-          if (c.ms)   // shower.py:596-598 passes no m_lepton (electron default); |p| enters here directly
-            mcs32(dir, pmag, (float)E, (float)(T.t.rho * (last / kCmToM)), (float)T.t.A, (float)T.t.Z,
-                  (float)T.t.Z23, (float)c.rescale, rng);
-          x += disp.x; y += disp.y; z += disp.z;
-          if (pmag > 0.f) { px = (double)pmag * dir.x; py = (double)pmag * dir.y; pz = (double)pmag * dir.z; }
-          else { px = py = pz = 0.0; }
+          active = false;
+          finish = true;
         }
-        active = false;
-        finish = true;
+      } else {
+        // float32 substep: the energy lost along the track is accumulated in
+        // float32 and subtracted from the float64 energy once at the end
+        const float mf = (float)mass;
+        stop = !(Ef >= pmef);
+        float mfp = 0.f;
+        if (!stop) {
+          ++L.substeps;
+          mfp = mfp32(T, pid, Ef);
+          const float u_hard = rng.uf();
+          const float q = fmaf(14.f, rng.uf(), 6.f);
+          dzf = mfp / q;
+          if (u_hard > __expf(-1.f / q)) {
+            stop = true;
+          } else {
+            const float dE = lossesf * dzf;
+            lossf += dE;
+            Ef = (float)E0 - lossf;
+            if (Ef <= mf) Ef = mf;
+            const float pmag = sqrtf((Ef - mf) * (Ef + mf));
+            if (pmag > 0.f) {
+              disp.x = fmaf(dir.x, dzf, disp.x); disp.y = fmaf(dir.y, dzf, disp.y); disp.z = fmaf(dir.z, dzf, disp.z);
+            }
+            if (c.ms)
+              mcs32(dir, pmag, Ef, (float)T.t.rho * (dzf / (float)kCmToM), (float)T.t.A, (float)T.t.Z,
+                    (float)T.t.Z23, (float)c.rescale, rng);
+          }
+        }
+        if (stop) {
+          const float distC = rng.uf();
+          float last;
+          if (Ef < pmef) last = distC * dzf;
+          else {
+            if (mfp == 0.f) mfp = mfp32(T, pid, Ef);
+            last = -mfp * log1pf(expm1f(-dzf / mfp) * distC);
+          }
+          lossf += lossesf * last;
+          E = E0 - (double)lossf;                     // float64 bookkeeping, once per step
+          if (E <= mass) E = mass;
+          Ef = (float)E;
+          const float pmag = sqrtf((Ef - mf) * (Ef + mf));
+          if (pmag > 0.f) {
+            disp.x = fmaf(dir.x, last, disp.x); disp.y = fmaf(dir.y, last, disp.y); disp.z = fmaf(dir.z, last, disp.z);
+          }
+          if (c.ms)   // shower.py:596-598 passes no m_lepton; the width uses |p| directly here
+            mcs32(dir, pmag, Ef, (float)T.t.rho * (last / (float)kCmToM), (float)T.t.A, (float)T.t.Z,
+                  (float)T.t.Z23, (float)c.rescale, rng);
+          x += (double)disp.x; y += (double)disp.y; z += (double)disp.z;
+          px = (double)(pmag * dir.x); py = (double)(pmag * dir.y); pz = (double)(pmag * dir.z);
+          active = false;
+          finish = true;
+        }
       }
     }
+    // ---- end of propagation: tallies, process choice, task or retirement
+    int process = -1;
+    bool emit = false;
+    double edep = 0.0;
     if (finish) {
       const int sp = species_of(pid);
       atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of((float)z, 0.f, zmax)], 1u);
       const double eloss = E0 - E;
       L.e_cont += eloss;
-      atomicAdd(c.tally.prim_count + prim, 1u);
-      const int process = choose_process_b(T, pid, E, rng);
-      if (process >= 0 && E > pme) {
-        // park the post-propagation state in place and list a sampling task
+      if (PREC == 0) process = choose_process_b(T, pid, E, rng);
+      else process = choose32(T, pid, (float)E, rng.uf());
+      emit = process >= 0 && E > pme;
+      if (emit) {
+        // park the post-propagation state in place for the sampler
         c.q.E[i] = E; c.q.px[i] = px; c.q.py[i] = py; c.q.pz[i] = pz;
         c.q.x[i] = x; c.q.y[i] = y; c.q.z[i] = z;
         c.q.draw[i] = (uint32_t)rng.n;
-        c.q.row[i] = T.t.map_base[process] + lu_key(T, process, E);
-        const unsigned mask = __activemask();
-        const unsigned grp = __match_any_sync(mask, process);
-        const int leader = __ffs(grp) - 1;
-        unsigned long long base = 0;
-        if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(c.ctr + 8 + process, (unsigned long long)__popc(grp));
-        base = __shfl_sync(grp, base, leader);
-        const unsigned long long slot = base + __popc(grp & lanemask_lt());
-        c.idx[(int64_t)process * c.list_cap + (int64_t)slot] = (int32_t)i;
-        if (eloss != 0.0) atomicAdd(c.tally.prim_edep + prim, eloss);
+        c.q.row[i] = T.t.map_base[process] + (PREC == 0 ? lu_key(T, process, E) : lu_key32(T, process, (float)E));
+        edep = eloss;
       } else {
         ++L.ended;
         L.e_ended += E;
-        atomicAdd(c.tally.prim_edep + prim, eloss + E);
+        edep = eloss + E;
       }
     }
+    primary_tally(c.tally, finish, prim, edep);
+    publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
   }
+  publish_rest(c, buf, bcnt);
   flush_tally(c.tally, L, sh_hist);
 }
 
 // ------------------------------------------------------------ phase 2
 struct Daughter { double E, px, py, pz; int pid; };
 
-// Mixed engine: daughters in the parent frame with float64 energies (forms
-// without cancellation), float64 momentum magnitudes, float32 directions.
-struct KinOut { double E[2], P[2]; float3 d[2]; int pid[2]; };
+// Mixed engine: daughters in the parent frame with float32 angles, float32
+// momentum magnitudes and the energy split closed in float64
+// (E_a + E_b = E_in + target mass for the two-body processes).
+struct KinOut { double E[2]; float P[2]; float3 d[2]; int pid[2]; };
 
-__device__ __forceinline__ void set_dir(KinOut& k, int j, double pxx, double pyy, double pzz) {
-  const double p = sqrt(pxx * pxx + pyy * pyy + pzz * pzz);
+__device__ __forceinline__ void set_dir32(KinOut& k, int j, float pxx, float pyy, float pzz) {
+  const float p = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz);
   k.P[j] = p;
-  k.d[j] = p > 0 ? make_float3((float)(pxx / p), (float)(pyy / p), (float)(pzz / p)) : make_float3(0.f, 0.f, 1.f);
+  k.d[j] = p > 0.f ? make_float3(pxx / p, pyy / p, pzz / p) : make_float3(0.f, 0.f, 1.f);
 }
 
-__device__ void kin_mixed(int process, int pid, double E, double mass, const double* x, double omx, double opx,
-                          float ph, KinOut& k) {
+__device__ void kin_mixed(int process, int pid, double E, double mass, const MapPt32* x, float ph, KinOut& k) {
   float sph, cph;
   sincosf(ph, &sph, &cph);
-  const double me = kMe;
+  const float me = (float)kMe;
   switch (process) {
     case PT_BREM: case PT_MUONBREM: {        // kinematics.py:10-41
-      const double Eg = 0.001;
-      const double w = Eg + x[0] * (E - mass - Eg);
-      const double epp = E - w;
+      const float Ef = (float)E, mf = (float)mass;
+      const float w = fmaf(x[0].x, (float)(E - mass - 0.001), 0.001f);
+      const double epp = E - (double)w;        // energy closes in float64
+      const float eppf = (float)epp;
       float st, ct, stp, ctp, sp, cp;
-      sincosf((float)((x[1] + x[2]) / 2), &st, &ct);
-      sincosf((float)((x[1] - x[2]) * E / (2 * (E - w))), &stp, &ctp);
+      sincosf(0.5f * (x[1].x + x[2].x), &st, &ct);
+      sincosf((x[1].x - x[2].x) * Ef / (2.f * eppf), &stp, &ctp);
       st = fabsf(st); stp = fabsf(stp);        // the reference takes sqrt(1 - cos^2)
-      sincospif((float)(2.0 * (x[3] - 0.5)), &sp, &cp);
+      sincospif(2.f * (x[3].x - 0.5f), &sp, &cp);
       const float sal = sph, cal = cph;        // azimuth 'al' of kinematics.py:33
-      k.E[1] = w; k.P[1] = w; k.pid[1] = 22;
+      k.E[1] = (double)w; k.P[1] = w; k.pid[1] = 22;
       k.d[1] = make_float3(cal * st, sal * st, ct);
       k.E[0] = epp; k.pid[0] = pid;
-      k.P[0] = sqrt((epp - mass) * (epp + mass));
+      k.P[0] = sqrtf((eppf - mf) * (eppf + mf));
       const float3 v = make_float3(sal * sp * stp + cal * (ctp * st - cp * ct * stp),
                                    ctp * sal * st - (cp * ct * sal + cal * sp) * stp, ct * ctp + cp * st * stp);
       const float inv = rsqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
@@ -363,63 +566,68 @@ __device__ void kin_mixed(int process, int pid, double E, double mass, const dou
       break;
     }
     case PT_PAIRPROD: {                       // kinematics.py:70-102
-      const double w = E;
-      const double epp = me + x[0] * (w - 2 * me);
-      const double epm = me + omx * (w - 2 * me);
+      const float wf = (float)E, span = (float)(E - 2 * kMe);
+      const float eppf = fmaf(x[0].x, span, me);
+      const double epm = E - (double)eppf;     // energy closes in float64
+      const float epmf = (float)epm;
       float stp, ctp, stm, ctm, s2, c2;
-      sincosf((float)(w * (x[1] + x[2]) / (2 * epp)), &stp, &ctp);
-      sincosf((float)(w * (x[1] - x[2]) / (2 * epm)), &stm, &ctm);
+      sincosf(wf * (x[1].x + x[2].x) / (2.f * eppf), &stp, &ctp);
+      sincosf(wf * (x[1].x - x[2].x) / (2.f * epmf), &stm, &ctm);
       stp = fabsf(stp); stm = fabsf(stm);
-      sincosf((float)(x[3] * 2 * kPi) + ph, &s2, &c2);
-      k.E[0] = epp; k.P[0] = sqrt((epp - me) * (epp + me)); k.pid[0] = -11;
+      sincosf(2.f * (float)kPi * x[3].x + ph, &s2, &c2);
+      k.E[0] = (double)eppf; k.P[0] = sqrtf((eppf - me) * (eppf + me)); k.pid[0] = -11;
       k.d[0] = make_float3(stp * cph, stp * sph, ctp);
-      k.E[1] = epm; k.P[1] = sqrt((epm - me) * (epm + me)); k.pid[1] = 11;
+      k.E[1] = epm; k.P[1] = sqrtf((epmf - me) * (epmf + me)); k.pid[1] = 11;
       k.d[1] = make_float3(stm * c2, stm * s2, ctm);
       break;
     }
     case PT_COMP: {                           // kinematics.py:104-132, mV = 0
-      const double s = me * me + 2 * E * me, rs = sqrt(s);
-      const double Ee = (s + me * me) / (2 * rs), EV = (s - me * me) / (2 * rs), pF = EV;
-      const double g0 = Ee / me, sq = sqrt((g0 - 1) * (g0 + 1)), b0 = sq / g0;
-      const double omb = 1.0 / (g0 * (g0 + sq));                 // 1 - b0
-      const double pT = pF * sqrt(omx * opx);
-      k.E[0] = g0 * Ee + b0 * g0 * pF * x[0]; k.pid[0] = 11;
-      set_dir(k, 0, -pT * sph, -pT * cph, b0 * g0 * Ee + g0 * pF * x[0]);
-      k.E[1] = g0 * EV * (omb + b0 * omx); k.pid[1] = 22;      // g0 (EV - b0 pF c)
-      set_dir(k, 1, pT * sph, pT * cph, g0 * EV * (omx - omb));  // g0 (b0 EV - pF c)
+      const float Eg = (float)E, s = me * me + 2.f * Eg * me, rs = sqrtf(s);
+      const float Ee = (s + me * me) / (2.f * rs), EV = (s - me * me) / (2.f * rs), pF = EV;
+      const float g0 = Ee / me, sq = sqrtf((g0 - 1.f) * (g0 + 1.f)), b0 = sq / g0;
+      const float omb = 1.f / (g0 * (g0 + sq));                 // 1 - b0
+      const float pT = pF * sqrtf(x[0].omx * x[0].opx);
+      const float Eph = g0 * EV * fmaf(b0, x[0].omx, omb);      // g0 (EV - b0 pF c)
+      k.E[1] = (double)Eph; k.pid[1] = 22;
+      set_dir32(k, 1, pT * sph, pT * cph, g0 * EV * (x[0].omx - omb));
+      k.E[0] = (E + kMe) - (double)Eph; k.pid[0] = 11;          // E_e + E_V = E_gamma + m_e
+      set_dir32(k, 0, -pT * sph, -pT * cph, b0 * g0 * Ee + g0 * pF * x[0].x);
       break;
     }
     case PT_ANN: {                            // kinematics.py:301-334, mV = 0
-      const double s = 2 * me * (E + me), Eg = sqrt(s) / 2;
-      const double g0 = Eg / me, sq = sqrt((g0 - 1) * (g0 + 1)), b0 = sq / g0;
-      const double omb = 1.0 / (g0 * (g0 + sq));
-      const double pT = Eg * sqrt(omx * opx);
-      k.E[0] = g0 * Eg * (omb + b0 * omx); k.pid[0] = 22;
-      set_dir(k, 0, -pT * sph, -pT * cph, g0 * Eg * (omx - omb));
-      k.E[1] = g0 * Eg * (1 + b0 * x[0]); k.pid[1] = 22;
-      set_dir(k, 1, pT * sph, pT * cph, g0 * Eg * (b0 + x[0]));
+      const float s = 2.f * me * ((float)E + me), Eg = 0.5f * sqrtf(s);
+      const float g0 = Eg / me, sq = sqrtf((g0 - 1.f) * (g0 + 1.f)), b0 = sq / g0;
+      const float omb = 1.f / (g0 * (g0 + sq));
+      const float pT = Eg * sqrtf(x[0].omx * x[0].opx);
+      const float E1 = g0 * Eg * fmaf(b0, x[0].omx, omb);
+      k.E[0] = (double)E1; k.pid[0] = 22;
+      set_dir32(k, 0, -pT * sph, -pT * cph, g0 * Eg * (x[0].omx - omb));
+      k.E[1] = (E + kMe) - (double)E1; k.pid[1] = 22;
+      set_dir32(k, 1, pT * sph, pT * cph, g0 * Eg * (b0 + x[0].x));
       break;
     }
     case PT_MOLLER: case PT_BHABHA: {         // kinematics.py:213-237 (b0 = pF/Ee0)
-      const double s = 2 * me * me + 2 * E * me, Ee0 = sqrt(s) / 2;
-      const double pF = sqrt((Ee0 - me) * (Ee0 + me)), g0 = Ee0 / me, b0 = pF / Ee0;
-      const double pT = pF * sqrt(omx * opx);
-      k.E[0] = g0 * (Ee0 + b0 * pF * x[0]); k.pid[0] = pid;
-      set_dir(k, 0, -pT * sph, -pT * cph, g0 * pF * opx);
-      k.E[1] = g0 * (me * me + pF * pF * omx) / Ee0; k.pid[1] = 11;   // g0 (Ee0 - b0 pF c)
-      set_dir(k, 1, pT * sph, pT * cph, g0 * pF * omx);
+      const float s = 2.f * me * me + 2.f * (float)E * me, Ee0 = 0.5f * sqrtf(s);
+      const float pF = sqrtf((Ee0 - me) * (Ee0 + me)), g0 = Ee0 / me;
+      const float pT = pF * sqrtf(x[0].omx * x[0].opx);
+      const float Eb = g0 * fmaf(pF * pF, x[0].omx, me * me) / Ee0;   // g0 (Ee0 - b0 pF c)
+      k.E[1] = (double)Eb; k.pid[1] = 11;
+      set_dir32(k, 1, pT * sph, pT * cph, g0 * pF * x[0].omx);
+      k.E[0] = (E + kMe) - (double)Eb; k.pid[0] = pid;
+      set_dir32(k, 0, -pT * sph, -pT * cph, g0 * pF * x[0].opx);
       break;
     }
     default: {                                // kinematics.py:239-265 (b0 = pe/Ee0)
-      const double mm = kMmu, s = me * me + mm * mm + 2 * E * me, rs = sqrt(s);
-      const double Ee0 = (s + me * me - mm * mm) / (2 * rs), Em0 = (s + mm * mm - me * me) / (2 * rs);
-      const double pe = sqrt((Ee0 - me) * (Ee0 + me)), pm = sqrt((Em0 - mm) * (Em0 + mm));
-      const double g0 = Ee0 / me, b0 = pe / Ee0;
-      const double st = sqrt(omx * opx);
-      k.E[0] = g0 * (Em0 + b0 * pm * x[0]); k.pid[0] = pid;
-      set_dir(k, 0, pm * st * sph, pm * st * cph, b0 * g0 * Em0 + g0 * pm * x[0]);
-      k.E[1] = g0 * (me * me + pe * pe * omx) / Ee0; k.pid[1] = 11;     // g0 (Ee0 - b0 pe c)
-      set_dir(k, 1, -pe * st * sph, -pe * st * cph, g0 * pe * omx);
+      const float mm = (float)kMmu, s = me * me + mm * mm + 2.f * (float)E * me, rs = sqrtf(s);
+      const float Ee0 = (s + me * me - mm * mm) / (2.f * rs), Em0 = (s + mm * mm - me * me) / (2.f * rs);
+      const float pe = sqrtf((Ee0 - me) * (Ee0 + me)), pm = sqrtf((Em0 - mm) * (Em0 + mm));
+      const float g0 = Ee0 / me, b0 = pe / Ee0;
+      const float st = sqrtf(x[0].omx * x[0].opx);
+      const float Eel = g0 * fmaf(pe * pe, x[0].omx, me * me) / Ee0;  // g0 (Ee0 - b0 pe c)
+      k.E[1] = (double)Eel; k.pid[1] = 11;
+      set_dir32(k, 1, -pe * st * sph, -pe * st * cph, g0 * pe * x[0].omx);
+      k.E[0] = (E + kMe) - (double)Eel; k.pid[0] = pid;
+      set_dir32(k, 0, pm * st * sph, pm * st * cph, b0 * g0 * Em0 + g0 * pm * x[0].x);
       break;
     }
   }
@@ -437,6 +645,8 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
   const int64_t total = (int64_t)sh_off[8];
   const Tabs& T = c.T;
   LocalTally L;
+  WarpPool pool;
+  OutPool opool;
   bool active = false;
   int process = 0, d = 1, row = 0;
   uint64_t i = 0;
@@ -447,13 +657,14 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
   const float4* g32[4] = {nullptr, nullptr, nullptr, nullptr};
   const double* g64[4] = {nullptr, nullptr, nullptr, nullptr};
   int ninc[4] = {1, 1, 1, 1};
-  uint64_t yk[4] = {0, 0, 0, 0};
 
   for (;;) {
+    __syncwarp();
     const bool need = !active;
-    const int64_t t = warp_pop(c.ctr + 1, total, need);
-    if (need) {
-      if (t < 0) break;
+    const int64_t t = pool_take(pool, c.ctr + 1, total, need, 64);
+    const bool fresh = need && t >= 0;
+    if (__all_sync(kFull, !active && !fresh)) break;
+    if (fresh) {
       process = 0;
       while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
       i = (uint64_t)c.idx[(int64_t)process * c.list_cap + (t - (int64_t)sh_off[process])];
@@ -493,105 +704,107 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
       }
       active = true;
     }
-    // ---- one proposal (d uniforms for y, then the accept uniform)
-    bool accept;
+    bool accept = false;
     double xd[4] = {0, 0, 0, 0};
-    if (PREC == 0) {
-      double jac = 1.0;
-      for (int k = 0; k < d; ++k) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
-      const double f = dsigma_any(T, process, xd, E);
-      accept = maxF * rng.u() < (jac / neval) * f;
-    } else {
-      MapPt32 xm[4];
-      float jac = 1.f;
-      for (int k = 0; k < d; ++k) {
-        yk[k] = rng.next_u64();
-        xm[k] = map_dim32(g32[k], ninc[k], (float)(yk[k] >> 40) * 0x1p-24f, jac);
+    MapPt32 xm[4];
+    if (active) {
+      // ---- one proposal (d uniforms for y, then the accept uniform)
+      if (PREC == 0) {
+        double jac = 1.0;
+        for (int k = 0; k < d; ++k) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
+        const double f = dsigma_any(T, process, xd, E);
+        accept = maxF * rng.u() < (jac / neval) * f;
+      } else {
+        float jac = 1.f;
+        for (int k = 0; k < d; ++k) xm[k] = map_dim32(g32[k], ninc[k], rng.uf(), jac);
+        float r;
+        switch (process) {
+          case PT_BREM: case PT_MUONBREM: r = brem32_ratio(S32, xm, jac); break;
+          case PT_PAIRPROD: r = pair32_ratio(S32, xm, jac); break;
+          case PT_COMP: r = comp32_ratio(S32, xm[0], jac); break;
+          case PT_ANN: r = ann32_ratio(S32, xm[0], jac); break;
+          case PT_MOLLER: r = moller32_ratio(S32, xm[0], jac); break;
+          case PT_BHABHA: r = bhabha32_ratio(S32, xm[0], jac); break;
+          default: r = muone32_ratio(S32, xm[0], jac); break;
+        }
+        accept = rng.uf() < r;
       }
-      float r;
-      switch (process) {
-        case PT_BREM: case PT_MUONBREM: r = brem32_ratio(S32, xm, jac); break;
-        case PT_PAIRPROD: r = pair32_ratio(S32, xm, jac); break;
-        case PT_COMP: r = comp32_ratio(S32, xm[0], jac); break;
-        case PT_ANN: r = ann32_ratio(S32, xm[0], jac); break;
-        case PT_MOLLER: r = moller32_ratio(S32, xm[0], jac); break;
-        case PT_BHABHA: r = bhabha32_ratio(S32, xm[0], jac); break;
-        default: r = muone32_ratio(S32, xm[0], jac); break;
-      }
-      accept = rng.uf() < r;
-      if (accept) {   // the accepted point in float64 from the same draws
-        double jd = 1.0;
-        for (int k = 0; k < d; ++k) xd[k] = map_dim(g64[k], ninc[k], (double)(yk[k] >> 11) * 0x1p-53, jd);
-      }
-    }
-    ++props;
-    ++L.props;
-    if (!accept) {
-      if (props >= cap) {
+      ++props;
+      ++L.props;
+      if (!accept && props >= cap) {
         raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
         active = false;
       }
-      continue;
     }
     // ---- accepted: kinematics and daughters (sample_scattering, shower.py:467-507)
-    active = false;
-    ++L.sampled;
-    const double mass = c.q.mass[i];
-    const int pid = c.q.pid[i];
-    const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
     Daughter dg[2];
-    const double ph = 2.0 * kPi * rng.u();
-    if (PREC == 0) {
-      const Rot R = rotation_from(pf);
-      V4 a, b;
-      int pa, pb;
-      switch (process) {
-        case PT_BREM: case PT_MUONBREM: kin_brem(E, mass, xd, ph, a, b); pa = pid; pb = 22; break;
-        case PT_PAIRPROD: kin_pairprod(E, xd, ph, a, b); pa = -11; pb = 11; break;
-        case PT_COMP: kin_compton(E, xd[0], ph, a, b); pa = 11; pb = 22; break;
-        case PT_ANN: kin_ann(E, xd[0], ph, a, b); pa = 22; pb = 22; break;
-        case PT_MOLLER: case PT_BHABHA: kin_ee(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
-        default: kin_mue(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
-      }
-      const V4 la = to_lab(R, a), lb = to_lab(R, b);
-      dg[0] = {la.e, la.x, la.y, la.z, pa};
-      dg[1] = {lb.e, lb.x, lb.y, lb.z, pb};
-    } else {
-      KinOut k;
-      kin_mixed(process, pid, E, mass, xd, 1.0 - xd[0], 1.0 + xd[0], (float)ph, k);
-      const double pn = sqrt(pf[1] * pf[1] + pf[2] * pf[2] + pf[3] * pf[3]);
-      const float3 pd = pn > 0 ? make_float3((float)(pf[1] / pn), (float)(pf[2] / pn), (float)(pf[3] / pn))
-                               : make_float3(0.f, 0.f, 1.f);
-      const Rot32 R = rot32_from(pd);
-      for (int j = 0; j < 2; ++j) {
-        const float3 v = rot32_apply(R, k.d[j]);
-        dg[j] = {k.E[j], k.P[j] * v.x, k.P[j] * v.y, k.P[j] * v.z, k.pid[j]};
-      }
-    }
-    const int want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
+    int want = 0;
+    int prim = 0;
     double below = 0.0;
-    for (int j = 0; j < 2; ++j)
-      if (!(dg[j].E > c.min_energy)) { ++L.below; L.e_below += dg[j].E; below += dg[j].E; }
-    const int prim = c.q.prim[i];
-    if (below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
-    const unsigned long long base = warp_reserve(c.ctr + 2, want);
-    int slot = 0;
-    const uint64_t key = c.q.key[i];
-    const int gen = c.q.gen[i];
-    const double x0 = c.q.x[i], y0 = c.q.y[i], z0 = c.q.z[i];
-    for (int j = 0; j < 2; ++j) {
-      if (!(dg[j].E > c.min_energy)) continue;
-      const uint64_t q = (c.tail + base + (unsigned long long)slot++) & c.mask;
-      ++L.pushed;
-      c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
-      c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
-      c.q.mass[q] = table_mass(dg[j].pid);
-      c.q.key[q] = daughter_key(key, j);
-      c.q.pid[q] = dg[j].pid;
-      c.q.prim[q] = prim;
-      c.q.gen[q] = gen + 1;
+    if (accept) {
+      active = false;
+      ++L.sampled;
+      const double mass = c.q.mass[i];
+      const int pid = c.q.pid[i];
+      const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
+      if (PREC == 0) {
+        const double ph = 2.0 * kPi * rng.u();
+        const Rot R = rotation_from(pf);
+        V4 a, b;
+        int pa, pb;
+        switch (process) {
+          case PT_BREM: case PT_MUONBREM: kin_brem(E, mass, xd, ph, a, b); pa = pid; pb = 22; break;
+          case PT_PAIRPROD: kin_pairprod(E, xd, ph, a, b); pa = -11; pb = 11; break;
+          case PT_COMP: kin_compton(E, xd[0], ph, a, b); pa = 11; pb = 22; break;
+          case PT_ANN: kin_ann(E, xd[0], ph, a, b); pa = 22; pb = 22; break;
+          case PT_MOLLER: case PT_BHABHA: kin_ee(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
+          default: kin_mue(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
+        }
+        const V4 la = to_lab(R, a), lb = to_lab(R, b);
+        dg[0] = {la.e, la.x, la.y, la.z, pa};
+        dg[1] = {lb.e, lb.x, lb.y, lb.z, pb};
+      } else {
+        const float ph = 2.f * (float)kPi * rng.uf();
+        KinOut k;
+        kin_mixed(process, pid, E, mass, xm, ph, k);
+        const float fx = (float)pf[1], fy = (float)pf[2], fz = (float)pf[3];
+        const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
+        const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
+        const Rot32 R = rot32_from(pd);
+        for (int j = 0; j < 2; ++j) {
+          const float3 v = rot32_apply(R, k.d[j]);
+          dg[j] = {k.E[j], (double)(k.P[j] * v.x), (double)(k.P[j] * v.y), (double)(k.P[j] * v.z), k.pid[j]};
+        }
+      }
+      want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
+      for (int j = 0; j < 2; ++j)
+        if (!(dg[j].E > c.min_energy)) { ++L.below; L.e_below += dg[j].E; below += dg[j].E; }
+      prim = c.q.prim[i];
+    }
+    if (accept && below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
+    uint64_t slots[2] = {0, 0};
+    out_take(opool, c.ctr + 2, want, slots);
+    if (want) {
+      int slot = 0;
+      const uint64_t key = c.q.key[i];
+      const int gen = c.q.gen[i];
+      const double x0 = c.q.x[i], y0 = c.q.y[i], z0 = c.q.z[i];
+      for (int j = 0; j < 2; ++j) {
+        if (!(dg[j].E > c.min_energy)) continue;
+        const uint64_t q = (c.tail + slots[slot++]) & c.mask;
+        ++L.pushed;
+        c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
+        c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
+        c.q.mass[q] = table_mass(dg[j].pid);
+        c.q.key[q] = daughter_key(key, j);
+        c.q.pid[q] = dg[j].pid;
+        c.q.prim[q] = prim;
+        c.q.gen[q] = gen + 1;
+      }
     }
   }
+  // unused slots of the warp's last chunk become dead entries
+  for (uint64_t r = opool.next + (threadIdx.x & 31); r < opool.end; r += 32) c.q.pid[(c.tail + r) & c.mask] = 0;
   flush_tally(c.tally, L, nullptr);
 }
 
@@ -634,7 +847,7 @@ struct BatchScratch {
 static size_t ring_bytes(int64_t cap) { return (size_t)cap * (9 * 8 + 5 * 4) + 16 * 256; }
 
 pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
-  int64_t c2 = 1;
+  int64_t c2 = 1 << 10;
   while (c2 < cap) c2 <<= 1;
   BatchScratch* s = *out;
   if (s && s->cap >= c2) return PT_OK;
@@ -714,9 +927,14 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
   const void* kp = o->precision ? (const void*)k_propagate<1> : (const void*)k_propagate<0>;
   const void* ks = o->precision ? (const void*)k_sample<1> : (const void*)k_sample<0>;
-  const int rb_p = resident_blocks(kp), rb_s = resident_blocks(ks);
+  const int rb_p = resident_blocks(kp);
+  int rb_s = resident_blocks(ks);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
   const int64_t cap = S->cap;
+  {  // a small ring gets fewer sampler blocks so their slot pools stay a quarter of it at most
+    const int64_t lim = cap / (4 * (int64_t)kWarps * kOutChunk);
+    if (rb_s > lim) rb_s = (int)(lim > 0 ? lim : 1);
+  }
   const int64_t feed_max = cap / 16;          // primaries added per refill
   uint64_t head = 0, tail = 0;
   int64_t fed = 0, nl = 1, nw = 0;
@@ -733,7 +951,10 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
       fed += m;
       live += m;
     }
-    int64_t k = (cap - live) / 2;
+    // daughters take at most 2 slots per entry, plus up to one partly used
+    // output chunk per sampler warp
+    const int64_t slack = (int64_t)rb_s * kWarps * kOutChunk;
+    int64_t k = (cap - live - slack) / 2;
     if (k > live) k = live;
     if (k > S->list_cap) k = S->list_cap;
     if (k <= 0) return PT_OOM;                // unreachable: live stays below the capacity

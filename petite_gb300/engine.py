@@ -140,6 +140,13 @@ class SMEngine:
         self._keep["ns_y"] = f64(ns_y)
         self._keep["ns_x32"] = torch.as_tensor(ns_x.astype(np.float32), device=dev)
         self._keep["ns_y32"] = torch.as_tensor(ns_y.astype(np.float32), device=dev)
+        slopes = []
+        for x, y in tables.nsigma:
+            sl = np.zeros_like(x)
+            sl[:-1] = (y[1:] - y[:-1]) / (x[1:] - x[:-1])
+            slopes.append(sl)
+        self._keep["ns_s32"] = torch.as_tensor(np.concatenate(slopes).astype(np.float32), device=dev)
+        self._keep["map_energy32"] = torch.as_tensor(tables.map_energy.astype(np.float32), device=dev)
         pt = _lib.PtTables()
         for p in range(_lib.N_PROC):
             pt.map_base[p] = int(tables.map_base[p])
@@ -157,6 +164,15 @@ class SMEngine:
         pt.ns_y = self._keep["ns_y"].data_ptr()
         pt.ns_x32 = self._keep["ns_x32"].data_ptr()
         pt.ns_y32 = self._keep["ns_y32"].data_ptr()
+        pt.ns_s32 = self._keep["ns_s32"].data_ptr()
+        pt.map_energy32 = self._keep["map_energy32"].data_ptr()
+        for sl, (x, _) in enumerate(tables.nsigma):
+            pt.ns_lnx0[sl] = float(np.log(x[0]))
+            pt.ns_invdlog[sl] = float((len(x) - 1) / np.log(x[-1] / x[0]))
+        for p in range(_lib.N_PROC):
+            e = tables.map_energy[tables.map_base[p]:tables.map_base[p] + tables.map_rows[p]]
+            pt.map_lnE0[p] = float(np.log(e[0]))
+            pt.map_invdlog[p] = float((len(e) - 1) / np.log(e[-1] / e[0])) if len(e) > 1 else 0.0
         pt.Z, pt.A, pt.rho = tables.Z, tables.A, tables.rho
         pt.dEdx_GeV_per_m = tables.dEdx * 0.1
         pt.Eg_min, pt.Ee_min = tables.Eg_min, tables.Ee_min
