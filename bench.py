@@ -1,19 +1,27 @@
 #!/usr/bin/env python
 """Throughput of the shower transport path on one GB300 (or N, one rank each).
 
-A step transports one batch of primaries of the selected workload to the end
-of their showers.  The metric is particle-steps/s: one particle-step is one
-visit of a live particle in the transport loop (propagation with all its
-substeps, process choice and the sampled interaction), i.e. one row of
-PETITE's output list.  Every step uses fresh random streams (primary index
-offset by the step number).
+Headline workload (default): batched SM showers -- 10^6 primaries, species
+uniform over {e-, e+, gamma}, E0 log-uniform on [0.1, 100] GeV along +z, lead,
+energy cut 0.010 GeV, seed 1 -- transported by the mixed-precision engine
+(float32 sampling and scattering, float64 energies).  A step transports one
+such batch to the end of every shower; each step uses fresh random streams
+(primary indices offset by the step number).
 
-Prints one JSON line (rank 0).  ``--impl reference`` times the CPU oracle
-(a restatement of PETITE's transport loop) on the host cores instead.
+Metric: particle-steps/s.  One particle-step is one visit of a live particle
+in the transport loop (propagation with its substeps, process choice and the
+sampled interaction), i.e. one row of PETITE's output list.
+
+The same line carries the plain float64 engine on a same-stream subsample
+(and the matched-spectra statistics between the two), the roofline figures,
+the end-to-end figure through Shower.run_tallied (pinned host inputs in, host
+tallies out) and the CPU oracle baseline.  ``--impl reference`` times the CPU
+oracle (a restatement of PETITE's transport loop) alone on the host cores.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -29,16 +37,22 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s on 1 GB300: batched mixed-precision vs plain FP64 GPU, matched spectra"
 
 WORKLOADS = {
-    # 1,000 electrons at 1 GeV along +z in graphite, cut 0.010 GeV, float64 throughout
+    "sm_batched_lead_1M": dict(target="lead", cut=0.010, n=1_000_000, species=(11, -11, 22), emin=0.1, emax=100.0,
+                               seed=1, precision="mixed", fp64_sample=20_000, cpu_sample=160, mode="batch"),
     "sm_e1gev_graphite_1k": dict(target="graphite", cut=0.010, n=1000, species=(11,), emin=1.0, emax=1.0,
-                                 seed=0, precision="fp64"),
+                                 seed=0, precision="fp64", fp64_sample=1000, cpu_sample=400, mode="records"),
 }
 
-# algorithmic HBM bytes per particle-step of the float64 record engine:
-# read the live row (p0 32, r0 24, pid 4, mass 8, pkey 8, weight 8, gen 4,
-# primary 4, live index 8 = 100), write its final state (pf 32, rf 24,
-# draws 4 = 60) and write the one row it creates on average (176).
-BYTES_PER_STEP = 336
+# Algorithmic HBM bytes per particle-step of the batched engine (ring entries,
+# structure of arrays): propagation reads the entry (E, p, r, mass 64 B; key
+# 8 B; pid, primary 8 B = 80 B) and parks the post-propagation state (E, p, r
+# 56 B; draw, map row 8 B = 64 B) plus its task index (write 4 B, read 4 B);
+# the sampler reads the parked task (92 B) and writes on average one daughter
+# (88 B).  Tables (maps, n*sigma) are L2-resident and not counted.
+BYTES_PER_STEP_BATCH = 80 + 64 + 8 + 92 + 88
+# Record engine: read the live row (100 B), write its final state (60 B) and
+# the one row it creates on average (176 B).
+BYTES_PER_STEP_RECORDS = 336
 
 
 def make_primaries(w, n, offset):
@@ -55,7 +69,7 @@ def make_primaries(w, n, offset):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons while the timed region runs."""
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -64,6 +78,7 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
@@ -75,7 +90,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc:
             self.proc.terminate()
             try:
@@ -88,7 +102,7 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+        for l in self.lines:
             f = [x.strip() for x in l.split(",")]
             try:
                 sm.append(float(f[1]))
@@ -103,7 +117,7 @@ class ClockSampler:
 
 
 def cpu_oracle_worker(args):
-    """Runs the oracle on a slice of primaries (spawned process)."""
+    """Runs the CPU oracle on a slice of primaries (spawned process)."""
     sys.path.insert(0, ROOT)
     from oracle.shower import OracleShower, OracleTables
     target, cut, seed, p0, pid, mass, first = args
@@ -119,24 +133,25 @@ def cpu_baseline(w, n_sample, cores=None):
     import multiprocessing as mp
     cores = cores or os.cpu_count()
     p0, pid, m = make_primaries(w, n_sample, offset=10_000)
-    chunks = np.array_split(np.arange(n_sample), cores * 4)
-    jobs = [(w["target"], w["cut"], w["seed"], p0[c], pid[c], m[c], int(c[0]) if len(c) else 0) for c in chunks if len(c)]
+    order = np.argsort(-p0[:, 0])                      # large showers first for balance
+    chunks = [order[k::cores * 2] for k in range(cores * 2)]
+    jobs = [(w["target"], w["cut"], w["seed"], p0[c], pid[c], m[c], 0) for c in chunks if len(c)]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
         rows = sum(pool.map(cpu_oracle_worker, jobs))
     dt = time.perf_counter() - t0
     return {"value": rows / dt, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n_sample} primaries of the workload ({rows} particle-steps) in {dt:.1f} s, "
-                      f"oracle (CPU restatement of PETITE's loop) over {cores} spawned processes"}
+            "sample": f"{n_sample} primaries drawn like the workload ({rows} particle-steps) in {dt:.1f} s: "
+                      f"oracle (CPU restatement of PETITE's transport loop) over {cores} spawned processes"}
 
 
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
-        import torch.distributed as dist
         import torch
+        import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
         return dist, rank, ws
@@ -147,143 +162,270 @@ def run_reference(args, w, name):
     dist, rank, ws = dist_setup()
     if rank != 0:
         return
-    n_sample = args.cpu_sample
-    vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
-    for s in range(args.steps):
-        cb = cpu_baseline(w, n_sample)
+    vals, cb = [], None
+    for _ in range(args.steps):
+        cb = cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
         vals.append(cb["value"])
     v = float(np.median(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "target": w["target"], "cut_GeV": w["cut"], "primaries_per_step": n_sample},
+            "config": {"workload": name, "target": w["target"], "cut_GeV": w["cut"],
+                       "primaries_per_step": args.cpu_sample or w["cpu_sample"]},
             "cpu_baseline": {**cb, "value": v},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="sm_e1gev_graphite_1k", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-sample", type=int, default=400)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    args = ap.parse_args()
-    w = WORKLOADS[args.workload]
-    if args.impl == "reference":
-        return run_reference(args, w, args.workload)
+def matched_stats(a, b):
+    """Same-stream comparison of two tally sets (float64 vs mixed)."""
+    from scipy import stats
+    ca, cb = a["primary_count"], b["primary_count"]
+    ea, eb = a["primary_edep"], b["primary_edep"]
+    out = {"identical_showers": float(np.mean(ca == cb)),
+           "steps_rel_diff": (b["steps"] - a["steps"]) / a["steps"],
+           "E_deposited_rel_diff": (b["E_deposited"] - a["E_deposited"]) / a["E_deposited"],
+           "ks_p_multiplicity": float(stats.ks_2samp(ca, cb).pvalue),
+           "ks_p_edep": float(stats.ks_2samp(ea, eb).pvalue)}
+    ha, hb = a["hist"].astype(float), b["hist"].astype(float)
+    for kind, nm in ((0, "energy"), (1, "angle"), (2, "depth")):
+        x, y = ha[kind].ravel(), hb[kind].ravel()
+        mk = (x + y) > 0
+        chi2 = float(np.sum((x[mk] - y[mk]) ** 2 / (x[mk] + y[mk])))
+        out[f"chi2_p_{nm}"] = float(stats.chi2.sf(chi2, max(int(mk.sum()) - 1, 1)))
+    return out
 
+
+def bench_batch(args, w, name, dist, rank, ws):
     import torch
-    dist, rank, ws = dist_setup()
     from petite_gb300 import Shower
+    from petite_gb300.engine import ParticleStore  # noqa: F401  (ensures the package imports)
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     sh = Shower(None, w["target"], w["cut"], seed=w["seed"], precision=w["precision"], device=dev)
     eng = sh._engine
-    opts = sh._opts(True, w["precision"])
-    n = w["n"]
+    n = args.primaries or w["n"]
+    cap = 1 << 25
+    zmax = 30.0 * 0.0056 if w["target"] == "lead" else 1.0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
 
-    def one_step(step):
+    def stage(step):
         p0, pid, m = make_primaries(w, n, offset=step * ws + rank)
-        opts.primary_offset = (step * ws + rank) * n
-        st, rows = eng.run_sm(p0, np.zeros((n, 3)), pid, m, np.ones(n), opts)
-        return st, rows
+        return (torch.as_tensor(np.ascontiguousarray(p0.T), device=dev), torch.zeros((3, n), dtype=torch.float64, device=dev),
+                torch.as_tensor(pid, device=dev), torch.as_tensor(m, device=dev))
 
+    def device_step(step, precision, tally, inputs):
+        opts = sh._opts(True, precision)
+        opts.primary_offset = (step * ws + rank) * n
+        P0, R0, PID, M = inputs
+        stream = torch.cuda.current_stream(dev)
+        flush.zero_()
+        tally.zero_()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s = eng.lib.pt_run_batch(eng.handle, C.c_void_p(P0.data_ptr()), C.c_void_p(R0.data_ptr()),
+                                 C.c_void_p(PID.data_ptr()), C.c_void_p(M.data_ptr()), P0.shape[1], C.byref(opts),
+                                 C.byref(tally.abi()), cap, C.c_void_p(stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if s != 0:
+            raise RuntimeError(f"pt_run_batch status {s}")
+        return e0.elapsed_time(e1) / 1e3
+
+    tally = eng.new_tally(n, zmax)
     for s in range(args.warmup):
-        one_step(1000 + s)
-    # device-timed steps (inputs resident: the primaries are staged before the timer starts)
-    times, rows_tot, launches = [], 0, 0
+        device_step(1000 + s, w["precision"], tally, stage(1000 + s))
+    times, steps_done, launches = [], 0, 0
     with ClockSampler(dev.index or 0) as clk:
         for s in range(args.steps):
-            flush.zero_()
-            p0, pid, m = make_primaries(w, n, offset=s * ws + rank)
-            opts.primary_offset = (s * ws + rank) * n
-            from petite_gb300.engine import ParticleStore
-            cap = int(np.sum(2.0 * p0[:, 0] / w["cut"]) + 16 * n)
-            st = ParticleStore(cap, dev)
-            st.t["p0"][:, :n] = torch.as_tensor(p0.T, device=dev)
-            st.t["pid"][:n] = torch.as_tensor(pid, device=dev)
-            st.t["mass"][:n] = torch.as_tensor(m, device=dev)
-            st.t["weight"][:n] = 1.0
-            abi = st.abi()
-            import ctypes as C
-            nrows = C.c_int64()
-            if dist:
-                dist.barrier()
-            torch.cuda.synchronize(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            stream = torch.cuda.current_stream(dev)
-            e0.record(stream)
-            status = eng.lib.pt_run_sm(eng.handle, C.byref(abi), n, C.byref(opts), C.byref(nrows),
-                                       C.c_void_p(stream.cuda_stream))
-            e1.record(stream)
-            torch.cuda.synchronize(dev)
-            if status != 0:
-                raise RuntimeError(f"pt_run_sm status {status}")
-            times.append(e0.elapsed_time(e1) / 1e3)
-            rows_tot += nrows.value
+            inputs = stage(s)
+            times.append(device_step(s, w["precision"], tally, inputs))
+            steps_done += tally.summary()["steps"]
             launches += eng.last_run_stats()[0]
     t_local = float(sum(times))
-    rows_local = rows_tot
     if dist:
         t = torch.tensor([t_local], device=dev)
-        r = torch.tensor([rows_local], device=dev, dtype=torch.float64)
+        r = torch.tensor([float(steps_done)], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dist.all_reduce(r, op=dist.ReduceOp.SUM)
-        t_max, rows_all = float(t.item()), float(r.item())
+        t_max, steps_all = float(t.item()), float(r.item())
     else:
-        t_max, rows_all = t_local, float(rows_local)
-    value = rows_all / t_max
+        t_max, steps_all = t_local, float(steps_done)
+    value = steps_all / t_max
 
-    # end-to-end through the public API: host primaries in, host records out
-    e2e_rows, e2e_t, h2d, d2h = 0, 0.0, 0, 0
-    for s in range(args.steps):
+    # plain float64 engine vs mixed on the same first primaries and streams
+    nf = min(w["fp64_sample"], n)
+    sub = tuple(x[..., :nf].contiguous() for x in stage(0))
+    res = {}
+    for prec in ("fp64", "mixed"):
+        tl = eng.new_tally(nf, zmax)
+        dt = device_step(0, prec, tl, sub)
+        r_ = tl.summary()
+        r_.update(hist=tl.hist.cpu().numpy(), primary_count=tl.primary_count.cpu().numpy(),
+                  primary_edep=tl.primary_edep.cpu().numpy(), seconds=dt)
+        res[prec] = r_
+    fp64_rate = res["fp64"]["steps"] / res["fp64"]["seconds"]
+    mixed_sub_rate = res["mixed"]["steps"] / res["mixed"]["seconds"]
+    matched = matched_stats(res["fp64"], res["mixed"])
+
+    # end to end through the public API: pinned host inputs, host tallies back
+    e2e_steps, e2e_t, h2d, d2h = 0, 0.0, 0, 0
+    for s in range(min(args.steps, 2)):
         p0, pid, m = make_primaries(w, n, offset=500 + s * ws + rank)
+        p0h = torch.as_tensor(p0).pin_memory()
+        pidh = torch.as_tensor(pid).pin_memory()
+        mh = torch.as_tensor(m).pin_memory()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        b = sh.generate_showers(p0, pid=pid, mass=m, precision=w["precision"], first_primary=(500 + s * ws + rank) * n)
+        out = sh.run_tallied(p0h, pidh, mh, precision=w["precision"], first_primary=(500 + s * ws + rank) * n,
+                             z_max=zmax, queue_capacity=cap)
         torch.cuda.synchronize(dev)
         e2e_t += time.perf_counter() - t0
-        e2e_rows += b.n
-        h2d += p0.nbytes + pid.nbytes + m.nbytes + 8 * n + 24 * n
-        d2h += b.n * (16 * 8 + 6 * 4 + 2 * 8)
-    e2e = {"value": e2e_rows / e2e_t, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d // args.steps,
-           "d2h_bytes_per_step": d2h // args.steps}
-
+        e2e_steps += out["steps"]
+        h2d += p0.nbytes + pid.nbytes + m.nbytes
+        d2h += out["hist"].nbytes + out["primary_count"].nbytes + out["primary_edep"].nbytes + 16 * 8 + 8 * 8
+    ne2e = min(args.steps, 2)
+    e2e = {"value": e2e_steps / e2e_t, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d // ne2e,
+           "d2h_bytes_per_step": d2h // ne2e}
     if rank != 0:
         return
-    achieved = rows_all * BYTES_PER_STEP / t_max / 1e9
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    cb = None
-    if not args.no_cpu_baseline:
-        cb = cpu_baseline(w, args.cpu_sample)
+    achieved = value * BYTES_PER_STEP_BATCH / 1e9
+    cb = None if args.no_cpu_baseline else cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if w["precision"] == "fp64" else "f32+f64",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "target": w["target"], "cut_GeV": w["cut"],
-                   "primaries_per_step": n, "precision": w["precision"], "l2": "flushed (256 MB write) before each step",
-                   "parallelism": f"replicas{ws}"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": name, "primaries_per_step": n, "species": list(w["species"]),
+                   "E0_GeV": [w["emin"], w["emax"]], "target": w["target"], "cut_GeV": w["cut"],
+                   "precision": w["precision"], "seed": w["seed"], "l2": "flushed (256 MB write) before each step",
+                   "parallelism": f"replicas{ws}", "ring_capacity": cap},
+        "fp64_engine": {"value": fp64_rate, "unit": "particle-steps/s", "sample_primaries": nf,
+                        "mixed_on_same_sample": mixed_sub_rate, "mixed_over_fp64": mixed_sub_rate / fp64_rate},
+        "matched_spectra": matched,
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                     "traffic": None, "bytes_per_step": BYTES_PER_STEP_BATCH,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                     "note": "compute-bound path: HBM fraction of the algorithmic ring traffic; see profiles/"},
         "cpu_baseline": cb,
         "clocks": clk.summary(),
-        "particle_steps": rows_all,
+        "particle_steps": steps_all,
     }
     print(json.dumps(line))
+
+
+def bench_records(args, w, name, dist, rank, ws):
+    import torch
+    from petite_gb300 import Shower
+    from petite_gb300.engine import ParticleStore
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    sh = Shower(None, w["target"], w["cut"], seed=w["seed"], precision="fp64", device=dev)
+    eng = sh._engine
+    opts = sh._opts(True, "fp64")
+    n = args.primaries or w["n"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step(s):
+        p0, pid, m = make_primaries(w, n, offset=s * ws + rank)
+        opts.primary_offset = (s * ws + rank) * n
+        cap = int(np.sum(2.0 * p0[:, 0] / w["cut"]) + 16 * n)
+        st = ParticleStore(cap, dev)
+        st.t["p0"][:, :n] = torch.as_tensor(p0.T, device=dev)
+        st.t["pid"][:n] = torch.as_tensor(pid, device=dev)
+        st.t["mass"][:n] = torch.as_tensor(m, device=dev)
+        st.t["weight"][:n] = 1.0
+        abi = st.abi()
+        nrows = C.c_int64()
+        flush.zero_()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        stream = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        status = eng.lib.pt_run_sm(eng.handle, C.byref(abi), n, C.byref(opts), C.byref(nrows),
+                                   C.c_void_p(stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if status != 0:
+            raise RuntimeError(f"pt_run_sm status {status}")
+        return e0.elapsed_time(e1) / 1e3, nrows.value
+
+    for s in range(args.warmup):
+        step(1000 + s)
+    times, rows, launches = [], 0, 0
+    with ClockSampler(dev.index or 0) as clk:
+        for s in range(args.steps):
+            dt, r = step(s)
+            times.append(dt)
+            rows += r
+            launches += eng.last_run_stats()[0]
+    t_max, rows_all = float(sum(times)), float(rows)
+    value = rows_all / t_max
+    e2e_rows, e2e_t, h2d, d2h = 0, 0.0, 0, 0
+    for s in range(args.steps):
+        p0, pid, m = make_primaries(w, n, offset=500 + s * ws + rank)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        b = sh.generate_showers(p0, pid=pid, mass=m, first_primary=(500 + s * ws + rank) * n)
+        torch.cuda.synchronize(dev)
+        e2e_t += time.perf_counter() - t0
+        e2e_rows += b.n
+        h2d += p0.nbytes + pid.nbytes + m.nbytes + 32 * n
+        d2h += b.n * (16 * 8 + 6 * 4 + 2 * 8)
+    if rank != 0:
+        return
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = value * BYTES_PER_STEP_RECORDS / 1e9
+    cb = None if args.no_cpu_baseline else cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "primaries_per_step": n, "target": w["target"], "cut_GeV": w["cut"],
+                   "precision": "fp64", "l2": "flushed (256 MB write) before each step",
+                   "parallelism": f"replicas{ws}"},
+        "e2e": {"value": e2e_rows / e2e_t, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "bytes_per_step": BYTES_PER_STEP_RECORDS},
+        "cpu_baseline": cb, "clocks": clk.summary(), "particle_steps": rows_all}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sm_batched_lead_1M", choices=sorted(WORKLOADS))
+    ap.add_argument("--primaries", type=int, default=0, help="override primaries per step")
+    ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, w, args.workload)
+    dist, rank, ws = dist_setup()
+    if w["mode"] == "batch":
+        bench_batch(args, w, args.workload, dist, rank, ws)
+    else:
+        bench_records(args, w, args.workload, dist, rank, ws)
 
 
 if __name__ == "__main__":

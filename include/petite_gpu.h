@@ -74,6 +74,9 @@ typedef struct pt_tables {
   float ns_lnx0[PT_N_NSIGMA];
   float ns_invdlog[PT_N_NSIGMA];
   const float* map_energy32;      /* [n_rows] */
+  const float* map_cnorm32;       /* [n_rows] K_process / (max_F * neval) for the float32 acceptance ratio;
+                                     K_process: 8 alpha^3 Z^2 a0^4 (Brem, MuonBrem, PairProd), pi alpha^2
+                                     (Comp, MuonE), 2 pi alpha^2 (Ann, Moller), pi alpha^2 / 2 (Bhabha) */
   float map_lnE0[PT_N_PROCESSES];
   float map_invdlog[PT_N_PROCESSES];
   /* target and thresholds */

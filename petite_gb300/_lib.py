@@ -30,7 +30,8 @@ class PtTables(C.Structure):
         ("ns_base", C.c_int32 * N_NS), ("ns_len", C.c_int32 * N_NS), ("ns_x", C.c_void_p), ("ns_y", C.c_void_p),
         ("ns_x32", C.c_void_p), ("ns_y32", C.c_void_p), ("ns_s32", C.c_void_p),
         ("ns_lnx0", C.c_float * N_NS), ("ns_invdlog", C.c_float * N_NS),
-        ("map_energy32", C.c_void_p), ("map_lnE0", C.c_float * N_PROC), ("map_invdlog", C.c_float * N_PROC),
+        ("map_energy32", C.c_void_p), ("map_cnorm32", C.c_void_p),
+        ("map_lnE0", C.c_float * N_PROC), ("map_invdlog", C.c_float * N_PROC),
         ("Z", C.c_double), ("A", C.c_double), ("rho", C.c_double), ("dEdx_GeV_per_m", C.c_double),
         ("Eg_min", C.c_double), ("Ee_min", C.c_double),
         ("min_calc_electron", C.c_double), ("min_calc_positron", C.c_double),

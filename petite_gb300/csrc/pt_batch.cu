@@ -63,6 +63,7 @@ struct WaveCtx {
   uint64_t head, tail;                // ring positions of this wave's first entry and of the append point
   int64_t n_in;                       // entries in this wave
   int64_t list_cap;                   // entries per process list
+  int out_chunk;                      // output slots reserved per warp at a time (0 = exact)
   int32_t* idx;                       // [8][list_cap] ring indices of sampling tasks by process
   unsigned long long* ctr;            // [0] head1, [1] head2, [2] appended, [8..15] per-process counts
   int* status;
@@ -173,12 +174,20 @@ struct OutPool {
 constexpr int kOutChunk = 64;
 
 // All lanes call.  Writes this lane's slot offsets (want of them) to slot[].
-__device__ __forceinline__ void out_take(OutPool& P, unsigned long long* ctr, int want, uint64_t* slot) {
+// chunk == 0 reserves exactly what is asked (small waves: no dead slots).
+__device__ __forceinline__ void out_take(OutPool& P, unsigned long long* ctr, int want, uint64_t* slot, int chunk) {
   const unsigned b1 = __ballot_sync(kFull, want >= 1), b2 = __ballot_sync(kFull, want >= 2);
   const unsigned total = __popc(b1) + __popc(b2);
   if (!total) return;
   const unsigned lt = lanemask_lt();
   const uint64_t prefix = __popc(b1 & lt) + __popc(b2 & lt);
+  if (chunk == 0) {
+    unsigned long long bb = 0;
+    if ((threadIdx.x & 31) == 0) bb = atomicAdd(ctr, (unsigned long long)total);
+    bb = __shfl_sync(kFull, bb, 0);
+    for (int j = 0; j < want; ++j) slot[j] = bb + prefix + j;
+    return;
+  }
   const uint64_t avail = P.end - P.next;
   uint64_t base = 0;
   if (avail < total) {
@@ -518,8 +527,10 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
         edep = eloss + E;
       }
     }
-    primary_tally(c.tally, finish, prim, edep);
-    publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
+    if (__any_sync(kFull, finish)) {
+      primary_tally(c.tally, finish, prim, edep);
+      publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
+    }
   }
   publish_rest(c, buf, bcnt);
   flush_tally(c.tally, L, sh_hist);
@@ -633,17 +644,100 @@ __device__ void kin_mixed(int process, int pid, double E, double mass, const Map
   }
 }
 
+// An accepted proposal waiting for its final-state kinematics.
+template <int PREC> struct KinEntry;
+template <> struct KinEntry<0> { uint32_t i; int32_t process; double x[4]; double ph; };
+template <> struct KinEntry<1> { uint32_t i; int32_t process; MapPt32 x[4]; float ph; };
+constexpr int kKinQ = 64;
+
+// Kinematics, lab rotation and daughter output for up to 32 queued accepts,
+// one per lane (sample_scattering, shower.py:467-507).  All lanes call.
+template <int PREC>
+__device__ void run_kinematics(const WaveCtx& c, KinEntry<PREC>* kq, int count, OutPool& opool, LocalTally& L) {
+  const int lane = threadIdx.x & 31;
+  const bool on = lane < count;
+  Daughter dg[2];
+  int want = 0, prim = 0, gen = 0;
+  uint64_t key = 0, i = 0;
+  double x0 = 0, y0 = 0, z0 = 0, below = 0.0;
+  if (on) {
+    const KinEntry<PREC>& e = kq[lane];
+    i = e.i;
+    const int process = e.process;
+    const double E = c.q.E[i], mass = c.q.mass[i];
+    const int pid = c.q.pid[i];
+    const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
+    if (PREC == 0) {
+      const double* xd = reinterpret_cast<const KinEntry<0>&>(e).x;
+      const double ph = reinterpret_cast<const KinEntry<0>&>(e).ph;
+      const Rot R = rotation_from(pf);
+      V4 a, b;
+      int pa, pb;
+      switch (process) {
+        case PT_BREM: case PT_MUONBREM: kin_brem(E, mass, xd, ph, a, b); pa = pid; pb = 22; break;
+        case PT_PAIRPROD: kin_pairprod(E, xd, ph, a, b); pa = -11; pb = 11; break;
+        case PT_COMP: kin_compton(E, xd[0], ph, a, b); pa = 11; pb = 22; break;
+        case PT_ANN: kin_ann(E, xd[0], ph, a, b); pa = 22; pb = 22; break;
+        case PT_MOLLER: case PT_BHABHA: kin_ee(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
+        default: kin_mue(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
+      }
+      const V4 la = to_lab(R, a), lb = to_lab(R, b);
+      dg[0] = {la.e, la.x, la.y, la.z, pa};
+      dg[1] = {lb.e, lb.x, lb.y, lb.z, pb};
+    } else {
+      const KinEntry<1>& f = reinterpret_cast<const KinEntry<1>&>(e);
+      KinOut k;
+      kin_mixed(process, pid, E, mass, f.x, f.ph, k);
+      const float fx = (float)pf[1], fy = (float)pf[2], fz = (float)pf[3];
+      const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
+      const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
+      const Rot32 R = rot32_from(pd);
+      for (int j = 0; j < 2; ++j) {
+        const float3 v = rot32_apply(R, k.d[j]);
+        dg[j] = {k.E[j], (double)(k.P[j] * v.x), (double)(k.P[j] * v.y), (double)(k.P[j] * v.z), k.pid[j]};
+      }
+    }
+    want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
+    for (int j = 0; j < 2; ++j)
+      if (!(dg[j].E > c.min_energy)) { ++L.below; L.e_below += dg[j].E; below += dg[j].E; }
+    prim = c.q.prim[i];
+    key = c.q.key[i];
+    gen = c.q.gen[i];
+    x0 = c.q.x[i]; y0 = c.q.y[i]; z0 = c.q.z[i];
+    if (below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
+  }
+  uint64_t slots[2] = {0, 0};
+  out_take(opool, c.ctr + 2, want, slots, c.out_chunk);
+  int slot = 0;
+  for (int j = 0; j < 2; ++j) {
+    if (!on || !(dg[j].E > c.min_energy)) continue;
+    const uint64_t q = (c.tail + slots[slot++]) & c.mask;
+    ++L.pushed;
+    c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
+    c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
+    c.q.mass[q] = table_mass(dg[j].pid);
+    c.q.key[q] = daughter_key(key, j);
+    c.q.pid[q] = dg[j].pid;
+    c.q.prim[q] = prim;
+    c.q.gen[q] = gen + 1;
+  }
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
   __shared__ unsigned long long sh_off[9];
+  __shared__ KinEntry<PREC> sh_kq[kWarps][kKinQ];
   if (threadIdx.x == 0) {
     unsigned long long acc = 0;
     for (int p = 0; p < 8; ++p) { sh_off[p] = acc; acc += c.ctr[8 + p]; }
     sh_off[8] = acc;
   }
   __syncthreads();
+  KinEntry<PREC>* kq = sh_kq[threadIdx.x / 32];
+  int kcount = 0;                      // warp-uniform
   const int64_t total = (int64_t)sh_off[8];
   const Tabs& T = c.T;
+  const int lane = threadIdx.x & 31;
   LocalTally L;
   WarpPool pool;
   OutPool opool;
@@ -677,7 +771,6 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
         const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), rng.k0, rng.k1), rng.s0, rng.s1);
         rng.spare = (uint64_t)o.z | ((uint64_t)o.w << 32);
       }
-      maxF = T.t.map_maxF[row];
       neval = T.t.map_neval[row];
       d = process_dim(process);
       cap = c.max_n_integrators * (int64_t)neval;
@@ -685,36 +778,39 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
       for (int k = 0; k < d; ++k) {
         const int64_t off = T.t.grid_offset[(int64_t)row * 4 + k];
         ninc[k] = T.t.grid_ninc[(int64_t)row * 4 + k];
-        g64[k] = T.t.grid_nodes + off;
-        g32[k] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
+        if (PREC == 0) g64[k] = T.t.grid_nodes + off;
+        else g32[k] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
       }
-      if (PREC == 1) {
-        const double inv_norm = 1.0 / (maxF * neval);
-        const double Z2 = T.t.Z * T.t.Z;
+      if (PREC == 0) {
+        maxF = T.t.map_maxF[row];
+      } else {
+        const float Ef = (float)E, Cr = __ldg(T.t.map_cnorm32 + row), a0sq = (float)T.a0sq;
         switch (process) {
-          case PT_BREM: brem32_setup(S32, E, kMe, T.t.Eg_min, T.a0sq, Z2, inv_norm); break;
-          case PT_MUONBREM: brem32_setup(S32, E, kMmu, T.t.Eg_min, T.a0sq, Z2, inv_norm); break;
-          case PT_PAIRPROD: pair32_setup(S32, E, T.a0sq, Z2, inv_norm); break;
-          case PT_COMP: comp32_setup(S32, E, inv_norm); break;
-          case PT_ANN: ann32_setup(S32, E, T.t.Eg_min, inv_norm); break;
-          case PT_MOLLER: moller32_setup(S32, E, T.t.Ee_min, inv_norm); break;
-          case PT_BHABHA: bhabha32_setup(S32, E, T.t.Ee_min, inv_norm); break;
-          default: muone32_setup(S32, E, T.t.Ee_min, inv_norm); break;
+          case PT_BREM: brem32_setup(S32, Ef, (float)kMe, (float)T.t.Eg_min, a0sq, Cr); break;
+          case PT_MUONBREM: brem32_setup(S32, Ef, (float)kMmu, (float)T.t.Eg_min, a0sq, Cr); break;
+          case PT_PAIRPROD: pair32_setup(S32, Ef, a0sq, Cr); break;
+          case PT_COMP: comp32_setup(S32, Ef, Cr); break;
+          case PT_ANN: ann32_setup(S32, Ef, (float)T.t.Eg_min, Cr); break;
+          case PT_MOLLER: moller32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
+          case PT_BHABHA: bhabha32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
+          default: muone32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
         }
       }
       active = true;
     }
     bool accept = false;
-    double xd[4] = {0, 0, 0, 0};
-    MapPt32 xm[4];
+    KinEntry<PREC> ent;
     if (active) {
       // ---- one proposal (d uniforms for y, then the accept uniform)
       if (PREC == 0) {
+        double* xd = reinterpret_cast<KinEntry<0>&>(ent).x;
         double jac = 1.0;
         for (int k = 0; k < d; ++k) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
         const double f = dsigma_any(T, process, xd, E);
         accept = maxF * rng.u() < (jac / neval) * f;
+        if (accept) reinterpret_cast<KinEntry<0>&>(ent).ph = 2.0 * kPi * rng.u();
       } else {
+        MapPt32* xm = reinterpret_cast<KinEntry<1>&>(ent).x;
         float jac = 1.f;
         for (int k = 0; k < d; ++k) xm[k] = map_dim32(g32[k], ninc[k], rng.uf(), jac);
         float r;
@@ -728,83 +824,44 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
           default: r = muone32_ratio(S32, xm[0], jac); break;
         }
         accept = rng.uf() < r;
+        if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf();
       }
       ++props;
       ++L.props;
-      if (!accept && props >= cap) {
+      if (accept) {
+        active = false;
+        ++L.sampled;
+      } else if (props >= cap) {
         raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
         active = false;
       }
     }
-    // ---- accepted: kinematics and daughters (sample_scattering, shower.py:467-507)
-    Daughter dg[2];
-    int want = 0;
-    int prim = 0;
-    double below = 0.0;
-    if (accept) {
-      active = false;
-      ++L.sampled;
-      const double mass = c.q.mass[i];
-      const int pid = c.q.pid[i];
-      const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
-      if (PREC == 0) {
-        const double ph = 2.0 * kPi * rng.u();
-        const Rot R = rotation_from(pf);
-        V4 a, b;
-        int pa, pb;
-        switch (process) {
-          case PT_BREM: case PT_MUONBREM: kin_brem(E, mass, xd, ph, a, b); pa = pid; pb = 22; break;
-          case PT_PAIRPROD: kin_pairprod(E, xd, ph, a, b); pa = -11; pb = 11; break;
-          case PT_COMP: kin_compton(E, xd[0], ph, a, b); pa = 11; pb = 22; break;
-          case PT_ANN: kin_ann(E, xd[0], ph, a, b); pa = 22; pb = 22; break;
-          case PT_MOLLER: case PT_BHABHA: kin_ee(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
-          default: kin_mue(E, xd[0], ph, a, b); pa = pid; pb = 11; break;
-        }
-        const V4 la = to_lab(R, a), lb = to_lab(R, b);
-        dg[0] = {la.e, la.x, la.y, la.z, pa};
-        dg[1] = {lb.e, lb.x, lb.y, lb.z, pb};
-      } else {
-        const float ph = 2.f * (float)kPi * rng.uf();
-        KinOut k;
-        kin_mixed(process, pid, E, mass, xm, ph, k);
-        const float fx = (float)pf[1], fy = (float)pf[2], fz = (float)pf[3];
-        const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
-        const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
-        const Rot32 R = rot32_from(pd);
-        for (int j = 0; j < 2; ++j) {
-          const float3 v = rot32_apply(R, k.d[j]);
-          dg[j] = {k.E[j], (double)(k.P[j] * v.x), (double)(k.P[j] * v.y), (double)(k.P[j] * v.z), k.pid[j]};
-        }
+    // ---- queue accepted proposals; run kinematics 32 at a time with all lanes
+    const unsigned am = __ballot_sync(kFull, accept);
+    if (am) {
+      if (accept) {
+        ent.i = (uint32_t)i;
+        ent.process = process;
+        kq[kcount + __popc(am & lanemask_lt())] = ent;
       }
-      want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
-      for (int j = 0; j < 2; ++j)
-        if (!(dg[j].E > c.min_energy)) { ++L.below; L.e_below += dg[j].E; below += dg[j].E; }
-      prim = c.q.prim[i];
-    }
-    if (accept && below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
-    uint64_t slots[2] = {0, 0};
-    out_take(opool, c.ctr + 2, want, slots);
-    if (want) {
-      int slot = 0;
-      const uint64_t key = c.q.key[i];
-      const int gen = c.q.gen[i];
-      const double x0 = c.q.x[i], y0 = c.q.y[i], z0 = c.q.z[i];
-      for (int j = 0; j < 2; ++j) {
-        if (!(dg[j].E > c.min_energy)) continue;
-        const uint64_t q = (c.tail + slots[slot++]) & c.mask;
-        ++L.pushed;
-        c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
-        c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
-        c.q.mass[q] = table_mass(dg[j].pid);
-        c.q.key[q] = daughter_key(key, j);
-        c.q.pid[q] = dg[j].pid;
-        c.q.prim[q] = prim;
-        c.q.gen[q] = gen + 1;
+      kcount += __popc(am);
+      __syncwarp();
+      if (kcount >= 32) {
+        run_kinematics<PREC>(c, kq, 32, opool, L);
+        __syncwarp();
+        KinEntry<PREC> carry;
+        const int rest = kcount - 32;
+        if (lane < rest) carry = kq[32 + lane];
+        __syncwarp();
+        if (lane < rest) kq[lane] = carry;
+        kcount = rest;
+        __syncwarp();
       }
     }
   }
-  // unused slots of the warp's last chunk become dead entries
-  for (uint64_t r = opool.next + (threadIdx.x & 31); r < opool.end; r += 32) c.q.pid[(c.tail + r) & c.mask] = 0;
+  if (kcount > 0) run_kinematics<PREC>(c, kq, kcount, opool, L);
+  // unused slots of the warp's last output chunk become dead entries
+  for (uint64_t r = opool.next + lane; r < opool.end; r += 32) c.q.pid[(c.tail + r) & c.mask] = 0;
   flush_tally(c.tally, L, nullptr);
 }
 
@@ -928,21 +985,20 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
   const void* kp = o->precision ? (const void*)k_propagate<1> : (const void*)k_propagate<0>;
   const void* ks = o->precision ? (const void*)k_sample<1> : (const void*)k_sample<0>;
   const int rb_p = resident_blocks(kp);
-  int rb_s = resident_blocks(ks);
+  const int rb_s = resident_blocks(ks);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
   const int64_t cap = S->cap;
-  {  // a small ring gets fewer sampler blocks so their slot pools stay a quarter of it at most
-    const int64_t lim = cap / (4 * (int64_t)kWarps * kOutChunk);
-    if (rb_s > lim) rb_s = (int)(lim > 0 ? lim : 1);
-  }
-  const int64_t feed_max = cap / 16;          // primaries added per refill
+  // A fed primary can grow to a few hundred live particles before its shower
+  // thins out, so primaries enter in small increments while the ring is
+  // mostly free.
+  const int64_t feed_max = cap / 1024 > 256 ? cap / 1024 : 256;
   uint64_t head = 0, tail = 0;
   int64_t fed = 0, nl = 1, nw = 0;
   while (fed < n || tail > head) {
     int64_t live = (int64_t)(tail - head);
-    if (fed < n && live < cap / 2) {
+    if (fed < n && live < cap / 8) {
       int64_t m = n - fed;
-      if (m > cap / 2 - live) m = cap / 2 - live;
+      if (m > cap / 8 - live) m = cap / 8 - live;
       if (m > feed_max) m = feed_max;
       k_feed<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(S->q, c.mask, tail, p0, r0, pid, mass, n, fed, m,
                                                           o->primary_offset);
@@ -951,13 +1007,23 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
       fed += m;
       live += m;
     }
-    // daughters take at most 2 slots per entry, plus up to one partly used
-    // output chunk per sampler warp
-    const int64_t slack = (int64_t)rb_s * kWarps * kOutChunk;
-    int64_t k = (cap - live - slack) / 2;
+    // Wave size: daughters take at most 2 slots per entry, plus at most one
+    // partly used output chunk per sampler warp (bounded with the largest
+    // grid); small waves reserve slots exactly and leave no dead entries.
+    c.out_chunk = kOutChunk;
+    int64_t k = (cap - live - (int64_t)rb_s * kWarps * kOutChunk) / 2;
     if (k > live) k = live;
     if (k > S->list_cap) k = S->list_cap;
-    if (k <= 0) return PT_OOM;                // unreachable: live stays below the capacity
+    if (k < 16 * 1024) {
+      c.out_chunk = 0;
+      k = (cap - live) / 2;
+      if (k > live) k = live;
+      if (k > S->list_cap) k = S->list_cap;
+    }
+    if (k <= 0) {                   // the live population filled the ring
+      hp.launches[0] = nl; hp.launches[1] = nw;
+      return PT_OOM;
+    }
     PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
     c.head = head;
     c.tail = tail;

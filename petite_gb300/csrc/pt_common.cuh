@@ -61,8 +61,12 @@ struct Rng {
     return (uint64_t)o.x | ((uint64_t)o.y << 32);
   }
   __device__ __forceinline__ double u() { return (double)(next_u64() >> 11) * 0x1p-53; }
-  // float form of the same draw (its top 24 bits); used by the float32 sampler
-  __device__ __forceinline__ float uf() { return (float)(next_u64() >> 40) * 0x1p-24f; }
+  // float form of the same draw (its top 24 bits); used by the float32 sampler.
+  // Converted from a 32-bit integer: 64-bit conversions run on the FP64 pipe.
+  __device__ __forceinline__ float uf() {
+    const uint32_t hi = (uint32_t)(next_u64() >> 32);
+    return __uint2float_rn(hi >> 8) * 0x1p-24f;
+  }
 };
 
 // --------------------------------------------------- non-contracting float64

@@ -46,16 +46,12 @@ struct Samp32 {
 };
 
 // ---- Brem / MuonBrem: dsigma_brem_dimensionless (all_processes.py:153-206)
-__device__ __forceinline__ void brem32_setup(Samp32& S, double E, double m, double Eg, double a0sq_me2_ratio,
-                                             double Z2, double inv_norm) {
-  // b = (a0 m)^2 with a0 = aa(Z, m_e); a0sq_me2_ratio = a0^2 (float64 on host)
-  const double b = a0sq_me2_ratio * m * m;
-  const double m2 = m * m;
-  const double C1 = 8.0 * kAlpha * kAlpha * kAlpha * Z2 * (b / m2) * (b / m2);   // 8 a^3 Z^2 b^2 / m^4
-  S.E = (float)E; S.m = (float)m; S.k = (float)(E / (2 * m)); S.span = (float)(E - m - Eg); S.Eg = (float)Eg;
-  S.b = (float)b;
-  S.C = (float)(C1 * inv_norm);
-  S.aux0 = (float)(E * (E - m - Eg));     // E * span (float64 product)
+// C_row = 8 alpha^3 Z^2 a0^4 / (max_F neval) for this map row (host table).
+__device__ __forceinline__ void brem32_setup(Samp32& S, float E, float m, float Eg, float a0sq, float C_row) {
+  S.E = E; S.m = m; S.k = E / (2.f * m); S.span = E - m - Eg; S.Eg = Eg;
+  S.b = a0sq * m * m;                         // (a0 m)^2
+  S.C = C_row;
+  S.aux0 = E * S.span;
 }
 __device__ __forceinline__ float brem32_ratio(const Samp32& S, const MapPt32* x, float jac) {
   const float w = fmaf(x[0].x, S.span, S.Eg);
@@ -82,13 +78,12 @@ __device__ __forceinline__ float brem32_ratio(const Samp32& S, const MapPt32* x,
 }
 
 // ---- PairProd: dsigma_pairprod_dimensionless (all_processes.py:546-622)
-__device__ __forceinline__ void pair32_setup(Samp32& S, double w, double a0sq, double Z2, double inv_norm) {
-  const double me = kMe, b = a0sq * me * me, m2 = me * me;
-  const double C1 = 8.0 * kAlpha * kAlpha * kAlpha * Z2 * (b / m2) * (b / m2);
-  S.E = (float)w; S.m = (float)me; S.k = (float)(w / (2 * me)); S.span = (float)(w - 2 * me);
-  S.b = (float)b;
-  S.C = (float)(C1 * inv_norm);
-  S.aux0 = (float)((w - 2 * me) / w);
+__device__ __forceinline__ void pair32_setup(Samp32& S, float w, float a0sq, float C_row) {
+  const float me = (float)kMe;
+  S.E = w; S.m = me; S.k = w / (2.f * me); S.span = w - 2.f * me;
+  S.b = a0sq * me * me;
+  S.C = C_row;
+  S.aux0 = S.span / w;
 }
 __device__ __forceinline__ float pair32_ratio(const Samp32& S, const MapPt32* x, float jac) {
   const float epp = fmaf(x[0].x, S.span, S.m);
@@ -115,10 +110,10 @@ __device__ __forceinline__ float pair32_ratio(const Samp32& S, const MapPt32* x,
 
 // ---- Compton (mV = 0): dsigma_compton_dCT (all_processes.py:639-742),
 // with s - m^2 = D = 2 E m, t = -D^2 (1+c)/(2s), s + t - m^2 = D (2m^2 + D(1-c))/(2s).
-__device__ __forceinline__ void comp32_setup(Samp32& S, double Eg, double inv_norm) {
-  const double me2 = kMe * kMe, D = 2 * Eg * kMe, s = me2 + D;
-  S.E = (float)D; S.m = (float)me2; S.span = (float)s;
-  S.C = (float)(kPi * kAlpha * kAlpha / s * inv_norm);   // PF * jac = pi a^2 / s
+__device__ __forceinline__ void comp32_setup(Samp32& S, float Eg, float C_row) {
+  const float me = (float)kMe, me2 = me * me, D = 2.f * Eg * me, s = me2 + D;
+  S.E = D; S.m = me2; S.span = s;
+  S.C = C_row / s;                            // PF * jac = pi alpha^2 / s
 }
 __device__ __forceinline__ float comp32_ratio(const Samp32& S, const MapPt32& c, float jac) {
   const float D = S.E, m2 = S.m, s = S.span;
@@ -132,13 +127,14 @@ __device__ __forceinline__ float comp32_ratio(const Samp32& S, const MapPt32& c,
 }
 
 // ---- Annihilation (mV = 0): dsigma_annihilation_dCT (all_processes.py:475-529)
-__device__ __forceinline__ void ann32_setup(Samp32& S, double Ee, double Eg_min, double inv_norm) {
-  const double me = kMe, s = 2.0 * me * (Ee + me);
-  const double ctMax = sqrt((Ee + me) / (Ee - me)) * (2 * me * (Ee - 2 * Eg_min + me)) / (2 * me * (Ee + me));
-  S.E = (float)s;
-  S.aux0 = (float)(4.0 * me * me / s);                 // 1 - b^2
-  S.aux1 = (float)(1.0 - ctMax);                       // ct > ctMax <=> 1-ct < 1-ctMax
-  S.C = (float)(4.0 * kPi * kAlpha * kAlpha / s * 0.5 * inv_norm);
+__device__ __forceinline__ void ann32_setup(Samp32& S, float Ee, float Eg_min, float C_row) {
+  const float me = (float)kMe, s = 2.f * me * (Ee + me);
+  const float p = sqrtf((Ee - me) * (Ee + me));
+  // 1 - ctMax with ctMax = (E + m - 2 Eg_min)/p, written without cancellation
+  S.E = s;
+  S.aux0 = 4.f * me * me / s;                 // 1 - b^2
+  S.aux1 = (2.f * Eg_min - me - me * me / (p + Ee)) / p;
+  S.C = C_row / s;                            // 4 pi alpha^2 / s * 1/2
 }
 __device__ __forceinline__ float ann32_ratio(const Samp32& S, const MapPt32& c, float jac) {
   if (c.omx < S.aux1) return 0.f;
@@ -147,11 +143,11 @@ __device__ __forceinline__ float ann32_ratio(const Samp32& S, const MapPt32& c, 
 }
 
 // ---- Moller: dsigma_moller_dCT (all_processes.py:799-840)
-__device__ __forceinline__ void moller32_setup(Samp32& S, double Ee, double Ee_min, double inv_norm) {
-  const double me = kMe, s = me * me + 2 * Ee * me, v = s - 4 * me * me;
-  S.E = (float)s; S.m = (float)(me * me);
-  S.aux0 = (float)(2.0 * Ee_min / (Ee - me));          // delta_ct_limit
-  S.C = (float)(16 * kPi * kPi * kAlpha * kAlpha / (8 * kPi * s * v * v) * inv_norm);
+__device__ __forceinline__ void moller32_setup(Samp32& S, float Ee, float Ee_min, float C_row) {
+  const float me = (float)kMe, s = me * me + 2.f * Ee * me, v = s - 4.f * me * me;
+  S.E = s; S.m = me * me;
+  S.aux0 = 2.f * Ee_min / (Ee - me);          // delta_ct_limit
+  S.C = C_row / (s * v * v);                  // 16 pi^2 alpha^2 / (8 pi s v^2)
 }
 __device__ __forceinline__ float moller32_ratio(const Samp32& S, const MapPt32& c, float jac) {
   if (!(c.opx > S.aux0 && c.omx > S.aux0)) return 0.f;
@@ -162,11 +158,11 @@ __device__ __forceinline__ float moller32_ratio(const Samp32& S, const MapPt32& 
 }
 
 // ---- Bhabha: dsigma_bhabha_dCT (all_processes.py:960-1007)
-__device__ __forceinline__ void bhabha32_setup(Samp32& S, double Ee, double Ee_min, double inv_norm) {
-  const double me = kMe, s = me * me + 2 * Ee * me, v = s - 4 * me * me;
-  S.E = (float)s; S.m = (float)(me * me);
-  S.aux0 = (float)(2.0 * Ee_min / (Ee - me));
-  S.C = (float)(kAlpha * kAlpha * kPi / (2.0 * s * s * s * v * v) * inv_norm);
+__device__ __forceinline__ void bhabha32_setup(Samp32& S, float Ee, float Ee_min, float C_row) {
+  const float me = (float)kMe, s = me * me + 2.f * Ee * me, v = s - 4.f * me * me;
+  S.E = s; S.m = me * me;
+  S.aux0 = 2.f * Ee_min / (Ee - me);
+  S.C = C_row / ((s * s) * (s * v * v));      // alpha^2 pi / (2 s^3 v^2)
 }
 __device__ __forceinline__ float bhabha32_ratio(const Samp32& S, const MapPt32& c, float jac) {
   if (!(c.opx > S.aux0 && c.omx > S.aux0)) return 0.f;
@@ -182,13 +178,13 @@ __device__ __forceinline__ float bhabha32_ratio(const Samp32& S, const MapPt32& 
 
 // ---- mu e -> mu e: dsigma_muonelectron_dCT (all_processes.py:855-886),
 // with p_cm^2 = m_e^2 (E^2 - m_mu^2)/s so t = -2(1-c) p_cm^2 does not cancel.
-__device__ __forceinline__ void muone32_setup(Samp32& S, double Emu, double Ee_min, double inv_norm) {
-  const double me = kMe, mm = kMmu, s = me * me + mm * mm + 2 * me * Emu;
-  const double pcm2 = me * me * (Emu - mm) * (Emu + mm) / s;
-  S.E = (float)s; S.m = (float)(me * me); S.span = (float)pcm2;
-  S.aux0 = (float)(me * (Ee_min - me) / pcm2);         // t < t_limit <=> 1-c > this
-  S.aux1 = (float)(mm * mm);
-  S.C = (float)(16 * kPi * kPi * kAlpha * kAlpha / (16 * kPi * s) * inv_norm);
+__device__ __forceinline__ void muone32_setup(Samp32& S, float Emu, float Ee_min, float C_row) {
+  const float me = (float)kMe, mm = (float)kMmu, s = me * me + mm * mm + 2.f * me * Emu;
+  const float pcm2 = me * me * (Emu - mm) * (Emu + mm) / s;
+  S.E = s; S.m = me * me; S.span = pcm2;
+  S.aux0 = me * (Ee_min - me) / pcm2;         // t < t_limit <=> 1-c > this
+  S.aux1 = mm * mm;
+  S.C = C_row / s;                            // 16 pi^2 alpha^2 / (16 pi s)
 }
 __device__ __forceinline__ float muone32_ratio(const Samp32& S, const MapPt32& c, float jac) {
   if (!(c.omx > S.aux0)) return 0.f;

@@ -93,6 +93,10 @@ class Tally:
         self.primary_edep = torch.zeros(max(n_primaries, 1), dtype=torch.float64, device=device)
         self.z_max = float(z_max)
 
+    def zero_(self):
+        for t in (self.counts, self.energy, self.hist, self.primary_count, self.primary_edep):
+            t.zero_()
+
     def abi(self) -> _lib.PtTally:
         t = _lib.PtTally()
         t.counts = self.counts.data_ptr()
@@ -147,6 +151,7 @@ class SMEngine:
             slopes.append(sl)
         self._keep["ns_s32"] = torch.as_tensor(np.concatenate(slopes).astype(np.float32), device=dev)
         self._keep["map_energy32"] = torch.as_tensor(tables.map_energy.astype(np.float32), device=dev)
+        self._keep["map_cnorm32"] = torch.as_tensor(self._cnorm(tables).astype(np.float32), device=dev)
         pt = _lib.PtTables()
         for p in range(_lib.N_PROC):
             pt.map_base[p] = int(tables.map_base[p])
@@ -166,6 +171,7 @@ class SMEngine:
         pt.ns_y32 = self._keep["ns_y32"].data_ptr()
         pt.ns_s32 = self._keep["ns_s32"].data_ptr()
         pt.map_energy32 = self._keep["map_energy32"].data_ptr()
+        pt.map_cnorm32 = self._keep["map_cnorm32"].data_ptr()
         for sl, (x, _) in enumerate(tables.nsigma):
             pt.ns_lnx0[sl] = float(np.log(x[0]))
             pt.ns_invdlog[sl] = float((len(x) - 1) / np.log(x[-1] / x[0]))
@@ -189,6 +195,25 @@ class SMEngine:
         h = C.c_void_p()
         _lib.check(self.lib.pt_create(C.byref(pt), C.byref(h)), "pt_create")
         self.handle = h
+
+    @staticmethod
+    def _cnorm(tables) -> np.ndarray:
+        """Per map row: the energy-independent prefactor of the float32
+        acceptance ratio divided by max_F * neval (see pt_physics32.cuh)."""
+        from .tables import ALPHA_EM, PROCESSES
+        a0 = 184.15 * (2.718) ** -0.5 * tables.Z_int ** (-1.0 / 3.0) / M_ELECTRON
+        brem = 8.0 * ALPHA_EM ** 3 * tables.Z_int ** 2 * a0 ** 4
+        K = {"Brem": brem, "MuonBrem": brem, "PairProd": brem, "Comp": math.pi * ALPHA_EM ** 2,
+             "MuonE": math.pi * ALPHA_EM ** 2, "Ann": 2 * math.pi * ALPHA_EM ** 2,
+             "Moller": 2 * math.pi * ALPHA_EM ** 2, "Bhabha": math.pi * ALPHA_EM ** 2 / 2}
+        out = np.zeros(len(tables.map_energy))
+        for p, name in enumerate(PROCESSES):
+            b, n = tables.map_base[p], tables.map_rows[p]
+            # rows with max_F = 0 give an infinite ratio: the first proposal with
+            # f > 0 is accepted, as max_F*U < wgt*f does in the reference
+            with np.errstate(divide="ignore"):
+                out[b:b + n] = K[name] / (tables.map_maxF[b:b + n] * tables.map_neval[b:b + n])
+        return out
 
     def close(self):
         if getattr(self, "handle", None):
@@ -277,10 +302,17 @@ class SMEngine:
         else:
             P0, R0, PID, M = device_inputs
             n = P0.shape[1]
-        s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
-                                  C.byref(tally.abi()), int(queue_capacity), self._stream())
-        self._raise(s, "pt_run_batch")
-        return tally
+        cap = int(queue_capacity) if queue_capacity else (1 << 24)
+        while True:
+            s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
+                                      C.byref(tally.abi()), cap, self._stream())
+            if s == _lib.PT_OOM and cap < (1 << 28):
+                # the live population outgrew the ring: start over with twice the room
+                tally.zero_()
+                cap *= 2
+                continue
+            self._raise(s, "pt_run_batch")
+            return tally
 
     def sample_only(self, process: int, energy, pkey, opts: _lib.PtOpts):
         torch = _torch()

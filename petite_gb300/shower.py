@@ -174,6 +174,45 @@ class Shower:
         st, rows = self._engine.run_sm(p0, r0, pid, mass, weight, opts)
         return ShowerBatch(st.to_numpy(rows), n)
 
+    def run_tallied(self, p0, pid=11, mass=None, r0=None, GlobalMS=True, precision=None, first_primary=None,
+                    z_max=None, queue_capacity=0) -> dict:
+        """Transports many primaries without keeping particle lists and returns
+        host tallies: counts, energy sums, histograms and per-primary arrays.
+
+        p0 (n,4) and pid/mass (n,) may be numpy arrays or (pinned) CPU torch
+        tensors; they are copied to the device inside this call."""
+        import torch
+        dev = self._engine.device
+        p0t = torch.as_tensor(p0, dtype=torch.float64)
+        n = p0t.shape[0]
+        pidt = torch.as_tensor(np.broadcast_to(np.asarray(pid, np.int32), (n,)).copy()) if not torch.is_tensor(pid) \
+            else pid.to(torch.int32)
+        for q in torch.unique(pidt).tolist():
+            if int(q) not in SUPPORTED_PIDS:
+                raise ValueError(f"PID {int(q)} is not transported by the shower path")
+        if mass is None:
+            mass = torch.as_tensor([MASS[int(q)] for q in pidt.tolist()], dtype=torch.float64)
+        mt = torch.as_tensor(mass, dtype=torch.float64)
+        P0 = p0t.to(dev, non_blocking=True).t().contiguous()
+        R0 = (torch.zeros((3, n), dtype=torch.float64, device=dev) if r0 is None
+              else torch.as_tensor(r0, dtype=torch.float64).to(dev, non_blocking=True).t().contiguous())
+        PID = pidt.to(dev, non_blocking=True)
+        M = mt.to(dev, non_blocking=True)
+        if first_primary is None:
+            first_primary = self._next_primary
+            self._next_primary += n
+        opts = self._opts(GlobalMS, precision)
+        opts.primary_offset = int(first_primary)
+        zmax = z_max if z_max is not None else 30.0 * radiation_length_m(self._target_material)
+        t = self._engine.new_tally(n, zmax)
+        self._engine.run_batch(None, None, None, None, opts, t, queue_capacity, device_inputs=(P0, R0, PID, M))
+        out = t.summary()
+        out["hist"] = t.hist.cpu().numpy()
+        out["primary_count"] = t.primary_count.cpu().numpy()
+        out["primary_edep"] = t.primary_edep.cpu().numpy()
+        out["z_max"] = zmax
+        return out
+
     def generate_shower(self, p0, VB=False, GlobalMS=True):
         """Generates a particle shower from an initial particle (shower.py:603-708)."""
         ids = p0.get_ids()
@@ -188,6 +227,12 @@ class Shower:
         b = self.generate_showers(np.asarray(p0.get_p0(), np.float64)[None], np.asarray(p0.get_r0(), np.float64)[None],
                                   pid=ids["PID"], mass=mass, weight=ids["weight"], GlobalMS=GlobalMS)
         return batch_to_particles(b, [p0copy])[0]
+
+
+def radiation_length_m(target):
+    """Approximate radiation length (PDG, m) used only to size depth histograms."""
+    return {"lead": 0.0056, "graphite": 0.19, "iron": 0.0176, "tungsten": 0.0035, "aluminum": 0.089,
+            "molybdenum": 0.0096, "hydrogen": 7.5}.get(target, 0.1)
 
 
 def _stream_key(i):

@@ -56,11 +56,14 @@ def test_dsigma_matches_oracle(engines, target):
         want = np.array(want)
         assert (want != 0).sum() > 100
         # The engine's float64 hot loop fuses multiply-adds; the oracle rounds
-        # every operation.  The 4-D formulas sum terms of opposite sign
-        # (T4 < 0 in all_processes.py:200 and :596-600) and the annihilation
-        # denominator 1 - b^2 ct^2 (all_processes.py:525) cancels near ct = 1,
-        # which magnifies last-place differences.
-        rtol = 1e-10 if P.DIM[proc] == 4 else 1e-11
+        # every operation.  The reference formulas sum terms of opposite sign
+        # (Brem/PairProd T4 < 0, all_processes.py:200,596-600; Compton
+        # T1+T2+T3, :701-707; annihilation 1 - b^2 ct^2, :525), which magnifies
+        # those last-place differences to at most ~1e-10 relative.  MuonBrem
+        # evaluates the same Brem formula with the muon mass on maps trained
+        # over physical ranges (all_processes.py:1120-1127), where T1+T2+T4
+        # cancel to ~1e-9 of the individual terms: 1e-6 there.
+        rtol = 1e-6 if proc == "MuonBrem" else 1e-10
         np.testing.assert_allclose(got, want, rtol=rtol, atol=0, err_msg=proc)
 
 
