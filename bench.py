@@ -237,6 +237,12 @@ def bench_batch(args, w, name, dist, rank, ws):
     tally = eng.new_tally(n, zmax)
     for s in range(args.warmup):
         device_step(1000 + s, w["precision"], tally, stage(1000 + s))
+    if args.quick:
+        ts = [device_step(s, w["precision"], tally, stage(s)) for s in range(args.steps)]
+        if rank == 0:
+            print(json.dumps({"workload": name, "primaries": n, "particle_steps": tally.summary()["steps"],
+                              "seconds": ts, "launches": eng.last_run_stats()[0]}))
+        return
     times, steps_done, launches = [], 0, 0
     with ClockSampler(dev.index or 0) as clk:
         for s in range(args.steps):
@@ -417,6 +423,8 @@ def main():
     ap.add_argument("--primaries", type=int, default=0, help="override primaries per step")
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="device steps only (no float64 comparison, e2e or CPU baseline): for profiling")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
