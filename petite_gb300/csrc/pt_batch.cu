@@ -21,6 +21,7 @@
 // as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
 // builds directions in float32 and keeps energies in float64.
 #include <cstdio>
+#include <type_traits>
 
 #include "pt_internal.cuh"
 #include "pt_physics32.cuh"
@@ -36,8 +37,12 @@ constexpr int kHB = PT_HIST_BINS;
 constexpr int kHist = 3 * 4 * kHB;
 constexpr int kBuf = 64;        // per-warp, per-process task buffer (published at >= 32)
 
-struct Ring {
-  double *E, *px, *py, *pz, *x, *y, *z, *mass;
+// Ring entry fields.  Energies are float64 in both engines; the mixed engine
+// keeps momenta, positions and masses in float32.
+template <int PREC> struct RingT {
+  using R = typename std::conditional<PREC == 0, double, float>::type;
+  double* E;
+  R *px, *py, *pz, *x, *y, *z, *mass;
   uint64_t* key;
   int32_t *pid, *prim, *gen, *row;
   uint32_t* draw;
@@ -52,13 +57,13 @@ struct Tally {
   float z_max;
 };
 
-struct WaveCtx {
+template <int PREC> struct WaveCtx {
   Tabs T;
   double min_energy, rescale;
   int64_t max_n_integrators;
   int ms;
   uint64_t seed;
-  Ring q;
+  RingT<PREC> q;
   uint64_t mask;                      // ring capacity - 1
   uint64_t head, tail;                // ring positions of this wave's first entry and of the append point
   int64_t n_in;                       // entries in this wave
@@ -293,7 +298,8 @@ __device__ int choose_process_b(const Tabs& T, int pid, double E, Rng& rng) {
 // Publishes this iteration's sampling tasks: lanes with `emit` append ring
 // index `i` to the warp's buffer for `process`; full buffers go to the global
 // per-process lists 32 at a time.  All 32 lanes call it.
-__device__ __forceinline__ void publish_tasks(const WaveCtx& c, int32_t (*buf)[kBuf], int* cnt, bool emit,
+template <class Ctx>
+__device__ __forceinline__ void publish_tasks(const Ctx& c, int32_t (*buf)[kBuf], int* cnt, bool emit,
                                               int process, int32_t i) {
   unsigned left = __ballot_sync(kFull, emit);
   const int lane = threadIdx.x & 31;
@@ -321,7 +327,8 @@ __device__ __forceinline__ void publish_tasks(const WaveCtx& c, int32_t (*buf)[k
   }
 }
 
-__device__ __forceinline__ void publish_rest(const WaveCtx& c, int32_t (*buf)[kBuf], int* cnt) {
+template <class Ctx>
+__device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf], int* cnt) {
   const int lane = threadIdx.x & 31;
   for (int p = 0; p < 8; ++p) {
     if (!cnt[p]) continue;
@@ -336,7 +343,7 @@ __device__ __forceinline__ void publish_rest(const WaveCtx& c, int32_t (*buf)[kB
 
 // ------------------------------------------------------------ phase 1
 template <int PREC>
-__global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
+__global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
@@ -536,8 +543,209 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx c) {
   flush_tally(c.tally, L, sh_hist);
 }
 
+// ------------------------------------------------ phase 1, mixed precision
+// A particle whose propagation ended, waiting for the process choice and its
+// sampling task.  Finished particles are queued per warp and handled 32 at a
+// time so this per-particle work runs with every lane busy.
+struct FinEntry {
+  uint32_t i, draw;
+  int32_t pid, prim;
+  double E, E0;
+  float px, py, pz, x, y, z, u, pme;
+};
+
+__device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t (*buf)[kBuf], int* bcnt,
+                           LocalTally& L, unsigned int* sh_hist) {
+  const int lane = threadIdx.x & 31;
+  const bool on = lane < count;
+  int process = -1, prim = 0;
+  bool emit = false;
+  double edep = 0.0;
+  uint32_t i = 0;
+  if (on) {
+    const FinEntry& e = fq[lane];
+    i = e.i;
+    prim = e.prim;
+    const int sp = species_of(e.pid);
+    atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of(e.z, 0.f, c.tally.z_max)], 1u);
+    const double eloss = e.E0 - e.E;
+    L.e_cont += eloss;
+    const float Ef = (float)e.E;
+    process = choose32(c.T, e.pid, Ef, e.u);             // shower.py:665-698
+    emit = process >= 0 && Ef > e.pme;
+    if (emit) {                                          // park the state for the sampler
+      c.q.E[i] = e.E; c.q.px[i] = e.px; c.q.py[i] = e.py; c.q.pz[i] = e.pz;
+      c.q.x[i] = e.x; c.q.y[i] = e.y; c.q.z[i] = e.z;
+      c.q.draw[i] = e.draw;
+      c.q.row[i] = c.T.t.map_base[process] + lu_key32(c.T, process, Ef);
+      edep = eloss;
+    } else {
+      ++L.ended;
+      L.e_ended += e.E;
+      edep = eloss + e.E;
+    }
+  }
+  primary_tally(c.tally, on, prim, edep);
+  publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
+}
+
+__global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
+  __shared__ unsigned int sh_hist[kHist];
+  __shared__ int32_t sh_buf[kWarps][8][kBuf];
+  __shared__ FinEntry sh_fin[kWarps][64];
+  for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
+  __syncthreads();
+  const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
+  int32_t (*buf)[kBuf] = sh_buf[w];
+  FinEntry* fq = sh_fin[w];
+  int bcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int fcount = 0;                                        // warp-uniform
+  const Tabs& T = c.T;
+  const float mc[4] = {(float)T.t.min_calc_photon, (float)T.t.min_calc_electron, (float)T.t.min_calc_positron,
+                       (float)T.t.min_calc_muon};
+  const float minE = (float)c.min_energy;
+  const float lossesf = (float)T.t.dEdx_GeV_per_m;
+  const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
+  const float rescale = (float)c.rescale;
+  LocalTally L;
+  WarpPool pool;
+  bool active = false;
+  uint32_t i = 0;
+  double E0 = 0.0;
+  float Ef = 0.f, mf = 0.f, pmef = 0.f, lossf = 0.f, dzf = 0.f, pmag = 0.f;
+  float3 dir = make_float3(0.f, 0.f, 1.f), pos = make_float3(0.f, 0.f, 0.f), disp = make_float3(0.f, 0.f, 0.f);
+  int pid = 0, prim = 0;
+  Rng rng;
+
+  for (;;) {
+    __syncwarp();
+    const bool need = !active;
+    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, 128);
+    const bool fresh = need && got >= 0;
+    if (__all_sync(kFull, !active && !fresh)) break;
+    bool fin = false;
+    if (fresh) {
+      i = (uint32_t)((c.head + (uint64_t)got) & c.mask);
+      pid = c.q.pid[i];
+    }
+    // a dead entry (pid 0, left by the sampler's slot pool) is consumed without work
+    if (fresh && pid != 0) {
+      E0 = c.q.E[i];
+      const float px = c.q.px[i], py = c.q.py[i], pz = c.q.pz[i];
+      pos = make_float3(c.q.x[i], c.q.y[i], c.q.z[i]);
+      mf = c.q.mass[i];
+      prim = c.q.prim[i];
+      rng.init(c.seed, c.q.key[i]);
+      Ef = (float)E0;
+      const int sp = species_of(pid);
+      pmef = fmaxf(fmaxf(mc[sp], minE), mf);             // shower.py:532-533
+      ++L.steps;
+      ++L.species[sp];
+      const float pt = sqrtf(px * px + py * py);
+      pmag = sqrtf(pt * pt + pz * pz);
+      atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f(Ef), -2.f, 2.f)], 1u);
+      const float th = atan2f(pt, pz);
+      atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(th > 0.f ? log10f(th) : -6.f, -6.f, 0.5f)], 1u);
+      dir = pmag > 0.f ? make_float3(px / pmag, py / pmag, pz / pmag) : make_float3(0.f, 0.f, 1.f);
+      disp = make_float3(0.f, 0.f, 0.f);
+      lossf = 0.f;
+      if (Ef < pmef) {
+        fin = true;                                      // ends without moving (shower.py:534-536)
+      } else if (pid == 22) {                            // shower.py:538-553
+        const float dist = -mfp32(T, pid, Ef) * log1pf(-rng.uf());
+        disp = make_float3(dir.x * dist, dir.y * dist, dir.z * dist);
+        fin = true;
+      } else {
+        active = true;
+        dzf = 0.f;
+      }
+    }
+    if (active) {
+      // one iteration of the substep loop (shower.py:559-581) in float32; the
+      // lost energy accumulates in float32 and leaves the float64 energy once
+      bool stop = !(Ef >= pmef);
+      float mfp = 0.f;
+      if (!stop) {
+        ++L.substeps;
+        mfp = mfp32(T, pid, Ef);
+        const float u_hard = rng.uf();
+        const float q = fmaf(14.f, rng.uf(), 6.f);
+        dzf = mfp / q;
+        if (u_hard > __expf(-1.f / q)) {
+          stop = true;
+        } else {
+          lossf = fmaf(lossesf, dzf, lossf);
+          Ef = (float)E0 - lossf;
+          if (Ef <= mf) Ef = mf;
+          pmag = sqrtf((Ef - mf) * (Ef + mf));
+          if (pmag > 0.f) {
+            disp.x = fmaf(dir.x, dzf, disp.x); disp.y = fmaf(dir.y, dzf, disp.y); disp.z = fmaf(dir.z, dzf, disp.z);
+          }
+          if (c.ms) mcs32(dir, pmag, Ef, rho_cm * dzf, A, Z, Z23, rescale, rng);
+        }
+      }
+      if (stop) {
+        const float distC = rng.uf();                    // shower.py:583-598
+        float last;
+        if (Ef < pmef) last = distC * dzf;
+        else {
+          if (mfp == 0.f) mfp = mfp32(T, pid, Ef);
+          last = -mfp * log1pf(expm1f(-dzf / mfp) * distC);
+        }
+        lossf = fmaf(lossesf, last, lossf);
+        Ef = (float)E0 - lossf;
+        if (Ef <= mf) Ef = mf;
+        pmag = sqrtf((Ef - mf) * (Ef + mf));
+        if (pmag > 0.f) {
+          disp.x = fmaf(dir.x, last, disp.x); disp.y = fmaf(dir.y, last, disp.y); disp.z = fmaf(dir.z, last, disp.z);
+        }
+        // shower.py:596-598 passes no m_lepton; the width uses |p| directly here
+        if (c.ms) mcs32(dir, pmag, Ef, rho_cm * last, A, Z, Z23, rescale, rng);
+        active = false;
+        fin = true;
+      }
+    }
+    const unsigned fm = __ballot_sync(kFull, fin);
+    if (fm) {
+      if (fin) {
+        FinEntry e;
+        e.i = i;
+        e.pid = pid;
+        e.prim = prim;
+        const bool moved = lossf != 0.f;
+        double E = moved ? E0 - (double)lossf : E0;      // float64 energy bookkeeping
+        if (moved && E <= (double)mf) E = (double)mf;
+        e.E = E;
+        e.E0 = E0;
+        e.px = pmag * dir.x; e.py = pmag * dir.y; e.pz = pmag * dir.z;
+        e.x = pos.x + disp.x; e.y = pos.y + disp.y; e.z = pos.z + disp.z;
+        e.u = rng.uf();                                  // the process-choice draw
+        e.draw = (uint32_t)rng.n;
+        e.pme = pmef;
+        fq[fcount + __popc(fm & lanemask_lt())] = e;
+      }
+      fcount += __popc(fm);
+      __syncwarp();
+      if (fcount >= 32) {
+        run_finish(c, fq, 32, buf, bcnt, L, sh_hist);
+        __syncwarp();
+        const int rest = fcount - 32;
+        FinEntry carry;
+        if (lane < rest) carry = fq[32 + lane];
+        __syncwarp();
+        if (lane < rest) fq[lane] = carry;
+        fcount = rest;
+        __syncwarp();
+      }
+    }
+  }
+  if (fcount > 0) run_finish(c, fq, fcount, buf, bcnt, L, sh_hist);
+  publish_rest(c, buf, bcnt);
+  flush_tally(c.tally, L, sh_hist);
+}
+
 // ------------------------------------------------------------ phase 2
-struct Daughter { double E, px, py, pz; int pid; };
+template <class R> struct DaughterT { double E; R px, py, pz; int pid; };
 
 // Mixed engine: daughters in the parent frame with float32 angles, float32
 // momentum magnitudes and the energy split closed in float64
@@ -653,21 +861,24 @@ constexpr int kKinQ = 64;
 // Kinematics, lab rotation and daughter output for up to 32 queued accepts,
 // one per lane (sample_scattering, shower.py:467-507).  All lanes call.
 template <int PREC>
-__device__ void run_kinematics(const WaveCtx& c, KinEntry<PREC>* kq, int count, OutPool& opool, LocalTally& L) {
+__device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int count, OutPool& opool, LocalTally& L) {
+  using R = typename RingT<PREC>::R;
   const int lane = threadIdx.x & 31;
   const bool on = lane < count;
-  Daughter dg[2];
+  DaughterT<R> dg[2];
   int want = 0, prim = 0, gen = 0;
   uint64_t key = 0, i = 0;
-  double x0 = 0, y0 = 0, z0 = 0, below = 0.0;
+  R x0 = 0, y0 = 0, z0 = 0;
+  double below = 0.0;
   if (on) {
     const KinEntry<PREC>& e = kq[lane];
     i = e.i;
     const int process = e.process;
-    const double E = c.q.E[i], mass = c.q.mass[i];
+    const double E = c.q.E[i];
     const int pid = c.q.pid[i];
-    const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
-    if (PREC == 0) {
+    if constexpr (PREC == 0) {
+      const double mass = c.q.mass[i];
+      const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
       const double* xd = reinterpret_cast<const KinEntry<0>&>(e).x;
       const double ph = reinterpret_cast<const KinEntry<0>&>(e).ph;
       const Rot R = rotation_from(pf);
@@ -687,14 +898,14 @@ __device__ void run_kinematics(const WaveCtx& c, KinEntry<PREC>* kq, int count, 
     } else {
       const KinEntry<1>& f = reinterpret_cast<const KinEntry<1>&>(e);
       KinOut k;
-      kin_mixed(process, pid, E, mass, f.x, f.ph, k);
-      const float fx = (float)pf[1], fy = (float)pf[2], fz = (float)pf[3];
+      kin_mixed(process, pid, E, c.q.mass[i], f.x, f.ph, k);
+      const float fx = c.q.px[i], fy = c.q.py[i], fz = c.q.pz[i];
       const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
       const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
-      const Rot32 R = rot32_from(pd);
+      const Rot32 Rm = rot32_from(pd);
       for (int j = 0; j < 2; ++j) {
-        const float3 v = rot32_apply(R, k.d[j]);
-        dg[j] = {k.E[j], (double)(k.P[j] * v.x), (double)(k.P[j] * v.y), (double)(k.P[j] * v.z), k.pid[j]};
+        const float3 v = rot32_apply(Rm, k.d[j]);
+        dg[j] = {k.E[j], k.P[j] * v.x, k.P[j] * v.y, k.P[j] * v.z, k.pid[j]};
       }
     }
     want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
@@ -715,7 +926,7 @@ __device__ void run_kinematics(const WaveCtx& c, KinEntry<PREC>* kq, int count, 
     ++L.pushed;
     c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
     c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
-    c.q.mass[q] = table_mass(dg[j].pid);
+    c.q.mass[q] = (R)table_mass(dg[j].pid);
     c.q.key[q] = daughter_key(key, j);
     c.q.pid[q] = dg[j].pid;
     c.q.prim[q] = prim;
@@ -724,7 +935,7 @@ __device__ void run_kinematics(const WaveCtx& c, KinEntry<PREC>* kq, int count, 
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
+__global__ void __launch_bounds__(kThreads) k_sample(WaveCtx<PREC> c) {
   __shared__ unsigned long long sh_off[9];
   __shared__ KinEntry<PREC> sh_kq[kWarps][kKinQ];
   if (threadIdx.x == 0) {
@@ -865,7 +1076,8 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx c) {
   flush_tally(c.tally, L, nullptr);
 }
 
-__global__ void k_feed(Ring q, uint64_t mask, uint64_t tail, const double* p0, const double* r0, const int32_t* pid,
+template <int PREC>
+__global__ void k_feed(RingT<PREC> q, uint64_t mask, uint64_t tail, const double* p0, const double* r0, const int32_t* pid,
                        const double* mass, int64_t n_total, int64_t first, int64_t n, int64_t offset) {
   const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (j >= n) return;
@@ -885,7 +1097,6 @@ struct BatchScratch {
   int64_t cap = 0;          // ring capacity (power of two)
   int64_t list_cap = 0;     // entries per process list (= max wave size)
   void* mem = nullptr;
-  Ring q;
   int32_t* idx = nullptr;
   unsigned long long* ctr = nullptr;
   unsigned long long* h_ctr = nullptr;
@@ -922,16 +1133,26 @@ pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
     batch_scratch_free(s);
     return PT_OOM;
   }
-  char* p = (char*)s->mem;
-  auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
-  Ring& q = s->q;
-  q.E = (double*)take(c2 * 8); q.px = (double*)take(c2 * 8); q.py = (double*)take(c2 * 8);
-  q.pz = (double*)take(c2 * 8); q.x = (double*)take(c2 * 8); q.y = (double*)take(c2 * 8);
-  q.z = (double*)take(c2 * 8); q.mass = (double*)take(c2 * 8); q.key = (uint64_t*)take(c2 * 8);
-  q.pid = (int32_t*)take(c2 * 4); q.prim = (int32_t*)take(c2 * 4); q.gen = (int32_t*)take(c2 * 4);
-  q.row = (int32_t*)take(c2 * 4); q.draw = (uint32_t*)take(c2 * 4);
   *out = s;
   return PT_OK;
+}
+
+// Lays out the ring arrays for one engine form in the scratch memory.
+template <int PREC>
+static RingT<PREC> carve_ring(BatchScratch* s) {
+  using R = typename RingT<PREC>::R;
+  const int64_t c2 = s->cap;
+  char* p = (char*)s->mem;
+  auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
+  RingT<PREC> q;
+  q.E = (double*)take(c2 * 8);
+  q.px = (R*)take(c2 * sizeof(R)); q.py = (R*)take(c2 * sizeof(R)); q.pz = (R*)take(c2 * sizeof(R));
+  q.x = (R*)take(c2 * sizeof(R)); q.y = (R*)take(c2 * sizeof(R)); q.z = (R*)take(c2 * sizeof(R));
+  q.mass = (R*)take(c2 * sizeof(R));
+  q.key = (uint64_t*)take(c2 * 8);
+  q.pid = (int32_t*)take(c2 * 4); q.prim = (int32_t*)take(c2 * 4); q.gen = (int32_t*)take(c2 * 4);
+  q.row = (int32_t*)take(c2 * 4); q.draw = (uint32_t*)take(c2 * 4);
+  return q;
 }
 
 void batch_scratch_free(BatchScratch* s) {
@@ -953,27 +1174,18 @@ static int resident_blocks(const void* kernel) {
   return sms * per;
 }
 
-extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const int32_t* pid,
-                                  const double* mass, int64_t n, const pt_opts* o, pt_tally* tally,
-                                  int64_t queue_capacity, void* stream) {
-  if (!h || !o || !tally || n < 0) return PT_BAD_ARG;
-  if (n == 0) return PT_OK;
-  if (!p0 || !r0 || !pid || !mass || !tally->counts || !tally->energy || !tally->hist || !tally->primary_count ||
-      !tally->primary_edep || (o->precision != 0 && o->precision != 1) || n > 0x7fffffff)
-    return PT_BAD_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
-  BatchScratch* S = nullptr;
-  pt_status s = batch_scratch_get(h, &S, queue_capacity > 0 ? queue_capacity : ((int64_t)1 << 24));
-  if (s != PT_OK) return s;
+template <int PREC>
+static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0, const double* r0, const int32_t* pid,
+                                const double* mass, int64_t n, const pt_opts* o, pt_tally* tally, cudaStream_t st) {
   HandleParts hp = handle_parts(h);
-  WaveCtx c;
+  WaveCtx<PREC> c;
   c.T = *hp.T;
   c.min_energy = o->min_energy;
   c.rescale = o->rescale_MCS;
   c.max_n_integrators = o->max_n_integrators;
   c.ms = o->multiple_scattering;
   c.seed = o->seed;
-  c.q = S->q;
+  c.q = carve_ring<PREC>(S);
   c.mask = (uint64_t)S->cap - 1;
   c.list_cap = S->list_cap;
   c.idx = S->idx;
@@ -982,8 +1194,8 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
   c.err_info = hp.err_info;
   c.tally = {tally->counts, tally->energy, tally->hist, tally->primary_count, tally->primary_edep,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
-  const void* kp = o->precision ? (const void*)k_propagate<1> : (const void*)k_propagate<0>;
-  const void* ks = o->precision ? (const void*)k_sample<1> : (const void*)k_sample<0>;
+  const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate<0>;
+  const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);
   const int rb_s = resident_blocks(ks);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
@@ -1000,8 +1212,8 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
       int64_t m = n - fed;
       if (m > cap / 8 - live) m = cap / 8 - live;
       if (m > feed_max) m = feed_max;
-      k_feed<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(S->q, c.mask, tail, p0, r0, pid, mass, n, fed, m,
-                                                          o->primary_offset);
+      k_feed<PREC><<<(unsigned)((m + 255) / 256), 256, 0, st>>>(c.q, c.mask, tail, p0, r0, pid, mass, n, fed, m,
+                                                                o->primary_offset);
       ++nl;
       tail += (uint64_t)m;
       fed += m;
@@ -1031,13 +1243,9 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
     const int64_t want_blocks = (k + kThreads - 1) / kThreads;
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
-    if (o->precision) {
-      k_propagate<1><<<gp, kThreads, 0, st>>>(c);
-      k_sample<1><<<gs, kThreads, 0, st>>>(c);
-    } else {
-      k_propagate<0><<<gp, kThreads, 0, st>>>(c);
-      k_sample<0><<<gs, kThreads, 0, st>>>(c);
-    }
+    if constexpr (PREC == 1) k_propagate_mixed<<<gp, kThreads, 0, st>>>(c);
+    else k_propagate<0><<<gp, kThreads, 0, st>>>(c);
+    k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
     PT_CUDA(cudaGetLastError());
     nl += 3;
     ++nw;
@@ -1056,4 +1264,20 @@ extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* 
   hp.launches[0] = nl;
   hp.launches[1] = nw;
   return PT_OK;
+}
+
+extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const int32_t* pid,
+                                  const double* mass, int64_t n, const pt_opts* o, pt_tally* tally,
+                                  int64_t queue_capacity, void* stream) {
+  if (!h || !o || !tally || n < 0) return PT_BAD_ARG;
+  if (n == 0) return PT_OK;
+  if (!p0 || !r0 || !pid || !mass || !tally->counts || !tally->energy || !tally->hist || !tally->primary_count ||
+      !tally->primary_edep || (o->precision != 0 && o->precision != 1) || n > 0x7fffffff)
+    return PT_BAD_ARG;
+  BatchScratch* S = nullptr;
+  const pt_status s = batch_scratch_get(h, &S, queue_capacity > 0 ? queue_capacity : ((int64_t)1 << 24));
+  if (s != PT_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (o->precision == 1) return run_batch_impl<1>(h, S, p0, r0, pid, mass, n, o, tally, st);
+  return run_batch_impl<0>(h, S, p0, r0, pid, mass, n, o, tally, st);
 }
