@@ -297,9 +297,10 @@ __device__ int choose_process_b(const Tabs& T, int pid, double E, Rng& rng) {
 
 // Publishes this iteration's sampling tasks: lanes with `emit` append ring
 // index `i` to the warp's buffer for `process`; full buffers go to the global
-// per-process lists 32 at a time.  All 32 lanes call it.
+// per-process lists 32 at a time.  `cnt` (shared, per warp) is written by
+// lane 0 only.  All 32 lanes call it.
 template <class Ctx>
-__device__ __forceinline__ void publish_tasks(const Ctx& c, int32_t (*buf)[kBuf], int* cnt, bool emit,
+__device__ __forceinline__ void publish_tasks(const Ctx& c, int32_t (*buf)[kBuf], volatile int* cnt, bool emit,
                                               int process, int32_t i) {
   unsigned left = __ballot_sync(kFull, emit);
   const int lane = threadIdx.x & 31;
@@ -307,38 +308,42 @@ __device__ __forceinline__ void publish_tasks(const Ctx& c, int32_t (*buf)[kBuf]
     const int leader = __ffs(left) - 1;
     const int p = __shfl_sync(kFull, process, leader);
     const unsigned m = __ballot_sync(kFull, emit && process == p);
-    if (emit && process == p) buf[p][cnt[p] + __popc(m & lanemask_lt())] = i;
-    cnt[p] += __popc(m);
+    const int cp = cnt[p];
+    if (emit && process == p) buf[p][cp + __popc(m & lanemask_lt())] = i;
+    int now = cp + __popc(m);
     left &= ~m;
     __syncwarp();
-    if (cnt[p] >= 32) {
+    if (now >= 32) {
       unsigned long long base = 0;
       if (lane == 0) base = atomicAdd(c.ctr + 8 + p, 32ull);
       base = __shfl_sync(kFull, base, 0);
       c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
       __syncwarp();
-      const int rest = cnt[p] - 32;
-      int32_t carry = lane < rest ? buf[p][32 + lane] : 0;
+      const int rest = now - 32;
+      const int32_t carry = lane < rest ? buf[p][32 + lane] : 0;
       __syncwarp();
       if (lane < rest) buf[p][lane] = carry;
-      cnt[p] = rest;
-      __syncwarp();
+      now = rest;
     }
+    if (lane == 0) cnt[p] = now;
+    __syncwarp();
   }
 }
 
 template <class Ctx>
-__device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf], int* cnt) {
+__device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf], volatile int* cnt) {
   const int lane = threadIdx.x & 31;
   for (int p = 0; p < 8; ++p) {
-    if (!cnt[p]) continue;
+    const int cp = cnt[p];
+    if (!cp) continue;
     unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(c.ctr + 8 + p, (unsigned long long)cnt[p]);
+    if (lane == 0) base = atomicAdd(c.ctr + 8 + p, (unsigned long long)cp);
     base = __shfl_sync(kFull, base, 0);
-    if (lane < cnt[p]) c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
-    cnt[p] = 0;
+    if (lane < cp) c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
+    __syncwarp();
+    if (lane == 0) cnt[p] = 0;
+    __syncwarp();
   }
-  __syncwarp();
 }
 
 // ------------------------------------------------------------ phase 1
@@ -346,10 +351,12 @@ template <int PREC>
 __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
+  __shared__ int sh_bcnt[kWarps][8];
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
+  if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
   int32_t (*buf)[kBuf] = sh_buf[threadIdx.x / 32];
-  int bcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  volatile int* bcnt = sh_bcnt[threadIdx.x / 32];
   const Tabs& T = c.T;
   LocalTally L;
   WarpPool pool;
@@ -554,7 +561,7 @@ struct FinEntry {
   float px, py, pz, x, y, z, u, pme;
 };
 
-__device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t (*buf)[kBuf], int* bcnt,
+__device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t (*buf)[kBuf], volatile int* bcnt,
                            LocalTally& L, unsigned int* sh_hist) {
   const int lane = threadIdx.x & 31;
   const bool on = lane < count;
@@ -592,17 +599,19 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
 __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
+  __shared__ int sh_bcnt[kWarps][8];
   __shared__ FinEntry sh_fin[kWarps][64];
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
+  if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
   const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
   int32_t (*buf)[kBuf] = sh_buf[w];
   FinEntry* fq = sh_fin[w];
-  int bcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  volatile int* bcnt = sh_bcnt[w];
   int fcount = 0;                                        // warp-uniform
   const Tabs& T = c.T;
-  const float mc[4] = {(float)T.t.min_calc_photon, (float)T.t.min_calc_electron, (float)T.t.min_calc_positron,
-                       (float)T.t.min_calc_muon};
+  const float mc0 = (float)T.t.min_calc_photon, mc1 = (float)T.t.min_calc_electron,
+              mc2 = (float)T.t.min_calc_positron, mc3 = (float)T.t.min_calc_muon;
   const float minE = (float)c.min_energy;
   const float lossesf = (float)T.t.dEdx_GeV_per_m;
   const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
@@ -638,7 +647,8 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       rng.init(c.seed, c.q.key[i]);
       Ef = (float)E0;
       const int sp = species_of(pid);
-      pmef = fmaxf(fmaxf(mc[sp], minE), mf);             // shower.py:532-533
+      const float mcs = sp == 0 ? mc0 : (sp == 1 ? mc1 : (sp == 2 ? mc2 : mc3));
+      pmef = fmaxf(fmaxf(mcs, minE), mf);                // shower.py:532-533
       ++L.steps;
       ++L.species[sp];
       const float pt = sqrtf(px * px + py * py);
@@ -935,7 +945,7 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(kThreads) k_sample(WaveCtx<PREC> c) {
+__global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<PREC> c) {
   __shared__ unsigned long long sh_off[9];
   __shared__ KinEntry<PREC> sh_kq[kWarps][kKinQ];
   if (threadIdx.x == 0) {
@@ -986,11 +996,14 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx<PREC> c) {
       d = process_dim(process);
       cap = c.max_n_integrators * (int64_t)neval;
       props = 0;
-      for (int k = 0; k < d; ++k) {
-        const int64_t off = T.t.grid_offset[(int64_t)row * 4 + k];
-        ninc[k] = T.t.grid_ninc[(int64_t)row * 4 + k];
-        if (PREC == 0) g64[k] = T.t.grid_nodes + off;
-        else g32[k] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k < d) {
+          const int64_t off = T.t.grid_offset[(int64_t)row * 4 + k];
+          ninc[k] = T.t.grid_ninc[(int64_t)row * 4 + k];
+          if (PREC == 0) g64[k] = T.t.grid_nodes + off;
+          else g32[k] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
+        }
       }
       if (PREC == 0) {
         maxF = T.t.map_maxF[row];
@@ -1016,14 +1029,18 @@ __global__ void __launch_bounds__(kThreads) k_sample(WaveCtx<PREC> c) {
       if (PREC == 0) {
         double* xd = reinterpret_cast<KinEntry<0>&>(ent).x;
         double jac = 1.0;
-        for (int k = 0; k < d; ++k) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < d) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
         const double f = dsigma_any(T, process, xd, E);
         accept = maxF * rng.u() < (jac / neval) * f;
         if (accept) reinterpret_cast<KinEntry<0>&>(ent).ph = 2.0 * kPi * rng.u();
       } else {
         MapPt32* xm = reinterpret_cast<KinEntry<1>&>(ent).x;
         float jac = 1.f;
-        for (int k = 0; k < d; ++k) xm[k] = map_dim32(g32[k], ninc[k], rng.uf(), jac);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < d) xm[k] = map_dim32(g32[k], ninc[k], rng.uf(), jac);
         float r;
         switch (process) {
           case PT_BREM: case PT_MUONBREM: r = brem32_ratio(S32, xm, jac); break;
