@@ -346,9 +346,9 @@ __device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf],
   }
 }
 
-// ------------------------------------------------------------ phase 1
-template <int PREC>
-__global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
+// ------------------------------------------------------------ phase 1, float64
+// Same device functions and operation order as the record engine (pt_run_sm).
+__global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
   __shared__ int sh_bcnt[kWarps][8];
@@ -363,12 +363,9 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
   bool active = false;
   uint64_t i = 0;
   double E0 = 0, E = 0, px = 0, py = 0, pz = 0, x = 0, y = 0, z = 0, mass = 0, pme = 0, dz = 0;
-  float3 dir = make_float3(0.f, 0.f, 1.f), disp = make_float3(0.f, 0.f, 0.f);
-  float Ef = 0.f, lossf = 0.f, dzf = 0.f, pmef = 0.f;
   int pid = 0, prim = 0;
   Rng rng;
   const double losses = T.t.dEdx_GeV_per_m;
-  const float lossesf = (float)losses;
   const float zmax = c.tally.z_max;
 
   for (;;) {
@@ -395,38 +392,26 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
       atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f((float)E0), -2.f, 2.f)], 1u);
       const float th = atan2f(sqrtf((float)px * (float)px + (float)py * (float)py), (float)pz);
       atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(th > 0.f ? log10f(th) : -6.f, -6.f, 0.5f)], 1u);
-      if (PREC == 1) {
-        const float pn = sqrtf((float)px * (float)px + (float)py * (float)py + (float)pz * (float)pz);
-        dir = pn > 0.f ? make_float3((float)px / pn, (float)py / pn, (float)pz / pn) : make_float3(0.f, 0.f, 1.f);
-        disp = make_float3(0.f, 0.f, 0.f);
-        Ef = (float)E0; lossf = 0.f; pmef = (float)pme;
-      }
       if (E0 < pme) {
         finish = true;
       } else if (pid == 22) {               // shower.py:538-553
-        if (PREC == 0) {
-          const double mfp = mfp_of(T, pid, E);
-          const double distC = rng.u();
-          const double dist = (S(mfp) * S(log((S(1.0) / (S(1.0) - S(distC))).v))).v;
-          const double n = norm3_np(px, py, pz);
-          x = (S(x) + S(px) / S(n) * S(dist)).v;
-          y = (S(y) + S(py) / S(n) * S(dist)).v;
-          z = (S(z) + S(pz) / S(n) * S(dist)).v;
-        } else {
-          const float dist = -mfp32(T, pid, Ef) * log1pf(-rng.uf());
-          x += (double)(dir.x * dist); y += (double)(dir.y * dist); z += (double)(dir.z * dist);
-        }
+        const double mfp = mfp_of(T, pid, E);
+        const double distC = rng.u();
+        const double dist = (S(mfp) * S(log((S(1.0) / (S(1.0) - S(distC))).v))).v;
+        const double n = norm3_np(px, py, pz);
+        x = (S(x) + S(px) / S(n) * S(dist)).v;
+        y = (S(y) + S(py) / S(n) * S(dist)).v;
+        z = (S(z) + S(pz) / S(n) * S(dist)).v;
         finish = true;
       } else {
         active = true;
         dz = 0.0;
-        dzf = 0.f;
       }
     }
     if (active) {
       // one iteration of the substep loop (shower.py:559-581)
       bool stop;
-      if (PREC == 0) {
+      {
         stop = !(E >= pme);
         if (!stop) {
           ++L.substeps;
@@ -462,58 +447,6 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
           active = false;
           finish = true;
         }
-      } else {
-        // float32 substep: the energy lost along the track is accumulated in
-        // float32 and subtracted from the float64 energy once at the end
-        const float mf = (float)mass;
-        stop = !(Ef >= pmef);
-        float mfp = 0.f;
-        if (!stop) {
-          ++L.substeps;
-          mfp = mfp32(T, pid, Ef);
-          const float u_hard = rng.uf();
-          const float q = fmaf(14.f, rng.uf(), 6.f);
-          dzf = mfp / q;
-          if (u_hard > __expf(-1.f / q)) {
-            stop = true;
-          } else {
-            const float dE = lossesf * dzf;
-            lossf += dE;
-            Ef = (float)E0 - lossf;
-            if (Ef <= mf) Ef = mf;
-            const float pmag = sqrtf((Ef - mf) * (Ef + mf));
-            if (pmag > 0.f) {
-              disp.x = fmaf(dir.x, dzf, disp.x); disp.y = fmaf(dir.y, dzf, disp.y); disp.z = fmaf(dir.z, dzf, disp.z);
-            }
-            if (c.ms)
-              mcs32(dir, pmag, Ef, (float)T.t.rho * (dzf / (float)kCmToM), (float)T.t.A, (float)T.t.Z,
-                    (float)T.t.Z23, (float)c.rescale, rng);
-          }
-        }
-        if (stop) {
-          const float distC = rng.uf();
-          float last;
-          if (Ef < pmef) last = distC * dzf;
-          else {
-            if (mfp == 0.f) mfp = mfp32(T, pid, Ef);
-            last = -mfp * log1pf(expm1f(-dzf / mfp) * distC);
-          }
-          lossf += lossesf * last;
-          E = E0 - (double)lossf;                     // float64 bookkeeping, once per step
-          if (E <= mass) E = mass;
-          Ef = (float)E;
-          const float pmag = sqrtf((Ef - mf) * (Ef + mf));
-          if (pmag > 0.f) {
-            disp.x = fmaf(dir.x, last, disp.x); disp.y = fmaf(dir.y, last, disp.y); disp.z = fmaf(dir.z, last, disp.z);
-          }
-          if (c.ms)   // shower.py:596-598 passes no m_lepton; the width uses |p| directly here
-            mcs32(dir, pmag, Ef, (float)T.t.rho * (last / (float)kCmToM), (float)T.t.A, (float)T.t.Z,
-                  (float)T.t.Z23, (float)c.rescale, rng);
-          x += (double)disp.x; y += (double)disp.y; z += (double)disp.z;
-          px = (double)(pmag * dir.x); py = (double)(pmag * dir.y); pz = (double)(pmag * dir.z);
-          active = false;
-          finish = true;
-        }
       }
     }
     // ---- end of propagation: tallies, process choice, task or retirement
@@ -525,15 +458,14 @@ __global__ void __launch_bounds__(kThreads) k_propagate(WaveCtx<0> c) {
       atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of((float)z, 0.f, zmax)], 1u);
       const double eloss = E0 - E;
       L.e_cont += eloss;
-      if (PREC == 0) process = choose_process_b(T, pid, E, rng);
-      else process = choose32(T, pid, (float)E, rng.uf());
+      process = choose_process_b(T, pid, E, rng);
       emit = process >= 0 && E > pme;
       if (emit) {
         // park the post-propagation state in place for the sampler
         c.q.E[i] = E; c.q.px[i] = px; c.q.py[i] = py; c.q.pz[i] = pz;
         c.q.x[i] = x; c.q.y[i] = y; c.q.z[i] = z;
         c.q.draw[i] = (uint32_t)rng.n;
-        c.q.row[i] = T.t.map_base[process] + (PREC == 0 ? lu_key(T, process, E) : lu_key32(T, process, (float)E));
+        c.q.row[i] = T.t.map_base[process] + lu_key(T, process, E);
         edep = eloss;
       } else {
         ++L.ended;
@@ -558,7 +490,7 @@ struct FinEntry {
   uint32_t i, draw;
   int32_t pid, prim;
   double E, E0;
-  float px, py, pz, x, y, z, u, pme;
+  float px, py, pz, x, y, z, u, pme, th0;   // th0: polar angle of p0 (creation histogram)
 };
 
 __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t (*buf)[kBuf], volatile int* bcnt,
@@ -574,6 +506,8 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
     i = e.i;
     prim = e.prim;
     const int sp = species_of(e.pid);
+    atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f((float)e.E0), -2.f, 2.f)], 1u);
+    atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(e.th0 > 0.f ? log10f(e.th0) : -6.f, -6.f, 0.5f)], 1u);
     atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of(e.z, 0.f, c.tally.z_max)], 1u);
     const double eloss = e.E0 - e.E;
     L.e_cont += eloss;
@@ -616,12 +550,13 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
   const float lossesf = (float)T.t.dEdx_GeV_per_m;
   const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
   const float rescale = (float)c.rescale;
+  const float me = (float)kMe;
   LocalTally L;
   WarpPool pool;
   bool active = false;
   uint32_t i = 0;
   double E0 = 0.0;
-  float Ef = 0.f, mf = 0.f, pmef = 0.f, lossf = 0.f, dzf = 0.f, pmag = 0.f;
+  float Ef = 0.f, mf = 0.f, pmef = 0.f, lossf = 0.f, dzf = 0.f, pmag = 0.f, th0 = 0.f, mtab = 0.f;
   float3 dir = make_float3(0.f, 0.f, 1.f), pos = make_float3(0.f, 0.f, 0.f), disp = make_float3(0.f, 0.f, 0.f);
   int pid = 0, prim = 0;
   Rng rng;
@@ -649,68 +584,57 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       const int sp = species_of(pid);
       const float mcs = sp == 0 ? mc0 : (sp == 1 ? mc1 : (sp == 2 ? mc2 : mc3));
       pmef = fmaxf(fmaxf(mcs, minE), mf);                // shower.py:532-533
+      mtab = sp == 0 ? 0.f : (sp == 3 ? (float)kMmu : me);   // mass_dict[PID] (particle.py:4-13)
       ++L.steps;
       ++L.species[sp];
       const float pt = sqrtf(px * px + py * py);
       pmag = sqrtf(pt * pt + pz * pz);
-      atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f(Ef), -2.f, 2.f)], 1u);
-      const float th = atan2f(pt, pz);
-      atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(th > 0.f ? log10f(th) : -6.f, -6.f, 0.5f)], 1u);
+      th0 = atan2f(pt, pz);
       dir = pmag > 0.f ? make_float3(px / pmag, py / pmag, pz / pmag) : make_float3(0.f, 0.f, 1.f);
       disp = make_float3(0.f, 0.f, 0.f);
       lossf = 0.f;
-      if (Ef < pmef) {
-        fin = true;                                      // ends without moving (shower.py:534-536)
-      } else if (pid == 22) {                            // shower.py:538-553
-        const float dist = -mfp32(T, pid, Ef) * log1pf(-rng.uf());
-        disp = make_float3(dir.x * dist, dir.y * dist, dir.z * dist);
-        fin = true;
-      } else {
-        active = true;
-        dzf = 0.f;
-      }
+      dzf = 0.f;
+      if (Ef < pmef) fin = true;                         // ends without moving (shower.py:534-536)
+      else active = true;
     }
     if (active) {
-      // one iteration of the substep loop (shower.py:559-581) in float32; the
-      // lost energy accumulates in float32 and leaves the float64 energy once
-      bool stop = !(Ef >= pmef);
-      float mfp = 0.f;
-      if (!stop) {
+      // One step of propagate_particle (shower.py:538-598), the same body for
+      // every lane: a photon's flight, a charged substep, or the charged
+      // particle's final partial increment; only the step length differs.
+      float step, mlep = mtab;
+      bool last = true;
+      const bool charged = pid != 22;
+      if (!charged) {
+        step = -mfp32(T, pid, Ef) * log1pf(-rng.uf());  // mfp log(1/(1-u))
+      } else if (!(Ef >= pmef)) {
+        step = rng.uf() * dzf;                            // shower.py:584-585
+        mlep = me;                                        // shower.py:596-598: electron mass
+      } else {
         ++L.substeps;
-        mfp = mfp32(T, pid, Ef);
+        const float mfp = mfp32(T, pid, Ef);
         const float u_hard = rng.uf();
-        const float q = fmaf(14.f, rng.uf(), 6.f);
+        const float q = fmaf(14.f, rng.uf(), 6.f);       // delta_z = mfp / U(6, 20)
         dzf = mfp / q;
-        if (u_hard > __expf(-1.f / q)) {
-          stop = true;
+        if (u_hard > __expf(-1.f / q)) {                 // hard scatter: final increment
+          step = -mfp * log1pf(expm1f(-1.f / q) * rng.uf());
+          mlep = me;
         } else {
-          lossf = fmaf(lossesf, dzf, lossf);
-          Ef = (float)E0 - lossf;
-          if (Ef <= mf) Ef = mf;
-          pmag = sqrtf((Ef - mf) * (Ef + mf));
-          if (pmag > 0.f) {
-            disp.x = fmaf(dir.x, dzf, disp.x); disp.y = fmaf(dir.y, dzf, disp.y); disp.z = fmaf(dir.z, dzf, disp.z);
-          }
-          if (c.ms) mcs32(dir, pmag, Ef, rho_cm * dzf, A, Z, Z23, rescale, rng);
+          step = dzf;
+          last = false;
         }
       }
-      if (stop) {
-        const float distC = rng.uf();                    // shower.py:583-598
-        float last;
-        if (Ef < pmef) last = distC * dzf;
-        else {
-          if (mfp == 0.f) mfp = mfp32(T, pid, Ef);
-          last = -mfp * log1pf(expm1f(-dzf / mfp) * distC);
-        }
-        lossf = fmaf(lossesf, last, lossf);
+      if (charged) {                                      // lose_energy (particle.py:143-153)
+        lossf = fmaf(lossesf, step, lossf);
         Ef = (float)E0 - lossf;
         if (Ef <= mf) Ef = mf;
         pmag = sqrtf((Ef - mf) * (Ef + mf));
-        if (pmag > 0.f) {
-          disp.x = fmaf(dir.x, last, disp.x); disp.y = fmaf(dir.y, last, disp.y); disp.z = fmaf(dir.z, last, disp.z);
-        }
-        // shower.py:596-598 passes no m_lepton; the width uses |p| directly here
-        if (c.ms) mcs32(dir, pmag, Ef, rho_cm * last, A, Z, Z23, rescale, rng);
+      }
+      if (pmag > 0.f) {
+        disp.x = fmaf(dir.x, step, disp.x); disp.y = fmaf(dir.y, step, disp.y); disp.z = fmaf(dir.z, step, disp.z);
+      }
+      // Lynch-Dahl momentum p = m_lepton * beta * gamma = |p| m_lepton / m
+      if (charged && c.ms) mcs32(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, rng, pmag / Ef);
+      if (last) {
         active = false;
         fin = true;
       }
@@ -732,6 +656,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
         e.u = rng.uf();                                  // the process-choice draw
         e.draw = (uint32_t)rng.n;
         e.pme = pmef;
+        e.th0 = th0;
         fq[fcount + __popc(fm & lanemask_lt())] = e;
       }
       fcount += __popc(fm);
@@ -1211,7 +1136,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.err_info = hp.err_info;
   c.tally = {tally->counts, tally->energy, tally->hist, tally->primary_count, tally->primary_edep,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
-  const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate<0>;
+  const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate_fp64;
   const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);
   const int rb_s = resident_blocks(ks);
@@ -1261,7 +1186,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
     if constexpr (PREC == 1) k_propagate_mixed<<<gp, kThreads, 0, st>>>(c);
-    else k_propagate<0><<<gp, kThreads, 0, st>>>(c);
+    else k_propagate_fp64<<<gp, kThreads, 0, st>>>(c);
     k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
     PT_CUDA(cudaGetLastError());
     nl += 3;

@@ -196,8 +196,9 @@ __device__ __forceinline__ float muone32_ratio(const Samp32& S, const MapPt32& c
 }
 
 // -------------------------------------------- multiple scattering, float32
-// Lynch-Dahl width (moliere.py:196-219,265-284) with the momentum taken as
-// |p| directly (the reference's m*beta/sqrt(1-beta^2) is the same quantity),
+// Lynch-Dahl width (moliere.py:196-219,265-284).  The reference's momentum
+// m_lepton*beta/sqrt(1-beta^2) with beta = |p|/E equals |p| m_lepton / m; the
+// caller passes that product as pmag (well conditioned, unlike 1 - beta^2),
 // same four draws as the float64 form, frame rotation of moliere.py:287-348
 // written algebraically (its branches reduce to ca = vx/rho, sa = -vy/rho,
 // cb = vz/r, sb = -rho/r).
@@ -208,11 +209,11 @@ __device__ __forceinline__ float lynch_dahl_g(float v) {
 }
 
 __device__ __forceinline__ void mcs32(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
-                                      float rescale, Rng& rng) {
+                                      float rescale, Rng& rng, float beta_p = -1.f) {
   if (!(pmag > 0.f)) return;             // a particle at rest draws nothing (moliere.py:359-363)
   const float u_sign = rng.uf(), u_ang = rng.uf(), u_rad = rng.uf(), u_phi = rng.uf();
   (void)u_ang;   // the Gaussian pair's angle cancels in the space angle
-  const float beta = pmag / E;
+  const float beta = beta_p >= 0.f ? beta_p : pmag / E;
   const float p = pmag * 1000.f;                         // MeV
   const float pb = p * beta;
   const float chic2 = 0.157f * Z * (Z + 1.f) * (t / A) / (pb * pb);
