@@ -43,16 +43,43 @@ WORKLOADS = {
                                  seed=0, precision="fp64", fp64_sample=1000, cpu_sample=400, mode="records"),
 }
 
-# Algorithmic HBM bytes per particle-step of the batched engine (ring entries,
-# structure of arrays): propagation reads the entry (E, p, r, mass 64 B; key
-# 8 B; pid, primary 8 B = 80 B) and parks the post-propagation state (E, p, r
-# 56 B; draw, map row 8 B = 64 B) plus its task index (write 4 B, read 4 B);
-# the sampler reads the parked task (92 B) and writes on average one daughter
-# (88 B).  Tables (maps, n*sigma) are L2-resident and not counted.
-BYTES_PER_STEP_BATCH = 80 + 64 + 8 + 92 + 88
+# Algorithmic HBM bytes of the batched engine's two kernels, per unit of work,
+# for the ring's structure of arrays (E and key are 8 B; momentum, position
+# and mass 8 B in the float64 form and 4 B in the mixed form; pid, primary,
+# generation, map row and draw counter 4 B each).  Tables (maps, n*sigma) are
+# L2-resident and not counted.
+#   propagation, per particle-step: read E, p, r, mass, key, pid, primary;
+#     per sampled particle: park E, p, r, draw, row and write its task index.
+#   sampler, per sampled particle: read the task index and E, p, r, key, pid,
+#     primary, generation, row, draw; per pushed daughter: write E, p, r,
+#     mass, key, pid, primary, generation.
+def ring_bytes(precision):
+    f = 8 if precision == "fp64" else 4
+    return {"prop_per_step": 8 + 7 * f + 8 + 8,
+            "prop_per_sampled": 8 + 6 * f + 8 + 4,
+            "sample_per_sampled": 4 + 8 + 6 * f + 8 + 20,
+            "sample_per_pushed": 8 + 7 * f + 8 + 12}
 # Record engine: read the live row (100 B), write its final state (60 B) and
 # the one row it creates on average (176 B).
 BYTES_PER_STEP_RECORDS = 336
+
+
+# DRAM traffic per particle-step of each batched kernel, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum over every launch of the
+# kernel, divided by the run's particle-steps); the capture and its command
+# are summarised in the named profile.  The bench scales it to its own
+# launches by the particle-steps they process.
+NCU_TRAFFIC = {
+    "propagate": {"bytes_per_step": 65.26, "profile": "profiles/dram_traffic_lead_20k.md"},
+    "sample": {"bytes_per_step": 236.53, "profile": "profiles/dram_traffic_lead_20k.md"},
+}
+
+
+def measured_traffic(kernel, kd, kt):
+    t = NCU_TRAFFIC.get(kernel)
+    if not t or kd["launches"] == 0:
+        return None
+    return t["bytes_per_step"] * kt["steps"] / kd["launches"]
 
 
 def make_primaries(w, n, offset):
@@ -204,7 +231,7 @@ def bench_batch(args, w, name, dist, rank, ws):
     sh = Shower(None, w["target"], w["cut"], seed=w["seed"], precision=w["precision"], device=dev)
     eng = sh._engine
     n = args.primaries or w["n"]
-    cap = 1 << 25
+    cap = 1 << args.ring_log2
     zmax = 30.0 * 0.0056 if w["target"] == "lead" else 1.0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
 
@@ -240,16 +267,27 @@ def bench_batch(args, w, name, dist, rank, ws):
     if args.quick:
         ts = [device_step(s, w["precision"], tally, stage(s)) for s in range(args.steps)]
         if rank == 0:
-            print(json.dumps({"workload": name, "primaries": n, "particle_steps": tally.summary()["steps"],
-                              "seconds": ts, "launches": eng.last_run_stats()[0]}))
+            summ = tally.summary()
+            print(json.dumps({"workload": name, "primaries": n, "particle_steps": summ["steps"],
+                              "sampled": summ["sampled"], "pushed": summ["pushed"], "seconds": ts,
+                              "launches_waves": eng.last_run_stats(), "kernel_seconds": eng.last_kernel_times()}))
         return
     times, steps_done, launches = [], 0, 0
+    kt = {"prop_s": 0.0, "sample_s": 0.0, "steps": 0, "sampled": 0, "pushed": 0, "waves": 0}
     with ClockSampler(dev.index or 0) as clk:
         for s in range(args.steps):
             inputs = stage(s)
             times.append(device_step(s, w["precision"], tally, inputs))
-            steps_done += tally.summary()["steps"]
-            launches += eng.last_run_stats()[0]
+            summ = tally.summary()
+            steps_done += summ["steps"]
+            nl, nw = eng.last_run_stats()
+            launches += nl
+            tp, ts_ = eng.last_kernel_times()
+            kt["prop_s"] += tp
+            kt["sample_s"] += ts_
+            kt["waves"] += nw
+            for key in ("steps", "sampled", "pushed"):
+                kt[key] += summ[key]
     t_local = float(sum(times))
     if dist:
         t = torch.tensor([t_local], device=dev)
@@ -303,7 +341,19 @@ def bench_batch(args, w, name, dist, rank, ws):
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = value * BYTES_PER_STEP_BATCH / 1e9
+    rb = ring_bytes(w["precision"])
+    kernels = {
+        "propagate": {"seconds": kt["prop_s"], "launches": kt["waves"],
+                      "bytes": kt["steps"] * rb["prop_per_step"] + kt["sampled"] * rb["prop_per_sampled"]},
+        "sample": {"seconds": kt["sample_s"], "launches": kt["waves"],
+                   "bytes": kt["sampled"] * rb["sample_per_sampled"] + kt["pushed"] * rb["sample_per_pushed"]},
+    }
+    for kd in kernels.values():
+        kd["GB_per_s"] = kd["bytes"] / kd["seconds"] / 1e9 if kd["seconds"] > 0 else 0.0
+        kd["share_of_step"] = kd["seconds"] / t_local if t_local > 0 else 0.0
+    top = max(kernels, key=lambda k_: kernels[k_]["seconds"])
+    achieved = kernels[top]["GB_per_s"]
+    traffic = measured_traffic(top, kernels[top], kt)
     cb = None if args.no_cpu_baseline else cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -319,9 +369,13 @@ def bench_batch(args, w, name, dist, rank, ws):
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "bytes_per_step": BYTES_PER_STEP_BATCH,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
-                     "note": "compute-bound path: HBM fraction of the algorithmic ring traffic; see profiles/"},
+                     "traffic": traffic, "kernel": top,
+                     "algorithmic_bytes_per_launch": kernels[top]["bytes"] / max(kernels[top]["launches"], 1),
+                     "avg_launch_ms": 1e3 * kernels[top]["seconds"] / max(kernels[top]["launches"], 1),
+                     "kernels": kernels,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
+                     "note": "issue-bound kernels (Philox, transcendental and table work per byte); "
+                             "HBM fraction of the algorithmic ring traffic"},
         "cpu_baseline": cb,
         "clocks": clk.summary(),
         "particle_steps": steps_all,
@@ -423,6 +477,7 @@ def main():
     ap.add_argument("--primaries", type=int, default=0, help="override primaries per step")
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ring-log2", type=int, default=25, help="batched engine: log2 of the ring capacity")
     ap.add_argument("--quick", action="store_true",
                     help="device steps only (no float64 comparison, e2e or CPU baseline): for profiling")
     args = ap.parse_args()

@@ -175,6 +175,12 @@ pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const i
  * (transport iterations).  Diagnostic; no reference counterpart. */
 pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* waves);
 
+/* Device time of the last pt_run_batch on this handle, summed over its waves
+ * and measured with CUDA events on the run's stream: the propagation kernel
+ * and the sampler kernel, in milliseconds.  Diagnostic; no reference
+ * counterpart. */
+pt_status pt_last_kernel_times(pt_handle* h, double* propagate_ms, double* sample_ms);
+
 /* Shower.draw_sample (shower.py:401-465) for a batch: for each i, draws the
  * final-state variables of `process` at energy energy[i] from stream key
  * pkey[i] starting at draw 0.  Writes x[i*4 + d], proposals[i], lu_key[i]. */

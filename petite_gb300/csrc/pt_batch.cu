@@ -1043,6 +1043,7 @@ struct BatchScratch {
   unsigned long long* ctr = nullptr;
   unsigned long long* h_ctr = nullptr;
   int* h_status = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // around each wave's two kernels
 };
 
 #define PT_CUDA(call)                                                                 \
@@ -1070,7 +1071,8 @@ pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
       cudaMalloc(&s->idx, (size_t)8 * s->list_cap * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&s->ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&s->h_ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMallocHost(&s->h_status, sizeof(int)) != cudaSuccess) {
+      cudaMallocHost(&s->h_status, sizeof(int)) != cudaSuccess || cudaEventCreate(&s->ev[0]) != cudaSuccess ||
+      cudaEventCreate(&s->ev[1]) != cudaSuccess || cudaEventCreate(&s->ev[2]) != cudaSuccess) {
     cudaGetLastError();
     batch_scratch_free(s);
     return PT_OOM;
@@ -1104,6 +1106,8 @@ void batch_scratch_free(BatchScratch* s) {
   cudaFree(s->ctr);
   cudaFreeHost(s->h_ctr);
   cudaFreeHost(s->h_status);
+  for (cudaEvent_t e : s->ev)
+    if (e) cudaEventDestroy(e);
   delete s;
 }
 
@@ -1148,6 +1152,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   const int64_t feed_max = cap / 1024 > 256 ? cap / 1024 : 256;
   uint64_t head = 0, tail = 0;
   int64_t fed = 0, nl = 1, nw = 0;
+  hp.kernel_ms[0] = hp.kernel_ms[1] = 0.0;
   while (fed < n || tail > head) {
     int64_t live = (int64_t)(tail - head);
     if (fed < n && live < cap / 8) {
@@ -1185,9 +1190,12 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     const int64_t want_blocks = (k + kThreads - 1) / kThreads;
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
+    PT_CUDA(cudaEventRecord(S->ev[0], st));
     if constexpr (PREC == 1) k_propagate_mixed<<<gp, kThreads, 0, st>>>(c);
     else k_propagate_fp64<<<gp, kThreads, 0, st>>>(c);
+    PT_CUDA(cudaEventRecord(S->ev[1], st));
     k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
+    PT_CUDA(cudaEventRecord(S->ev[2], st));
     PT_CUDA(cudaGetLastError());
     nl += 3;
     ++nw;
@@ -1200,6 +1208,11 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
         PT_CUDA(cudaMemcpy(hp.last_info, hp.err_info, 3 * sizeof(double), cudaMemcpyDeviceToHost));
       return (pt_status)*S->h_status;
     }
+    float ms_p = 0.f, ms_s = 0.f;
+    PT_CUDA(cudaEventElapsedTime(&ms_p, S->ev[0], S->ev[1]));
+    PT_CUDA(cudaEventElapsedTime(&ms_s, S->ev[1], S->ev[2]));
+    hp.kernel_ms[0] += ms_p;
+    hp.kernel_ms[1] += ms_s;
     head += (uint64_t)k;
     tail += S->h_ctr[2];
   }

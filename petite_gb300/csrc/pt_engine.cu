@@ -280,6 +280,7 @@ struct pt_handle {
   int* h_status = nullptr;
   double last_info[3] = {0, 0, 0};
   int64_t launches[2] = {0, 0};   // kernel launches, waves of the last run
+  double kernel_ms[2] = {0, 0};   // batched run: propagation and sampler device time
   BatchScratch* batch = nullptr;
 };
 
@@ -290,7 +291,7 @@ pt_status batch_scratch_get(pt_handle* h, BatchScratch** out, int64_t ring_capac
 }
 
 HandleParts handle_parts(pt_handle* h) {
-  return HandleParts{&h->T, h->status, h->err_info, h->last_info, h->launches};
+  return HandleParts{&h->T, h->status, h->err_info, h->last_info, h->launches, h->kernel_ms};
 }
 
 static const char* kMessages[] = {
@@ -441,6 +442,13 @@ extern "C" pt_status pt_last_run_stats(pt_handle* h, int64_t* launches, int64_t*
   if (!h) return PT_BAD_ARG;
   if (launches) *launches = h->launches[0];
   if (waves) *waves = h->launches[1];
+  return PT_OK;
+}
+
+extern "C" pt_status pt_last_kernel_times(pt_handle* h, double* propagate_ms, double* sample_ms) {
+  if (!h) return PT_BAD_ARG;
+  if (propagate_ms) *propagate_ms = h->kernel_ms[0];
+  if (sample_ms) *sample_ms = h->kernel_ms[1];
   return PT_OK;
 }
 

@@ -18,5 +18,6 @@ struct HandleParts {
   double* err_info;
   double* last_info;
   int64_t* launches;   // [0] kernel launches, [1] waves of the last run
+  double* kernel_ms;   // device time of the last batched run: [0] propagation, [1] sampler
 };
 HandleParts handle_parts(pt_handle* h);

@@ -281,6 +281,12 @@ class SMEngine:
         _lib.check(self.lib.pt_last_run_stats(self.handle, C.byref(l), C.byref(w)), "pt_last_run_stats")
         return int(l.value), int(w.value)
 
+    def last_kernel_times(self):
+        """Device seconds of the last batched run: (propagation, sampler)."""
+        a, b = C.c_double(), C.c_double()
+        _lib.check(self.lib.pt_last_kernel_times(self.handle, C.byref(a), C.byref(b)), "pt_last_kernel_times")
+        return a.value / 1e3, b.value / 1e3
+
     def new_tally(self, n_primaries: int, z_max: float = 1.0) -> "Tally":
         return Tally(n_primaries, self.device, z_max)
 

@@ -1,0 +1,76 @@
+"""The C ABI without a GPU: every function declared in include/*.h is exported
+by the built library and bound by the ctypes layer, and the ctypes structures
+have the header's layout (offsets checked against a gcc-compiled probe)."""
+import ctypes as C
+import glob
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w ]*?[\s*]+(pt_\w+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return names
+
+
+def test_header_declares_the_bound_exports():
+    from petite_gb300 import _lib
+    names = declared_functions()
+    assert len(names) == len(set(names))
+    assert set(names) == set(_lib.EXPORTS)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc not available")
+    from petite_gb300 import _lib
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_strerror_needs_no_device(lib):
+    from petite_gb300 import _lib
+    assert lib.pt_strerror(_lib.PT_NO_SAMPLE) == b"No Sample Found"
+    assert lib.pt_strerror(_lib.PT_OK) == b"ok"
+    assert lib.pt_strerror(99) == b"unknown status"
+
+
+def test_struct_layout_matches_header(tmp_path):
+    """Offsets of every field of the four ABI structures, from gcc on the
+    header, against the ctypes definitions."""
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    from petite_gb300 import _lib
+    structs = {"pt_tables": _lib.PtTables, "pt_particles": _lib.PtParticles, "pt_opts": _lib.PtOpts,
+               "pt_tally": _lib.PtTally}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "petite_gpu.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for cname, cls in structs.items():
+        assert got[(cname, "sizeof")] == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
