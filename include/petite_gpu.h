@@ -142,6 +142,25 @@ typedef struct pt_opts {
 pt_status pt_run_sm(pt_handle* h, pt_particles* out, int64_t n_primaries,
                     const pt_opts* opts, int64_t* n_rows, void* stream);
 
+/* pt_run_sm without any allocation.  No counterpart in the reference: it is
+ * for callers that cannot allocate device memory during a run (a host whose
+ * free device memory belongs to its own caching pool or a fixed budget, where
+ * cudaMalloc may fail, or that cannot accept the device-wide synchronisation
+ * of cudaFree).  Same kernels, streams and results as pt_run_sm; the scratch
+ * (live lists, counters, status, error record) is one static device array of
+ * 8 MB per device instead of handle memory grown with cudaMalloc.
+ *  - out->capacity must not exceed 2^19 rows (524288); larger stores are
+ *    rejected with PT_BAD_ARG and a message on stderr.
+ *  - The first call on each device looks up the array's address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - The status word, error record and counters are zeroed (cudaMemsetAsync)
+ *    at the start of every call.
+ *  - All calls on a device share the one array: calls that overlap in time
+ *    (other streams, other host threads, other handles) race on it. */
+pt_status pt_run_sm_noalloc(pt_handle* h, pt_particles* out, int64_t n_primaries,
+                            const pt_opts* opts, int64_t* n_rows, void* stream);
+
 /* Tallies of a batched run (all device pointers; accumulated, never cleared
  * by the library).  Histograms: [kind][species][PT_HIST_BINS] with kinds
  * 0 = log10(E0/GeV) at creation in [-2, 2], 1 = log10(polar angle of p0 / rad)

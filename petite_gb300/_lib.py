@@ -18,7 +18,10 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE
 PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
-           "pt_last_kernel_times", "pt_run_sm", "pt_run_batch", "pt_sample_only", "pt_dsigma")
+           "pt_last_kernel_times", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch", "pt_sample_only", "pt_dsigma")
+
+# pt_run_sm_noalloc: largest particle-store capacity (its static scratch)
+NOALLOC_MAX_ROWS = 1 << 19
 
 
 class PtTables(C.Structure):
@@ -100,6 +103,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_last_kernel_times.restype = C.c_int
     lib.pt_run_sm.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
     lib.pt_run_sm.restype = C.c_int
+    lib.pt_run_sm_noalloc.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
+    lib.pt_run_sm_noalloc.restype = C.c_int
     lib.pt_run_batch.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp]
     lib.pt_run_batch.restype = C.c_int
     lib.pt_sample_only.argtypes = [vp, i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp, vp]

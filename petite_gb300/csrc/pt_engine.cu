@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "pt_internal.cuh"
@@ -430,6 +431,120 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
     if (s != PT_OK) {
       *n_rows = (int64_t)h->h_counters[1];
       return s;
+    }
+    n_in = (int64_t)h->h_counters[0];
+    cur ^= 1;
+  }
+  *n_rows = (int64_t)h->h_counters[1];
+  return PT_OK;
+}
+
+// ------------------------------------------------- pt_run_sm without allocation
+// pt_run_sm grows two live lists with cudaMalloc/cudaFree as the particle
+// store grows.  Some callers cannot allocate device memory during a run: a
+// host that has handed the device's free memory to its own caching pool
+// (PyTorch's allocator, or an application with a fixed device-memory
+// budget), where a cudaMalloc may fail, and callers that cannot accept the
+// device-wide synchronisation of cudaFree.  pt_run_sm_noalloc runs the same
+// kernels with their scratch (both live lists, the wave counters, the status
+// word and the error record) in one static device array, located once per
+// device with cudaGetSymbolAddress.
+namespace {
+constexpr int64_t kNoAllocMaxRows = int64_t(1) << 19;       // live-list entries (= particle rows)
+constexpr size_t kNoAllocListBytes = size_t(kNoAllocMaxRows) * sizeof(int64_t);
+constexpr size_t kNoAllocCtrOff = 2 * kNoAllocListBytes;    // 4 x u64 counters: [0] n_out, [1] n_rows
+constexpr size_t kNoAllocStatusOff = kNoAllocCtrOff + 256;  // int status
+constexpr size_t kNoAllocInfoOff = kNoAllocStatusOff + 256; // 4 x f64 error record
+constexpr size_t kNoAllocBytes = kNoAllocInfoOff + 256;     // 8 MB + 768 B
+constexpr int kNoAllocMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices];
+cudaError_t g_noalloc_err[kNoAllocMaxDevices];
+std::once_flag g_noalloc_once[kNoAllocMaxDevices];
+
+// Device address of the static scratch on the current device (set up on the
+// first call per device).
+pt_status noalloc_scratch(unsigned char** out) {
+  int dev = 0;
+  PT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return PT_BAD_ARG;
+  std::call_once(g_noalloc_once[dev], [dev] {
+    g_noalloc_err[dev] = cudaGetSymbolAddress((void**)&g_noalloc_ptr[dev], g_noalloc_scratch);
+  });
+  if (g_noalloc_err[dev] != cudaSuccess || !g_noalloc_ptr[dev]) {
+    fprintf(stderr, "petite_gpu: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(g_noalloc_err[dev]));
+    return PT_CUDA_ERR;
+  }
+  *out = g_noalloc_ptr[dev];
+  return PT_OK;
+}
+}  // namespace
+
+extern "C" pt_status pt_run_sm_noalloc(pt_handle* h, pt_particles* P, int64_t n_primaries, const pt_opts* o,
+                                       int64_t* n_rows, void* stream) {
+  if (!h || !P || !o || !n_rows || n_primaries < 0 || n_primaries > P->capacity) return PT_BAD_ARG;
+  if (o->precision != 0) return PT_BAD_ARG;
+  if (P->capacity > kNoAllocMaxRows) {
+    fprintf(stderr, "petite_gpu: pt_run_sm_noalloc: particle capacity %lld exceeds the static scratch limit of %lld rows\n",
+            (long long)P->capacity, (long long)kNoAllocMaxRows);
+    return PT_BAD_ARG;
+  }
+  *n_rows = n_primaries;
+  if (n_primaries == 0) return PT_OK;
+  unsigned char* base = nullptr;
+  pt_status s = noalloc_scratch(&base);
+  if (s != PT_OK) return s;
+  int64_t* live[2] = {(int64_t*)base, (int64_t*)(base + kNoAllocListBytes)};
+  unsigned long long* counters = (unsigned long long*)(base + kNoAllocCtrOff);
+  int* status = (int*)(base + kNoAllocStatusOff);
+  double* err_info = (double*)(base + kNoAllocInfoOff);
+  cudaStream_t st = (cudaStream_t)stream;
+  // zero on entry: the status word, the error record and both counters; the
+  // live lists are written before they are read
+  PT_CUDA(cudaMemsetAsync(base + kNoAllocCtrOff, 0, kNoAllocBytes - kNoAllocCtrOff, st));
+  const int tb = 256;
+  k_init_primaries<<<(unsigned)((n_primaries + tb - 1) / tb), tb, 0, st>>>(*P, n_primaries, o->primary_offset);
+  k_iota<<<(unsigned)((n_primaries + tb - 1) / tb), tb, 0, st>>>(live[0], n_primaries);
+  // the row count starts at n_primaries, copied from the handle's pinned
+  // host word (made by pt_create; every earlier copy into it has completed)
+  h->h_counters[1] = (unsigned long long)n_primaries;
+  PT_CUDA(cudaMemcpyAsync(counters + 1, h->h_counters + 1, sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
+  RunCtx c;
+  c.T = h->T;
+  c.min_energy = o->min_energy;
+  c.rescale = o->rescale_MCS;
+  c.max_n_integrators = o->max_n_integrators;
+  c.ms = o->multiple_scattering;
+  c.seed = o->seed;
+  c.P = *P;
+  c.n_out = counters + 0;
+  c.n_rows = counters + 1;
+  c.status = status;
+  c.err_info = err_info;
+  int cur = 0;
+  int64_t n_in = n_primaries;
+  const int tbt = 128;
+  h->launches[0] = 2;
+  h->launches[1] = 0;
+  while (n_in > 0) {
+    ++h->launches[0];
+    ++h->launches[1];
+    PT_CUDA(cudaMemsetAsync(counters + 0, 0, sizeof(unsigned long long), st));
+    c.live_in = live[cur];
+    c.n_in = n_in;
+    c.live_out = live[cur ^ 1];
+    c.live_cap = kNoAllocMaxRows;
+    k_transport_fp64<<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
+    PT_CUDA(cudaGetLastError());
+    PT_CUDA(cudaMemcpyAsync(h->h_counters, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaMemcpyAsync(h->h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PT_CUDA(cudaStreamSynchronize(st));
+    if (h->h_status[0] != PT_OK) {
+      PT_CUDA(cudaMemcpy(h->last_info, err_info, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+      *n_rows = (int64_t)h->h_counters[1];
+      return (pt_status)h->h_status[0];
     }
     n_in = (int64_t)h->h_counters[0];
     cur ^= 1;
