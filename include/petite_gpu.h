@@ -212,6 +212,123 @@ pt_status pt_sample_only(pt_handle* h, int32_t process, const double* energy,
 pt_status pt_dsigma(pt_handle* h, int32_t process, const double* x, const double* energy,
                     int64_t n, int32_t precision, double* value, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Dark-vector production on an SM shower (DarkShower, dark_shower.py).
+ * ------------------------------------------------------------------------ */
+enum { PT_N_DARK = 4, PT_DARK_MAX_MASSES = 8 };
+/* Dark process codes (dark_shower.py:49); PT_DARK_BOUND is added to the
+ * output process code when the bound-electron form produced the vector
+ * ("DarkAnn_bound", "DarkComp_bound", dark_shower.py:799-802). */
+enum { PT_DARKBREM = 0, PT_DARKANN = 1, PT_DARKCOMP = 2, PT_DARKMUONBREM = 3, PT_DARK_BOUND = 4 };
+
+/* VEGAS maps of the dark processes for one target, for up to
+ * PT_DARK_MAX_MASSES vector masses (dark_maps.pkl, dark_shower.py:148-201):
+ * rows of (mass m, process p) are [map_base[m*PT_N_DARK+p], +map_rows[...]). */
+typedef struct pt_dark_maps {
+  int32_t n_masses;
+  double mass[PT_DARK_MAX_MASSES];
+  int32_t map_base[PT_DARK_MAX_MASSES * PT_N_DARK];
+  int32_t map_rows[PT_DARK_MAX_MASSES * PT_N_DARK];
+  int32_t n_rows;
+  const double* map_energy;       /* [n_rows] */
+  const double* map_maxF;         /* [n_rows] max_F[target] * maxF_fudge_global */
+  const double* map_neval;        /* [n_rows] */
+  const int64_t* grid_offset;     /* [n_rows*4] */
+  const int32_t* grid_ninc;       /* [n_rows*4] */
+  const double* grid_nodes;
+  int64_t n_nodes;
+  double Z, A;                    /* target Z_T and A_T (A_T is also the target mass
+                                     draw_dark_sample passes, dark_shower.py:673) */
+} pt_dark_maps;
+
+/* One DarkShower's per-mass tables (dark_shower.py:69-130, 219-593), all
+ * device pointers.  Index k of the four weight and dR/dE tables:
+ * 0 = electron DarkBrem, 1 = positron DarkBrem, 2 = positron DarkAnn,
+ * 3 = muon DarkMuonBrem. */
+typedef struct pt_dark_params {
+  int32_t mass_index;             /* map block sampled (the mV estimator) */
+  int32_t bound_electron;         /* 1: bound-electron DarkAnn/DarkComp (the reference default) */
+  int32_t active;                 /* bit p: dark process p active */
+  double mV;                      /* vector mass used in the cross sections and kinematics */
+  double coupling;                /* g_e^2 / (4 pi alpha_em) */
+  double Zeff;
+  double E_res, E_compth;         /* resonant annihilation and Compton threshold energies */
+  double min_dark[5];             /* e- DarkBrem, e+ DarkBrem, e+ DarkAnn, gamma DarkComp, mu DarkMuonBrem */
+  double min_calc_photon;         /* the SM photon minimum (GetBSMWeights, dark_shower.py:612) */
+  const double* w_x[4];           /* track-length weights, interp1d(fill 0) tables */
+  const double* w_y[4];
+  int32_t w_n[4];
+  const double* dr_Ei[4];         /* dR/dE: saved energies [dr_n] */
+  const double* dr_bins[4];       /* [dr_n][dr_nbmax][2] (bin energy, weight) */
+  const int32_t* dr_nbins[4];     /* [dr_n] bins used */
+  int32_t dr_n[4];
+  int32_t dr_nbmax[4];
+  const double* nsc_lx;           /* DarkComp n*sigma, log10 energies and log10 values */
+  const double* nsc_ly;
+  int32_t nsc_n;
+} pt_dark_params;
+
+/* Vectors produced by pt_run_dark (device pointers; SoA like pt_particles). */
+typedef struct pt_dark_out {
+  double* p4;          /* [4][capacity] lab four-momentum */
+  double* r;           /* [3][capacity] production point (the parent's final position) */
+  double* weight;      /* [capacity] */
+  int64_t* parent;     /* [capacity] SM row */
+  int32_t* process;    /* [capacity] dark process code (+PT_DARK_BOUND) */
+  int32_t* draws;      /* [capacity] uniforms used (diagnostic) */
+  int64_t capacity;
+  double* yield;       /* [PT_N_DARK] summed weights per process (accumulated) */
+  double* yield_E;     /* [PT_N_DARK] summed weight * E_V per process (accumulated) */
+} pt_dark_out;
+
+typedef struct pt_dark pt_dark;
+
+/* DarkShower.__init__ (dark_shower.py:69-130): binds the dark maps of one
+ * target to an SM handle (whose tables give the photon n*sigma of
+ * GetBSMWeights and the multiple-scattering constants). */
+pt_status pt_dark_create(pt_handle* sm, const pt_dark_maps* maps, pt_dark** out);
+void pt_dark_destroy(pt_dark* d);
+
+/* The dark differential cross sections draw_dark_sample evaluates
+ * (dark_shower.py:673-684): dsig_dx_dcostheta_dark_brem_exact_tree_level
+ * (all_processes.py:208-372; DarkBrem with m_e, DarkMuonBrem with m_mu),
+ * dsigma_compton_dCT with mV (:624-742) and dsigma_radiative_return_du
+ * (:400-466), at x[i*4 + d], energy[i] and mass mV. */
+pt_status pt_dark_dsigma(pt_dark* d, int32_t process, const double* x, const double* energy, int64_t n, double mV,
+                         double* value, void* stream);
+
+/* DarkShower.draw_dark_sample (dark_shower.py:649-704) for a batch, stream
+ * key[i] from draw 0: x[i*4 + d], proposals[i] (-1 when no sample was found:
+ * the reference returns None), lu_key[i]. */
+pt_status pt_dark_sample_only(pt_dark* d, const pt_dark_params* prm, int32_t process, const double* energy,
+                              const uint64_t* key, int64_t n, const pt_opts* opts, double* x, int64_t* proposals,
+                              int32_t* lu_key, void* stream);
+
+/* DarkShower.generate_dark_shower (dark_shower.py:806-849) over the rows of
+ * an SM particle store: for every row and active process, GetBSMWeights
+ * (:595-647) and, when positive, produce_bsm_particle (:721-804).  Row k,
+ * process p draws from the stream mix64(pkey[k] + 0x9E3779B97F4A7C15*(3+p)).
+ * Vectors are appended to `out` (any order; parent/process identify them);
+ * *n_out returns the count.  PT_OOM if out->capacity is too small. */
+pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles* sm, int64_t n_rows,
+                      const pt_opts* opts, pt_dark_out* out, int64_t* n_out, void* stream);
+
+/* Dark-vector yield at fixed uniforms: for pair i, the map block
+ * mass_index[i] of `process` at LU_Key(energy[i]) and n_samples points whose
+ * uniforms are draws 4j..4j+3 of stream (seed, mix64(4*i + process + 1)):
+ * yield[i] = mean(jac * dsigma(x; energy[i], mV[i])) (the map's cross-section
+ * estimate, find_maxes.py:143-147) and moment[i] = mean(jac * dsigma * E_V).
+ * No counterpart in the reference as one function. */
+pt_status pt_dark_yield(pt_dark* d, int32_t process, const double* energy, const double* mV,
+                        const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
+                        double* yield, double* moment, void* stream);
+
+/* Adjoint of pt_dark_yield with respect to mV: recomputes every sample and
+ * writes g_mV[i] = g_yield[i] * d yield[i]/d mV + g_moment[i] * d moment[i]/d mV. */
+pt_status pt_dark_yield_adjoint(pt_dark* d, int32_t process, const double* energy, const double* mV,
+                                const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
+                                const double* g_yield, const double* g_moment, double* g_mV, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

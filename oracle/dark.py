@@ -1,0 +1,488 @@
+"""CPU restatement of PETITE's dark-vector production on an SM shower (oracle).
+
+TEST INFRASTRUCTURE: used only by ``tests/`` and the CPU baseline of
+``bench.py``; the product never imports it.
+
+Follows ``src/PETITE/``:
+
+* dark bremsstrahlung dsigma     all_processes.py:208-372 (``Log`` variables:
+                                 x, log10(1-cos theta), log10 t~), with the
+                                 form factor of all_processes.py:112-133
+* radiative return dsigma/du     all_processes.py:400-466, radiative_return.py:26-80
+* dark Compton dsigma/dcos       all_processes.py:624-742 (mV > 0 branch)
+* kinematics                     kinematics.py:43-68 (l -> l V), 134-183 (bound
+                                 electron Compton), 267-299 (radiative return),
+                                 radiative_return.py:18-24 (boost)
+* draw_dark_sample               dark_shower.py:649-704
+* draw_pe_sample                 dark_shower.py:706-719
+* GetBSMWeights                  dark_shower.py:595-647
+* produce_bsm_particle           dark_shower.py:721-804
+
+Expressions keep the reference's operation order so float64 results agree to
+a few ulp.  Random numbers come from :mod:`oracle.philox` streams: the stream
+of an SM particle ``k`` and dark process ``p`` is ``dark_key(pkey_k, p)``.
+"""
+from __future__ import annotations
+
+import math
+from bisect import bisect_right
+
+import numpy as np
+
+from . import physics as P
+from .philox import Stream, mix64
+from .shower import interp, map_point
+
+DARK_PROCESSES = ("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")
+DARK_CODE = {p: i for i, p in enumerate(DARK_PROCESSES)}
+DARK_DIM = {"DarkComp": 1, "DarkBrem": 3, "DarkAnn": 1, "DarkMuonBrem": 3}   # dark_shower.py:67
+V_PID = 4900022
+
+
+def dark_key(pkey: int, process: str) -> int:
+    """Stream key of dark process `process` produced by the particle `pkey`
+    (daughters use multipliers 1 and 2; dark processes 3..6)."""
+    return mix64((int(pkey) + 0x9E3779B97F4A7C15 * (3 + DARK_CODE[process])) & 0xFFFFFFFFFFFFFFFF)
+
+
+# ------------------------------------------------------------ cross sections
+def g_el_inel_over_t2(Z, A, t):
+    """Gelastic_inelastic_over_tsquared, all_processes.py:112-133."""
+    me = P.m_electron
+    c1 = (111 * Z ** (-1 / 3) / me) ** 2
+    c2 = 0.164 * P.GeV ** 2 * A ** (-2 / 3)
+    Gel = (1.0 / (1.0 + c1 * t)) ** 2 * (1 + t / c2) ** (-2)
+    ap2 = (773.0 * Z ** (-2.0 / 3) / me) ** 2
+    Ginel = (Z / ((c1 ** 2 * Z ** 2)) * (ap2 / (1.0 + ap2 * t)) ** 2.0
+             * ((1.0 + (2.79 ** 2 - 1.0) * t / (4.0 * P.m_proton ** 2)) / (1.0 + t / 0.71) ** 4))
+    return Z ** 2 * c1 ** 2 * (Gel + Ginel)
+
+
+def dsigma_dark_brem(xv, E, mV, MT, m_lep, Z, A):
+    """dsig_dx_dcostheta_dark_brem_exact_tree_level.__call__ (all_processes.py:227-372),
+    method "Log": xv = (x = E_V/E, log10(1 - cos theta), log10 t~)."""
+    x, l1mct, lttilde = xv
+    one_minus_ct = 10 ** l1mct
+    ct = 1.0 - one_minus_ct
+    ttilde = 10 ** lttilde
+    jac = one_minus_ct * ttilde * math.log(10.0) ** 2
+    k = math.sqrt(math.fabs((x * E) ** 2 - mV ** 2))
+    p = math.sqrt(E ** 2 - m_lep ** 2)
+    V = math.sqrt(p ** 2 + k ** 2 - 2 * p * k * ct)
+    ut = -2 * (x * E ** 2 - k * p * ct) + mV ** 2
+    Er = (1 - x) * E + MT
+    discr = ut ** 2 + 4 * MT * ut * Er + 4 * MT ** 2 * V ** 2
+    rd = math.sqrt(abs(discr))
+    den = 2 * Er ** 2 - 2 * V ** 2
+    Qp = math.fabs((V * (ut + 2 * MT * Er) + Er * rd) / den)
+    Qm = math.fabs((V * (ut + 2 * MT * Er) - Er * rd) / den)
+    tp = 2 * MT * (math.sqrt(MT ** 2 + Qp ** 2) - MT)
+    tm = 2 * MT * (math.sqrt(MT ** 2 + Qm ** 2) - MT)
+    tconv = (2 * MT * (MT + E) * math.sqrt(E ** 2 + m_lep ** 2) / (MT * (MT + 2 * E) + m_lep ** 2)) ** 2
+    t = ttilde * tconv
+    q0 = -t / (2 * MT)
+    q = math.sqrt(t ** 2 / (4 * MT ** 2) + t)
+    cq = -(V ** 2 + q ** 2 + m_lep ** 2 - (E + q0 - x * E) ** 2) / (2 * V * q)
+    mm = mV ** 2 + 2 * m_lep ** 2
+    Am2 = -8 * MT * (4 * E ** 2 * MT - t * (2 * E + MT)) * mm
+    A1 = 8 * MT ** 2 / ut
+    Am1 = (8 / ut) * (MT ** 2 * (2 * t * ut + ut ** 2 + 4 * E ** 2 * (2 * (x - 1) * mm - t * ((x - 2) * x + 2))
+                                 + 2 * t * (-(mV ** 2) + 2 * m_lep ** 2 + t))
+                      - 2 * E * MT * t * ((1 - x) * ut + (x - 2) * (mm + t)) + t ** 2 * (ut - mV ** 2))
+    A0 = (8 / ut ** 2) * (MT ** 2 * (2 * t * ut + (t - 4 * E ** 2 * (x - 1) ** 2) * mm)
+                          + 2 * E * MT * t * (ut - (x - 1) * mm))
+    Y = -t + 2 * q0 * E - 2 * q * p * (p - k * ct) * cq / V
+    W = math.fabs(Y ** 2 - 4 * q ** 2 * p ** 2 * k ** 2 * (1 - ct ** 2) * (1 - cq ** 2) / V ** 2)
+    allowed = (x * E >= mV and discr >= 0 and tp > tm and t > tm and t < tp and math.fabs(cq) <= 1.0 and W > 0)
+    if not allowed:
+        return 0.0
+    phi_int = (A0 + Y * A1 + Am1 / math.sqrt(W) + Y * Am2 / W ** 1.5) / (8 * MT ** 2)
+    ff = g_el_inel_over_t2(Z, A, t)
+    ans = ff * P.alpha_em ** 3 * k * E * phi_int / (p * math.sqrt(k ** 2 + p ** 2 - 2 * p * k * ct))
+    return ans * tconv * jac
+
+
+def _kf_beta(s):
+    return (2. * P.alpha_em / math.pi) * (math.log(s / P.m_electron ** 2) - 1.)
+
+
+def fl_kf(x, s):
+    """radiative_return.py:26-36 (Kuraev-Fadin structure function)."""
+    beta = _kf_beta(s)
+    if x >= 1.0:
+        x = 1. - 1e-10
+    return (beta / 16.) * ((8. + 3. * beta) * (1. - x) ** (beta / 2. - 1.) - 4. * (1. + x))
+
+
+def fl_kf_scaled(x, s):
+    """radiative_return.py:38-47."""
+    beta = _kf_beta(s)
+    return (beta / 16.) * ((8. + 3. * beta) - 4. * (1. + x) * (1. - x) ** (1. - beta / 2.))
+
+
+def transformed_lumi(s, y, u):
+    """transformed_lepton_luminosity_integrand, radiative_return.py:61-80."""
+    beta = _kf_beta(s)
+    x = 1. - u ** (2. / beta)
+    return fl_kf(y / x, s) * fl_kf_scaled(x, s) * (1. / x) * (2. / beta)
+
+
+def dsigma_radiative_return(u0, Ee, mV):
+    """dsigma_radiative_return_du.__call__, all_processes.py:419-466."""
+    me = P.m_electron
+    s = 2.0 * me * (Ee + me)
+    if s < mV ** 2:
+        return 0.0
+    beta = (2.0 * P.alpha_em / math.pi) * (math.log(s / me ** 2) - 1.0)
+    umax = (1.0 - mV ** 2 / s) ** (beta / 2.0)
+    betaf = math.sqrt(1.0 - 4.0 * (me ** 2) / (mV ** 2))
+    prefac = (4.0 * math.pi ** 2) * P.alpha_em * betaf * (3.0 / 2.0 - betaf ** 2 / 2.0) / s * umax
+    x1 = 1.0 - (u0 * umax) ** (2.0 / beta)
+    x2 = mV ** 2 / (x1 * s)
+    if not (x2 < 1.0 and x1 > 0.0 and u0 < 1.0):
+        return 0.0
+    return 2.0 * prefac * transformed_lumi(s, mV ** 2 / s, u0 * umax)
+
+
+def dsigma_dark(process, xv, E, mV, Z, A):
+    """The differential cross section draw_dark_sample evaluates
+    (dark_shower.py:673-684): target mass = A_T, lepton mass by process."""
+    if process == "DarkBrem":
+        return dsigma_dark_brem(xv, E, mV, A, P.m_electron, Z, A)
+    if process == "DarkMuonBrem":
+        return dsigma_dark_brem(xv, E, mV, A, P.m_muon, Z, A)
+    if process == "DarkComp":
+        return P.dsigma_compton(xv[0], E, mV)
+    if process == "DarkAnn":
+        return dsigma_radiative_return(xv[0], E, mV)
+    raise Exception("Your process is not in the list")
+
+
+# --------------------------------------------------------------- kinematics
+def l_to_lV(ep, m_lep, xv, mV, al):
+    """l_to_lV_fourvecs, kinematics.py:43-68 (al = azimuth)."""
+    w = xv[0] * ep
+    ct = (1 - 10 ** xv[1])
+    p, k = math.sqrt(ep ** 2 - m_lep ** 2), math.sqrt(w ** 2 - mV ** 2)
+    cal, sal = math.cos(al), math.sin(al)
+    st = math.sqrt(1.0 - ct ** 2)
+    return (ep, 0, 0, p), (w, k * cal * st, k * sal * st, k * ct)
+
+
+def boost(p, v):
+    """radiative_return.py:18-24: v in the rest frame of p."""
+    def lor(a, b):
+        return a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3]
+    rsq = math.sqrt(lor(p, p))
+    v0 = lor(p, v) / rsq
+    c1 = (v[0] + v0) / (rsq + p[0])
+    return (v0, v[1] - c1 * p[1], v[2] - c1 * p[2], v[3] - c1 * p[3])
+
+
+def radiative_return_V(Ee, u0, mV):
+    """radiative_return_fourvecs, kinematics.py:267-299: the V four-vector."""
+    me = P.m_electron
+    s = 2. * me * (me + Ee)
+    beta = (2. * P.alpha_em / math.pi) * (math.log(s / me ** 2) - 1.)
+    umax = (1. - mV ** 2 / s) ** (beta / 2.)
+    x1 = 1. - (u0 * umax) ** (2. / beta)
+    x2 = mV ** 2 / (x1 * s)
+    E1 = x1 * math.sqrt(s) / 2.
+    E2 = x2 * math.sqrt(s) / 2.
+    pV = (E1 + E2, 0. + 0., 0. + 0., E1 + -E2)
+    return boost((math.sqrt(s) / 2., 0., 0., -math.sqrt(s / 4. - me ** 2)), pV)
+
+
+def compton_bound(Eg, ct, mV, Pe, cte, ph, phie):
+    """compton_fourvecs_boundelectron, kinematics.py:134-183: the V four-vector."""
+    me = P.m_electron
+    s = me ** 2 + 2 * Eg * (math.sqrt(me ** 2 + Pe ** 2) - cte * Pe)
+    rs = math.sqrt(s)
+    Ee = (s - mV ** 2 + me ** 2) / (2 * rs)
+    EV = (s + mV ** 2 - me ** 2) / (2 * rs)
+    pF = math.sqrt(Ee ** 2 - me ** 2)
+    bnum = math.sqrt(Eg ** 2 + 2 * cte * Eg * Pe + Pe ** 2)
+    bden = Eg + math.sqrt(me ** 2 + Pe ** 2)
+    b0 = bnum / bden
+    g0 = 1.0 / math.sqrt(1.0 - b0 ** 2)
+    st = math.sqrt(1 - ct ** 2)
+    EVLab = g0 * EV - b0 * g0 * pF * ct
+    v = (pF * st * math.sin(ph), pF * st * math.cos(ph), b0 * g0 * EV - g0 * pF * ct)
+    ctz = (Eg + cte * Pe) / math.sqrt(Eg ** 2 + 2 * cte * Eg * Pe + Pe ** 2)
+    stz = math.sqrt(1.0 - ctz ** 2)
+    cf, sf = math.cos(phie), math.sin(phie)
+    R = ((ctz * cf, -sf, stz * cf), (ctz * sf, cf, stz * sf), (-stz, 0, ctz))
+    return (EVLab, R[0][0] * v[0] + R[0][1] * v[1] + R[0][2] * v[2],
+            R[1][0] * v[0] + R[1][1] * v[1] + R[1][2] * v[2],
+            R[2][0] * v[0] + R[2][1] * v[1] + R[2][2] * v[2])
+
+
+def electron_wave_function(pe, Zeff):
+    """dark_shower.py:706-708."""
+    lam = P.alpha_em * Zeff * P.m_electron
+    return 32 / math.pi * lam ** 5 * pe ** 2 / (pe ** 2 + lam ** 2) ** 4
+
+
+def draw_pe_sample(Zeff, s: Stream):
+    """dark_shower.py:710-719: accept-reject on [0, 1 MeV]."""
+    c = electron_wave_function(P.alpha_em * Zeff * P.m_electron / math.sqrt(3), Zeff)
+    pe_max = 1e-3
+    while True:
+        x = 0 + (pe_max - 0) * s.next()
+        u = 0 + (1 - 0) * s.next()
+        if u < electron_wave_function(x, Zeff) / (c):
+            return x
+
+
+# ------------------------------------------------------------------ tables
+def closest_lesser(masses, v):
+    """DarkShower.closest_lesser_value (dark_shower.py:158-165) for masses at
+    or above the smallest one (below it the reference wraps to the last)."""
+    arr = np.asarray(masses, dtype=float)
+    i = int(np.abs(arr - v).argmin())
+    return float(arr[i]) if arr[i] <= v else float(arr[i - 1])
+
+
+class DarkTables:
+    """One DarkShower's tables for (target, mV) from the bundled
+    ``dark_tables.npz`` (maps rebuilt with PETITE's find_maxes; weight, dR/dE
+    and bound-electron tables as PETITE's DarkShower constructor builds them)."""
+
+    def __init__(self, npz_path, target, mV, maxF_fudge=1.0, Zeff=29.508, kinetic_mixing=1.0):
+        z = np.load(npz_path, allow_pickle=False)
+        masses = [float(m) for m in z["masses"]]
+        targets = [str(t) for t in z["targets"]]
+        if target not in targets:
+            raise Exception("Target Material is not in library")
+        if mV < masses[0]:
+            raise ValueError("no dark map at or below this mass")
+        self.mV = closest_lesser(masses, mV)
+        key = f"m{self.mV}"
+        j = targets.index(target)
+        ti = P.TARGETS[target]
+        self.Z, self.A, self.rho, self.dEdx = ti["Z_T"], ti["A_T"], ti["rho"], ti["dEdx"]
+        self.Zeff = Zeff
+        g_e = kinetic_mixing * math.sqrt(4 * math.pi * P.alpha_em)
+        self.coupling = g_e ** 2 / (4 * math.pi * P.alpha_em)
+        self.maps = {}
+        for p in DARK_PROCESSES:
+            E = z[f"{key}/{p}/energy"]
+            grid, nn = z[f"{key}/{p}/grid"], z[f"{key}/{p}/nnodes"]
+            self.maps[p] = [dict(E=float(E[i]), neval=int(z[f"{key}/{p}/neval"][i]),
+                                 maxF=float(z[f"{key}/{p}/max_F"][i, j]) * maxF_fudge,
+                                 grid=[grid[i, k, :nn[i, k]].tolist() for k in range(grid.shape[1])])
+                            for i in range(len(E))]
+        self.map_E = {p: np.array([r["E"] for r in rows]) for p, rows in self.maps.items()}
+        pre = f"{key}/{target}"
+        self.E_res = float(z[f"{pre}/E_res"])
+        self.E_compth = float(z[f"{pre}/E_compth"])
+        md = z[f"{pre}/min_dark"]
+        self.min_dark = {(11, "DarkBrem"): md[0], (-11, "DarkBrem"): md[1], (-11, "DarkAnn"): md[2],
+                         (22, "DarkComp"): md[3], (13, "DarkMuonBrem"): md[4], (-13, "DarkMuonBrem"): md[4]}
+        self.weights = {k: (z[f"{pre}/weights/{k}"][:, 0].tolist(), z[f"{pre}/weights/{k}"][:, 1].tolist())
+                        for k in ("brem_elec", "brem_positron", "ann", "muon_brem")}
+        self.drate = {k: (z[f"{pre}/drate/{k}/Ei"], z[f"{pre}/drate/{k}/bins"], z[f"{pre}/drate/{k}/nbins"])
+                      for k in ("brem_elec", "brem_positron", "ann", "muon_brem")}
+        # set_dark_NSigmas (dark_shower.py:286-297): DarkComp, log-log, fill -20
+        DCS = z[f"{pre}/xsec/DarkComp_bound"]
+        nZ = self.rho / P.m_proton_grams / self.A
+        ne = nZ * self.Z
+        self.nsc = (np.log10(DCS[:, 0] + 1e-20).tolist(), np.log10(ne * P.GeVsqcm2 * DCS[:, 1] + 1e-20).tolist())
+
+
+def _interp_fill(v, table, fill):
+    xs, ys = table
+    if not (v >= xs[0]) or v > xs[-1]:
+        return fill
+    return interp(v, table)
+
+
+def _np_sum(a):
+    """numpy's pairwise sum of a short 1-D float64 array."""
+    n = len(a)
+    if n < 8:
+        r = 0.0
+        for x in a:
+            r += x
+        return r
+    r = [float(x) for x in a[:8]]
+    i = 8
+    while i + 8 <= n:
+        for j in range(8):
+            r[j] += a[i + j]
+        i += 8
+    res = ((r[0] + r[1]) + (r[2] + r[3])) + ((r[4] + r[5]) + (r[6] + r[7]))
+    while i < n:
+        res += a[i]
+        i += 1
+    return res
+
+
+class DarkOracle:
+    """GetBSMWeights, draw_dark_sample and produce_bsm_particle on one SM
+    particle record (fields of :class:`oracle.shower.Rec`)."""
+
+    def __init__(self, dark: DarkTables, sm_tables, seed, max_n_integrators=10000, rescale=1.0):
+        self.d, self.sm, self.seed = dark, sm_tables, seed
+        self.max_n_integrators = max_n_integrators
+        self.rescale = rescale
+
+    # dark_shower.py:595-647 (bound-electron form)
+    def weight(self, pid, E, process):
+        d = self.d
+        key = (pid, process)
+        if key not in d.min_dark:
+            return 0.0
+        if E < d.min_dark[key]:
+            return 0.0
+        if pid == 22:
+            if E < self.sm.min_calc[22]:
+                return 0.0
+            nd = 10 ** _interp_fill(math.log10(E), d.nsc, -20.0)
+            return d.coupling * nd / (interp(E, self.sm.ns["PairProd"]) + interp(E, self.sm.ns["Comp"]))
+        name = {(11, "DarkBrem"): "brem_elec", (-11, "DarkBrem"): "brem_positron", (-11, "DarkAnn"): "ann",
+                (13, "DarkMuonBrem"): "muon_brem", (-13, "DarkMuonBrem"): "muon_brem"}[key]
+        return d.coupling * interp(E, d.weights[name])
+
+    # dark_shower.py:649-704
+    def draw(self, E, process, s: Stream, count=None):
+        rows, energies = self.d.maps[process], self.d.map_E[process]
+        key = int(np.argmin(np.abs(energies - E))) + 1
+        if key >= len(rows):
+            key = len(rows) - 1
+        row = rows[key]
+        dim = DARK_DIM[process]
+        proposals = 0
+        for _ in range(self.max_n_integrators):
+            for _ in range(row["neval"]):
+                y = [s.next() for _ in range(dim)]
+                x, jac = map_point(row["grid"], y)
+                wgt = jac / row["neval"]
+                proposals += 1
+                f = dsigma_dark(process, x, E, self.d.mV, self.d.Z, self.d.A)
+                if row["maxF"] * s.next() < wgt * f:
+                    if count is not None:
+                        count.append(proposals)
+                    return x, key
+        if count is not None:
+            count.append(-1)
+        return None, key
+
+    # dark_shower.py:721-804; returns (V four-vector, weight) or None
+    def produce(self, r, process, wg, s: Stream):
+        d, me, mV = self.d, P.m_electron, self.d.mV
+        pf = tuple(r.pf)
+        table = None
+        if process == "DarkAnn" and r.pid == -11:
+            table = "ann"
+        elif process == "DarkBrem":
+            table = "brem_elec" if r.pid == 11 else "brem_positron"
+        elif process == "DarkMuonBrem":
+            table = "muon_brem"
+        if table is not None:
+            Ei_all, bins_all, nb_all = d.drate[table]
+            E0 = r.p0[0]
+            if E0 < Ei_all.min():
+                j = int(np.argmin(Ei_all))
+            elif E0 > Ei_all.max():
+                j = int(np.argmax(Ei_all))
+            else:
+                j = int(np.flatnonzero(Ei_all == max(e for e in Ei_all if e <= E0))[0])
+            nb = int(nb_all[j])
+            en, w = bins_all[j, :nb, 0], bins_all[j, :nb, 1]
+            tot = _np_sum(w)
+            if tot == 0.0:
+                return None
+            p = [x / tot for x in w]
+            cdf, c = [], 0.0
+            for x in p:
+                c += x
+                cdf.append(c)
+            u = s.next()
+            idx = bisect_right([c_ / cdf[-1] for c_ in cdf], u)
+            E_int = en[idx] + (E0 - Ei_all[j])
+            dist = (r.p0[0] - E_int) / (d.dEdx * 0.1)
+            ps = tuple(r.p0)
+            if P.norm3(ps[1], ps[2], ps[3]) > 0:
+                u1, u2, u3, u4 = s.next(), s.next(), s.next(), s.next()
+                ps = P.scattered_momentum_fast(ps, d.rho * (dist / P.cmtom), d.A, d.Z, self.rescale,
+                                               P.m_electron, u1, u2, u3, u4)
+            pf = P.lose_energy(ps, r.mass, E0 - E_int)
+        E0 = pf[0]
+        RM = P.rotation_matrix_from(pf)
+        if process == "DarkAnn" and E0 <= d.E_res:
+            v = (math.sqrt(E0 ** 2 - me ** 2 + mV ** 2), 0, 0, math.sqrt(E0 ** 2 - me ** 2))
+        elif process == "DarkComp" and E0 <= d.E_compth:
+            v = (math.sqrt(E0 ** 2 + mV ** 2), 0, 0, E0)
+        else:
+            x, _ = self.draw(E0, process, s)
+            if x is None:
+                return None
+            if process == "DarkComp":
+                pe = draw_pe_sample(d.Zeff, s)
+                c0 = -1 + (1 - -1) * s.next()
+                ss = me ** 2 + 2 * E0 * (math.sqrt(me ** 2 + pe ** 2) - c0 * pe)
+                Ee = (ss - mV ** 2 + me ** 2) / (2 * math.sqrt(ss))
+                if Ee < me:
+                    v, wg = (mV, 0, 0, 0), 0.0
+                else:
+                    ph = 0 + (2.0 * math.pi - 0) * s.next()
+                    phie_u = s.next()
+                    v = compton_bound(E0, x[0], mV, pe, c0, ph, 0 + (2.0 * math.pi - 0) * phie_u)
+            elif process in ("DarkBrem", "DarkMuonBrem"):
+                al = 0 + (2.0 * math.pi - 0) * s.next()
+                v = l_to_lV(E0, r.mass, x, mV, al)[1]
+            elif process == "DarkAnn":
+                v = radiative_return_V(E0, x[0], mV)
+        lab = (v[0],
+               RM[0][0] * v[1] + RM[0][1] * v[2] + RM[0][2] * v[3],
+               RM[1][0] * v[1] + RM[1][1] * v[2] + RM[1][2] * v[3],
+               RM[2][0] * v[1] + RM[2][1] * v[2] + RM[2][2] * v[3])
+        return lab, wg
+
+    # dark_shower.py:806-849 over SM records
+    def dark_shower(self, records, processes=DARK_PROCESSES):
+        out = []
+        for k, r in enumerate(records):
+            for p in processes:
+                wg = self.weight(r.pid, r.p0[0], p)
+                if wg > 0.0:
+                    s = Stream(self.seed, dark_key(r.pkey, p))
+                    res = self.produce(r, p, wg, s)
+                    if res is not None:
+                        v, w = res
+                        out.append((k, p, w * r.weight, v, tuple(r.rf)))
+        return out
+
+
+# ------------------------------------------------------------- dark yield
+def yield_uniforms(seed, pair, process, j):
+    """Draws 4j..4j+3 of the stream (seed, mix64(4*pair + process + 1))."""
+    from .philox import uniforms
+    return uniforms(seed, mix64(4 * pair + DARK_CODE[process] + 1), 4 * j, 4)
+
+
+def dark_yield(dark: DarkTables, process, E, mV, pair, n_samples, seed):
+    """Mean of jac*dsigma and of jac*dsigma*E_V over the map row LU_Key(E),
+    at the uniforms of :func:`yield_uniforms` (float64, sequential)."""
+    rows, energies = dark.maps[process], dark.map_E[process]
+    key = int(np.argmin(np.abs(energies - E))) + 1
+    if key >= len(rows):
+        key = len(rows) - 1
+    grid = rows[key]["grid"]
+    dim = DARK_DIM[process]
+    from .philox import uniforms
+    u_all = uniforms(seed, mix64(4 * pair + DARK_CODE[process] + 1), 0, 4 * n_samples).reshape(n_samples, 4)
+    sy = sm = 0.0
+    for j in range(n_samples):
+        x, jac = map_point(grid, u_all[j, :dim])
+        f = dsigma_dark(process, x, E, mV, dark.Z, dark.A)
+        if process == "DarkBrem" or process == "DarkMuonBrem":
+            ev = x[0] * E
+        elif process == "DarkComp":
+            ev = P.compton(E, x[0], 0.0, mV)[1][0]
+        else:
+            ev = radiative_return_V(E, x[0], mV)[0]
+        sy += jac * f
+        sm += jac * f * ev
+    return sy / n_samples, sm / n_samples

@@ -18,7 +18,9 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE
 PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
-           "pt_last_kernel_times", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch", "pt_sample_only", "pt_dsigma")
+           "pt_last_kernel_times", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch", "pt_sample_only", "pt_dsigma",
+           "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
+           "pt_dark_yield", "pt_dark_yield_adjoint")
 
 # pt_run_sm_noalloc: largest particle-store capacity (its static scratch)
 NOALLOC_MAX_ROWS = 1 << 19
@@ -64,6 +66,36 @@ class PtOpts(C.Structure):
                 ("primary_offset", C.c_int64)]
 
 
+N_DARK = 4
+DARK_MAX_MASSES = 8
+DARK_BOUND = 4
+
+
+class PtDarkMaps(C.Structure):
+    _fields_ = [("n_masses", C.c_int32), ("mass", C.c_double * DARK_MAX_MASSES),
+                ("map_base", C.c_int32 * (DARK_MAX_MASSES * N_DARK)), ("map_rows", C.c_int32 * (DARK_MAX_MASSES * N_DARK)),
+                ("n_rows", C.c_int32), ("map_energy", C.c_void_p), ("map_maxF", C.c_void_p), ("map_neval", C.c_void_p),
+                ("grid_offset", C.c_void_p), ("grid_ninc", C.c_void_p), ("grid_nodes", C.c_void_p),
+                ("n_nodes", C.c_int64), ("Z", C.c_double), ("A", C.c_double)]
+
+
+class PtDarkParams(C.Structure):
+    _fields_ = [("mass_index", C.c_int32), ("bound_electron", C.c_int32), ("active", C.c_int32),
+                ("mV", C.c_double), ("coupling", C.c_double), ("Zeff", C.c_double),
+                ("E_res", C.c_double), ("E_compth", C.c_double), ("min_dark", C.c_double * 5),
+                ("min_calc_photon", C.c_double),
+                ("w_x", C.c_void_p * 4), ("w_y", C.c_void_p * 4), ("w_n", C.c_int32 * 4),
+                ("dr_Ei", C.c_void_p * 4), ("dr_bins", C.c_void_p * 4), ("dr_nbins", C.c_void_p * 4),
+                ("dr_n", C.c_int32 * 4), ("dr_nbmax", C.c_int32 * 4),
+                ("nsc_lx", C.c_void_p), ("nsc_ly", C.c_void_p), ("nsc_n", C.c_int32)]
+
+
+class PtDarkOut(C.Structure):
+    _fields_ = [("p4", C.c_void_p), ("r", C.c_void_p), ("weight", C.c_void_p), ("parent", C.c_void_p),
+                ("process", C.c_void_p), ("draws", C.c_void_p), ("capacity", C.c_int64),
+                ("yield_", C.c_void_p), ("yield_E", C.c_void_p)]
+
+
 class PetiteGPUError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
@@ -105,6 +137,19 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_run_sm.restype = C.c_int
     lib.pt_run_sm_noalloc.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
     lib.pt_run_sm_noalloc.restype = C.c_int
+    lib.pt_dark_create.argtypes = [vp, C.POINTER(PtDarkMaps), C.POINTER(vp)]
+    lib.pt_dark_destroy.argtypes = [vp]
+    lib.pt_dark_destroy.restype = None
+    lib.pt_dark_dsigma.argtypes = [vp, i32, vp, vp, i64, C.c_double, vp, vp]
+    lib.pt_dark_sample_only.argtypes = [vp, C.POINTER(PtDarkParams), i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp,
+                                        vp]
+    lib.pt_run_dark.argtypes = [vp, C.POINTER(PtDarkParams), C.POINTER(PtParticles), i64, C.POINTER(PtOpts),
+                                C.POINTER(PtDarkOut), C.POINTER(i64), vp]
+    lib.pt_dark_yield.argtypes = [vp, i32, vp, vp, vp, i64, i64, C.c_uint64, vp, vp, vp]
+    lib.pt_dark_yield_adjoint.argtypes = [vp, i32, vp, vp, vp, i64, i64, C.c_uint64, vp, vp, vp, vp]
+    for f in ("pt_dark_create", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark", "pt_dark_yield",
+              "pt_dark_yield_adjoint"):
+        getattr(lib, f).restype = C.c_int
     lib.pt_run_batch.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp]
     lib.pt_run_batch.restype = C.c_int
     lib.pt_sample_only.argtypes = [vp, i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp, vp]

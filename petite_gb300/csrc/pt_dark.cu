@@ -1,0 +1,591 @@
+// pt_dark.cu -- dark-vector production and the differentiable dark yield.
+//
+//  * pt_run_dark: DarkShower.generate_dark_shower (dark_shower.py:806-849)
+//    over an SM particle store.  One thread per (SM row, active dark process)
+//    runs GetBSMWeights (:595-647) and produce_bsm_particle (:721-804): the
+//    interaction energy from the dR/dE table, multiple scattering and the
+//    continuous loss up to it, draw_dark_sample's accept/reject loop on the
+//    dark map (:649-704), the bound-electron momentum (:706-719) and the
+//    vector's four-momentum (kinematics.py:43-68,104-183,267-299).
+//  * pt_dark_yield / pt_dark_yield_adjoint: the map estimate of a dark cross
+//    section at fixed uniforms and its derivative with respect to the vector
+//    mass, one block per (pair), samples split over the block's threads and
+//    summed in a fixed order.
+#include <cmath>
+#include <cstdio>
+#include <new>
+
+#include "pt_dark.cuh"
+#include "pt_internal.cuh"
+#include "pt_physics.cuh"
+
+using namespace pt;
+
+struct pt_dark {
+  Tabs T;                 // SM tables of the bound handle
+  pt_dark_maps M;
+  int* status = nullptr;
+  double* err_info = nullptr;
+  unsigned long long* counter = nullptr;
+  int* h_status = nullptr;
+  unsigned long long* h_counter = nullptr;
+};
+
+namespace {
+
+#define PT_CUDA(call)                                                                 \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess) {                                                          \
+      fprintf(stderr, "petite_gpu: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
+      return PT_CUDA_ERR;                                                             \
+    }                                                                                 \
+  } while (0)
+
+__device__ void dark_raise(int* status, double* info, int code, int process, double E, int key) {
+  if (atomicCAS(status, 0, code) == 0 && info) {
+    info[0] = process; info[1] = E; info[2] = key;
+  }
+}
+
+constexpr int kMaxPeTrials = 1 << 22;   // draw_pe_sample accepts ~1 in 3 trials
+
+// interp1d(kind='linear', bounds_error=False, fill_value=fill) on 1-D tables
+__device__ __forceinline__ double interp_fill(const double* xs, const double* ys, int n, double v, double fill) {
+  if (!(v >= xs[0]) || v > xs[n - 1]) return (v != v) ? v : fill;
+  return interp_tab(xs, ys, n, v);
+}
+
+// ------------------------------------------------------------- dark maps
+__device__ __forceinline__ int dark_lu_key(const pt_dark_maps& M, int block, double E) {
+  const double* Ei = M.map_energy + M.map_base[block];
+  const int n = M.map_rows[block];
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (Ei[mid] < E) lo = mid + 1; else hi = mid;
+  }
+  int best;
+  if (lo == 0) best = 0;
+  else if (lo == n) best = n - 1;
+  else best = (fabs(Ei[lo - 1] - E) <= fabs(Ei[lo] - E)) ? lo - 1 : lo;
+  int key = best + 1;
+  if (key >= n) key = n - 1;
+  return key;
+}
+
+__device__ __forceinline__ int dark_dim(int p) { return (p == PT_DARKBREM || p == PT_DARKMUONBREM) ? 3 : 1; }
+
+template <class T>
+__device__ __forceinline__ T dark_dsigma(const pt_dark_maps& M, int p, const double* x, double E, T mV) {
+  switch (p) {
+    case PT_DARKBREM: return dsig_dark_brem(x, E, mV, M.A, kMe, M.Z, M.A);
+    case PT_DARKMUONBREM: return dsig_dark_brem(x, E, mV, M.A, kMmu, M.Z, M.A);
+    case PT_DARKCOMP: return dsig_dark_compton(x[0], E, mV);
+    default: return dsig_radiative_return(x[0], E, mV);
+  }
+}
+
+// draw_dark_sample (dark_shower.py:649-704); false when no sample was found
+// within max_n_integrators*neval proposals (the reference returns None).
+__device__ bool draw_dark(const pt_dark_maps& M, int block, int p, double E, double mV, int64_t max_n_integrators,
+                          Rng& rng, double* x, int& key, int64_t& proposals) {
+  key = dark_lu_key(M, block, E);
+  const int r = M.map_base[block] + key;
+  const double maxF = M.map_maxF[r];
+  const int neval = (int)M.map_neval[r];
+  const int d = dark_dim(p);
+  proposals = 0;
+  for (int64_t used = 0; used < max_n_integrators; ++used) {
+    for (int j = 0; j < neval; ++j) {
+      double jac = 1.0;
+      for (int k = 0; k < d; ++k) {
+        const double y = rng.u();
+        x[k] = map_dim(M.grid_nodes + M.grid_offset[r * 4 + k], M.grid_ninc[r * 4 + k], y, jac);
+      }
+      const double wgt = jac / neval;
+      ++proposals;
+      const double f = dark_dsigma<double>(M, p, x, E, mV);
+      if (maxF * rng.u() < wgt * f) return true;
+    }
+  }
+  return false;
+}
+
+// ----------------------------------------------------------- GetBSMWeights
+__device__ double bsm_weight(const Tabs& T, const pt_dark_params& P, int pid, double E, int p) {
+  if (!((P.active >> p) & 1)) return 0.0;
+  int k;                                     // weight table / min_dark slot
+  if (p == PT_DARKBREM && pid == 11) k = 0;
+  else if (p == PT_DARKBREM && pid == -11) k = 1;
+  else if (p == PT_DARKANN && pid == -11) k = 2;
+  else if (p == PT_DARKCOMP && pid == 22) k = 3;
+  else if (p == PT_DARKMUONBREM && (pid == 13 || pid == -13)) k = 4;
+  else return 0.0;
+  if (E < P.min_dark[k]) return 0.0;
+  if (k == 3) {
+    if (E < P.min_calc_photon) return 0.0;
+    const double nd = pow(10.0, interp_fill(P.nsc_lx, P.nsc_ly, P.nsc_n, log10(E), -20.0));
+    return P.coupling * nd / (nsig(T, 1, E) + nsig(T, 3, E));
+  }
+  const int w = (k == 4) ? 3 : k;
+  return P.coupling * interp_tab(P.w_x[w], P.w_y[w], P.w_n[w], E);
+}
+
+// np.sum of the bin weights as numpy computes it for a short 1-D array:
+// sequential below 8 elements, else eight partial sums combined pairwise and
+// the remainder added in order.
+__device__ double np_sum_weights(const double* bins, int nb) {
+  if (nb < 8) {
+    double tot = 0.0;
+    for (int i = 0; i < nb; ++i) tot = (S(tot) + S(bins[2 * i + 1])).v;
+    return tot;
+  }
+  double r[8];
+  for (int i = 0; i < 8; ++i) r[i] = bins[2 * i + 1];
+  int i = 8;
+  for (; i + 8 <= nb; i += 8)
+    for (int j = 0; j < 8; ++j) r[j] = (S(r[j]) + S(bins[2 * (i + j) + 1])).v;
+  double tot = (((S(r[0]) + S(r[1])) + (S(r[2]) + S(r[3]))) + ((S(r[4]) + S(r[5])) + (S(r[6]) + S(r[7])))).v;
+  for (; i < nb; ++i) tot = (S(tot) + S(bins[2 * i + 1])).v;
+  return tot;
+}
+
+// numpy.random.choice(energies, p=w/tot): cumsum of w/tot, normalised by its
+// last entry, searchsorted(u, side='right').
+__device__ int drate_choice(const double* bins, int nb, double tot, double u) {
+  double last = 0.0;
+  for (int i = 0; i < nb; ++i) last = (S(last) + S(bins[2 * i + 1]) / S(tot)).v;
+  double cum = 0.0;
+  for (int i = 0; i < nb; ++i) {
+    cum = (S(cum) + S(bins[2 * i + 1]) / S(tot)).v;
+    if ((S(cum) / S(last)).v > u) return i;
+  }
+  return nb - 1;
+}
+
+struct DarkRow {
+  int pid;
+  double p0[4], pf[4], rf[3], mass, weight;
+  uint64_t key;
+};
+
+// produce_bsm_particle (dark_shower.py:721-804).  Returns false when the
+// reference returns None; on true, V and wg hold the vector and its weight.
+__device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
+                            const DarkRow& r, int p, double& wg, double* V, Rng& rng, int* status, double* info) {
+  double pf[4] = {r.pf[0], r.pf[1], r.pf[2], r.pf[3]};
+  int table = -1;
+  if (p == PT_DARKANN && r.pid == -11) table = 2;
+  else if (p == PT_DARKBREM) table = (r.pid == 11) ? 0 : 1;
+  else if (p == PT_DARKMUONBREM) table = 3;
+  if (table >= 0) {
+    const double* Ei = P.dr_Ei[table];
+    const int n = P.dr_n[table];
+    const double E0 = r.p0[0];
+    int j;
+    if (E0 < Ei[0]) j = 0;
+    else if (E0 > Ei[n - 1]) j = n - 1;
+    else {                                            // largest saved energy <= E0
+      int lo = 0, hi = n - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (Ei[mid] <= E0) lo = mid; else hi = mid - 1;
+      }
+      j = lo;
+    }
+    const double* bins = P.dr_bins[table] + (size_t)j * P.dr_nbmax[table] * 2;
+    const int nb = P.dr_nbins[table][j];
+    const double tot = np_sum_weights(bins, nb);
+    if (tot == 0.0) return false;                 // dark_shower.py:742-743, before any draw
+    const int idx = drate_choice(bins, nb, tot, rng.u());
+    const double E_int = (S(bins[2 * idx]) + (S(E0) - S(Ei[j]))).v;
+    const double dEdx = T.t.dEdx_GeV_per_m;
+    const double dist = ((S(E0) - S(E_int)) / S(dEdx)).v;
+    double ps[4] = {r.p0[0], r.p0[1], r.p0[2], r.p0[3]};
+    mcs_fast(ps, (S(T.t.rho) * (S(dist) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, o.rescale_MCS, kMe, rng);
+    pf[0] = ps[0]; pf[1] = ps[1]; pf[2] = ps[2]; pf[3] = ps[3];
+    lose_energy(pf, r.mass, (S(E0) - S(E_int)).v);
+  }
+  const double E0 = pf[0];
+  const Rot R = rotation_from(pf);
+  const double mV = P.mV, me = kMe;
+  V4 v;
+  const bool bound = P.bound_electron != 0;
+  if (p == PT_DARKANN && bound && E0 <= P.E_res) {
+    const double pz = sqrt((S(E0) * S(E0) - S(me) * S(me)).v);
+    v = {sqrt((S(E0) * S(E0) - S(me) * S(me) + S(mV) * S(mV)).v), 0.0, 0.0, pz};
+  } else if (p == PT_DARKCOMP && bound && E0 <= P.E_compth) {
+    v = {sqrt((S(E0) * S(E0) + S(mV) * S(mV)).v), 0.0, 0.0, E0};
+  } else {
+    double x[4] = {0, 0, 0, 0};
+    int key;
+    int64_t props;
+    const int block = P.mass_index * PT_N_DARK + p;
+    if (!draw_dark(M, block, p, E0, mV, o.max_n_integrators, rng, x, key, props)) return false;
+    if (p == PT_DARKCOMP && bound) {
+      // draw_pe_sample (dark_shower.py:706-719)
+      const S lam = S(kAlpha) * S(P.Zeff) * S(me);
+      const S lam5(pow(lam.v, 5.0));
+      auto wave = [&](S pe) {
+        return S(32.0) / S(kPi) * lam5 * (pe * pe) / S(pow((pe * pe + lam * lam).v, 4.0));
+      };
+      const S c = wave(lam / S(sqrt(3.0)));
+      double pe = -1.0;
+      for (int it = 0; it < kMaxPeTrials; ++it) {
+        const S xx = S(0.0) + (S(1e-3) - S(0.0)) * S(rng.u());
+        const S uu = S(0.0) + (S(1.0) - S(0.0)) * S(rng.u());
+        if (uu.v < (wave(xx) / c).v) { pe = xx.v; break; }
+      }
+      if (pe < 0.0) { dark_raise(status, info, PT_TIMEOUT, p, E0, 0); return false; }
+      const double c0 = (S(-1.0) + (S(1.0) - S(-1.0)) * S(rng.u())).v;
+      const S s = S(me) * S(me) + S(2.0) * S(E0) * (ssqrt(S(me) * S(me) + S(pe) * S(pe)) - S(c0) * S(pe));
+      const S Ee = (s - S(mV) * S(mV) + S(me) * S(me)) / (S(2.0) * ssqrt(s));
+      if (Ee.v < me) {
+        v = {mV, 0.0, 0.0, 0.0};
+        wg = 0.0;
+      } else {
+        // compton_fourvecs_boundelectron (kinematics.py:134-183), the V row
+        const S Eg(E0), ct(x[0]), Pe(pe), cte(c0), mv(mV), m(me);
+        const S rs = ssqrt(s);
+        const S EV = (s + mv * mv - m * m) / (S(2.0) * rs);
+        const S pF = ssqrt(Ee * Ee - m * m);
+        const S bnum = ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
+        const S bden = Eg + ssqrt(m * m + Pe * Pe);
+        const S b0 = bnum / bden;
+        const S g0 = S(1.0) / ssqrt(S(1.0) - b0 * b0);
+        const S ph = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+        const S st = ssqrt(S(1.0) - ct * ct);
+        const S EVL = g0 * EV - b0 * g0 * pF * ct;
+        const S a0 = pF * st * S(sin(ph.v)), a1 = pF * st * S(cos(ph.v)), a2 = b0 * g0 * EV - g0 * pF * ct;
+        const S ctz = (Eg + cte * Pe) / ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
+        const S stz = ssqrt(S(1.0) - ctz * ctz);
+        const S phe = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+        const S cf(cos(phe.v)), sf(sin(phe.v));
+        v = {EVL.v, (ctz * cf * a0 + (-sf) * a1 + stz * cf * a2).v, (ctz * sf * a0 + cf * a1 + stz * sf * a2).v,
+             ((-stz) * a0 + S(0.0) * a1 + ctz * a2).v};
+      }
+    } else if (p == PT_DARKBREM || p == PT_DARKMUONBREM) {
+      // l_to_lV_fourvecs (kinematics.py:43-68), the V row
+      const S ep(E0), m(r.mass), mv(mV);
+      const S w = S(x[0]) * ep;
+      const S ct = S(1.0) - S(pow(10.0, x[1]));
+      const S k = ssqrt(w * w - mv * mv);
+      const S al = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+      const S cal(cos(al.v)), sal(sin(al.v));
+      const S st = ssqrt(S(1.0) - ct * ct);
+      (void)m;
+      v = {w.v, (k * cal * st).v, (k * sal * st).v, (k * ct).v};
+    } else if (p == PT_DARKANN) {
+      // radiative_return_fourvecs (kinematics.py:267-299) with boost
+      // (radiative_return.py:18-24)
+      const S s = S(2.0) * S(me) * (S(me) + S(E0));
+      const double beta = (S(2.0) * S(kAlpha) / S(kPi) * (S(log((s / (S(me) * S(me))).v)) - S(1.0))).v;
+      const S umax = S(pow((S(1.0) - S(mV) * S(mV) / s).v, beta / 2.0));
+      const S x1 = S(1.0) - S(pow((S(x[0]) * umax).v, 2.0 / beta));
+      const S x2 = S(mV) * S(mV) / (x1 * s);
+      const S rs = ssqrt(s);
+      const S E1 = x1 * rs / S(2.0), E2 = x2 * rs / S(2.0);
+      const S q0 = rs / S(2.0), q3 = -ssqrt(s / S(4.0) - S(me) * S(me));
+      const S w0 = E1 + E2, w3 = E1 + (-E2);
+      const S rsq = ssqrt(q0 * q0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * q3);
+      const S v0 = (q0 * w0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * w3) / rsq;
+      const S c1 = (w0 + v0) / (rsq + q0);
+      v = {v0.v, (S(0.0) - c1 * S(0.0)).v, (S(0.0) - c1 * S(0.0)).v, (w3 - c1 * q3).v};
+    } else {
+      // compton_fourvecs with mV (kinematics.py:104-132), the V row
+      const S Eg(E0), ct(x[0]), m(me), mv(mV);
+      const S s = m * m + S(2.0) * Eg * m;
+      const S rs = ssqrt(s);
+      const S Ee0 = (s + m * m) / (S(2.0) * rs);
+      const S Ee = (s - mv * mv + m * m) / (S(2.0) * rs);
+      const S EV = (s + mv * mv - m * m) / (S(2.0) * rs);
+      const S pF = ssqrt(Ee * Ee - m * m);
+      const S g0 = Ee0 / m;
+      const S b0 = S(1.0) / g0 * ssqrt(g0 * g0 - S(1.0));
+      const S ph = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+      const S st = ssqrt(S(1.0) - ct * ct);
+      v = {(g0 * EV - b0 * g0 * pF * ct).v, (pF * st * S(sin(ph.v))).v, (pF * st * S(cos(ph.v))).v,
+           (b0 * g0 * EV - g0 * pF * ct).v};
+    }
+  }
+  const V4 lab = to_lab(R, v);
+  V[0] = lab.e; V[1] = lab.x; V[2] = lab.y; V[3] = lab.z;
+  return true;
+}
+
+__global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, pt_particles sm, int64_t n_rows,
+                           pt_dark_out out, unsigned long long* counter, int* status, double* info) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= n_rows * PT_N_DARK) return;
+  const int64_t row = t / PT_N_DARK;
+  const int p = (int)(t % PT_N_DARK);
+  DarkRow r;
+  r.pid = sm.pid[row];
+  const int64_t cap = sm.capacity;
+  for (int c = 0; c < 4; ++c) { r.p0[c] = sm.p0[c * cap + row]; r.pf[c] = sm.pf[c * cap + row]; }
+  for (int c = 0; c < 3; ++c) r.rf[c] = sm.rf[c * cap + row];
+  r.mass = sm.mass[row];
+  r.weight = sm.weight[row];
+  r.key = sm.pkey[row];
+  double wg = bsm_weight(T, P, r.pid, r.p0[0], p);
+  if (!(wg > 0.0)) return;
+  Rng rng;
+  rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
+  double V[4];
+  if (!produce_bsm(T, M, P, o, r, p, wg, V, rng, status, info)) return;
+  const double w = (S(wg) * S(r.weight)).v;
+  if (out.yield) atomicAdd(out.yield + p, w);
+  if (out.yield_E) atomicAdd(out.yield_E + p, w * V[0]);
+  if (!out.p4) return;
+  const unsigned long long slot = atomicAdd(counter, 1ull);
+  if ((int64_t)slot >= out.capacity) { dark_raise(status, nullptr, PT_OOM, p, r.p0[0], 0); return; }
+  const int64_t oc = out.capacity;
+  for (int c = 0; c < 4; ++c) out.p4[c * oc + slot] = V[c];
+  for (int c = 0; c < 3; ++c) out.r[c * oc + slot] = r.rf[c];
+  out.weight[slot] = w;
+  out.parent[slot] = row;
+  out.process[slot] = p + ((P.bound_electron && (p == PT_DARKANN || p == PT_DARKCOMP)) ? PT_DARK_BOUND : 0);
+  out.draws[slot] = (int32_t)rng.n;
+}
+
+__global__ void k_dark_sample_only(pt_dark_maps M, pt_dark_params P, int p, const double* E, const uint64_t* key,
+                                   int64_t n, uint64_t seed, int64_t max_n_integrators, double* x, int64_t* props,
+                                   int32_t* keys) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Rng rng;
+  rng.init(seed, key[i]);
+  double xx[4] = {0, 0, 0, 0};
+  int lk;
+  int64_t pr;
+  const bool ok = draw_dark(M, P.mass_index * PT_N_DARK + p, p, E[i], P.mV, max_n_integrators, rng, xx, lk, pr);
+  for (int k = 0; k < 4; ++k) x[i * 4 + k] = xx[k];
+  props[i] = ok ? pr : -1;
+  keys[i] = lk;
+}
+
+__global__ void k_dark_dsigma(pt_dark_maps M, int p, const double* x, const double* E, int64_t n, double mV,
+                              double* out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double xx[4];
+  for (int k = 0; k < 4; ++k) xx[k] = x[i * 4 + k];
+  out[i] = dark_dsigma<double>(M, p, xx, E[i], mV);
+}
+
+// ------------------------------------------------------------- dark yield
+constexpr int kYieldThreads = 256;
+
+template <class T>
+__device__ __forceinline__ T dark_EV(int p, const double* x, double E, T mV) {
+  if (p == PT_DARKCOMP) return dark_compton_EV(x[0], E, mV);
+  if (p == PT_DARKANN) return dark_ann_EV(x[0], E, mV);
+  return T(mV * 0.0) + x[0] * E;               // l_to_lV: E_V = x E
+}
+
+// One block per pair.  Sample j uses draws 4j..4j+3 of the pair's stream
+// (Philox blocks 2j and 2j+1); the block's partial sums are combined in a
+// fixed tree order, so results do not depend on timing.
+template <class T, bool ADJ>
+__global__ void __launch_bounds__(kYieldThreads) k_dark_yield(pt_dark_maps M, int p, const double* Ein,
+                                                               const double* mVin, const int32_t* mass_index,
+                                                               int64_t n_samples, uint64_t seed, double* yield,
+                                                               double* moment, const double* gY, const double* gM,
+                                                               double* g_mV) {
+  __shared__ double sh_y[kYieldThreads], sh_m[kYieldThreads];
+  const int64_t i = blockIdx.x;
+  const double E = Ein[i];
+  T mV;
+  if constexpr (ADJ) mV = T{mVin[i], 1.0};
+  else mV = mVin[i];
+  const int block = mass_index[i] * PT_N_DARK + p;
+  const int key = dark_lu_key(M, block, E);
+  const int r = M.map_base[block] + key;
+  const int d = dark_dim(p);
+  const uint32_t s0 = (uint32_t)seed, s1 = (uint32_t)(seed >> 32);
+  const uint64_t skey = mix64((uint64_t)i * 4 + (uint64_t)p + 1);
+  const uint32_t k0 = (uint32_t)skey, k1 = (uint32_t)(skey >> 32);
+  double acc_y = 0.0, acc_m = 0.0;
+  for (int64_t j = threadIdx.x; j < n_samples; j += kYieldThreads) {
+    double u[4];
+    const uint64_t b0 = 2 * (uint64_t)j;
+    uint4 o = philox4x32_10(make_uint4((uint32_t)b0, (uint32_t)(b0 >> 32), k0, k1), s0, s1);
+    u[0] = (double)(((uint64_t)o.x | ((uint64_t)o.y << 32)) >> 11) * 0x1p-53;
+    u[1] = (double)(((uint64_t)o.z | ((uint64_t)o.w << 32)) >> 11) * 0x1p-53;
+    if (d > 2) {
+      const uint64_t b1 = b0 + 1;
+      o = philox4x32_10(make_uint4((uint32_t)b1, (uint32_t)(b1 >> 32), k0, k1), s0, s1);
+      u[2] = (double)(((uint64_t)o.x | ((uint64_t)o.y << 32)) >> 11) * 0x1p-53;
+      u[3] = 0.0;
+    }
+    double x[4] = {0, 0, 0, 0};
+    double jac = 1.0;
+    for (int k = 0; k < d; ++k) x[k] = map_dim(M.grid_nodes + M.grid_offset[r * 4 + k], M.grid_ninc[r * 4 + k], u[k], jac);
+    const T f = dark_dsigma<T>(M, p, x, E, mV);
+    const T fe = f * dark_EV<T>(p, x, E, mV);
+    if constexpr (ADJ) {
+      acc_y += jac * f.d;
+      acc_m += jac * fe.d;
+    } else {
+      acc_y += jac * f;
+      acc_m += jac * fe;
+    }
+  }
+  sh_y[threadIdx.x] = acc_y;
+  sh_m[threadIdx.x] = acc_m;
+  __syncthreads();
+  for (int w = kYieldThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh_y[threadIdx.x] += sh_y[threadIdx.x + w];
+      sh_m[threadIdx.x] += sh_m[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ny = sh_y[0] / (double)n_samples, nm = sh_m[0] / (double)n_samples;
+    if constexpr (ADJ) g_mV[i] = gY[i] * ny + gM[i] * nm;
+    else { yield[i] = ny; moment[i] = nm; }
+  }
+}
+
+pt_status read_dark_status(pt_dark* d, cudaStream_t st) {
+  PT_CUDA(cudaMemcpyAsync(d->h_status, d->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PT_CUDA(cudaStreamSynchronize(st));
+  return (pt_status)d->h_status[0];
+}
+
+}  // namespace
+
+extern "C" pt_status pt_dark_create(pt_handle* sm, const pt_dark_maps* m, pt_dark** out) {
+  if (!sm || !m || !out) return PT_BAD_ARG;
+  *out = nullptr;
+  if (m->n_masses <= 0 || m->n_masses > PT_DARK_MAX_MASSES || m->n_rows <= 0 || !m->map_energy || !m->map_maxF ||
+      !m->map_neval || !m->grid_offset || !m->grid_ninc || !m->grid_nodes)
+    return PT_BAD_TABLE;
+  for (int b = 0; b < m->n_masses * PT_N_DARK; ++b)
+    if (m->map_rows[b] < 0 || m->map_base[b] < 0 || m->map_base[b] + m->map_rows[b] > m->n_rows) return PT_BAD_TABLE;
+  pt_dark* d = new (std::nothrow) pt_dark();
+  if (!d) return PT_OOM;
+  d->T = *handle_parts(sm).T;
+  d->M = *m;
+  if (cudaMalloc(&d->status, sizeof(int)) != cudaSuccess || cudaMalloc(&d->err_info, 4 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d->counter, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&d->h_status, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost(&d->h_counter, sizeof(unsigned long long)) != cudaSuccess) {
+    pt_dark_destroy(d);
+    return PT_CUDA_ERR;
+  }
+  *out = d;
+  return PT_OK;
+}
+
+extern "C" void pt_dark_destroy(pt_dark* d) {
+  if (!d) return;
+  cudaFree(d->status);
+  cudaFree(d->err_info);
+  cudaFree(d->counter);
+  cudaFreeHost(d->h_status);
+  cudaFreeHost(d->h_counter);
+  delete d;
+}
+
+extern "C" pt_status pt_dark_dsigma(pt_dark* d, int32_t process, const double* x, const double* energy, int64_t n,
+                                    double mV, double* value, void* stream) {
+  if (!d || process < 0 || process >= PT_N_DARK || n < 0) return PT_BAD_ARG;
+  if (n == 0) return PT_OK;
+  if (!x || !energy || !value) return PT_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  k_dark_dsigma<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d->M, process, x, energy, n, mV, value);
+  PT_CUDA(cudaGetLastError());
+  PT_CUDA(cudaStreamSynchronize(st));
+  return PT_OK;
+}
+
+static bool mass_block_ok(const pt_dark* d, const pt_dark_params* prm, int p) {
+  if (prm->mass_index < 0 || prm->mass_index >= d->M.n_masses) return false;
+  return d->M.map_rows[prm->mass_index * PT_N_DARK + p] >= 2;
+}
+
+extern "C" pt_status pt_dark_sample_only(pt_dark* d, const pt_dark_params* prm, int32_t process, const double* energy,
+                                         const uint64_t* key, int64_t n, const pt_opts* o, double* x,
+                                         int64_t* proposals, int32_t* lu_key, void* stream) {
+  if (!d || !prm || !o || process < 0 || process >= PT_N_DARK || n < 0) return PT_BAD_ARG;
+  if (!mass_block_ok(d, prm, process)) return PT_BAD_TABLE;
+  if (n == 0) return PT_OK;
+  if (!energy || !key || !x || !proposals || !lu_key) return PT_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  k_dark_sample_only<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(d->M, *prm, process, energy, key, n, o->seed,
+                                                                  o->max_n_integrators, x, proposals, lu_key);
+  PT_CUDA(cudaGetLastError());
+  PT_CUDA(cudaStreamSynchronize(st));
+  return PT_OK;
+}
+
+extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles* sm, int64_t n_rows,
+                                 const pt_opts* o, pt_dark_out* out, int64_t* n_out, void* stream) {
+  if (!d || !prm || !sm || !o || !out || !n_out || n_rows < 0 || n_rows > sm->capacity) return PT_BAD_ARG;
+  if (prm->mass_index < 0 || prm->mass_index >= d->M.n_masses) return PT_BAD_TABLE;
+  for (int p = 0; p < PT_N_DARK; ++p)
+    if (((prm->active >> p) & 1) && !mass_block_ok(d, prm, p)) return PT_BAD_TABLE;
+  for (int k = 0; k < 4; ++k)
+    if (!prm->w_x[k] || !prm->w_y[k] || prm->w_n[k] < 2 || !prm->dr_Ei[k] || !prm->dr_bins[k] || !prm->dr_nbins[k] ||
+        prm->dr_n[k] < 1 || prm->dr_nbmax[k] < 1)
+      return PT_BAD_TABLE;
+  if (!prm->nsc_lx || !prm->nsc_ly || prm->nsc_n < 2) return PT_BAD_TABLE;
+  if (out->p4 && (!out->r || !out->weight || !out->parent || !out->process || !out->draws || out->capacity < 0))
+    return PT_BAD_ARG;
+  *n_out = 0;
+  if (n_rows == 0) return PT_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  PT_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
+  PT_CUDA(cudaMemsetAsync(d->counter, 0, sizeof(unsigned long long), st));
+  const int64_t work = n_rows * PT_N_DARK;
+  const int tb = 128;
+  k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(d->T, d->M, *prm, *o, *sm, n_rows, *out, d->counter,
+                                                             d->status, d->err_info);
+  PT_CUDA(cudaGetLastError());
+  PT_CUDA(cudaMemcpyAsync(d->h_counter, d->counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  const pt_status s = read_dark_status(d, st);
+  *n_out = (int64_t)d->h_counter[0];
+  return s;
+}
+
+template <bool ADJ>
+static pt_status dark_yield_launch(pt_dark* d, int32_t process, const double* energy, const double* mV,
+                                   const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
+                                   double* yield, double* moment, const double* gY, const double* gM, double* g_mV,
+                                   void* stream) {
+  if (!d || process < 0 || process >= PT_N_DARK || n_pairs < 0 || n_samples <= 0 || n_pairs > 0x7fffffff)
+    return PT_BAD_ARG;
+  if (n_pairs == 0) return PT_OK;
+  if (!energy || !mV || !mass_index) return PT_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if constexpr (ADJ) {
+    if (!gY || !gM || !g_mV) return PT_BAD_ARG;
+    k_dark_yield<Dual, true><<<(unsigned)n_pairs, kYieldThreads, 0, st>>>(d->M, process, energy, mV, mass_index,
+                                                                        n_samples, seed, nullptr, nullptr, gY, gM,
+                                                                        g_mV);
+  } else {
+    if (!yield || !moment) return PT_BAD_ARG;
+    k_dark_yield<double, false><<<(unsigned)n_pairs, kYieldThreads, 0, st>>>(
+        d->M, process, energy, mV, mass_index, n_samples, seed, yield, moment, nullptr, nullptr, nullptr);
+  }
+  PT_CUDA(cudaGetLastError());
+  return PT_OK;
+}
+
+extern "C" pt_status pt_dark_yield(pt_dark* d, int32_t process, const double* energy, const double* mV,
+                                   const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
+                                   double* yield, double* moment, void* stream) {
+  return dark_yield_launch<false>(d, process, energy, mV, mass_index, n_pairs, n_samples, seed, yield, moment,
+                                  nullptr, nullptr, nullptr, stream);
+}
+
+extern "C" pt_status pt_dark_yield_adjoint(pt_dark* d, int32_t process, const double* energy, const double* mV,
+                                           const int32_t* mass_index, int64_t n_pairs, int64_t n_samples,
+                                           uint64_t seed, const double* g_yield, const double* g_moment,
+                                           double* g_mV, void* stream) {
+  return dark_yield_launch<true>(d, process, energy, mV, mass_index, n_pairs, n_samples, seed, nullptr, nullptr,
+                                 g_yield, g_moment, g_mV, stream);
+}

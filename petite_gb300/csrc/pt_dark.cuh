@@ -1,0 +1,208 @@
+// pt_dark.cuh -- dark-vector physics of PETITE (DarkShower), float64.
+//
+// The differential cross sections are templates over the scalar type of the
+// dark-vector mass: `double` for sampling and yields, `Dual` (value and
+// derivative with respect to mV) for the adjoint of the dark yield.  Every
+// other input is a plain double.  Expressions keep the reference's
+// operation order; each function cites the PETITE function it follows
+// (paths inside src/PETITE/).
+#pragma once
+#include "pt_common.cuh"
+
+namespace pt {
+
+// ------------------------------------------------------------ dual numbers
+struct Dual {
+  double v, d;
+};
+__device__ __forceinline__ Dual mkd(double v, double d = 0.0) { return Dual{v, d}; }
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ Dual operator+(double a, Dual b) { return {a + b.v, b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, double b) { return {a.v - b, a.d}; }
+__device__ __forceinline__ Dual operator-(double a, Dual b) { return {a - b.v, -b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+  const double q = a.v / b.v;
+  return {q, (a.d - q * b.d) / b.v};
+}
+__device__ __forceinline__ Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+__device__ __forceinline__ Dual operator/(double a, Dual b) {
+  const double q = a / b.v;
+  return {q, -q * b.d / b.v};
+}
+
+__device__ __forceinline__ double val(double x) { return x; }
+__device__ __forceinline__ double val(Dual x) { return x.v; }
+__device__ __forceinline__ double dsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ Dual dsqrt(Dual x) {
+  const double s = sqrt(x.v);
+  return {s, x.d == 0.0 ? 0.0 : x.d / (2.0 * s)};
+}
+__device__ __forceinline__ double dabs(double x) { return fabs(x); }
+__device__ __forceinline__ Dual dabs(Dual x) { return x.v < 0.0 ? -x : x; }
+__device__ __forceinline__ double dpow(double x, double e) { return pow(x, e); }
+__device__ __forceinline__ Dual dpow(Dual x, double e) {
+  const double p = pow(x.v, e);
+  return {p, x.d == 0.0 ? 0.0 : e * pow(x.v, e - 1.0) * x.d};
+}
+__device__ __forceinline__ double dlog(double x) { return log(x); }
+__device__ __forceinline__ Dual dlog(Dual x) { return {log(x.v), x.d / x.v}; }
+template <class T>
+__device__ __forceinline__ T sqr(T x) { return x * x; }
+
+constexpr double kMproton = 938.272088 * kMeV;
+constexpr double kLn10 = 2.302585092994046;
+
+// ------------------------------------------------------ dark bremsstrahlung
+// Gelastic_inelastic_over_tsquared (all_processes.py:112-133)
+__device__ __forceinline__ double g_el_inel_over_t2(double Z, double A, double t) {
+  const double c1 = sqr(111 * pow(Z, -1.0 / 3) / kMe);
+  const double c2 = 0.164 * pow(A, -2.0 / 3);
+  const double Gel = sqr(1.0 / (1.0 + c1 * t)) * pow(1 + t / c2, -2.0);
+  const double ap2 = sqr(773.0 * pow(Z, -2.0 / 3) / kMe);
+  const double Ginel = Z / (sqr(c1) * sqr(Z)) * sqr(ap2 / (1.0 + ap2 * t)) *
+                       ((1.0 + (2.79 * 2.79 - 1.0) * t / (4.0 * sqr(kMproton))) / pow(1.0 + t / 0.71, 4.0));
+  return sqr(Z) * sqr(c1) * (Gel + Ginel);
+}
+
+// dsig_dx_dcostheta_dark_brem_exact_tree_level.__call__, method "Log"
+// (all_processes.py:227-372): x = (E_V/E, log10(1 - cos theta), log10 t~),
+// target mass MT, lepton mass m.
+template <class T>
+__device__ T dsig_dark_brem(const double* xv, double E, T mV, double MT, double m, double Z, double A) {
+  const double x = xv[0];
+  const double omc = pow(10.0, xv[1]);
+  const double ct = 1.0 - omc;
+  const double tt = pow(10.0, xv[2]);
+  const double jac = omc * tt * (kLn10 * kLn10);
+  const T mV2 = mV * mV;
+  const T k = dsqrt(dabs(sqr(x * E) - mV2));
+  const double p = sqrt(E * E - m * m);
+  const T V = dsqrt(p * p + k * k - 2 * p * k * ct);
+  const T ut = -2 * (x * (E * E) - k * p * ct) + mV2;
+  const double Er = (1 - x) * E + MT;
+  const T discr = ut * ut + 4 * MT * ut * Er + 4 * (MT * MT) * (V * V);
+  const T rd = dsqrt(dabs(discr));
+  const T den = 2 * (Er * Er) - 2 * (V * V);
+  const T Qp = dabs((V * (ut + 2 * MT * Er) + Er * rd) / den);
+  const T Qm = dabs((V * (ut + 2 * MT * Er) - Er * rd) / den);
+  const T tp = 2 * MT * (dsqrt(MT * MT + Qp * Qp) - MT);
+  const T tm = 2 * MT * (dsqrt(MT * MT + Qm * Qm) - MT);
+  const double tconv = sqr(2 * MT * (MT + E) * sqrt(E * E + m * m) / (MT * (MT + 2 * E) + m * m));
+  const double t = tt * tconv;
+  const double q0 = -t / (2 * MT);
+  const double q = sqrt(t * t / (4 * (MT * MT)) + t);
+  const T cq = -(V * V + q * q + m * m - sqr(E + q0 - x * E)) / (2 * V * q);
+  const T mm = mV2 + 2 * (m * m);
+  const T Am2 = -8 * MT * (4 * (E * E) * MT - t * (2 * E + MT)) * mm;
+  const T A1 = 8 * (MT * MT) / ut;
+  const T Am1 = (8 / ut) * ((MT * MT) * (2 * t * ut + ut * ut +
+                                         4 * (E * E) * (2 * (x - 1) * mm - t * ((x - 2) * x + 2)) +
+                                         2 * t * (-mV2 + 2 * (m * m) + t)) -
+                            2 * E * MT * t * ((1 - x) * ut + (x - 2) * (mm + t)) + (t * t) * (ut - mV2));
+  const T A0 = (8 / (ut * ut)) * ((MT * MT) * (2 * t * ut + (t - 4 * (E * E) * sqr(x - 1)) * mm) +
+                                  2 * E * MT * t * (ut - (x - 1) * mm));
+  const T Y = -t + 2 * q0 * E - 2 * q * p * (p - k * ct) * cq / V;
+  const T W = dabs(Y * Y - 4 * (q * q) * (p * p) * (k * k) * (1 - ct * ct) * (1 - cq * cq) / (V * V));
+  const bool allowed = (x * E >= val(mV)) && (val(discr) >= 0) && (val(tp) > val(tm)) && (t > val(tm)) &&
+                       (t < val(tp)) && (fabs(val(cq)) <= 1.0) && (val(W) > 0);
+  if (!allowed) return T(mV * 0.0);
+  const T phi = (A0 + Y * A1 + Am1 / dsqrt(W) + Y * Am2 / dpow(W, 1.5)) / (8 * (MT * MT));
+  const double ff = g_el_inel_over_t2(Z, A, t);
+  const T ans = ff * (kAlpha * kAlpha * kAlpha) * k * E * phi / (p * dsqrt(k * k + p * p - 2 * p * k * ct));
+  return ans * tconv * jac;
+}
+
+// ----------------------------------------------------------- dark Compton
+// dsigma_compton_dCT.__call__ with mV > 0 (all_processes.py:639-742)
+template <class T>
+__device__ T dsig_dark_compton(double ct, double Eg, T mV) {
+  const double me = kMe, me2 = me * me, me4 = me2 * me2;
+  const double s = me2 + 2 * Eg * me;
+  if (s < val(sqr(me + mV))) return T(mV * 0.0);
+  const T mV2 = mV * mV;
+  const T root = dsqrt(me4 + sqr(mV2 - s) - 2 * me2 * (mV2 + s));
+  const T jac = (s - me2) / (2 * s) * dsqrt(sqr(s - mV2) - 2 * me2 * (s + mV2) + me4);
+  const T t = -1.0 / 2 * (me4 + s * (-mV2 + s + ct * root) - me2 * (mV2 + 2 * s + ct * root)) / s;
+  const double PF = 2.0 * kPi * (kAlpha * kAlpha) / sqr(s - me2);
+  const T T1 = (2.0 * me2 * (mV2 - 3 * s) - 3 * me4 - 2 * mV2 * s + 2 * (mV2 * mV2) + s * s) /
+               ((me2 - s) * (me2 + mV2 - s - t));
+  const T T2 = (2 * me2 * (2 * me2 + mV2)) / sqr(me2 + mV2 - s - t);
+  const T T3 = ((me2 + s) * (me2 + mV2 + s) + t * (s - me2)) / sqr(me2 - s);
+  return PF * jac * (T1 + T2 + T3);
+}
+
+// ------------------------------------------------ radiative return (DarkAnn)
+// Kuraev-Fadin structure functions (radiative_return.py:26-47)
+__device__ __forceinline__ double kf_beta(double s) {
+  return (2. * kAlpha / kPi) * (log(s / (kMe * kMe)) - 1.);
+}
+template <class T>
+__device__ __forceinline__ T fl_kf(T x, double beta) {
+  if (val(x) >= 1.0) x = T(x * 0.0) + (1. - 1e-10);
+  return (beta / 16.) * ((8. + 3. * beta) * dpow(1. - x, beta / 2. - 1.) - 4. * (1. + x));
+}
+template <class T>
+__device__ __forceinline__ T fl_kf_scaled(T x, double beta) {
+  return (beta / 16.) * ((8. + 3. * beta) - 4. * (1. + x) * dpow(1. - x, 1. - beta / 2.));
+}
+// dsigma_radiative_return_du.__call__ (all_processes.py:419-466) with
+// transformed_lepton_luminosity_integrand (radiative_return.py:61-80)
+template <class T>
+__device__ T dsig_radiative_return(double u0, double Ee, T mV) {
+  const double me = kMe;
+  const double s = 2.0 * me * (Ee + me);
+  const T mV2 = mV * mV;
+  if (s < val(mV2)) return T(mV * 0.0);
+  const double beta = kf_beta(s);
+  const T umax = dpow(1.0 - mV2 / s, beta / 2.0);
+  const T betaf = dsqrt(1.0 - 4.0 * (me * me) / mV2);
+  const T prefac = (4.0 * (kPi * kPi)) * kAlpha * betaf * (3.0 / 2.0 - betaf * betaf / 2.0) / s * umax;
+  const T u = u0 * umax;
+  const T x1 = 1.0 - dpow(u, 2.0 / beta);
+  const T x2 = mV2 / (x1 * s);
+  if (!(val(x2) < 1.0 && val(x1) > 0.0 && u0 < 1.0)) return T(mV * 0.0);
+  // transformed luminosity at (s, y = mV^2/s, u): x = 1 - u^(2/beta) (= x1)
+  const T y = mV2 / s;
+  const T lumi = fl_kf(y / x1, beta) * fl_kf_scaled(x1, beta) * (1. / x1) * (2. / beta);
+  return 2.0 * prefac * lumi;
+}
+
+// ------------------------------------------------ energies of the dark vector
+// Lab energy of V for the yield moments: x*E (kinematics.py:57), the Compton
+// form (kinematics.py:119-130) and the boosted radiative-return form
+// (kinematics.py:282-298).
+template <class T>
+__device__ T dark_compton_EV(double ct, double Eg, T mV) {
+  const double me = kMe;
+  const double s = me * me + 2 * Eg * me, rs = sqrt(s);
+  const T mV2 = mV * mV;
+  const double Ee0 = (s + me * me) / (2.0 * rs);
+  const T Ee = (s - mV2 + me * me) / (2 * rs);
+  const T EV = (s + mV2 - me * me) / (2 * rs);
+  const T pF = dsqrt(Ee * Ee - me * me);
+  const double g0 = Ee0 / me;
+  const double b0 = 1.0 / g0 * sqrt(g0 * g0 - 1.0);
+  return g0 * EV - b0 * g0 * pF * ct;
+}
+template <class T>
+__device__ T dark_ann_EV(double u0, double Ee, T mV) {
+  const double me = kMe;
+  const double s = 2. * me * (me + Ee), rs = sqrt(s);
+  const double beta = kf_beta(s);
+  const T mV2 = mV * mV;
+  const T umax = dpow(1. - mV2 / s, beta / 2.);
+  const T x1 = 1. - dpow(u0 * umax, 2. / beta);
+  const T x2 = mV2 / (x1 * s);
+  const T E1 = x1 * rs / 2., E2 = x2 * rs / 2.;
+  const double p0 = rs / 2., p3 = -sqrt(s / 4. - me * me);
+  const double rsq = sqrt(p0 * p0 - p3 * p3);
+  return (p0 * (E1 + E2) - p3 * (E1 - E2)) / rsq;
+}
+
+}  // namespace pt

@@ -252,6 +252,7 @@ def batch_to_particles(b: ShowerBatch, primaries):
             part.set_pf(b.pf[r].copy())
             part.set_rf(b.rf[r].copy())
             part.set_ended(True)
+            part._pkey = int(b.pkey[r])
             ids_of[r] = (part.get_ids()["ID"], part.get_ids()["generation_number"], part.get_ids()["PID"])
             out[k].append(part)
             continue
@@ -265,6 +266,7 @@ def batch_to_particles(b: ShowerBatch, primaries):
         part.set_pf(b.pf[r].copy())
         part.set_rf(b.rf[r].copy())
         part.set_ended(True)
+        part._pkey = int(b.pkey[r])          # random-stream key (dark production draws from it)
         ids_of[r] = (my_id, gen_parent + 1, int(b.pid[r]))
         out[k].append(part)
     return out

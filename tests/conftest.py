@@ -8,7 +8,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-BUNDLED_NPZ = os.path.join(ROOT, "petite_gb300", "data", "sm_tables.npz")
+BUNDLED_DIR = os.path.join(ROOT, "petite_gb300", "data")
+BUNDLED_NPZ = os.path.join(BUNDLED_DIR, "sm_tables.npz")
 
 
 def pytest_configure(config):

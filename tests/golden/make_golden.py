@@ -19,7 +19,9 @@ The particle being processed is tracked by wrapping the Shower instance's
 ``propagate_particle`` and ``sample_scattering``; daughters get the keys of
 ``oracle.philox.daughter_key``.
 
-Usage: python tests/golden/make_golden.py DICT_DIR   (DICT_DIR from rebuild_maps.py)
+Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|all]
+(DICT_DIR from rebuild_maps.py; for ``dark`` it must also hold the output of
+``rebuild_maps.py --dark``)
 """
 import copy
 import math
@@ -106,6 +108,19 @@ def install(router):
     random.uniform = r_uniform
     vegas.UNIFORM = lambda n: np.array([router.u() for _ in range(n)])
     return saved
+
+
+def install_dark(router):
+    """The dark module imports numpy's random() under its own name."""
+    import PETITE.dark_shower as ds
+    saved = ds.draw_U
+    ds.draw_U = lambda: router.u()
+    return saved
+
+
+def uninstall_dark(saved):
+    import PETITE.dark_shower as ds
+    ds.draw_U = saved
 
 
 def uninstall(saved):
@@ -332,6 +347,154 @@ def gen_units(dict_dir, out_path):
     print("units written", out_path)
 
 
+DARK_PROCS = ["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"]
+V_PROC_CODE = {"DarkBrem": 0, "DarkAnn": 1, "DarkComp": 2, "DarkMuonBrem": 3,
+               "DarkAnn_bound": 1, "DarkComp_bound": 2}
+
+
+def gen_dark(dict_dir, out_path):
+    """Dark-vector production: cross sections, kinematics, draw_dark_sample and
+    generate_dark_shower on routed SM showers (dark_shower.py:595-849)."""
+    refimport.setup()
+    import PETITE.all_processes as proc
+    from PETITE import kinematics as kin
+    from PETITE.dark_shower import DarkShower
+    from PETITE.particle import Particle
+    from PETITE.physical_constants import m_electron, m_muon, alpha_em
+    from oracle.dark import dark_key
+    rng = np.random.default_rng(777)
+    out = {}
+    fns = {"DarkBrem": proc.dsig_dx_dcostheta_dark_brem_exact_tree_level,
+           "DarkMuonBrem": proc.dsig_dx_dcostheta_dark_brem_exact_tree_level,
+           "DarkComp": proc.dsigma_compton_dCT, "DarkAnn": proc.dsigma_radiative_return_du}
+    showers = {}
+    for mV in (0.01, 0.1, 0.3):
+        for t in ("graphite", "lead"):
+            ds = DarkShower(dict_dir, t, 0.010, mV, active_processes=list(DARK_PROCS))
+            showers[(mV, t)] = ds
+            for pname in DARK_PROCS:
+                rows = ds._loaded_dark_samples[pname]
+                X, E, V = [], [], []
+                for r in rng.choice(len(rows), size=10, replace=False):
+                    Erow, info = rows[r]
+                    amap = info["adaptive_map"]
+                    d = len(amap.grid)
+                    for _ in range(6):
+                        Einc = float(Erow) * float(rng.uniform(0.9, 1.1))
+                        x, _ = amap.map_one(rng.random(d))
+                        ev = {'E_inc': Einc, 'm_e': m_electron, 'Z_T': ds._ZTarget, 'A_T': ds._ATarget,
+                              'mT': ds._ATarget, 'alpha_FS': alpha_em, 'mV': ds._mV, 'Eg_min': ds._Egamma_min,
+                              'Zeff': ds.Zeff,
+                              'm_lepton': m_muon if pname == "DarkMuonBrem" else m_electron}
+                        with np.errstate(all="ignore"):
+                            v = float(fns[pname](event_info=ev, ndim=d)(np.asarray(x)))
+                        X.append(np.pad(x, (0, 3 - d))); E.append(Einc); V.append(v)
+                out[f"dsigma/{mV}/{t}/{pname}/x"] = np.array(X)
+                out[f"dsigma/{mV}/{t}/{pname}/E"] = np.array(E)
+                out[f"dsigma/{mV}/{t}/{pname}/value"] = np.array(V)
+    router = StreamRouter(SEED)
+    saved = install(router)
+    saved_d = install_dark(router)
+    try:
+        # ---- dark kinematics with routed azimuths
+        K = []
+        for case in range(120):
+            kind = case % 5
+            mV = (0.01, 0.1, 0.3)[case % 3]
+            router.set_current(50_000 + case)
+            if kind in (0, 1):
+                m = m_electron if kind == 0 else m_muon
+                E = float(10 ** rng.uniform(0, 2))
+                part = Particle([E, 0, 0, math.sqrt(E * E - m * m)], [0, 0, 0], {"PID": 11 if kind == 0 else 13, "mass": m})
+                x = [rng.uniform(mV / E * 1.01, 0.999), rng.uniform(-6, -0.5), 0.0]
+                a, b = kin.l_to_lV_fourvecs(part, x, mV=mV)
+                extra = [0.0, 0.0]
+            elif kind == 2:
+                E = float(10 ** rng.uniform(0, 2)) + mV ** 2 / (2 * m_electron) + mV
+                part = Particle([E, 0, 0, E], [0, 0, 0], {"PID": 22, "mass": 0.0})
+                x = [rng.uniform(-1, 1), 0.0, 0.0]
+                a, b = kin.compton_fourvecs(part, x, mV=mV)
+                extra = [0.0, 0.0]
+            elif kind == 3:
+                E = float(10 ** rng.uniform(0, 2)) + mV ** 2 / (2 * m_electron) + mV
+                part = Particle([E, 0, 0, E], [0, 0, 0], {"PID": 22, "mass": 0.0})
+                x = [rng.uniform(-1, 1), 0.0, 0.0]
+                pe, cte = float(rng.uniform(0, 1e-3)), float(rng.uniform(-1, 1))
+                a, b = kin.compton_fourvecs_boundelectron(part, x, mV=mV, Pe=pe, cte=cte)
+                extra = [pe, cte]
+            else:
+                E = (mV ** 2 - 2 * m_electron ** 2) / (2 * m_electron) * float(rng.uniform(1.05, 3.0))
+                part = Particle([E, 0, 0, math.sqrt(E * E - m_electron ** 2)], [0, 0, 0], {"PID": -11, "mass": m_electron})
+                x = [rng.uniform(0.0, 0.999), 0.0, 0.0]
+                a, b = kin.radiative_return_fourvecs(part, x, mV=mV)
+                extra = [0.0, 0.0]
+            K.append(np.concatenate([[kind, mV, E], x, extra, a, b]))
+        out["kin/rows"] = np.array(K)
+        # ---- draw_dark_sample (VB: x and proposal count) on fixed streams
+        D = []
+        ds = showers[(0.1, "graphite")]
+        for case, (pname, E) in enumerate([(p, e) for p in DARK_PROCS for e in (0.5, 3.0, 20.0, 90.0)]):
+            if pname in ("DarkAnn", "DarkComp") and E < 10.0:
+                E = E + 10.0          # above the 0.1 GeV maps' first rows
+            router.set_current(60_000 + case)
+            x = ds.draw_dark_sample(E, process=pname, VB=True)
+            D.append(np.concatenate([[case, DARK_PROCS.index(pname), E], np.pad(x[:-1], (0, 3 - (len(x) - 1))), [x[-1]]]))
+        out["draw/rows"] = np.array(D)
+        # ---- dark showers on routed SM showers
+        for name, mV, t, pid, E0, n in (("e10_graphite_m0.1", 0.1, "graphite", 11, 10.0, 2),
+                                        ("e10_graphite_m0.03", 0.03, "graphite", 11, 10.0, 2),
+                                        ("g5_lead_m0.01", 0.01, "lead", 22, 5.0, 2)):
+            ds = showers.get((mV, t)) or DarkShower(dict_dir, t, 0.010, mV, active_processes=list(DARK_PROCS))
+            # a fresh router per case: streams restart at draw 0 for every key
+            router.streams.clear()
+            wrap_shower(ds, router)
+            orig_pb = ds.produce_bsm_particle
+            where = {}
+
+            def pb(p_original, process, weight=None, VB=False, _orig=orig_pb, _where=where):
+                router.set_current(dark_key(p_original._pkey, process))
+                v = _orig(p_original, process, weight=weight, VB=VB)
+                if v is not None:
+                    _where[id(v)] = (id(p_original), process)
+                return v
+
+            ds.produce_bsm_particle = pb
+            SMF, SMI, SMK, VV, WW = [], [], [], [], []
+            t0 = time.time()
+            for j in range(n):
+                m = 0.0 if pid == 22 else 0.000511
+                part = Particle([E0, 0.0, 0.0, math.sqrt(E0 * E0 - m * m)], [0.0, 0.0, 0.0], {"PID": pid})
+                part._pkey = primary_key(j)
+                sm = ds.generate_shower(part)
+                f, i, _, k, _ = shower_arrays(sm, router, j)
+                base = sum(len(x) for x in SMF)
+                index = {id(p): base + r for r, p in enumerate(sm)}
+                W = np.zeros((len(sm), len(DARK_PROCS)))
+                for r, p in enumerate(sm):
+                    for c, pc in enumerate(DARK_PROCS):
+                        W[r, c] = ds.GetBSMWeights(p, pc)
+                _, vs = ds.generate_dark_shower(ExDir=list(sm))
+                for v in vs:
+                    src, pc = where[id(v)]
+                    d = v.get_ids()
+                    VV.append(np.concatenate([[index[src], V_PROC_CODE[d["generation_process"]],
+                                               DARK_PROCS.index(pc), d["weight"]], v.get_p0(), v.get_r0()]))
+                SMF.append(f); SMI.append(i); SMK.append(k); WW.append(W)
+            out[f"shower/{name}/sm_f64"] = np.concatenate(SMF)
+            out[f"shower/{name}/sm_i64"] = np.concatenate(SMI)
+            out[f"shower/{name}/sm_pkey"] = np.concatenate(SMK)
+            out[f"shower/{name}/weights"] = np.concatenate(WW)
+            out[f"shower/{name}/V"] = np.array(VV)
+            out[f"shower/{name}/params"] = np.array([mV, E0, pid, n])
+            out[f"shower/{name}/target"] = np.array(t)
+            print(f"dark {name}: {len(out[f'shower/{name}/sm_f64'])} SM rows, {len(VV)} V, {time.time() - t0:.1f} s")
+    finally:
+        uninstall_dark(saved_d)
+        uninstall(saved)
+    np.savez_compressed(out_path, **out)
+    print("dark golden written", out_path)
+
+
 CASES = [
     # name, target, cut, pid, E0, n primaries, primary mass for the momentum
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 12, 0.000511),
@@ -347,3 +510,5 @@ if __name__ == "__main__":
         gen_units(d, os.path.join(HERE, "units.npz"))
     if which in ("all", "showers"):
         gen_showers(d, os.path.join(HERE, "showers.npz"), CASES)
+    if which in ("all", "dark"):
+        gen_dark(d, os.path.join(HERE, "dark.npz"))

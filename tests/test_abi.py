@@ -57,12 +57,13 @@ def test_struct_layout_matches_header(tmp_path):
         pytest.skip("gcc not available")
     from petite_gb300 import _lib
     structs = {"pt_tables": _lib.PtTables, "pt_particles": _lib.PtParticles, "pt_opts": _lib.PtOpts,
-               "pt_tally": _lib.PtTally}
+               "pt_tally": _lib.PtTally, "pt_dark_maps": _lib.PtDarkMaps, "pt_dark_params": _lib.PtDarkParams,
+               "pt_dark_out": _lib.PtDarkOut}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "petite_gpu.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
         for f, _ in cls._fields_:
-            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f.rstrip("_")}));')
     lines += ["  return 0;", "}"]
     src = tmp_path / "probe.c"
     src.write_text("\n".join(lines))

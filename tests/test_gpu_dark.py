@@ -1,0 +1,178 @@
+"""Dark-vector production and the differentiable dark yield on the GPU, through
+the C ABI, against the oracle and the reference's golden vectors."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import BUNDLED_DIR, BUNDLED_NPZ, GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5EED
+G = np.load(os.path.join(GOLDEN, "dark.npz"))
+DARK_NPZ = os.path.join(BUNDLED_DIR, "dark_tables.npz")
+
+
+@pytest.fixture(scope="module")
+def showers():
+    from petite_gb300.dark import DarkShower
+    out = {}
+    for mV, t in ((0.1, "graphite"), (0.03, "graphite"), (0.01, "lead"), (0.3, "graphite"), (0.01, "graphite"),
+                  (0.1, "lead"), (0.3, "lead")):
+        out[(mV, t)] = DarkShower(None, t, 0.010, mV, seed=SEED,
+                                  active_processes=["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"])
+    return out
+
+
+@pytest.mark.parametrize("mV", [0.01, 0.1, 0.3])
+@pytest.mark.parametrize("target", ["graphite", "lead"])
+def test_dark_dsigma_matches_oracle_and_reference(showers, mV, target):
+    from oracle import dark as D
+    from oracle import physics as P
+    eng = showers[(mV, target)]._dark_engine
+    ti = P.TARGETS[target]
+    for code, proc in enumerate(D.DARK_PROCESSES):
+        pre = f"dsigma/{mV}/{target}/{proc}"
+        X, E, V = G[f"{pre}/x"], G[f"{pre}/E"], G[f"{pre}/value"]
+        got = eng.dsigma(code, X, E, mV)
+        want = np.array([D.dsigma_dark(proc, x, e, mV, ti["Z_T"], ti["A_T"]) for x, e in zip(X, E)])
+        # fused multiply-adds and CUDA's pow/log against the oracle's rounded
+        # operations: the dark-brem form subtracts the nearly equal t+/- and
+        # W = |Y^2 - ...| terms, the radiative-return form raises 1-x to ~-1
+        rtol = 1e-8
+        np.testing.assert_allclose(got, want, rtol=rtol, atol=0, err_msg=proc)
+        np.testing.assert_allclose(got, V, rtol=rtol, atol=0, err_msg=proc)
+
+
+def test_draw_dark_sample_matches_reference(showers):
+    from oracle import dark as D
+    sh = showers[(0.1, "graphite")]
+    for row in G["draw/rows"]:
+        case, pi, E = int(row[0]), int(row[1]), row[2]
+        proc = D.DARK_PROCESSES[pi]
+        x, props, _ = sh._dark_engine.sample_only(sh._prm, pi, [E], [np.uint64(60_000 + case)], sh._opts())
+        assert props[0] == int(row[-1]), (proc, E)
+        np.testing.assert_allclose(x[0, :D.DARK_DIM[proc]], row[3:3 + D.DARK_DIM[proc]], rtol=1e-12, atol=0)
+
+
+def _store_from_golden(sh, name):
+    import torch
+    from petite_gb300.engine import ParticleStore
+    F, I, K = G[f"shower/{name}/sm_f64"], G[f"shower/{name}/sm_i64"], G[f"shower/{name}/sm_pkey"]
+    n = len(F)
+    st = ParticleStore(n, sh._engine.device)
+    dev = sh._engine.device
+    st.t["p0"][:, :n] = torch.as_tensor(F[:, 0:4].T.copy(), device=dev)
+    st.t["pf"][:, :n] = torch.as_tensor(F[:, 7:11].T.copy(), device=dev)
+    st.t["rf"][:, :n] = torch.as_tensor(F[:, 11:14].T.copy(), device=dev)
+    st.t["weight"][:n] = torch.as_tensor(F[:, 14].copy(), device=dev)
+    st.t["mass"][:n] = torch.as_tensor(F[:, 15].copy(), device=dev)
+    st.t["pid"][:n] = torch.as_tensor(I[:, 0].astype(np.int32), device=dev)
+    st.t["pkey"][:n] = torch.as_tensor(K.astype(np.uint64).view(np.int64), device=dev)
+    return st, n
+
+
+@pytest.mark.parametrize("name", ["e10_graphite_m0.1", "e10_graphite_m0.03", "g5_lead_m0.01"])
+def test_run_dark_matches_reference_showers(showers, name):
+    mV = float(G[f"shower/{name}/params"][0])
+    target = str(G[f"shower/{name}/target"])
+    sh = showers[(mV, target)]
+    st, n = _store_from_golden(sh, name)
+    res = sh._dark_engine.run_dark(sh._prm, st, n, sh._opts())
+    V = G[f"shower/{name}/V"]
+    want = V[np.lexsort((V[:, 2], V[:, 0]))]
+    proc = res["process"] % 4
+    o = np.lexsort((proc, res["parent"]))
+    assert res["n"] == len(want)
+    assert np.array_equal(res["parent"][o], want[:, 0].astype(np.int64))
+    assert np.array_equal(proc[o], want[:, 2].astype(np.int64))
+    assert np.array_equal(res["process"][o] >= 4, np.isin(want[:, 2], (1, 2)))     # *_bound forms
+    np.testing.assert_allclose(res["weight"][o], want[:, 3], rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(res["r"][o], want[:, 8:11])
+    np.testing.assert_allclose(res["p4"][o][:, 0], want[:, 4], rtol=1e-12, atol=0)
+    scale = np.abs(want[:, 4:8]).max(1)
+    err = np.abs(res["p4"][o] - want[:, 4:8]).max(1) / scale
+    assert err.max() <= 1e-9, err.max()
+    # summed yields
+    np.testing.assert_allclose(res["yield"][:3], [want[want[:, 2] == p, 3].sum() for p in range(3)], rtol=1e-12)
+
+
+def test_generate_dark_shower_dropin(showers):
+    from petite_gb300 import Particle
+    sh = showers[(0.1, "graphite")]
+    part = Particle([10.0, 0, 0, math.sqrt(100 - 0.000511 ** 2)], [0, 0, 0], {"PID": 11})
+    sm, vs = sh.generate_dark_shower(SParams=part)
+    assert len(sm) > 50 and len(vs) > 10
+    ids = {p.get_ids()["ID"]: p for p in sm}
+    for v in vs:
+        d = v.get_ids()
+        assert d["PID"] == 4900022
+        parent = ids[d["parent_ID"]]
+        assert d["ID"] == 2 * d["parent_ID"]
+        assert d["parent_PID"] == parent.get_ids()["PID"]
+        assert d["generation_number"] == parent.get_ids()["generation_number"] + 1
+        assert d["generation_process"] in ("DarkBrem", "DarkAnn_bound", "DarkComp_bound")
+        assert np.array_equal(v.get_r0(), parent.get_rf())
+        p4 = v.get_p0()
+        assert p4[0] ** 2 - p4[1] ** 2 - p4[2] ** 2 - p4[3] ** 2 == pytest.approx(0.1 ** 2, rel=1e-6)
+    w = sh.GetBSMWeights(sm[0], "DarkBrem")
+    assert w > 0
+
+
+def test_dark_yield_matches_oracle(showers):
+    from oracle import dark as D
+    from petite_gb300.dark import dark_yield
+    sh = showers[(0.1, "graphite")]
+    eng = sh._dark_engine
+    tabs = D.DarkTables(DARK_NPZ, "graphite", 0.1)
+    E = np.array([0.5, 2.0, 8.0, 30.0])
+    mV = np.array([0.1, 0.12, 0.2, 0.25])
+    for proc in ("DarkBrem", "DarkComp", "DarkAnn"):
+        Y, M = dark_yield(eng, proc, E, mV, n_samples=1500, seed=SEED, mass_index=np.full(4, eng.mass_index(0.1)))
+        Y, M = Y.cpu().numpy(), M.cpu().numpy()
+        for i in range(len(E)):
+            y, m = D.dark_yield(tabs, proc, E[i], mV[i], i, 1500, SEED)
+            np.testing.assert_allclose([Y[i], M[i]], [y, m], rtol=1e-8, atol=0, err_msg=proc)
+
+
+def test_dark_yield_gradient_matches_finite_differences(showers):
+    """4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV, mV log-uniform on
+    [0.001, 0.3] GeV, 10^4 map samples each: the adjoint d(yield)/d(mV) and
+    d(moment)/d(mV) against central differences of the forward kernel
+    (h = 1e-4 relative), within 1e-3 relative."""
+    import torch
+    from petite_gb300.dark import dark_yield, map_mass_index
+    sh = showers[(0.1, "graphite")]
+    eng = sh._dark_engine
+    rng = np.random.default_rng(4)
+    n = 4096
+    E = 10 ** rng.uniform(math.log10(0.05), 1.0, n)
+    mVh = 10 ** rng.uniform(-3, math.log10(0.3), n)
+    mi = map_mass_index(eng.data.masses, mVh)
+    h = 1e-4 * mVh
+    for proc in ("DarkBrem", "DarkComp", "DarkAnn"):
+        mV = torch.tensor(mVh, dtype=torch.float64, device=eng.device, requires_grad=True)
+        Y, M = dark_yield(eng, proc, E, mV, n_samples=10_000, seed=SEED, mass_index=mi)
+        (Y.sum()).backward()
+        gY = mV.grad.cpu().numpy().copy()
+        mV.grad = None
+        Y, M = dark_yield(eng, proc, E, mV, n_samples=10_000, seed=SEED, mass_index=mi)
+        (M.sum()).backward()
+        gM = mV.grad.cpu().numpy().copy()
+        with torch.no_grad():
+            Yp, Mp = dark_yield(eng, proc, E, mVh + h, n_samples=10_000, seed=SEED, mass_index=mi)
+            Ym, Mm = dark_yield(eng, proc, E, mVh - h, n_samples=10_000, seed=SEED, mass_index=mi)
+        fdY = (Yp - Ym).cpu().numpy() / (2 * h)
+        fdM = (Mp - Mm).cpu().numpy() / (2 * h)
+        Yv = Y.detach().cpu().numpy()
+        ok = np.isfinite(Yv) & (Yv > 0) & np.isfinite(fdY)
+        assert ok.sum() > 100, proc
+        # a sample that crosses a kinematic boundary between mV-h and mV+h
+        # makes the difference quotient jump; those pairs are rare and counted
+        relY = np.abs(gY[ok] - fdY[ok]) / np.maximum(np.abs(fdY[ok]), 1e-300)
+        relM = np.abs(gM[ok] - fdM[ok]) / np.maximum(np.abs(fdM[ok]), 1e-300)
+        print(proc, "pairs", ok.sum(), "median rel", np.median(relY), "frac>1e-3", np.mean(relY > 1e-3))
+        assert np.mean(relY <= 1e-3) > 0.99, (proc, np.sort(relY)[-10:])
+        assert np.mean(relM <= 1e-3) > 0.99, (proc, np.sort(relM)[-10:])

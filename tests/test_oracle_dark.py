@@ -1,0 +1,108 @@
+"""Pins the dark-vector oracle (oracle/dark.py) to golden vectors produced by
+the unmodified reference (tests/golden/make_golden.py, ``dark`` mode): the
+dark cross sections, the dark kinematics, draw_dark_sample on fixed streams
+and generate_dark_shower on routed SM showers."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import BUNDLED_DIR, BUNDLED_NPZ, GOLDEN
+from oracle import dark as D
+from oracle import physics as P
+from oracle.philox import Stream
+from oracle.shower import OracleTables
+
+G = np.load(os.path.join(GOLDEN, "dark.npz"))
+DARK_NPZ = os.path.join(BUNDLED_DIR, "dark_tables.npz")
+SEED = 0x5EED
+
+
+@pytest.mark.parametrize("mV", [0.01, 0.1, 0.3])
+@pytest.mark.parametrize("target", ["graphite", "lead"])
+@pytest.mark.parametrize("proc", D.DARK_PROCESSES)
+def test_dark_dsigma_matches_reference(mV, target, proc):
+    pre = f"dsigma/{mV}/{target}/{proc}"
+    X, E, V = G[f"{pre}/x"], G[f"{pre}/E"], G[f"{pre}/value"]
+    ti = P.TARGETS[target]
+    got = np.array([D.dsigma_dark(proc, x, e, mV, ti["Z_T"], ti["A_T"]) for x, e in zip(X, E)])
+    assert (V != 0).sum() >= 3
+    # The reference calls numpy ufuncs (np.log, np.power) on scalars; on an
+    # x86 host with AVX-512 numpy evaluates them with its SIMD routines, which
+    # are a few ulp from the correctly rounded libm values the oracle uses.
+    # The radiative-return form raises (1-x) to beta/2-1 ~ -0.99 and divides
+    # by x, which magnifies those ulp to ~1e-11 relative.
+    rtol = 2e-11 if proc == "DarkAnn" else 1e-12
+    np.testing.assert_allclose(got, V, rtol=rtol, atol=0)
+
+
+def test_dark_kinematics_match_reference():
+    rows = G["kin/rows"]
+    for case, row in enumerate(rows):
+        kind, mV, E = int(row[0]), row[1], row[2]
+        x, extra, b = row[3:6], row[6:8], row[12:16]
+        s = Stream(SEED, 50_000 + case)
+        if kind in (0, 1):
+            m = P.m_electron if kind == 0 else P.m_muon
+            v = D.l_to_lV(E, m, x, mV, 2.0 * math.pi * s.next())[1]
+        elif kind == 2:
+            v = P.compton(E, x[0], 2.0 * math.pi * s.next(), mV)[1]
+        elif kind == 3:
+            ph = 2.0 * math.pi * s.next()
+            v = D.compton_bound(E, x[0], mV, extra[0], extra[1], ph, 2.0 * math.pi * s.next())
+        else:
+            v = D.radiative_return_V(E, x[0], mV)
+        np.testing.assert_allclose(v, b, rtol=0, atol=1e-12 * max(abs(b[0]), 1.0), err_msg=str((case, kind)))
+
+
+def test_draw_dark_sample_matches_reference():
+    sm = OracleTables(BUNDLED_NPZ, "graphite")
+    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, "graphite", 0.1), sm, SEED)
+    for row in G["draw/rows"]:
+        case, pi, E = int(row[0]), int(row[1]), row[2]
+        proc = D.DARK_PROCESSES[pi]
+        cnt = []
+        x, _ = orc.draw(E, proc, Stream(SEED, 60_000 + case), cnt)
+        assert cnt[0] == int(row[-1]), (proc, E)
+        d = D.DARK_DIM[proc]
+        np.testing.assert_allclose(x, row[3:3 + d], rtol=1e-14, atol=0)
+
+
+class _Rec:
+    def __init__(self, f, i, key):
+        self.p0, self.r0, self.pf, self.rf = tuple(f[0:4]), tuple(f[4:7]), tuple(f[7:11]), tuple(f[11:14])
+        self.weight, self.mass = f[14], f[15]
+        self.pid = int(i[0])
+        self.pkey = int(key)
+
+
+def sm_records(name):
+    F, I, K = G[f"shower/{name}/sm_f64"], G[f"shower/{name}/sm_i64"], G[f"shower/{name}/sm_pkey"]
+    return [_Rec(F[k], I[k], K[k]) for k in range(len(F))]
+
+
+@pytest.mark.parametrize("name", ["e10_graphite_m0.1", "e10_graphite_m0.03", "g5_lead_m0.01"])
+def test_dark_shower_matches_reference(name):
+    mV = float(G[f"shower/{name}/params"][0])
+    target = str(G[f"shower/{name}/target"])
+    sm = OracleTables(BUNDLED_NPZ, target)
+    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, target, mV), sm, SEED)
+    recs = sm_records(name)
+    W = G[f"shower/{name}/weights"]
+    got_w = np.array([[orc.weight(r.pid, r.p0[0], p) for p in D.DARK_PROCESSES] for r in recs])
+    np.testing.assert_allclose(got_w, W, rtol=1e-12, atol=0)
+    out = orc.dark_shower(recs)
+    V = G[f"shower/{name}/V"]
+    got = np.array([[k, D.DARK_CODE[p], w, *v, *r] for k, p, w, v, r in out])
+    want = V[np.lexsort((V[:, 2], V[:, 0]))]
+    got = got[np.lexsort((got[:, 1], got[:, 0]))]
+    assert len(got) == len(want)
+    assert np.array_equal(got[:, :2], want[:, [0, 2]])
+    np.testing.assert_allclose(got[:, 2], want[:, 3], rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(got[:, 7:10], want[:, 8:11])
+    # V four-momenta: energies to 1e-12; directions carry the conditioning of
+    # the rotation to the lab frame and of 1 - cos(theta) near the beam axis
+    np.testing.assert_allclose(got[:, 3], want[:, 4], rtol=1e-12, atol=0)
+    scale = np.abs(want[:, 4:8]).max(1)
+    assert (np.abs(got[:, 3:7] - want[:, 4:8]).max(1) <= 1e-9 * scale).all()
