@@ -318,13 +318,19 @@ pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles*
  * uniforms are draws 4j..4j+3 of stream (seed, mix64(4*i + process + 1)):
  * yield[i] = mean(jac * dsigma(x; energy[i], mV[i])) (the map's cross-section
  * estimate, find_maxes.py:143-147) and moment[i] = mean(jac * dsigma * E_V).
+ * mV_anchor (may be NULL): for DarkBrem/DarkMuonBrem, each sample's log10 t~
+ * is carried along the momentum-transfer range from mass mV_anchor[i] to
+ * mV[i] (a change of variables; equal to the plain estimate at
+ * mV = mV_anchor), which makes the estimate smooth in mV around the anchor.
  * No counterpart in the reference as one function. */
 pt_status pt_dark_yield(pt_dark* d, int32_t process, const double* energy, const double* mV,
-                        const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
-                        double* yield, double* moment, void* stream);
+                        const double* mV_anchor, const int32_t* mass_index, int64_t n_pairs, int64_t n_samples,
+                        uint64_t seed, double* yield, double* moment, void* stream);
 
 /* Adjoint of pt_dark_yield with respect to mV: recomputes every sample and
- * writes g_mV[i] = g_yield[i] * d yield[i]/d mV + g_moment[i] * d moment[i]/d mV. */
+ * writes g_mV[i] = g_yield[i] * d yield[i]/d mV + g_moment[i] * d moment[i]/d mV,
+ * including the motion of the DarkBrem momentum-transfer range with mV (the
+ * derivative of the anchored estimate at its anchor). */
 pt_status pt_dark_yield_adjoint(pt_dark* d, int32_t process, const double* energy, const double* mV,
                                 const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
                                 const double* g_yield, const double* g_moment, double* g_mV, void* stream);

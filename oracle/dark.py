@@ -33,6 +33,83 @@ from . import physics as P
 from .philox import Stream, mix64
 from .shower import interp, map_point
 
+class Dual:
+    """Value and derivative with respect to one input (forward mode), for the
+    float64 reference gradient of the dark yield.  Comparisons use the value."""
+    __slots__ = ("v", "d")
+
+    def __init__(self, v, d=0.0):
+        self.v, self.d = float(v), float(d)
+
+    @staticmethod
+    def _c(x):
+        return x if isinstance(x, Dual) else Dual(x)
+
+    def __add__(a, b):
+        b = Dual._c(b)
+        return Dual(a.v + b.v, a.d + b.d)
+    __radd__ = __add__
+
+    def __sub__(a, b):
+        b = Dual._c(b)
+        return Dual(a.v - b.v, a.d - b.d)
+
+    def __rsub__(a, b):
+        return Dual._c(b) - a
+
+    def __mul__(a, b):
+        b = Dual._c(b)
+        return Dual(a.v * b.v, a.d * b.v + a.v * b.d)
+    __rmul__ = __mul__
+
+    def __truediv__(a, b):
+        b = Dual._c(b)
+        q = a.v / b.v
+        return Dual(q, (a.d - q * b.d) / b.v)
+
+    def __rtruediv__(a, b):
+        return Dual._c(b) / a
+
+    def __neg__(a):
+        return Dual(-a.v, -a.d)
+
+    def __abs__(a):
+        return -a if a.v < 0 else a
+
+    def __pow__(a, e):
+        p = a.v ** e
+        return Dual(p, 0.0 if (a.d == 0.0 or a.v == 0.0) else e * a.v ** (e - 1) * a.d)
+
+    def __rpow__(a, base):               # base ** a for a float base
+        p = base ** a.v
+        return Dual(p, p * math.log(base) * a.d)
+
+    def __lt__(a, b): return a.v < _val(b)
+    def __le__(a, b): return a.v <= _val(b)
+    def __gt__(a, b): return a.v > _val(b)
+    def __ge__(a, b): return a.v >= _val(b)
+    def __float__(a): return a.v
+
+
+def _val(x):
+    return x.v if isinstance(x, Dual) else x
+
+
+def _sqrt(x):
+    if isinstance(x, Dual):
+        s = math.sqrt(x.v)
+        return Dual(s, 0.0 if x.d == 0.0 else x.d / (2.0 * s))
+    return math.sqrt(x)
+
+
+def _fabs(x):
+    return abs(x) if isinstance(x, Dual) else math.fabs(x)
+
+
+def _log10(x):
+    return Dual(math.log10(x.v), x.d / (x.v * math.log(10.0))) if isinstance(x, Dual) else math.log10(x)
+
+
 DARK_PROCESSES = ("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")
 DARK_CODE = {p: i for i, p in enumerate(DARK_PROCESSES)}
 DARK_DIM = {"DarkComp": 1, "DarkBrem": 3, "DarkAnn": 1, "DarkMuonBrem": 3}   # dark_shower.py:67
@@ -66,22 +143,22 @@ def dsigma_dark_brem(xv, E, mV, MT, m_lep, Z, A):
     ct = 1.0 - one_minus_ct
     ttilde = 10 ** lttilde
     jac = one_minus_ct * ttilde * math.log(10.0) ** 2
-    k = math.sqrt(math.fabs((x * E) ** 2 - mV ** 2))
-    p = math.sqrt(E ** 2 - m_lep ** 2)
-    V = math.sqrt(p ** 2 + k ** 2 - 2 * p * k * ct)
+    k = _sqrt(_fabs((x * E) ** 2 - mV ** 2))
+    p = _sqrt(E ** 2 - m_lep ** 2)
+    V = _sqrt(p ** 2 + k ** 2 - 2 * p * k * ct)
     ut = -2 * (x * E ** 2 - k * p * ct) + mV ** 2
     Er = (1 - x) * E + MT
     discr = ut ** 2 + 4 * MT * ut * Er + 4 * MT ** 2 * V ** 2
-    rd = math.sqrt(abs(discr))
+    rd = _sqrt(_fabs(discr))
     den = 2 * Er ** 2 - 2 * V ** 2
-    Qp = math.fabs((V * (ut + 2 * MT * Er) + Er * rd) / den)
-    Qm = math.fabs((V * (ut + 2 * MT * Er) - Er * rd) / den)
-    tp = 2 * MT * (math.sqrt(MT ** 2 + Qp ** 2) - MT)
-    tm = 2 * MT * (math.sqrt(MT ** 2 + Qm ** 2) - MT)
-    tconv = (2 * MT * (MT + E) * math.sqrt(E ** 2 + m_lep ** 2) / (MT * (MT + 2 * E) + m_lep ** 2)) ** 2
+    Qp = _fabs((V * (ut + 2 * MT * Er) + Er * rd) / den)
+    Qm = _fabs((V * (ut + 2 * MT * Er) - Er * rd) / den)
+    tp = 2 * MT * (_sqrt(MT ** 2 + Qp ** 2) - MT)
+    tm = 2 * MT * (_sqrt(MT ** 2 + Qm ** 2) - MT)
+    tconv = (2 * MT * (MT + E) * _sqrt(E ** 2 + m_lep ** 2) / (MT * (MT + 2 * E) + m_lep ** 2)) ** 2
     t = ttilde * tconv
     q0 = -t / (2 * MT)
-    q = math.sqrt(t ** 2 / (4 * MT ** 2) + t)
+    q = _sqrt(t ** 2 / (4 * MT ** 2) + t)
     cq = -(V ** 2 + q ** 2 + m_lep ** 2 - (E + q0 - x * E) ** 2) / (2 * V * q)
     mm = mV ** 2 + 2 * m_lep ** 2
     Am2 = -8 * MT * (4 * E ** 2 * MT - t * (2 * E + MT)) * mm
@@ -92,13 +169,13 @@ def dsigma_dark_brem(xv, E, mV, MT, m_lep, Z, A):
     A0 = (8 / ut ** 2) * (MT ** 2 * (2 * t * ut + (t - 4 * E ** 2 * (x - 1) ** 2) * mm)
                           + 2 * E * MT * t * (ut - (x - 1) * mm))
     Y = -t + 2 * q0 * E - 2 * q * p * (p - k * ct) * cq / V
-    W = math.fabs(Y ** 2 - 4 * q ** 2 * p ** 2 * k ** 2 * (1 - ct ** 2) * (1 - cq ** 2) / V ** 2)
-    allowed = (x * E >= mV and discr >= 0 and tp > tm and t > tm and t < tp and math.fabs(cq) <= 1.0 and W > 0)
+    W = _fabs(Y ** 2 - 4 * q ** 2 * p ** 2 * k ** 2 * (1 - ct ** 2) * (1 - cq ** 2) / V ** 2)
+    allowed = (x * E >= mV and discr >= 0 and tp > tm and t > tm and t < tp and _fabs(cq) <= 1.0 and W > 0)
     if not allowed:
         return 0.0
-    phi_int = (A0 + Y * A1 + Am1 / math.sqrt(W) + Y * Am2 / W ** 1.5) / (8 * MT ** 2)
+    phi_int = (A0 + Y * A1 + Am1 / _sqrt(W) + Y * Am2 / W ** 1.5) / (8 * MT ** 2)
     ff = g_el_inel_over_t2(Z, A, t)
-    ans = ff * P.alpha_em ** 3 * k * E * phi_int / (p * math.sqrt(k ** 2 + p ** 2 - 2 * p * k * ct))
+    ans = ff * P.alpha_em ** 3 * k * E * phi_int / (p * _sqrt(k ** 2 + p ** 2 - 2 * p * k * ct))
     return ans * tconv * jac
 
 
@@ -142,6 +219,73 @@ def dsigma_radiative_return(u0, Ee, mV):
     if not (x2 < 1.0 and x1 > 0.0 and u0 < 1.0):
         return 0.0
     return 2.0 * prefac * transformed_lumi(s, mV ** 2 / s, u0 * umax)
+
+
+def dsigma_radiative_return_factored(u0, Ee, mV):
+    """dsigma_radiative_return with 1 - x2 written as (s - mV^2)(1 - u0^(2/beta))/(x1 s)
+    (the same quantity without cancellation near x2 -> 1); used for yields."""
+    me = P.m_electron
+    s = 2.0 * me * (Ee + me)
+    if s < mV ** 2:
+        return 0.0
+    beta = (2.0 * P.alpha_em / math.pi) * (math.log(s / me ** 2) - 1.0)
+    umax = (1.0 - mV ** 2 / s) ** (beta / 2.0)
+    betaf = _sqrt(1.0 - 4.0 * (me ** 2) / (mV ** 2))
+    prefac = (4.0 * math.pi ** 2) * P.alpha_em * betaf * (3.0 / 2.0 - betaf ** 2 / 2.0) / s * umax
+    omx1 = (u0 * umax) ** (2.0 / beta)
+    x1 = 1.0 - omx1
+    x2 = mV ** 2 / (x1 * s)
+    if not (x2 < 1.0 and x1 > 0.0 and u0 < 1.0):
+        return 0.0
+    omx2 = (s - mV ** 2) * (-math.expm1((2.0 / beta) * math.log(u0))) / (x1 * s)
+    fy = (beta / 16.) * ((8. + 3. * beta) * omx2 ** (beta / 2. - 1.) - 4. * (1. + x2))
+    base = omx1 if isinstance(x1, Dual) else 1. - x1      # 1 - x1 without cancellation for derivatives
+    fs = (beta / 16.) * ((8. + 3. * beta) - 4. * (1. + x1) * base ** (1. - beta / 2.))
+    return 2.0 * prefac * (fy * fs * (1. / x1) * (2. / beta))
+
+
+def dsigma_compton_dark(ct, Eg, mV):
+    """dsigma_compton_dCT with mV > 0 (all_processes.py:639-742) for a float or
+    Dual mass (same expressions as physics.dsigma_compton)."""
+    me = P.m_electron
+    s = me ** 2 + 2 * Eg * me
+    if s < (me + mV) ** 2:
+        return 0.0
+    root = _sqrt(me ** 4 + (mV ** 2 - s) ** 2 - 2 * me ** 2 * (mV ** 2 + s))
+    jac = (s - me ** 2) / (2 * s) * _sqrt((s - mV ** 2) ** 2 - 2 * me ** 2 * (s + mV ** 2) + me ** 4)
+    t = -1 / 2 * (me ** 4 + s * (-(mV ** 2) + s + ct * root) - me ** 2 * (mV ** 2 + 2 * s + ct * root)) / s
+    PF = 2.0 * math.pi * P.alpha_em ** 2 / (s - me ** 2) ** 2
+    T1 = (2.0 * me ** 2 * (mV ** 2 - 3 * s) - 3 * me ** 4 - 2 * mV ** 2 * s + 2 * mV ** 4 + s ** 2) \
+        / ((me ** 2 - s) * (me ** 2 + mV ** 2 - s - t))
+    T2 = (2 * me ** 2 * (2 * me ** 2 + mV ** 2)) / (me ** 2 + mV ** 2 - s - t) ** 2
+    T3 = ((me ** 2 + s) * (me ** 2 + mV ** 2 + s) + t * (s - me ** 2)) / (me ** 2 - s) ** 2
+    return PF * jac * (T1 + T2 + T3)
+
+
+def _ev(process, x, E, mV):
+    """Lab energy of V for the yield moments (kinematics.py:57,119-130,282-298)."""
+    if process in ("DarkBrem", "DarkMuonBrem"):
+        return x[0] * E
+    me = P.m_electron
+    if process == "DarkComp":
+        s = me ** 2 + 2 * E * me
+        rs = math.sqrt(s)
+        Ee0 = (s + me ** 2) / (2.0 * rs)
+        Ee = (s - mV ** 2 + me ** 2) / (2 * rs)
+        EV = (s + mV ** 2 - me ** 2) / (2 * rs)
+        pF = _sqrt(Ee ** 2 - me ** 2)
+        g0 = Ee0 / me
+        b0 = 1.0 / g0 * math.sqrt(g0 ** 2 - 1.0)
+        return g0 * EV - b0 * g0 * pF * x[0]
+    s = 2. * me * (me + E)
+    rs = math.sqrt(s)
+    beta = (2. * P.alpha_em / math.pi) * (math.log(s / me ** 2) - 1.)
+    umax = (1. - mV ** 2 / s) ** (beta / 2.)
+    x1 = 1. - (x[0] * umax) ** (2. / beta)
+    x2 = mV ** 2 / (x1 * s)
+    E1, E2 = x1 * rs / 2., x2 * rs / 2.
+    p0, p3 = rs / 2., -math.sqrt(s / 4. - me ** 2)
+    return (p0 * (E1 + E2) - p3 * (E1 - E2)) / math.sqrt(p0 * p0 - p3 * p3)
 
 
 def dsigma_dark(process, xv, E, mV, Z, A):
@@ -462,9 +606,7 @@ def yield_uniforms(seed, pair, process, j):
     return uniforms(seed, mix64(4 * pair + DARK_CODE[process] + 1), 4 * j, 4)
 
 
-def dark_yield(dark: DarkTables, process, E, mV, pair, n_samples, seed):
-    """Mean of jac*dsigma and of jac*dsigma*E_V over the map row LU_Key(E),
-    at the uniforms of :func:`yield_uniforms` (float64, sequential)."""
+def _yield_sum(dark, process, E, mV, pair, n_samples, seed, anchor=None):
     rows, energies = dark.maps[process], dark.map_E[process]
     key = int(np.argmin(np.abs(energies - E))) + 1
     if key >= len(rows):
@@ -473,16 +615,98 @@ def dark_yield(dark: DarkTables, process, E, mV, pair, n_samples, seed):
     dim = DARK_DIM[process]
     from .philox import uniforms
     u_all = uniforms(seed, mix64(4 * pair + DARK_CODE[process] + 1), 0, 4 * n_samples).reshape(n_samples, 4)
+    m = P.m_muon if process == "DarkMuonBrem" else P.m_electron
     sy = sm = 0.0
     for j in range(n_samples):
         x, jac = map_point(grid, u_all[j, :dim])
-        f = dsigma_dark(process, x, E, mV, dark.Z, dark.A)
-        if process == "DarkBrem" or process == "DarkMuonBrem":
-            ev = x[0] * E
-        elif process == "DarkComp":
-            ev = P.compton(E, x[0], 0.0, mV)[1][0]
+        if process in ("DarkBrem", "DarkMuonBrem") and anchor is not None:
+            f = dsigma_dark_brem_anchored(x, E, mV, anchor, dark.A, m, dark.Z, dark.A)
+            xa, xm = anchor / E, mV / E
+            ev = (xm + (x[0] - xa) / (1.0 - xa) * (1.0 - xm)) * E
         else:
-            ev = radiative_return_V(E, x[0], mV)[0]
-        sy += jac * f
-        sm += jac * f * ev
+            if process == "DarkAnn":
+                f = dsigma_radiative_return_factored(x[0], E, mV)
+            elif process == "DarkComp":
+                f = dsigma_compton_dark(x[0], E, mV)
+            else:
+                f = dsigma_dark_brem(x, E, mV, dark.A, m, dark.Z, dark.A)
+            ev = None
+        if _val(f) == 0.0:
+            continue
+        if ev is None:
+            ev = _ev(process, x, E, mV)
+        sy = sy + jac * f
+        sm = sm + jac * f * ev
     return sy / n_samples, sm / n_samples
+
+
+def dark_yield(dark: DarkTables, process, E, mV, pair, n_samples, seed):
+    """Mean of jac*dsigma and of jac*dsigma*E_V over the map row LU_Key(E),
+    at the uniforms of :func:`yield_uniforms` (float64, sequential); the
+    radiative return in its factored form (1 - x2 without cancellation)."""
+    return _yield_sum(dark, process, E, mV, pair, n_samples, seed)
+
+
+def dark_yield_gradient(dark: DarkTables, process, E, mV, pair, n_samples, seed):
+    """Float64 reference of d(yield)/d(mV) and d(moment)/d(mV): forward-mode
+    derivatives of the same sums, DarkBrem samples carried with mV."""
+    y, m = _yield_sum(dark, process, E, Dual(mV, 1.0), pair, n_samples, seed,
+                      anchor=mV if process in ("DarkBrem", "DarkMuonBrem") else None)
+    return (y.d if isinstance(y, Dual) else 0.0), (m.d if isinstance(m, Dual) else 0.0)
+
+
+# --------------------------------------------- anchored dark-brem estimate
+def _brem_limits_stable(x, ct, E, mV, MT, m):
+    """t- and t+ of all_processes.py:261-283 written without cancellation:
+    Q- = -ut (ut + 4 MT Er) / (2 (A + B)), t = 2 MT Q^2 / (sqrt(MT^2 + Q^2) + MT)."""
+    k = _sqrt(_fabs((x * E) ** 2 - mV ** 2))
+    p = _sqrt(E ** 2 - m ** 2)
+    V = _sqrt(p ** 2 + k ** 2 - 2 * p * k * ct)
+    ut = -2 * (x * E ** 2 - k * p * ct) + mV ** 2
+    Er = (1 - x) * E + MT
+    discr = ut ** 2 + 4 * MT * ut * Er + 4 * MT ** 2 * V ** 2
+    A_ = V * (ut + 2 * MT * Er)
+    B_ = Er * _sqrt(_fabs(discr))
+    den = 2 * Er ** 2 - 2 * V ** 2
+    Qp = abs((A_ + B_) / den)
+    Qm = abs(ut * (ut + 4 * MT * Er) / (2 * (A_ + B_)))
+    tp = 2 * MT * Qp ** 2 / (_sqrt(MT ** 2 + Qp ** 2) + MT)
+    tm = 2 * MT * Qm ** 2 / (_sqrt(MT ** 2 + Qm ** 2) + MT)
+    return discr, tm, tp
+
+
+def dsigma_dark_brem_anchored(xv, E, mV, a, MT, m_lep, Z, A):
+    """The dark-brem integrand with the sample (drawn for mass a) carried to
+    mass mV: x keeps its fraction of (mV/E, 1), log10 t~ its fraction of the
+    t-range; times the Jacobian of the move.  Equals dsigma_dark_brem at mV = a
+    up to rounding; smooth in mV."""
+    x0, l1mct, l0 = xv
+    omc = 10 ** l1mct
+    ct = 1.0 - omc
+    tconv = (2 * MT * (MT + E) * _sqrt(E ** 2 + m_lep ** 2) / (MT * (MT + 2 * E) + m_lep ** 2)) ** 2
+    xa = a / E
+    w = (x0 - xa) / (1.0 - xa)
+    if not (0.0 < w < 1.0):
+        return 0.0
+    d, tm, tp = _brem_limits_stable(x0, ct, E, a, MT, m_lep)
+    if not (d >= 0 and tp > tm and tm > 0):
+        return 0.0
+    lma, lpa = _log10(tm / tconv), _log10(tp / tconv)
+    v = (l0 - lma) / (lpa - lma)
+    if not (0.0 < v < 1.0):
+        return 0.0
+    xm = mV / E
+    x = xm + w * (1.0 - xm)
+    d, tm, tp = _brem_limits_stable(x, ct, E, mV, MT, m_lep)
+    if not (d >= 0 and tp > tm and tm > 0):
+        return 0.0
+    lm, lp = _log10(tm / tconv), _log10(tp / tconv)
+    l = lm + (lp - lm) * v
+    f = dsigma_dark_brem((x, l1mct, l), E, mV, MT, m_lep, Z, A)
+    return f * ((lp - lm) / (lpa - lma)) * ((1.0 - xm) / (1.0 - xa))
+
+
+def dark_yield_anchored(dark: DarkTables, process, E, mV, anchor, pair, n_samples, seed):
+    """dark_yield with DarkBrem samples carried from the anchor mass."""
+    a = anchor if process in ("DarkBrem", "DarkMuonBrem") else None
+    return _yield_sum(dark, process, E, mV, pair, n_samples, seed, anchor=a)

@@ -145,7 +145,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                                         vp]
     lib.pt_run_dark.argtypes = [vp, C.POINTER(PtDarkParams), C.POINTER(PtParticles), i64, C.POINTER(PtOpts),
                                 C.POINTER(PtDarkOut), C.POINTER(i64), vp]
-    lib.pt_dark_yield.argtypes = [vp, i32, vp, vp, vp, i64, i64, C.c_uint64, vp, vp, vp]
+    lib.pt_dark_yield.argtypes = [vp, i32, vp, vp, vp, vp, i64, i64, C.c_uint64, vp, vp, vp]
     lib.pt_dark_yield_adjoint.argtypes = [vp, i32, vp, vp, vp, i64, i64, C.c_uint64, vp, vp, vp, vp]
     for f in ("pt_dark_create", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark", "pt_dark_yield",
               "pt_dark_yield_adjoint"):

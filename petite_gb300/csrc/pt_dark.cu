@@ -383,16 +383,25 @@ __device__ __forceinline__ T dark_EV(int p, const double* x, double E, T mV) {
   if (p == PT_DARKANN) return dark_ann_EV(x[0], E, mV);
   return T(mV * 0.0) + x[0] * E;               // l_to_lV: E_V = x E
 }
+// E_V of the anchored dark-brem sample: x moves with mV as in
+// dsig_dark_brem_anchored
+template <class T>
+__device__ __forceinline__ T dark_EV_anchored(const double* x, double E, T mV, double a) {
+  const double xa = a / E;
+  const double w = (x[0] - xa) / (1.0 - xa);
+  const T xm = mV / E;
+  return (xm + w * (1.0 - xm)) * E;
+}
 
 // One block per pair.  Sample j uses draws 4j..4j+3 of the pair's stream
 // (Philox blocks 2j and 2j+1); the block's partial sums are combined in a
 // fixed tree order, so results do not depend on timing.
 template <class T, bool ADJ>
 __global__ void __launch_bounds__(kYieldThreads) k_dark_yield(pt_dark_maps M, int p, const double* Ein,
-                                                               const double* mVin, const int32_t* mass_index,
-                                                               int64_t n_samples, uint64_t seed, double* yield,
-                                                               double* moment, const double* gY, const double* gM,
-                                                               double* g_mV) {
+                                                               const double* mVin, const double* anchor,
+                                                               const int32_t* mass_index, int64_t n_samples,
+                                                               uint64_t seed, double* yield, double* moment,
+                                                               const double* gY, const double* gM, double* g_mV) {
   __shared__ double sh_y[kYieldThreads], sh_m[kYieldThreads];
   const int64_t i = blockIdx.x;
   const double E = Ein[i];
@@ -422,8 +431,20 @@ __global__ void __launch_bounds__(kYieldThreads) k_dark_yield(pt_dark_maps M, in
     double x[4] = {0, 0, 0, 0};
     double jac = 1.0;
     for (int k = 0; k < d; ++k) x[k] = map_dim(M.grid_nodes + M.grid_offset[r * 4 + k], M.grid_ninc[r * 4 + k], u[k], jac);
-    const T f = dark_dsigma<T>(M, p, x, E, mV);
-    const T fe = f * dark_EV<T>(p, x, E, mV);
+    T f, ev;
+    const bool brem = (p == PT_DARKBREM || p == PT_DARKMUONBREM);
+    if (brem && (ADJ || anchor)) {
+      // the kinematic ranges follow mV (d/dmV includes the moving edges)
+      const double a = ADJ ? mVin[i] : anchor[i];
+      f = dsig_dark_brem_anchored<T>(x, E, mV, a, M.A, p == PT_DARKBREM ? kMe : kMmu, M.Z, M.A);
+      if (val(f) == 0.0) continue;               // outside the allowed region: no value, no derivative
+      ev = dark_EV_anchored<T>(x, E, mV, a);
+    } else {
+      f = (p == PT_DARKANN) ? dsig_radiative_return<T, true>(x[0], E, mV) : dark_dsigma<T>(M, p, x, E, mV);
+      if (val(f) == 0.0) continue;
+      ev = dark_EV<T>(p, x, E, mV);
+    }
+    const T fe = f * ev;
     if constexpr (ADJ) {
       acc_y += jac * f.d;
       acc_m += jac * fe.d;
@@ -553,9 +574,9 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
 
 template <bool ADJ>
 static pt_status dark_yield_launch(pt_dark* d, int32_t process, const double* energy, const double* mV,
-                                   const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
-                                   double* yield, double* moment, const double* gY, const double* gM, double* g_mV,
-                                   void* stream) {
+                                   const double* anchor, const int32_t* mass_index, int64_t n_pairs,
+                                   int64_t n_samples, uint64_t seed, double* yield, double* moment, const double* gY,
+                                   const double* gM, double* g_mV, void* stream) {
   if (!d || process < 0 || process >= PT_N_DARK || n_pairs < 0 || n_samples <= 0 || n_pairs > 0x7fffffff)
     return PT_BAD_ARG;
   if (n_pairs == 0) return PT_OK;
@@ -563,29 +584,28 @@ static pt_status dark_yield_launch(pt_dark* d, int32_t process, const double* en
   cudaStream_t st = (cudaStream_t)stream;
   if constexpr (ADJ) {
     if (!gY || !gM || !g_mV) return PT_BAD_ARG;
-    k_dark_yield<Dual, true><<<(unsigned)n_pairs, kYieldThreads, 0, st>>>(d->M, process, energy, mV, mass_index,
-                                                                        n_samples, seed, nullptr, nullptr, gY, gM,
-                                                                        g_mV);
+    k_dark_yield<Dual, true><<<(unsigned)n_pairs, kYieldThreads, 0, st>>>(
+        d->M, process, energy, mV, nullptr, mass_index, n_samples, seed, nullptr, nullptr, gY, gM, g_mV);
   } else {
     if (!yield || !moment) return PT_BAD_ARG;
     k_dark_yield<double, false><<<(unsigned)n_pairs, kYieldThreads, 0, st>>>(
-        d->M, process, energy, mV, mass_index, n_samples, seed, yield, moment, nullptr, nullptr, nullptr);
+        d->M, process, energy, mV, anchor, mass_index, n_samples, seed, yield, moment, nullptr, nullptr, nullptr);
   }
   PT_CUDA(cudaGetLastError());
   return PT_OK;
 }
 
 extern "C" pt_status pt_dark_yield(pt_dark* d, int32_t process, const double* energy, const double* mV,
-                                   const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
-                                   double* yield, double* moment, void* stream) {
-  return dark_yield_launch<false>(d, process, energy, mV, mass_index, n_pairs, n_samples, seed, yield, moment,
-                                  nullptr, nullptr, nullptr, stream);
+                                   const double* mV_anchor, const int32_t* mass_index, int64_t n_pairs,
+                                   int64_t n_samples, uint64_t seed, double* yield, double* moment, void* stream) {
+  return dark_yield_launch<false>(d, process, energy, mV, mV_anchor, mass_index, n_pairs, n_samples, seed, yield,
+                                  moment, nullptr, nullptr, nullptr, stream);
 }
 
 extern "C" pt_status pt_dark_yield_adjoint(pt_dark* d, int32_t process, const double* energy, const double* mV,
                                            const int32_t* mass_index, int64_t n_pairs, int64_t n_samples,
                                            uint64_t seed, const double* g_yield, const double* g_moment,
                                            double* g_mV, void* stream) {
-  return dark_yield_launch<true>(d, process, energy, mV, mass_index, n_pairs, n_samples, seed, nullptr, nullptr,
-                                 g_yield, g_moment, g_mV, stream);
+  return dark_yield_launch<true>(d, process, energy, mV, nullptr, mass_index, n_pairs, n_samples, seed, nullptr,
+                                 nullptr, g_yield, g_moment, g_mV, stream);
 }

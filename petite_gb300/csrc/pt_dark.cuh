@@ -7,6 +7,8 @@
 // operation order; each function cites the PETITE function it follows
 // (paths inside src/PETITE/).
 #pragma once
+#include <type_traits>
+
 #include "pt_common.cuh"
 
 namespace pt {
@@ -46,12 +48,19 @@ __device__ __forceinline__ Dual dsqrt(Dual x) {
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }
 __device__ __forceinline__ Dual dabs(Dual x) { return x.v < 0.0 ? -x : x; }
 __device__ __forceinline__ double dpow(double x, double e) { return pow(x, e); }
+// The derivative is taken as 0 at x = 0 (where x^e underflowed but its
+// derivative's factor x^(e-1) may not have).
 __device__ __forceinline__ Dual dpow(Dual x, double e) {
   const double p = pow(x.v, e);
-  return {p, x.d == 0.0 ? 0.0 : e * pow(x.v, e - 1.0) * x.d};
+  return {p, (x.d == 0.0 || x.v == 0.0) ? 0.0 : e * pow(x.v, e - 1.0) * x.d};
 }
 __device__ __forceinline__ double dlog(double x) { return log(x); }
 __device__ __forceinline__ Dual dlog(Dual x) { return {log(x.v), x.d / x.v}; }
+__device__ __forceinline__ double dexp10(double x) { return pow(10.0, x); }
+__device__ __forceinline__ Dual dexp10(Dual x) {
+  const double e = pow(10.0, x.v);
+  return {e, e * 2.302585092994046 * x.d};
+}
 template <class T>
 __device__ __forceinline__ T sqr(T x) { return x * x; }
 
@@ -60,43 +69,85 @@ constexpr double kLn10 = 2.302585092994046;
 
 // ------------------------------------------------------ dark bremsstrahlung
 // Gelastic_inelastic_over_tsquared (all_processes.py:112-133)
-__device__ __forceinline__ double g_el_inel_over_t2(double Z, double A, double t) {
+template <class T>
+__device__ __forceinline__ T g_el_inel_over_t2(double Z, double A, T t) {
   const double c1 = sqr(111 * pow(Z, -1.0 / 3) / kMe);
   const double c2 = 0.164 * pow(A, -2.0 / 3);
-  const double Gel = sqr(1.0 / (1.0 + c1 * t)) * pow(1 + t / c2, -2.0);
+  const T Gel = sqr(1.0 / (1.0 + c1 * t)) * dpow(1 + t / c2, -2.0);
   const double ap2 = sqr(773.0 * pow(Z, -2.0 / 3) / kMe);
-  const double Ginel = Z / (sqr(c1) * sqr(Z)) * sqr(ap2 / (1.0 + ap2 * t)) *
-                       ((1.0 + (2.79 * 2.79 - 1.0) * t / (4.0 * sqr(kMproton))) / pow(1.0 + t / 0.71, 4.0));
+  const T Ginel = Z / (sqr(c1) * sqr(Z)) * sqr(ap2 / (1.0 + ap2 * t)) *
+                  ((1.0 + (2.79 * 2.79 - 1.0) * t / (4.0 * sqr(kMproton))) / dpow(1.0 + t / 0.71, 4.0));
   return sqr(Z) * sqr(c1) * (Gel + Ginel);
 }
 
-// dsig_dx_dcostheta_dark_brem_exact_tree_level.__call__, method "Log"
-// (all_processes.py:227-372): x = (E_V/E, log10(1 - cos theta), log10 t~),
-// target mass MT, lepton mass m.
+// Limits of the momentum transfer for fixed (x, cos theta)
+// (all_processes.py:261-283): t- and t+ and the discriminant.
 template <class T>
-__device__ T dsig_dark_brem(const double* xv, double E, T mV, double MT, double m, double Z, double A) {
-  const double x = xv[0];
-  const double omc = pow(10.0, xv[1]);
-  const double ct = 1.0 - omc;
-  const double tt = pow(10.0, xv[2]);
-  const double jac = omc * tt * (kLn10 * kLn10);
+struct BremLimits {
+  T k, V, ut, discr, tp, tm;
+};
+template <class T, class X>
+__device__ __forceinline__ BremLimits<T> dark_brem_limits(X x, double ct, double E, T mV, double MT, double m) {
+  BremLimits<T> L;
   const T mV2 = mV * mV;
-  const T k = dsqrt(dabs(sqr(x * E) - mV2));
+  L.k = dsqrt(dabs(sqr(x * E) - mV2));
   const double p = sqrt(E * E - m * m);
-  const T V = dsqrt(p * p + k * k - 2 * p * k * ct);
-  const T ut = -2 * (x * (E * E) - k * p * ct) + mV2;
-  const double Er = (1 - x) * E + MT;
-  const T discr = ut * ut + 4 * MT * ut * Er + 4 * (MT * MT) * (V * V);
-  const T rd = dsqrt(dabs(discr));
-  const T den = 2 * (Er * Er) - 2 * (V * V);
-  const T Qp = dabs((V * (ut + 2 * MT * Er) + Er * rd) / den);
-  const T Qm = dabs((V * (ut + 2 * MT * Er) - Er * rd) / den);
-  const T tp = 2 * MT * (dsqrt(MT * MT + Qp * Qp) - MT);
-  const T tm = 2 * MT * (dsqrt(MT * MT + Qm * Qm) - MT);
-  const double tconv = sqr(2 * MT * (MT + E) * sqrt(E * E + m * m) / (MT * (MT + 2 * E) + m * m));
-  const double t = tt * tconv;
-  const double q0 = -t / (2 * MT);
-  const double q = sqrt(t * t / (4 * (MT * MT)) + t);
+  L.V = dsqrt(p * p + L.k * L.k - 2 * p * L.k * ct);
+  L.ut = -2 * (x * (E * E) - L.k * p * ct) + mV2;
+  const X Er = (1 - x) * E + MT;
+  L.discr = L.ut * L.ut + 4 * MT * L.ut * Er + 4 * (MT * MT) * (L.V * L.V);
+  const T rd = dsqrt(dabs(L.discr));
+  const T den = 2 * (Er * Er) - 2 * (L.V * L.V);
+  const T Qp = dabs((L.V * (L.ut + 2 * MT * Er) + Er * rd) / den);
+  const T Qm = dabs((L.V * (L.ut + 2 * MT * Er) - Er * rd) / den);
+  L.tp = 2 * MT * (dsqrt(MT * MT + Qp * Qp) - MT);
+  L.tm = 2 * MT * (dsqrt(MT * MT + Qm * Qm) - MT);
+  return L;
+}
+
+// The same limits without cancellation, for the anchored form below:
+// Q- = (A - B)/den = -ut (ut + 4 MT Er) / (2 (A + B)) with A = V (ut + 2 MT Er),
+// B = Er sqrt(discr), and 2 MT (sqrt(MT^2 + Q^2) - MT) = 2 MT Q^2 / (sqrt(MT^2 + Q^2) + MT).
+template <class T, class X>
+__device__ __forceinline__ BremLimits<T> dark_brem_limits_stable(X x, double ct, double E, T mV, double MT,
+                                                                 double m) {
+  BremLimits<T> L;
+  const T mV2 = mV * mV;
+  L.k = dsqrt(dabs(sqr(x * E) - mV2));
+  const double p = sqrt(E * E - m * m);
+  L.V = dsqrt(p * p + L.k * L.k - 2 * p * L.k * ct);
+  L.ut = -2 * (x * (E * E) - L.k * p * ct) + mV2;
+  const X Er = (1 - x) * E + MT;
+  L.discr = L.ut * L.ut + 4 * MT * L.ut * Er + 4 * (MT * MT) * (L.V * L.V);
+  const T Aq = L.V * (L.ut + 2 * MT * Er);
+  const T Bq = Er * dsqrt(dabs(L.discr));
+  const T den = 2 * (Er * Er) - 2 * (L.V * L.V);
+  const T Qp = dabs((Aq + Bq) / den);
+  const T Qm = dabs(L.ut * (L.ut + 4 * MT * Er) / (2 * (Aq + Bq)));
+  L.tp = 2 * MT * (Qp * Qp) / (dsqrt(MT * MT + Qp * Qp) + MT);
+  L.tm = 2 * MT * (Qm * Qm) / (dsqrt(MT * MT + Qm * Qm) + MT);
+  return L;
+}
+
+__device__ __forceinline__ double dark_brem_tconv(double E, double MT, double m) {
+  return sqr(2 * MT * (MT + E) * sqrt(E * E + m * m) / (MT * (MT + 2 * E) + m * m));
+}
+
+// dsig_dx_dcostheta_dark_brem_exact_tree_level.__call__, method "Log"
+// (all_processes.py:227-372) at (x, cos theta, t~): the vector mass and t~
+// may carry derivatives.  omc = 1 - cos theta.
+template <class T, class X>
+__device__ T dark_brem_core(X x, double omc, T tt, double E, T mV, double MT, double m, double Z, double A,
+                            const BremLimits<T>& L) {
+  const double ct = 1.0 - omc;
+  const T jac = omc * tt * (kLn10 * kLn10);
+  const T mV2 = mV * mV;
+  const double p = sqrt(E * E - m * m);
+  const T &k = L.k, &V = L.V, &ut = L.ut;
+  const double tconv = dark_brem_tconv(E, MT, m);
+  const T t = tt * tconv;
+  const T q0 = -t / (2 * MT);
+  const T q = dsqrt(t * t / (4 * (MT * MT)) + t);
   const T cq = -(V * V + q * q + m * m - sqr(E + q0 - x * E)) / (2 * V * q);
   const T mm = mV2 + 2 * (m * m);
   const T Am2 = -8 * MT * (4 * (E * E) * MT - t * (2 * E + MT)) * mm;
@@ -109,13 +160,55 @@ __device__ T dsig_dark_brem(const double* xv, double E, T mV, double MT, double 
                                   2 * E * MT * t * (ut - (x - 1) * mm));
   const T Y = -t + 2 * q0 * E - 2 * q * p * (p - k * ct) * cq / V;
   const T W = dabs(Y * Y - 4 * (q * q) * (p * p) * (k * k) * (1 - ct * ct) * (1 - cq * cq) / (V * V));
-  const bool allowed = (x * E >= val(mV)) && (val(discr) >= 0) && (val(tp) > val(tm)) && (t > val(tm)) &&
-                       (t < val(tp)) && (fabs(val(cq)) <= 1.0) && (val(W) > 0);
+  const bool allowed = (val(x) * E >= val(mV)) && (val(L.discr) >= 0) && (val(L.tp) > val(L.tm)) &&
+                       (val(t) > val(L.tm)) && (val(t) < val(L.tp)) && (fabs(val(cq)) <= 1.0) && (val(W) > 0);
   if (!allowed) return T(mV * 0.0);
   const T phi = (A0 + Y * A1 + Am1 / dsqrt(W) + Y * Am2 / dpow(W, 1.5)) / (8 * (MT * MT));
-  const double ff = g_el_inel_over_t2(Z, A, t);
+  const T ff = g_el_inel_over_t2(Z, A, t);
   const T ans = ff * (kAlpha * kAlpha * kAlpha) * k * E * phi / (p * dsqrt(k * k + p * p - 2 * p * k * ct));
   return ans * tconv * jac;
+}
+
+// The reference's form: x = (E_V/E, log10(1 - cos theta), log10 t~).
+template <class T>
+__device__ T dsig_dark_brem(const double* xv, double E, T mV, double MT, double m, double Z, double A) {
+  const double omc = pow(10.0, xv[1]);
+  const BremLimits<T> L = dark_brem_limits(xv[0], 1.0 - omc, E, mV, MT, m);
+  return dark_brem_core<T>(xv[0], omc, T(mV * 0.0) + pow(10.0, xv[2]), E, mV, MT, m, Z, A, L);
+}
+
+// The same integrand with the samples carried along the kinematic ranges of
+// mV: a sample drawn for the anchor mass a at x0 sits at the fraction
+// w = (x0 - a/E) / (1 - a/E) of the range x > mV/E and, for its x, at the
+// fraction v = (l0 - l-(a)) / (l+(a) - l-(a)) of the log10 t~ range; for mass
+// mV it moves to x = mV/E + w (1 - mV/E) and l = l-(mV) + v (l+(mV) - l-(mV)),
+// with the Jacobian of both moves.  At mV = a this is the reference's
+// integrand; for other masses it integrates the same cross section (a change
+// of variables), but the kinematic edges no longer move through the fixed
+// samples, so the estimate is smooth in mV.
+template <class T>
+__device__ T dsig_dark_brem_anchored(const double* xv, double E, T mV, double a, double MT, double m, double Z,
+                                     double A) {
+  const double omc = pow(10.0, xv[1]);
+  const double ct = 1.0 - omc;
+  const double tconv = dark_brem_tconv(E, MT, m);
+  const double xa = a / E;
+  const double w = (xv[0] - xa) / (1.0 - xa);
+  if (!(w > 0.0 && w < 1.0)) return T(mV * 0.0);
+  const BremLimits<double> La = dark_brem_limits_stable(xv[0], ct, E, a, MT, m);
+  if (!(La.discr >= 0) || !(La.tp > La.tm) || !(La.tm > 0)) return T(mV * 0.0);
+  const double lma = log10(La.tm / tconv), lpa = log10(La.tp / tconv);
+  const double v = (xv[2] - lma) / (lpa - lma);
+  if (!(v > 0.0 && v < 1.0)) return T(mV * 0.0);
+  const T xm = mV / E;
+  const T x = xm + w * (1.0 - xm);
+  const BremLimits<T> L = dark_brem_limits_stable(x, ct, E, mV, MT, m);
+  if (!(val(L.discr) >= 0) || !(val(L.tp) > val(L.tm)) || !(val(L.tm) > 0)) return T(mV * 0.0);
+  const T lm = dlog(L.tm / tconv) / kLn10, lp = dlog(L.tp / tconv) / kLn10;
+  const T l = lm + (lp - lm) * v;
+  const T tt = dexp10(l);
+  const T jac = ((lp - lm) / (lpa - lma)) * ((1.0 - xm) / (1.0 - xa));
+  return dark_brem_core<T>(x, omc, tt, E, mV, MT, m, Z, A, L) * jac;
 }
 
 // ----------------------------------------------------------- dark Compton
@@ -147,13 +240,27 @@ __device__ __forceinline__ T fl_kf(T x, double beta) {
   if (val(x) >= 1.0) x = T(x * 0.0) + (1. - 1e-10);
   return (beta / 16.) * ((8. + 3. * beta) * dpow(1. - x, beta / 2. - 1.) - 4. * (1. + x));
 }
+// The same with 1 - x given separately (no cancellation as x -> 1).
 template <class T>
-__device__ __forceinline__ T fl_kf_scaled(T x, double beta) {
-  return (beta / 16.) * ((8. + 3. * beta) - 4. * (1. + x) * dpow(1. - x, 1. - beta / 2.));
+__device__ __forceinline__ T fl_kf_omx(T x, T omx, double beta) {
+  return (beta / 16.) * ((8. + 3. * beta) * dpow(omx, beta / 2. - 1.) - 4. * (1. + x));
+}
+// omx = 1 - x computed without cancellation (x = 1 - u^(2/beta) rounds to 1
+// for u < ~0.3 at these energies); the float64 form keeps the reference's 1 - x.
+template <class T>
+__device__ __forceinline__ T fl_kf_scaled(T x, T omx, double beta) {
+  T base;
+  if constexpr (std::is_same<T, double>::value) base = 1. - x;
+  else base = omx;
+  return (beta / 16.) * ((8. + 3. * beta) - 4. * (1. + x) * dpow(base, 1. - beta / 2.));
 }
 // dsigma_radiative_return_du.__call__ (all_processes.py:419-466) with
-// transformed_lepton_luminosity_integrand (radiative_return.py:61-80)
-template <class T>
+// transformed_lepton_luminosity_integrand (radiative_return.py:61-80).
+// FACTORED: evaluate 1 - x2 as (s - mV^2)(1 - u0^(2/beta)) / (x1 s), the same
+// quantity without the cancellation of 1 - x2 near the x2 -> 1 end (u0 -> 1),
+// where (1 - x2)^(beta/2 - 1) is nearly singular; the yield kernels use this
+// form so that the estimate is smooth in mV at fixed uniforms.
+template <class T, bool FACTORED = false>
 __device__ T dsig_radiative_return(double u0, double Ee, T mV) {
   const double me = kMe;
   const double s = 2.0 * me * (Ee + me);
@@ -164,12 +271,20 @@ __device__ T dsig_radiative_return(double u0, double Ee, T mV) {
   const T betaf = dsqrt(1.0 - 4.0 * (me * me) / mV2);
   const T prefac = (4.0 * (kPi * kPi)) * kAlpha * betaf * (3.0 / 2.0 - betaf * betaf / 2.0) / s * umax;
   const T u = u0 * umax;
-  const T x1 = 1.0 - dpow(u, 2.0 / beta);
+  const T omx1 = dpow(u, 2.0 / beta);
+  const T x1 = 1.0 - omx1;
   const T x2 = mV2 / (x1 * s);
   if (!(val(x2) < 1.0 && val(x1) > 0.0 && u0 < 1.0)) return T(mV * 0.0);
   // transformed luminosity at (s, y = mV^2/s, u): x = 1 - u^(2/beta) (= x1)
   const T y = mV2 / s;
-  const T lumi = fl_kf(y / x1, beta) * fl_kf_scaled(x1, beta) * (1. / x1) * (2. / beta);
+  T fy;
+  if constexpr (FACTORED) {
+    const double omu = -expm1((2.0 / beta) * log(u0));        // 1 - u0^(2/beta)
+    fy = fl_kf_omx(y / x1, (s - mV2) * omu / (x1 * s), beta);
+  } else {
+    fy = fl_kf(y / x1, beta);
+  }
+  const T lumi = fy * fl_kf_scaled(x1, omx1, beta) * (1. / x1) * (2. / beta);
   return 2.0 * prefac * lumi;
 }
 

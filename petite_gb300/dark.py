@@ -223,12 +223,13 @@ class DarkEngine:
         out["n"] = n
         return out
 
-    def yield_forward(self, process: int, energy, mV, mass_index, n_samples: int, seed: int):
+    def yield_forward(self, process: int, energy, mV, mass_index, n_samples: int, seed: int, anchor=None):
         import torch
         n = energy.shape[0]
         Y = torch.empty(n, dtype=torch.float64, device=self.device)
         M = torch.empty(n, dtype=torch.float64, device=self.device)
-        _lib.check(self.lib.pt_dark_yield(self.handle, process, energy.data_ptr(), mV.data_ptr(),
+        aptr = None if anchor is None else anchor.data_ptr()
+        _lib.check(self.lib.pt_dark_yield(self.handle, process, energy.data_ptr(), mV.data_ptr(), aptr,
                                           mass_index.data_ptr(), n, int(n_samples), int(seed) & (2 ** 64 - 1),
                                           Y.data_ptr(), M.data_ptr(), self.sm._stream()), "pt_dark_yield")
         return Y, M
@@ -498,11 +499,13 @@ def map_mass_index(masses, mV):
 
 
 def dark_yield(engine: DarkEngine, process: str, energy, mV, n_samples: int = 10_000, seed: int = 0,
-               mass_index=None):
+               mass_index=None, anchor=None):
     """Differentiable dark-vector yield per (energy, mV) pair: returns
     (yield, moment) tensors; yield = mean(jac * dsigma) over the map of
     `process` at fixed uniforms, moment = mean(jac * dsigma * E_V).
-    Gradients flow to mV through the hand-written adjoint kernel."""
+    Gradients flow to mV through the hand-written adjoint kernel.
+    ``anchor`` (masses): evaluate the DarkBrem estimate with its samples
+    carried from the anchor masses' momentum-transfer ranges (pt_dark_yield)."""
     import torch
     dev = engine.device
     energy = torch.as_tensor(energy, dtype=torch.float64, device=dev).contiguous()
@@ -510,5 +513,9 @@ def dark_yield(engine: DarkEngine, process: str, energy, mV, n_samples: int = 10
     if mass_index is None:
         mass_index = map_mass_index(engine.data.masses, mV.detach().cpu().numpy())
     mi = torch.as_tensor(np.asarray(mass_index, np.int32), device=dev).contiguous()
+    if anchor is not None:
+        a = torch.as_tensor(anchor, dtype=torch.float64, device=dev).contiguous()
+        with torch.no_grad():
+            return engine.yield_forward(DARK_CODE[process], energy, mV.contiguous(), mi, n_samples, seed, anchor=a)
     return _DarkYieldFn.get().apply(energy, mV.contiguous(), engine, DARK_CODE[process], mi, int(n_samples),
                                     int(seed))

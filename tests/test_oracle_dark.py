@@ -106,3 +106,18 @@ def test_dark_shower_matches_reference(name):
     np.testing.assert_allclose(got[:, 3], want[:, 4], rtol=1e-12, atol=0)
     scale = np.abs(want[:, 4:8]).max(1)
     assert (np.abs(got[:, 3:7] - want[:, 4:8]).max(1) <= 1e-9 * scale).all()
+
+
+@pytest.mark.parametrize("proc", ["DarkBrem", "DarkComp", "DarkAnn"])
+def test_reference_gradient_matches_finite_differences(proc):
+    """The float64 forward-mode reference of the dark-yield mass derivative
+    against central differences of the same estimate (h = 1e-4 relative)."""
+    tabs = D.DarkTables(DARK_NPZ, "graphite", 0.1)
+    for E, mV in ((20.0, 0.12), (30.0, 0.15), (90.0, 0.29)):
+        gy, gm = D.dark_yield_gradient(tabs, proc, E, mV, 1, 200, SEED)
+        h = 1e-4 * mV
+        yp, mp = D.dark_yield_anchored(tabs, proc, E, mV + h, mV, 1, 200, SEED)
+        ym, mm = D.dark_yield_anchored(tabs, proc, E, mV - h, mV, 1, 200, SEED)
+        assert gy != 0.0
+        assert abs(gy - (yp - ym) / (2 * h)) <= 1e-5 * abs(gy)
+        assert abs(gm - (mp - mm) / (2 * h)) <= 1e-5 * abs(gm)
