@@ -41,6 +41,13 @@ WORKLOADS = {
                                seed=1, precision="mixed", fp64_sample=20_000, cpu_sample=160, mode="batch"),
     "sm_e1gev_graphite_1k": dict(target="graphite", cut=0.010, n=1000, species=(11,), emin=1.0, emax=1.0,
                                  seed=0, precision="fp64", fp64_sample=1000, cpu_sample=400, mode="records"),
+    # dark vectors on SM showers: 10^5 e- at 10 GeV in graphite, cut 0.010 GeV,
+    # the shipped dark masses nearest below {0.01, 0.05, 0.1, 0.3} GeV
+    "dark_e10_graphite_1e5": dict(target="graphite", cut=0.010, n=100_000, species=(11,), emin=10.0, emax=10.0,
+                                  seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark"),
+    # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
+    # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
+    "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
 }
 
 # Algorithmic HBM bytes of the batched engine's two kernels, per unit of work,
@@ -188,6 +195,10 @@ def dist_setup():
 def run_reference(args, w, name):
     dist, rank, ws = dist_setup()
     if rank != 0:
+        return
+    if w["mode"] not in ("batch", "records"):
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {name} workload; "
+                          "the dark path is compared with the oracle in tests/test_gpu_dark.py"}))
         return
     vals, cb = [], None
     for _ in range(args.steps):
@@ -467,6 +478,118 @@ def bench_records(args, w, name, dist, rank, ws):
         "cpu_baseline": cb, "clocks": clk.summary(), "particle_steps": rows_all}))
 
 
+def bench_dark(args, w, name, dist, rank, ws):
+    """SM showers (float64 record engine) then dark-vector production for every
+    mass on the same rows; a step is the whole batch of primaries."""
+    import torch
+    from petite_gb300.dark import DarkShower
+    n = args.primaries or w["n"]
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    showers = [DarkShower(None, w["target"], w["cut"], m, seed=w["seed"], device=dev,
+                          active_processes=["DarkBrem", "DarkAnn", "DarkComp"]) for m in w["masses"]]
+    sm = showers[0]
+    chunk = min(w["chunk"], n)
+
+    def step(s):
+        rows = vecs = 0
+        ysum = np.zeros((len(showers), 4))
+        t_sm = t_dark = 0.0
+        for c0 in range(0, n, chunk):
+            m = min(chunk, n - c0)
+            p0, pid, mass = make_primaries(w, m, offset=s * ws + rank)
+            opts = sm._opts(True, "fp64")
+            opts.primary_offset = (s * ws + rank) * n + c0
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            st, nr = sm._engine.run_sm(p0, np.zeros((m, 3)), pid, mass, np.ones(m), opts)
+            torch.cuda.synchronize(dev)
+            t1 = time.perf_counter()
+            for k, d in enumerate(showers):
+                out = d._dark_engine.run_dark(d._prm, st, nr, d._opts(), keep_records=False)
+                ysum[k] += out["yield"]
+                vecs += out["n"]
+            torch.cuda.synchronize(dev)
+            t2 = time.perf_counter()
+            rows += nr
+            t_sm += t1 - t0
+            t_dark += t2 - t1
+            del st
+        return rows, vecs, ysum, t_sm, t_dark
+
+    for s in range(args.warmup):
+        step(1000 + s)
+    tot = [0, 0, np.zeros((len(showers), 4)), 0.0, 0.0]
+    with ClockSampler(dev.index or 0) as clk:
+        for s in range(args.steps):
+            r = step(s)
+            for i in range(5):
+                tot[i] = tot[i] + r[i]
+    rows, vecs, ysum, t_sm, t_dark = tot
+    if rank != 0:
+        return
+    per_mass = {f"{d.get_mV()}": {"yield_per_primary": (ysum[k] / (n * args.steps)).tolist()}
+                for k, d in enumerate(showers)}
+    print(json.dumps({
+        "metric": "dark-vector production: SM rows x dark masses per second (pt_run_dark)",
+        "value": rows * len(showers) / t_dark, "unit": "row-masses/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * (t_sm + t_dark) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "primaries_per_step": n, "E0_GeV": w["emin"], "target": w["target"],
+                   "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "chunk": chunk,
+                   "processes": ["DarkBrem", "DarkAnn_bound", "DarkComp_bound"]},
+        "sm_rows": rows, "sm_rows_per_s": rows / t_sm, "vectors": vecs, "vectors_per_s": vecs / t_dark,
+        "yields": per_mass, "clocks": clk.summary()}))
+
+
+def bench_yield(args, w, name, dist, rank, ws):
+    """Dark-vector yield and its mass derivative at fixed uniforms for 4096
+    (E, mV) pairs and the three electron/positron/photon dark processes."""
+    import torch
+    from petite_gb300.dark import DarkShower, dark_yield, map_mass_index
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    sh = DarkShower(None, w["target"], 0.010, 0.1, seed=w["seed"], device=dev)
+    eng = sh._dark_engine
+    rng = np.random.default_rng(w["seed"] + 17 * rank)
+    n = args.primaries or w["n"]
+    E = 10 ** rng.uniform(math.log10(0.05), 1.0, n)
+    mVh = 10 ** rng.uniform(-3, math.log10(0.3), n)
+    mi = map_mass_index(eng.data.masses, mVh)
+    Et = torch.as_tensor(E, device=dev)
+    procs = ("DarkBrem", "DarkComp", "DarkAnn")
+
+    def step():
+        mV = torch.tensor(mVh, dtype=torch.float64, device=dev, requires_grad=True)
+        loss = 0
+        for p in procs:
+            Y, M = dark_yield(eng, p, Et, mV, n_samples=w["samples"], seed=w["seed"], mass_index=mi)
+            loss = loss + Y.sum() + 1e-3 * M.sum()
+        loss.backward()
+        return mV.grad
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index or 0) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            g = step()
+        e1.record()
+        torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / 1e3
+    evals = args.steps * n * w["samples"] * len(procs) * 2          # forward and adjoint
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "dark yield + adjoint: map-sample evaluations/s (forward and d/dmV)",
+        "value": evals / t, "unit": "sample-evaluations/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "pairs": n, "samples_per_pair": w["samples"], "processes": list(procs),
+                   "target": w["target"]},
+        "grad_finite_fraction": float(torch.isfinite(g).float().mean().item()), "clocks": clk.summary()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -487,6 +610,10 @@ def main():
     dist, rank, ws = dist_setup()
     if w["mode"] == "batch":
         bench_batch(args, w, args.workload, dist, rank, ws)
+    elif w["mode"] == "dark":
+        bench_dark(args, w, args.workload, dist, rank, ws)
+    elif w["mode"] == "yield":
+        bench_yield(args, w, args.workload, dist, rank, ws)
     else:
         bench_records(args, w, args.workload, dist, rank, ws)
 

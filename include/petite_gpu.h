@@ -309,7 +309,8 @@ pt_status pt_dark_sample_only(pt_dark* d, const pt_dark_params* prm, int32_t pro
  * (:595-647) and, when positive, produce_bsm_particle (:721-804).  Row k,
  * process p draws from the stream mix64(pkey[k] + 0x9E3779B97F4A7C15*(3+p)).
  * Vectors are appended to `out` (any order; parent/process identify them);
- * *n_out returns the count.  PT_OOM if out->capacity is too small. */
+ * *n_out returns the count.  PT_OOM if out->capacity is too small.  With
+ * out->p4 == NULL only the yields and the count are accumulated. */
 pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles* sm, int64_t n_rows,
                       const pt_opts* opts, pt_dark_out* out, int64_t* n_out, void* stream);
 

@@ -337,8 +337,8 @@ __global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, 
   const double w = (S(wg) * S(r.weight)).v;
   if (out.yield) atomicAdd(out.yield + p, w);
   if (out.yield_E) atomicAdd(out.yield_E + p, w * V[0]);
+  const unsigned long long slot = atomicAdd(counter, 1ull);   // vectors produced (returned in *n_out)
   if (!out.p4) return;
-  const unsigned long long slot = atomicAdd(counter, 1ull);
   if ((int64_t)slot >= out.capacity) { dark_raise(status, nullptr, PT_OOM, p, r.p0[0], 0); return; }
   const int64_t oc = out.capacity;
   for (int c = 0; c < 4; ++c) out.p4[c * oc + slot] = V[c];

@@ -216,6 +216,8 @@ class DarkEngine:
             break
         n = int(n_out.value)
         out = {k: (v[..., :n].cpu().numpy()) for k, v in bufs.items()}
+        if not keep_records:
+            out = {}
         if "p4" in out:
             out["p4"], out["r"] = out["p4"].T.copy(), out["r"].T.copy()
         out["yield"] = yld.cpu().numpy()

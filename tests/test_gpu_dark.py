@@ -217,3 +217,43 @@ def test_dark_yield_gradient_matches_fp64_reference(showers):
                 assert g[i] == 0.0
                 continue
             assert abs(g[i] - ref) <= 1e-6 * abs(ref), (proc, E[i], mVh[i], g[i], ref)
+
+
+def test_dark_on_gpu_showers_matches_oracle(showers):
+    """SM showers from the GPU record engine, then pt_run_dark against the
+    oracle's produce_bsm_particle on the same rows and streams (10 GeV e-,
+    graphite, mV = 0.1 GeV)."""
+    import torch
+    from oracle import dark as D
+    from oracle.shower import OracleTables
+    sh = showers[(0.1, "graphite")]
+    n = 4
+    p = math.sqrt(100.0 - 0.000511 ** 2)
+    opts = sh._opts(True, "fp64")
+    opts.primary_offset = 77
+    st, nr = sh._engine.run_sm(np.tile([10.0, 0, 0, p], (n, 1)), np.zeros((n, 3)), np.full(n, 11, np.int32),
+                               np.full(n, 0.000511), np.ones(n), opts)
+    res = sh._dark_engine.run_dark(sh._prm, st, nr, sh._opts())
+    rows = st.to_numpy(nr)
+
+    class R:
+        pass
+    recs = []
+    for k in range(nr):
+        r = R()
+        r.p0, r.pf, r.rf = tuple(rows["p0"][k]), tuple(rows["pf"][k]), tuple(rows["rf"][k])
+        r.pid, r.mass, r.weight, r.pkey = int(rows["pid"][k]), float(rows["mass"][k]), 1.0, int(rows["pkey"][k])
+        recs.append(r)
+    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, "graphite", 0.1), OracleTables(BUNDLED_NPZ, "graphite"), SEED)
+    out = orc.dark_shower(recs, processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"))
+    want = np.array([[k, D.DARK_CODE[pp], w, *v] for k, pp, w, v, _ in out])
+    want = want[np.lexsort((want[:, 1], want[:, 0]))]
+    proc = res["process"] % 4
+    o = np.lexsort((proc, res["parent"]))
+    assert res["n"] == len(want) > 100
+    assert np.array_equal(res["parent"][o], want[:, 0].astype(np.int64))
+    assert np.array_equal(proc[o], want[:, 1].astype(np.int64))
+    np.testing.assert_allclose(res["weight"][o], want[:, 2], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(res["p4"][o][:, 0], want[:, 3], rtol=1e-12, atol=0)
+    for p_ in range(3):
+        np.testing.assert_allclose(res["yield"][p_], want[want[:, 1] == p_, 2].sum(), rtol=1e-12)
