@@ -612,8 +612,10 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       } else {
         ++L.substeps;
         const float mfp = mfp32(T, pid, Ef);
-        const float u_hard = rng.uf();
-        const float q = fmaf(14.f, rng.uf(), 6.f);       // delta_z = mfp / U(6, 20)
+        float u2[2];
+        rng.take(u2);
+        const float u_hard = u2[0];
+        const float q = fmaf(14.f, u2[1], 6.f);          // delta_z = mfp / U(6, 20)
         dzf = mfp / q;
         if (u_hard > __expf(-1.f / q)) {                 // hard scatter: final increment
           step = -mfp * log1pf(expm1f(-1.f / q) * rng.uf());
@@ -951,7 +953,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
     KinEntry<PREC> ent;
     if (active) {
       // ---- one proposal (d uniforms for y, then the accept uniform)
-      if (PREC == 0) {
+      if constexpr (PREC == 0) {
         double* xd = reinterpret_cast<KinEntry<0>&>(ent).x;
         double jac = 1.0;
 #pragma unroll
@@ -963,9 +965,19 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
       } else {
         MapPt32* xm = reinterpret_cast<KinEntry<1>&>(ent).x;
         float jac = 1.f;
+        float ua;                      // the accept draw
+        if (d == 4) {                  // four y draws and the accept draw in three Philox blocks
+          float u5[5];
+          rng.take(u5);
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (k < d) xm[k] = map_dim32(g32[k], ninc[k], rng.uf(), jac);
+          for (int k = 0; k < 4; ++k) xm[k] = map_dim32(g32[k], ninc[k], u5[k], jac);
+          ua = u5[4];
+        } else {
+          float u2[2];
+          rng.take(u2);
+          xm[0] = map_dim32(g32[0], ninc[0], u2[0], jac);
+          ua = u2[1];
+        }
         float r;
         switch (process) {
           case PT_BREM: case PT_MUONBREM: r = brem32_ratio(S32, xm, jac); break;
@@ -976,7 +988,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
           case PT_BHABHA: r = bhabha32_ratio(S32, xm[0], jac); break;
           default: r = muone32_ratio(S32, xm[0], jac); break;
         }
-        accept = rng.uf() < r;
+        accept = ua < r;
         if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf();
       }
       ++props;

@@ -67,6 +67,35 @@ struct Rng {
     const uint32_t hi = (uint32_t)(next_u64() >> 32);
     return __uint2float_rn(hi >> 8) * 0x1p-24f;
   }
+  // The float forms of the next D draws with a fixed number of Philox blocks,
+  // (D+1)/2, whatever the stream's parity: a warp whose lanes sit at
+  // different parities issues (D+1)/2 blocks instead of one per draw (the
+  // branch of next_u64 diverges).  The same draws as D calls of uf().
+  template <int D>
+  __device__ __forceinline__ void take(float (&u)[D]) {
+    constexpr int NB = (D + 1) / 2;
+    constexpr int KS = (D & 1) ? (D - 1) / 2 : D / 2 - 1;   // block holding the odd half left over
+    const bool odd = (n & 1ull) != 0;
+    const uint64_t b0 = (n + 1) >> 1;                      // first block not yet drawn from
+    uint32_t h[2 * NB];
+    uint64_t left = 0;
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+      const uint64_t blk = b0 + (uint64_t)k;
+      const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+      h[2 * k] = o.y;
+      h[2 * k + 1] = o.w;
+      if (k == KS) left = (uint64_t)o.z | ((uint64_t)o.w << 32);
+    }
+    const uint32_t sp = (uint32_t)(spare >> 32);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const uint32_t w = odd ? (j == 0 ? sp : h[j > 0 ? j - 1 : 0]) : h[j];
+      u[j] = __uint2float_rn(w >> 8) * 0x1p-24f;
+    }
+    n += D;
+    if (n & 1ull) spare = left;      // only the parity that ends inside block KS gets here
+  }
 };
 
 // --------------------------------------------------- non-contracting float64

@@ -208,11 +208,13 @@ __device__ __forceinline__ float lynch_dahl_g(float v) {
   return (1.f + v) * log1pf(v) / v - 1.f;
 }
 
+template <class R>
 __device__ __forceinline__ void mcs32(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
-                                      float rescale, Rng& rng, float beta_p = -1.f) {
+                                      float rescale, R& rng, float beta_p = -1.f) {
   if (!(pmag > 0.f)) return;             // a particle at rest draws nothing (moliere.py:359-363)
-  const float u_sign = rng.uf(), u_ang = rng.uf(), u_rad = rng.uf(), u_phi = rng.uf();
-  (void)u_ang;   // the Gaussian pair's angle cancels in the space angle
+  float u4[4];
+  rng.take(u4);
+  const float u_sign = u4[0], u_rad = u4[2], u_phi = u4[3];   // u4[1]: the Gaussian pair's angle cancels
   const float beta = beta_p >= 0.f ? beta_p : pmag / E;
   const float p = pmag * 1000.f;                         // MeV
   const float pb = p * beta;
