@@ -560,6 +560,8 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
   float3 dir = make_float3(0.f, 0.f, 1.f), pos = make_float3(0.f, 0.f, 0.f), disp = make_float3(0.f, 0.f, 0.f);
   int pid = 0, prim = 0;
   Rng rng;
+  float uc = 0.f;                 // the process-choice draw, already taken with the last step
+  bool have_uc = false;
 
   for (;;) {
     __syncwarp();
@@ -604,25 +606,32 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       float step, mlep = mtab;
       bool last = true;
       const bool charged = pid != 22;
+      // Every draw this step can take, in stream order, from four Philox
+      // blocks for all lanes: a photon's flight and its process choice; a
+      // substep's two draws, then the final increment's draw when the hard
+      // scatter ends it, the four of multiple scattering and the choice.
+      Rng::Drawn<8> dr;
+      rng.peek(dr);
+      int base = 1;                                       // first multiple-scattering draw
       if (!charged) {
-        step = -mfp32(T, pid, Ef) * log1pf(-rng.uf());  // mfp log(1/(1-u))
+        step = -mfp32(T, pid, Ef) * log1pf(-dr.u[0]);     // mfp log(1/(1-u))
       } else if (!(Ef >= pmef)) {
-        step = rng.uf() * dzf;                            // shower.py:584-585
+        step = dr.u[0] * dzf;                             // shower.py:584-585
         mlep = me;                                        // shower.py:596-598: electron mass
       } else {
         ++L.substeps;
         const float mfp = mfp32(T, pid, Ef);
-        float u2[2];
-        rng.take(u2);
-        const float u_hard = u2[0];
-        const float q = fmaf(14.f, u2[1], 6.f);          // delta_z = mfp / U(6, 20)
+        const float u_hard = dr.u[0];
+        const float q = fmaf(14.f, dr.u[1], 6.f);         // delta_z = mfp / U(6, 20)
         dzf = mfp / q;
         if (u_hard > __expf(-1.f / q)) {                 // hard scatter: final increment
-          step = -mfp * log1pf(expm1f(-1.f / q) * rng.uf());
+          step = -mfp * log1pf(expm1f(-1.f / q) * dr.u[2]);
           mlep = me;
+          base = 3;
         } else {
           step = dzf;
           last = false;
+          base = 2;
         }
       }
       if (charged) {                                      // lose_energy (particle.py:143-153)
@@ -634,8 +643,16 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       if (pmag > 0.f) {
         disp.x = fmaf(dir.x, step, disp.x); disp.y = fmaf(dir.y, step, disp.y); disp.z = fmaf(dir.z, step, disp.z);
       }
-      // Lynch-Dahl momentum p = m_lepton * beta * gamma = |p| m_lepton / m
-      if (charged && c.ms) mcs32(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, rng, pmag / Ef);
+      // Lynch-Dahl momentum p = m_lepton * beta * gamma = |p| m_lepton / m;
+      // a particle at rest draws nothing (moliere.py:359-363)
+      const bool scat = charged && c.ms && pmag > 0.f;
+      if (scat)
+        mcs32_u(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, pick(dr.u, base),
+                pick(dr.u, base + 2), pick(dr.u, base + 3), pmag / Ef);
+      const int after = base + (scat ? 4 : 0);
+      if (last) uc = pick(dr.u, after);                  // the process-choice draw
+      rng.advance(dr, after + (last ? 1 : 0));
+      have_uc = last;
       if (last) {
         active = false;
         fin = true;
@@ -655,7 +672,8 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
         e.E0 = E0;
         e.px = pmag * dir.x; e.py = pmag * dir.y; e.pz = pmag * dir.z;
         e.x = pos.x + disp.x; e.y = pos.y + disp.y; e.z = pos.z + disp.z;
-        e.u = rng.uf();                                  // the process-choice draw
+        e.u = have_uc ? uc : rng.uf();                   // the process-choice draw
+        have_uc = false;
         e.draw = (uint32_t)rng.n;
         e.pme = pmef;
         e.th0 = th0;

@@ -96,7 +96,63 @@ struct Rng {
     n += D;
     if (n & 1ull) spare = left;      // only the parity that ends inside block KS gets here
   }
+
+  // Look-ahead form for the float32 kernels: peek computes the float forms of
+  // the next D draws ((D+1)/2 blocks, as take does) without consuming them;
+  // advance then consumes the first `used` (0..D).  Only the odd halves' high
+  // words are kept for the leftover, so after advance only uf()/take()/peek()
+  // may follow (not u()).
+  template <int D>
+  struct Drawn {
+    float u[D];
+    uint32_t hi[(D + 1) / 2];        // high word of each block's odd half
+  };
+  template <int D>
+  __device__ __forceinline__ void peek(Drawn<D>& P) const {
+    constexpr int NB = (D + 1) / 2;
+    const bool odd = (n & 1ull) != 0;
+    const uint64_t b0 = (n + 1) >> 1;
+    uint32_t h[2 * NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+      const uint64_t blk = b0 + (uint64_t)k;
+      const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+      h[2 * k] = o.y;
+      h[2 * k + 1] = o.w;
+      P.hi[k] = o.w;
+    }
+    const uint32_t sp = (uint32_t)(spare >> 32);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const uint32_t w = odd ? (j == 0 ? sp : h[j > 0 ? j - 1 : 0]) : h[j];
+      P.u[j] = __uint2float_rn(w >> 8) * 0x1p-24f;
+    }
+  }
+  template <int D>
+  __device__ __forceinline__ void advance(const Drawn<D>& P, int used) {
+    if (used <= 0) return;
+    const uint64_t b0 = (n + 1) >> 1;
+    n += (uint64_t)used;
+    if (n & 1ull) {
+      const uint64_t k = (n >> 1) - b0;
+      uint32_t w = 0;
+#pragma unroll
+      for (int j = 0; j < (D + 1) / 2; ++j)
+        if ((uint64_t)j == k) w = P.hi[j];
+      spare = (uint64_t)w << 32;
+    }
+  }
 };
+
+// P.u[i] for a runtime index i < D, without an indexed (local-memory) access
+template <int D>
+__device__ __forceinline__ float pick(const float (&u)[D], int i) {
+  float r = u[0];
+#pragma unroll
+  for (int j = 1; j < D; ++j)
+    if (j == i) r = u[j];
+  return r;
+}
 
 // --------------------------------------------------- non-contracting float64
 // The reference evaluates expressions one rounding per operation (numpy

@@ -208,13 +208,22 @@ __device__ __forceinline__ float lynch_dahl_g(float v) {
   return (1.f + v) * log1pf(v) / v - 1.f;
 }
 
+// The scattering with its three used draws given (sign, Gaussian radius, phi;
+// the pair's angle draw cancels in the space angle).
+__device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
+                                        float rescale, float u_sign, float u_rad, float u_phi, float beta_p);
+
 template <class R>
 __device__ __forceinline__ void mcs32(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
                                       float rescale, R& rng, float beta_p = -1.f) {
   if (!(pmag > 0.f)) return;             // a particle at rest draws nothing (moliere.py:359-363)
   float u4[4];
   rng.take(u4);
-  const float u_sign = u4[0], u_rad = u4[2], u_phi = u4[3];   // u4[1]: the Gaussian pair's angle cancels
+  mcs32_u(dir, pmag, E, t, A, Z, Z23, rescale, u4[0], u4[2], u4[3], beta_p);
+}
+
+__device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
+                                        float rescale, float u_sign, float u_rad, float u_phi, float beta_p) {
   const float beta = beta_p >= 0.f ? beta_p : pmag / E;
   const float p = pmag * 1000.f;                         // MeV
   const float pb = p * beta;
