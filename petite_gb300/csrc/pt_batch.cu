@@ -21,6 +21,7 @@
 // as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
 // builds directions in float32 and keeps energies in float64.
 #include <cstdio>
+#include <cstdlib>
 #include <type_traits>
 
 #include "pt_internal.cuh"
@@ -31,6 +32,11 @@ using namespace pt;
 namespace {
 
 constexpr int kThreads = 128;
+// Idle lanes a warp gathers before refilling them (1 = refill at once); 8
+// measured best for both kernels on the 10^6-primary lead workload
+// (sweep of 1-24 with PETITE_REFILL_MIN).
+constexpr int kRefillMinPropagate = 8;
+constexpr int kRefillMinSample = 8;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kHB = PT_HIST_BINS;
@@ -74,6 +80,7 @@ template <int PREC> struct WaveCtx {
   int* status;
   double* err_info;
   Tally tally;
+  int refill_min[2];                  // idle lanes a warp gathers before refilling: [0] propagation, [1] sampler
 };
 
 __device__ void raise_status(int* status, double* info, int code, int process, double E, int key) {
@@ -556,6 +563,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
   bool active = false;
   uint32_t i = 0;
   double E0 = 0.0;
+  float E0f = 0.f;                // (float)E0, converted once per particle
   float Ef = 0.f, mf = 0.f, pmef = 0.f, lossf = 0.f, dzf = 0.f, pmag = 0.f, th0 = 0.f, mtab = 0.f;
   float3 dir = make_float3(0.f, 0.f, 1.f), pos = make_float3(0.f, 0.f, 0.f), disp = make_float3(0.f, 0.f, 0.f);
   int pid = 0, prim = 0;
@@ -565,7 +573,10 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
 
   for (;;) {
     __syncwarp();
-    const bool need = !active;
+    // a lane that is done waits until enough lanes are idle, so the refill's
+    // loads and set-up run for several lanes at once
+    const unsigned idle = __ballot_sync(kFull, !active);
+    const bool need = !active && (__popc(idle) >= c.refill_min[0] || idle == kFull);
     const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, 128);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
@@ -582,7 +593,8 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       mf = c.q.mass[i];
       prim = c.q.prim[i];
       rng.init(c.seed, c.q.key[i]);
-      Ef = (float)E0;
+      E0f = (float)E0;
+      Ef = E0f;
       const int sp = species_of(pid);
       const float mcs = sp == 0 ? mc0 : (sp == 1 ? mc1 : (sp == 2 ? mc2 : mc3));
       pmef = fmaxf(fmaxf(mcs, minE), mf);                // shower.py:532-533
@@ -636,7 +648,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       }
       if (charged) {                                      // lose_energy (particle.py:143-153)
         lossf = fmaf(lossesf, step, lossf);
-        Ef = (float)E0 - lossf;
+        Ef = E0f - lossf;
         if (Ef <= mf) Ef = mf;
         pmag = sqrtf((Ef - mf) * (Ef + mf));
       }
@@ -920,7 +932,8 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
 
   for (;;) {
     __syncwarp();
-    const bool need = !active;
+    const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
+    const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
     const int64_t t = pool_take(pool, c.ctr + 1, total, need, 64);
     const bool fresh = need && t >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
@@ -1170,6 +1183,15 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.err_info = hp.err_info;
   c.tally = {tally->counts, tally->energy, tally->hist, tally->primary_count, tally->primary_edep,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
+  c.refill_min[0] = kRefillMinPropagate;
+  c.refill_min[1] = kRefillMinSample;
+  if (const char* e = getenv("PETITE_REFILL_MIN")) {   // tuning sweeps: "prop,sample"
+    int a = 0, b = 0;
+    if (sscanf(e, "%d,%d", &a, &b) == 2 && a >= 1 && a <= 32 && b >= 1 && b <= 32) {
+      c.refill_min[0] = a;
+      c.refill_min[1] = b;
+    }
+  }
   const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate_fp64;
   const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);
