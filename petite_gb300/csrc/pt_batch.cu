@@ -81,6 +81,7 @@ template <int PREC> struct WaveCtx {
   double* err_info;
   Tally tally;
   int refill_min[2];                  // idle lanes a warp gathers before refilling: [0] propagation, [1] sampler
+  PhiloxRK rk;                        // round keys of `seed` (float32 kernels)
 };
 
 __device__ void raise_status(int* status, double* info, int code, int process, double E, int key) {
@@ -537,7 +538,7 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
   publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
 }
 
-__global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
+__global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
   __shared__ int sh_bcnt[kWarps][8];
@@ -623,7 +624,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
       // substep's two draws, then the final increment's draw when the hard
       // scatter ends it, the four of multiple scattering and the choice.
       Rng::Drawn<8> dr;
-      rng.peek(dr);
+      rng.peek(dr, c.rk);
       int base = 1;                                       // first multiple-scattering draw
       if (!charged) {
         step = -mfp32(T, pid, Ef) * log1pf(-dr.u[0]);     // mfp log(1/(1-u))
@@ -684,7 +685,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_mixed(WaveCtx<1> c) {
         e.E0 = E0;
         e.px = pmag * dir.x; e.py = pmag * dir.y; e.pz = pmag * dir.z;
         e.x = pos.x + disp.x; e.y = pos.y + disp.y; e.z = pos.z + disp.z;
-        e.u = have_uc ? uc : rng.uf();                   // the process-choice draw
+        e.u = have_uc ? uc : rng.uf(c.rk);               // the process-choice draw
         have_uc = false;
         e.draw = (uint32_t)rng.n;
         e.pme = pmef;
@@ -999,13 +1000,13 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
         float ua;                      // the accept draw
         if (d == 4) {                  // four y draws and the accept draw in three Philox blocks
           float u5[5];
-          rng.take(u5);
+          rng.take(u5, c.rk);
 #pragma unroll
           for (int k = 0; k < 4; ++k) xm[k] = map_dim32(g32[k], ninc[k], u5[k], jac);
           ua = u5[4];
         } else {
           float u2[2];
-          rng.take(u2);
+          rng.take(u2, c.rk);
           xm[0] = map_dim32(g32[0], ninc[0], u2[0], jac);
           ua = u2[1];
         }
@@ -1020,7 +1021,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
           default: r = muone32_ratio(S32, xm[0], jac); break;
         }
         accept = ua < r;
-        if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf();
+        if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf(c.rk);
       }
       ++props;
       ++L.props;
@@ -1183,6 +1184,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.err_info = hp.err_info;
   c.tally = {tally->counts, tally->energy, tally->hist, tally->primary_count, tally->primary_edep,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
+  c.rk = philox_round_keys(o->seed);
   c.refill_min[0] = kRefillMinPropagate;
   c.refill_min[1] = kRefillMinSample;
   if (const char* e = getenv("PETITE_REFILL_MIN")) {   // tuning sweeps: "prop,sample"

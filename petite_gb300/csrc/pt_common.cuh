@@ -33,6 +33,36 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
   return c;
 }
 
+// The same Philox4x32-10 with the key schedule of a fixed seed precomputed
+// (round r uses seed words + r * (0x9E3779B9, 0xBB67AE85)).  Kernels pass the
+// table as a by-value parameter, so each round key is an operand read from
+// the parameter space instead of two additions per round, and each round's
+// two products are single 32x32->64 multiplies.
+struct PhiloxRK {
+  uint32_t k[20];
+};
+__host__ __device__ inline PhiloxRK philox_round_keys(uint64_t seed) {
+  PhiloxRK R;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    R.k[2 * r] = k0;
+    R.k[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return R;
+}
+__device__ __forceinline__ uint4 philox_rk(uint4 c, const PhiloxRK& R) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+    c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ R.k[2 * r], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ R.k[2 * r + 1],
+                   (uint32_t)p0);
+  }
+  return c;
+}
+
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {   // SplitMix64 finaliser
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
@@ -67,12 +97,26 @@ struct Rng {
     const uint32_t hi = (uint32_t)(next_u64() >> 32);
     return __uint2float_rn(hi >> 8) * 0x1p-24f;
   }
+  // uf() with the precomputed round keys of this stream's seed
+  __device__ __forceinline__ float uf(const PhiloxRK& R) {
+    uint64_t v;
+    if (n & 1ull) {
+      v = spare;
+    } else {
+      const uint64_t blk = n >> 1;
+      const uint4 o = philox_rk(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), R);
+      spare = (uint64_t)o.z | ((uint64_t)o.w << 32);
+      v = (uint64_t)o.x | ((uint64_t)o.y << 32);
+    }
+    ++n;
+    return __uint2float_rn((uint32_t)(v >> 32) >> 8) * 0x1p-24f;
+  }
   // The float forms of the next D draws with a fixed number of Philox blocks,
   // (D+1)/2, whatever the stream's parity: a warp whose lanes sit at
   // different parities issues (D+1)/2 blocks instead of one per draw (the
   // branch of next_u64 diverges).  The same draws as D calls of uf().
   template <int D>
-  __device__ __forceinline__ void take(float (&u)[D]) {
+  __device__ __forceinline__ void take(float (&u)[D], const PhiloxRK& R) {
     constexpr int NB = (D + 1) / 2;
     constexpr int KS = (D & 1) ? (D - 1) / 2 : D / 2 - 1;   // block holding the odd half left over
     const bool odd = (n & 1ull) != 0;
@@ -82,7 +126,7 @@ struct Rng {
 #pragma unroll
     for (int k = 0; k < NB; ++k) {
       const uint64_t blk = b0 + (uint64_t)k;
-      const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+      const uint4 o = philox_rk(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), R);
       h[2 * k] = o.y;
       h[2 * k + 1] = o.w;
       if (k == KS) left = (uint64_t)o.z | ((uint64_t)o.w << 32);
@@ -108,7 +152,7 @@ struct Rng {
     uint32_t hi[(D + 1) / 2];        // high word of each block's odd half
   };
   template <int D>
-  __device__ __forceinline__ void peek(Drawn<D>& P) const {
+  __device__ __forceinline__ void peek(Drawn<D>& P, const PhiloxRK& R) const {
     constexpr int NB = (D + 1) / 2;
     const bool odd = (n & 1ull) != 0;
     const uint64_t b0 = (n + 1) >> 1;
@@ -116,7 +160,7 @@ struct Rng {
 #pragma unroll
     for (int k = 0; k < NB; ++k) {
       const uint64_t blk = b0 + (uint64_t)k;
-      const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+      const uint4 o = philox_rk(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), R);
       h[2 * k] = o.y;
       h[2 * k + 1] = o.w;
       P.hi[k] = o.w;

@@ -213,14 +213,6 @@ __device__ __forceinline__ float lynch_dahl_g(float v) {
 __device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
                                         float rescale, float u_sign, float u_rad, float u_phi, float beta_p);
 
-template <class R>
-__device__ __forceinline__ void mcs32(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
-                                      float rescale, R& rng, float beta_p = -1.f) {
-  if (!(pmag > 0.f)) return;             // a particle at rest draws nothing (moliere.py:359-363)
-  float u4[4];
-  rng.take(u4);
-  mcs32_u(dir, pmag, E, t, A, Z, Z23, rescale, u4[0], u4[2], u4[3], beta_p);
-}
 
 __device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
                                         float rescale, float u_sign, float u_rad, float u_phi, float beta_p) {
