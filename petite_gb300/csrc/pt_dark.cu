@@ -318,8 +318,9 @@ __global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, 
                            pt_dark_out out, unsigned long long* counter, int* status, double* info) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n_rows * PT_N_DARK) return;
-  const int64_t row = t / PT_N_DARK;
-  const int p = (int)(t % PT_N_DARK);
+  // process-major: a warp works on one dark process for 32 consecutive rows
+  const int p = (int)(t / n_rows);
+  const int64_t row = t - (int64_t)p * n_rows;
   DarkRow r;
   r.pid = sm.pid[row];
   const int64_t cap = sm.capacity;
