@@ -601,10 +601,14 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ring-log2", type=int, default=25, help="batched engine: log2 of the ring capacity")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
+                    help="batched engine: override the workload's precision (profiling the float64 form)")
     ap.add_argument("--quick", action="store_true",
                     help="device steps only (no float64 comparison, e2e or CPU baseline): for profiling")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.precision:
+        w["precision"] = args.precision
     if args.impl == "reference":
         return run_reference(args, w, args.workload)
     dist, rank, ws = dist_setup()
