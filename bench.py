@@ -77,8 +77,8 @@ BYTES_PER_STEP_RECORDS = 336
 # are summarised in the named profile.  The bench scales it to its own
 # launches by the particle-steps they process.
 NCU_TRAFFIC = {
-    "propagate": {"bytes_per_step": 65.26, "profile": "profiles/dram_traffic_lead_20k.md"},
-    "sample": {"bytes_per_step": 236.53, "profile": "profiles/dram_traffic_lead_20k.md"},
+    "propagate": {"bytes_per_step": 64.36, "profile": "profiles/dram_traffic_lead_20k.md"},
+    "sample": {"bytes_per_step": 231.10, "profile": "profiles/dram_traffic_lead_20k.md"},
 }
 
 
