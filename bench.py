@@ -34,6 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from petite_gb300.replicas import block_index, first_primary, reduce_job  # noqa: E402
+
 METRIC = "particle-steps/s on 1 GB300: batched mixed-precision vs plain FP64 GPU, matched spectra"
 
 WORKLOADS = {
@@ -247,13 +249,13 @@ def bench_batch(args, w, name, dist, rank, ws):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)   # > 129 MB L2
 
     def stage(step):
-        p0, pid, m = make_primaries(w, n, offset=step * ws + rank)
+        p0, pid, m = make_primaries(w, n, offset=block_index(step, rank, ws))
         return (torch.as_tensor(np.ascontiguousarray(p0.T), device=dev), torch.zeros((3, n), dtype=torch.float64, device=dev),
                 torch.as_tensor(pid, device=dev), torch.as_tensor(m, device=dev))
 
     def device_step(step, precision, tally, inputs):
         opts = sh._opts(True, precision)
-        opts.primary_offset = (step * ws + rank) * n
+        opts.primary_offset = first_primary(step, rank, ws, n)
         P0, R0, PID, M = inputs
         stream = torch.cuda.current_stream(dev)
         flush.zero_()
@@ -300,14 +302,7 @@ def bench_batch(args, w, name, dist, rank, ws):
             for key in ("steps", "sampled", "pushed"):
                 kt[key] += summ[key]
     t_local = float(sum(times))
-    if dist:
-        t = torch.tensor([t_local], device=dev)
-        r = torch.tensor([float(steps_done)], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(r, op=dist.ReduceOp.SUM)
-        t_max, steps_all = float(t.item()), float(r.item())
-    else:
-        t_max, steps_all = t_local, float(steps_done)
+    t_max, steps_all = reduce_job(t_local, steps_done, dist, dev)
     value = steps_all / t_max
 
     # plain float64 engine vs mixed on the same first primaries and streams
@@ -328,13 +323,13 @@ def bench_batch(args, w, name, dist, rank, ws):
     # end to end through the public API: pinned host inputs, host tallies back
     e2e_steps, e2e_t, h2d, d2h = 0, 0.0, 0, 0
     for s in range(min(args.steps, 2)):
-        p0, pid, m = make_primaries(w, n, offset=500 + s * ws + rank)
+        p0, pid, m = make_primaries(w, n, offset=500 + block_index(s, rank, ws))
         p0h = torch.as_tensor(p0).pin_memory()
         pidh = torch.as_tensor(pid).pin_memory()
         mh = torch.as_tensor(m).pin_memory()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        out = sh.run_tallied(p0h, pidh, mh, precision=w["precision"], first_primary=(500 + s * ws + rank) * n,
+        out = sh.run_tallied(p0h, pidh, mh, precision=w["precision"], first_primary=(500 + block_index(s, rank, ws)) * n,
                              z_max=zmax, queue_capacity=cap)
         torch.cuda.synchronize(dev)
         e2e_t += time.perf_counter() - t0
@@ -406,8 +401,8 @@ def bench_records(args, w, name, dist, rank, ws):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def step(s):
-        p0, pid, m = make_primaries(w, n, offset=s * ws + rank)
-        opts.primary_offset = (s * ws + rank) * n
+        p0, pid, m = make_primaries(w, n, offset=block_index(s, rank, ws))
+        opts.primary_offset = first_primary(s, rank, ws, n)
         cap = int(np.sum(2.0 * p0[:, 0] / w["cut"]) + 16 * n)
         st = ParticleStore(cap, dev)
         st.t["p0"][:, :n] = torch.as_tensor(p0.T, device=dev)
@@ -440,14 +435,14 @@ def bench_records(args, w, name, dist, rank, ws):
             times.append(dt)
             rows += r
             launches += eng.last_run_stats()[0]
-    t_max, rows_all = float(sum(times)), float(rows)
+    t_max, rows_all = reduce_job(float(sum(times)), float(rows), dist, dev)
     value = rows_all / t_max
     e2e_rows, e2e_t, h2d, d2h = 0, 0.0, 0, 0
     for s in range(args.steps):
-        p0, pid, m = make_primaries(w, n, offset=500 + s * ws + rank)
+        p0, pid, m = make_primaries(w, n, offset=500 + block_index(s, rank, ws))
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        b = sh.generate_showers(p0, pid=pid, mass=m, first_primary=(500 + s * ws + rank) * n)
+        b = sh.generate_showers(p0, pid=pid, mass=m, first_primary=(500 + block_index(s, rank, ws)) * n)
         torch.cuda.synchronize(dev)
         e2e_t += time.perf_counter() - t0
         e2e_rows += b.n
@@ -496,9 +491,9 @@ def bench_dark(args, w, name, dist, rank, ws):
         t_sm = t_dark = 0.0
         for c0 in range(0, n, chunk):
             m = min(chunk, n - c0)
-            p0, pid, mass = make_primaries(w, m, offset=s * ws + rank)
+            p0, pid, mass = make_primaries(w, m, offset=block_index(s, rank, ws))
             opts = sm._opts(True, "fp64")
-            opts.primary_offset = (s * ws + rank) * n + c0
+            opts.primary_offset = first_primary(s, rank, ws, n) + c0
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
             st, nr = sm._engine.run_sm(p0, np.zeros((m, 3)), pid, mass, np.ones(m), opts)
