@@ -595,7 +595,9 @@ def main():
     ap.add_argument("--primaries", type=int, default=0, help="override primaries per step")
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ring-log2", type=int, default=25, help="batched engine: log2 of the ring capacity")
+    ap.add_argument("--ring-log2", type=int, default=27,
+                    help="batched engine: log2 of the ring capacity (2^27: waves of ~1.2e7 entries; larger "
+                         "rings saturate on the 1e6-primary workload)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
                     help="batched engine: override the workload's precision (profiling the float64 form)")
     ap.add_argument("--quick", action="store_true",
