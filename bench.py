@@ -274,6 +274,12 @@ def bench_batch(args, w, name, dist, rank, ws):
             raise RuntimeError(f"pt_run_batch status {s}")
         return e0.elapsed_time(e1) / 1e3
 
+    tuning = None
+    if not args.no_autotune:
+        # work-distribution settings picked on a 1e5-primary calibration run
+        # of the same species and energies (outside the timed region)
+        from petite_gb300.autotune import autotune_batch
+        tuning = autotune_batch(sh, precision=w["precision"], n=100_000, ring_capacity=1 << 24, use_cache=False)
     tally = eng.new_tally(n, zmax)
     for s in range(args.warmup):
         device_step(1000 + s, w["precision"], tally, stage(1000 + s))
@@ -368,7 +374,7 @@ def bench_batch(args, w, name, dist, rank, ws):
         "config": {"workload": name, "primaries_per_step": n, "species": list(w["species"]),
                    "E0_GeV": [w["emin"], w["emax"]], "target": w["target"], "cut_GeV": w["cut"],
                    "precision": w["precision"], "seed": w["seed"], "l2": "flushed (256 MB write) before each step",
-                   "parallelism": f"replicas{ws}", "ring_capacity": cap},
+                   "parallelism": f"replicas{ws}", "ring_capacity": cap, "tuning": tuning},
         "fp64_engine": {"value": fp64_rate, "unit": "particle-steps/s", "sample_primaries": nf,
                         "mixed_on_same_sample": mixed_sub_rate, "mixed_over_fp64": mixed_sub_rate / fp64_rate},
         "matched_spectra": matched,
@@ -600,6 +606,7 @@ def main():
                          "rings saturate on the 1e6-primary workload)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
                     help="batched engine: override the workload's precision (profiling the float64 form)")
+    ap.add_argument("--no-autotune", action="store_true", help="batched engine: library default work distribution")
     ap.add_argument("--quick", action="store_true",
                     help="device steps only (no float64 comparison, e2e or CPU baseline): for profiling")
     args = ap.parse_args()

@@ -194,6 +194,20 @@ pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const i
  * (transport iterations).  Diagnostic; no reference counterpart. */
 pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* waves);
 
+/* Work-distribution settings of pt_run_batch (0 = library default).  No
+ * counterpart in the reference: chosen by petite_gb300.autotune.
+ *  refill_min[k]: idle lanes a warp gathers before refilling them, 1..32
+ *                 (k = 0 propagation kernel, 1 sampler kernel; default 8)
+ *  chunk[k]:      entries a warp claims from the wave's pool per atomic,
+ *                 32..4096 (defaults 128 and 64) */
+typedef struct pt_batch_tuning {
+  int32_t refill_min[2];
+  int32_t chunk[2];
+} pt_batch_tuning;
+/* Stores the settings on the handle (NULL restores the defaults);
+ * PT_BAD_ARG for a value out of range. */
+pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t);
+
 /* Device time of the last pt_run_batch on this handle, summed over its waves
  * and measured with CUDA events on the run's stream: the propagation kernel
  * and the sampler kernel, in milliseconds.  Diagnostic; no reference

@@ -18,7 +18,8 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE
 PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
-           "pt_last_kernel_times", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch", "pt_sample_only", "pt_dsigma",
+           "pt_last_kernel_times", "pt_set_batch_tuning", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch",
+           "pt_sample_only", "pt_dsigma",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
            "pt_dark_yield", "pt_dark_yield_adjoint")
 
@@ -96,6 +97,10 @@ class PtDarkOut(C.Structure):
                 ("yield_", C.c_void_p), ("yield_E", C.c_void_p)]
 
 
+class PtBatchTuning(C.Structure):
+    _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2)]
+
+
 class PetiteGPUError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
@@ -133,6 +138,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_last_run_stats.restype = C.c_int
     lib.pt_last_kernel_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pt_last_kernel_times.restype = C.c_int
+    lib.pt_set_batch_tuning.argtypes = [vp, C.POINTER(PtBatchTuning)]
+    lib.pt_set_batch_tuning.restype = C.c_int
     lib.pt_run_sm.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]
     lib.pt_run_sm.restype = C.c_int
     lib.pt_run_sm_noalloc.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]

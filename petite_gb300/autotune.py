@@ -1,0 +1,102 @@
+"""Autotuner for the batched engine's work distribution.
+
+Picks, for one GPU, target and precision, the settings of
+``pt_set_batch_tuning`` -- idle lanes gathered before a refill and pool
+entries claimed per atomic, for the propagation and the sampler kernel --
+by timing short calibration transports (CUDA events on the run's stream,
+``pt_last_kernel_times``) over a small grid, one coordinate at a time.
+Results are cached in ``$XDG_CACHE_HOME/petite_gb300/tuning.json`` (or
+``~/.cache/...``) keyed by device name, target and precision.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+
+import numpy as np
+
+GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128)}
+DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64)}
+
+
+def _cache_path():
+    base = os.environ.get("XDG_CACHE_HOME") or os.path.join(os.path.expanduser("~"), ".cache")
+    return os.path.join(base, "petite_gb300", "tuning.json")
+
+
+def _calibration_primaries(n, seed):
+    rng = np.random.default_rng(seed)
+    pid = np.array([11, -11, 22])[rng.integers(0, 3, n)].astype(np.int32)
+    E = 10 ** rng.uniform(-1.0, 2.0, n)
+    m = np.where(np.abs(pid) == 11, 0.000511, 0.0)
+    return np.c_[E, np.zeros(n), np.zeros(n), np.sqrt(E * E - m * m)], pid, m
+
+
+def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
+                   verbose=False):
+    """Tunes ``shower``'s engine and returns the chosen settings
+    ``{"refill_min": [p, s], "chunk": [p, s], "seconds": t}``."""
+    import torch
+    eng = shower._engine
+    key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}"
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        best = cache[key]
+        eng.set_tuning(best["refill_min"], best["chunk"])
+        return best
+
+    p0, pid, m = _calibration_primaries(n, seed)
+    dev = eng.device
+    P0 = torch.as_tensor(np.ascontiguousarray(p0.T), device=dev)
+    R0 = torch.zeros((3, n), dtype=torch.float64, device=dev)
+    PID = torch.as_tensor(pid, device=dev)
+    M = torch.as_tensor(m, device=dev)
+    tally = eng.new_tally(n, 1.0)
+
+    def run(cfg):
+        eng.set_tuning(cfg["refill_min"], cfg["chunk"])
+        opts = shower._opts(True, precision)
+        tally.zero_()
+        eng.run_batch(None, None, None, None, opts, tally, queue_capacity=ring_capacity,
+                      device_inputs=(P0, R0, PID, M))
+        tp, ts = eng.last_kernel_times()
+        return tp + ts
+
+    cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"])}
+    run(cfg)                                            # warm-up (scratch, caches)
+    best_t = run(cfg)
+    for name, values in GRID.items():
+        for v in values:
+            trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"])}
+            if name == "refill_min":
+                trial["refill_min"] = [v, v]
+            elif name == "chunk_propagate":
+                trial["chunk"][0] = v
+            else:
+                trial["chunk"][1] = v
+            if trial == cfg:
+                continue
+            t = run(trial)
+            if verbose:
+                print("autotune", trial, round(t, 4))
+            if t < best_t * 0.99:                       # a change must beat noise
+                best_t, cfg = t, trial
+    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "seconds": best_t}
+    eng.set_tuning(best["refill_min"], best["chunk"])
+    if use_cache:
+        cache[key] = best
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            with open(path, "w") as f:
+                json.dump(cache, f, indent=1)
+        except OSError:
+            pass
+    return best

@@ -21,7 +21,6 @@
 // as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
 // builds directions in float32 and keeps energies in float64.
 #include <cstdio>
-#include <cstdlib>
 #include <type_traits>
 
 #include "pt_internal.cuh"
@@ -32,11 +31,13 @@ using namespace pt;
 namespace {
 
 constexpr int kThreads = 128;
-// Idle lanes a warp gathers before refilling them (1 = refill at once); 8
-// measured best for both kernels on the 10^6-primary lead workload
-// (sweep of 1-24 with PETITE_REFILL_MIN).
+// Defaults of the runtime tuning (pt_set_batch_tuning): idle lanes a warp
+// gathers before refilling them (1 = refill at once), and work entries a
+// warp claims from the wave's pool per atomic.
 constexpr int kRefillMinPropagate = 8;
 constexpr int kRefillMinSample = 8;
+constexpr int kChunkPropagate = 128;
+constexpr int kChunkSample = 64;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kHB = PT_HIST_BINS;
@@ -81,6 +82,7 @@ template <int PREC> struct WaveCtx {
   double* err_info;
   Tally tally;
   int refill_min[2];                  // idle lanes a warp gathers before refilling: [0] propagation, [1] sampler
+  int chunk[2];                       // pool entries a warp claims per atomic: [0] propagation, [1] sampler
   PhiloxRK rk;                        // round keys of `seed` (float32 kernels)
 };
 
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
   for (;;) {
     __syncwarp();
     const bool need = !active;
-    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, 128);
+    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, c.chunk[0]);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool finish = false;
@@ -578,7 +580,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
     // loads and set-up run for several lanes at once
     const unsigned idle = __ballot_sync(kFull, !active);
     const bool need = !active && (__popc(idle) >= c.refill_min[0] || idle == kFull);
-    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, 128);
+    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, c.chunk[0]);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool fin = false;
@@ -935,7 +937,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
     __syncwarp();
     const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
     const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
-    const int64_t t = pool_take(pool, c.ctr + 1, total, need, 64);
+    const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
     const bool fresh = need && t >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     if (fresh) {
@@ -1185,15 +1187,11 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.tally = {tally->counts, tally->energy, tally->hist, tally->primary_count, tally->primary_edep,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
   c.rk = philox_round_keys(o->seed);
-  c.refill_min[0] = kRefillMinPropagate;
-  c.refill_min[1] = kRefillMinSample;
-  if (const char* e = getenv("PETITE_REFILL_MIN")) {   // tuning sweeps: "prop,sample"
-    int a = 0, b = 0;
-    if (sscanf(e, "%d,%d", &a, &b) == 2 && a >= 1 && a <= 32 && b >= 1 && b <= 32) {
-      c.refill_min[0] = a;
-      c.refill_min[1] = b;
-    }
-  }
+  const int32_t* tu = hp.tuning;      // 0 = default
+  c.refill_min[0] = tu[0] ? tu[0] : kRefillMinPropagate;
+  c.refill_min[1] = tu[1] ? tu[1] : kRefillMinSample;
+  c.chunk[0] = tu[2] ? tu[2] : kChunkPropagate;
+  c.chunk[1] = tu[3] ? tu[3] : kChunkSample;
   const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate_fp64;
   const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);

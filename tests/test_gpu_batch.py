@@ -86,3 +86,27 @@ def test_batch_no_sample_reports():
     p0, pid, m = primaries(4, species=(22,))
     with pytest.raises(Exception, match="No Sample Found"):
         run_batch(sh, p0, pid, m, "mixed")
+
+
+def test_work_distribution_does_not_change_results(lead):
+    """pt_set_batch_tuning changes only how warps share the work."""
+    p0, pid, m = primaries(400, seed=5)
+    eng = lead._engine
+    a = run_batch(lead, p0, pid, m, "mixed")
+    eng.set_tuning((1, 16), (32, 256))
+    b = run_batch(lead, p0, pid, m, "mixed")
+    eng.set_tuning((0, 0), (0, 0))
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    assert np.array_equal(a.hist.cpu().numpy(), b.hist.cpu().numpy())
+    with pytest.raises(Exception):
+        eng.set_tuning((0, 0), (16, 0))          # a pool chunk below one warp
+
+
+def test_autotune_picks_valid_settings(lead):
+    from petite_gb300.autotune import GRID, autotune_batch
+    best = autotune_batch(lead, n=2000, ring_capacity=1 << 18, use_cache=False)
+    assert best["refill_min"][0] in (8,) + GRID["refill_min"]
+    assert best["chunk"][0] in (128,) + GRID["chunk_propagate"]
+    assert best["chunk"][1] in (64,) + GRID["chunk_sample"]
+    assert best["seconds"] > 0
+    lead._engine.set_tuning((0, 0), (0, 0))
