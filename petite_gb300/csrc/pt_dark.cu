@@ -96,6 +96,9 @@ __device__ bool draw_dark(const pt_dark_maps& M, int block, int p, double E, dou
   const int neval = (int)M.map_neval[r];
   const int d = dark_dim(p);
   proposals = 0;
+  const bool brem = (p == PT_DARKBREM || p == PT_DARKMUONBREM);
+  const double mlep = p == PT_DARKMUONBREM ? kMmu : kMe;
+  const float tconv = brem ? (float)dark_brem_tconv(E, M.A, mlep) : 0.f;
   for (int64_t used = 0; used < max_n_integrators; ++used) {
     for (int j = 0; j < neval; ++j) {
       double jac = 1.0;
@@ -105,8 +108,19 @@ __device__ bool draw_dark(const pt_dark_maps& M, int block, int p, double E, dou
       }
       const double wgt = jac / neval;
       ++proposals;
+      const double u = rng.u();
+      // Screen: a sample clearly outside the allowed region is rejected; where
+      // the float32 estimate is trustworthy and the proposal is rejected even
+      // at four times that estimate, the float64 value (within a few per
+      // mille of it) cannot be accepted either.  Otherwise float64 decides.
+      float f32;
+      if (brem) {
+        const int sc = dark_brem_screen32(x, E, mV, M.A, mlep, M.Z, M.A, tconv, f32);
+        if (sc == kScreenOutside) continue;                          // integrand 0: rejected
+        if (sc == kScreenValue && maxF * u > 4.0 * wgt * (double)f32) continue;
+      }
       const double f = dark_dsigma<double>(M, p, x, E, mV);
-      if (maxF * rng.u() < wgt * f) return true;
+      if (maxF * u < wgt * f) return true;
     }
   }
   return false;

@@ -211,6 +211,105 @@ __device__ T dsig_dark_brem_anchored(const double* xv, double E, T mV, double a,
   return dark_brem_core<T>(x, omc, tt, E, mV, MT, m, Z, A, L) * jac;
 }
 
+// A float32 estimate of the dark-bremsstrahlung integrand, used only to
+// screen accept/reject decisions: it returns false whenever the estimate
+// cannot be trusted -- within 0.1-0.2 % of a kinematic edge (k = 0, t-/t+,
+// |cos theta_q| = 1, discriminant 0) or where a sum of terms cancels to less
+// than 1e-3 .. 1e-2 of their magnitudes.  Otherwise its relative error is far
+// below the factor the screen allows.  The forms avoid the cancellations of
+// the reference's expressions: p - k = (p^2 - k^2)/(p + k),
+// x E^2 - k p = (E^2 (x^2 m^2 + mV^2) - m^2 mV^2)/(x E^2 + k p),
+// V^2 - ((1-x)E)^2 = (p - k - (1-x)E)(p - k + (1-x)E) + 2 k p (1 - cos theta),
+// and the limits of dark_brem_limits_stable.
+enum { kScreenUnsure = 0, kScreenValue = 1, kScreenOutside = 2 };
+__device__ __forceinline__ int dark_brem_screen32(const double* xv, double E_, double mV_, double MT_, double m_,
+                                                  double Z_, double A_, float tconv, float& out) {
+  const float x = (float)xv[0], E = (float)E_, mV = (float)mV_, MT = (float)MT_, m = (float)m_;
+  const float omc = exp10f((float)xv[1]);
+  const float tt = exp10f((float)xv[2]);
+  const float xE = x * E;
+  if (xE < mV * 0.999f) return kScreenOutside;                      // x E >= mV fails
+  if (!(xE > mV * 1.001f) || !(x < 1.f)) return kScreenUnsure;
+  const float k = sqrtf((xE - mV) * (xE + mV));
+  const float p = sqrtf((E - m) * (E + m));
+  const float kp = k * p;
+  const float pmk = ((1.f - x) * (1.f + x) * E * E - m * m + mV * mV) / (p + k);
+  const float V2 = pmk * pmk + 2.f * kp * omc;
+  const float V = sqrtf(V2);
+  const float D = (E * E * (x * x * m * m + mV * mV) - m * m * mV * mV) / (x * E * E + kp);
+  const float ut = mV * mV - 2.f * D - 2.f * kp * omc;
+  const float Er = (1.f - x) * E + MT;
+  const float d1 = ut * ut, d2 = 4.f * MT * ut * Er, d3 = 4.f * MT * MT * V2;
+  const float discr = d1 + d2 + d3;
+  const float dscale = fabsf(d1) + fabsf(d2) + d3;
+  if (discr < -1e-3f * dscale) return kScreenOutside;                // discriminant < 0
+  if (!(discr > 1e-3f * dscale)) return kScreenUnsure;
+  const float Aq = V * (ut + 2.f * MT * Er), Bq = Er * sqrtf(discr);
+  if (!(Aq > 0.f)) return kScreenUnsure;
+  const float den = 2.f * (Er * Er - V2);
+  const float Qp = fabsf((Aq + Bq) / den);
+  const float Qm = fabsf(ut * (ut + 4.f * MT * Er) / (2.f * (Aq + Bq)));
+  const float tp = 2.f * MT * Qp * Qp / (sqrtf(MT * MT + Qp * Qp) + MT);
+  const float tm = 2.f * MT * Qm * Qm / (sqrtf(MT * MT + Qm * Qm) + MT);
+  const float t = tt * tconv;
+  if (tp > tm * 1.01f && (t < tm * 0.998f || t > tp * 1.002f)) return kScreenOutside;   // outside (t-, t+)
+  if (!(t > tm * 1.002f && t < tp * 0.998f)) return kScreenUnsure;
+  const float q0 = -t / (2.f * MT);
+  const float q = sqrtf(t * t / (4.f * MT * MT) + t);
+  const float a = (1.f - x) * E;
+  const float dk = -m * m / (p + E) + mV * mV / (k + xE);           // p - k - (1-x)E
+  const float n1 = dk * (pmk + a), n2 = 2.f * kp * omc, n3 = t * (1.f + a / MT), n4 = m * m;
+  const float num = n1 + n2 + n3 + n4;
+  if (!(fabsf(num) > 1e-3f * (fabsf(n1) + n2 + n3 + n4))) return kScreenUnsure;
+  const float cq = -num / (2.f * V * q);
+  if (fabsf(cq) > 1.001f) return kScreenOutside;                    // |cos theta_q| <= 1 fails
+  if (!(fabsf(cq) < 0.999f)) return kScreenUnsure;
+  const float y1 = -t + 2.f * q0 * E;
+  const float y2 = -2.f * q * p * (pmk + k * omc) * cq / V;
+  const float Y = y1 + y2;
+  if (!(fabsf(Y) > 1e-2f * (fabsf(y1) + fabsf(y2)))) return kScreenUnsure;
+  const float w2 = 4.f * q * q * p * p * k * k * (omc * (2.f - omc)) * ((1.f - cq) * (1.f + cq)) / V2;
+  const float Wr = Y * Y - w2;
+  if (!(fabsf(Wr) > 1e-2f * Y * Y)) return kScreenUnsure;
+  const float W = fabsf(Wr);
+  const float mm = mV * mV + 2.f * m * m;
+  const float Am2 = -8.f * MT * (4.f * E * E * MT - t * (2.f * E + MT)) * mm;
+  const float A1 = 8.f * MT * MT / ut;
+  const float i1 = 2.f * t * ut, i2 = ut * ut, i3 = 4.f * E * E * (2.f * (x - 1.f) * mm - t * ((x - 2.f) * x + 2.f)),
+              i4 = 2.f * t * (-mV * mV + 2.f * m * m + t);
+  const float inner = i1 + i2 + i3 + i4;
+  if (!(fabsf(inner) > 1e-3f * (fabsf(i1) + fabsf(i2) + fabsf(i3) + fabsf(i4)))) return kScreenUnsure;
+  const float b1 = MT * MT * inner, b2 = -2.f * E * MT * t * ((1.f - x) * ut + (x - 2.f) * (mm + t)),
+              b3 = t * t * (ut - mV * mV);
+  const float bs = b1 + b2 + b3;
+  if (!(fabsf(bs) > 1e-3f * (fabsf(b1) + fabsf(b2) + fabsf(b3)))) return kScreenUnsure;
+  const float Am1 = (8.f / ut) * bs;
+  const float c1 = MT * MT * (2.f * t * ut + (t - 4.f * E * E * (x - 1.f) * (x - 1.f)) * mm),
+              c2 = 2.f * E * MT * t * (ut - (x - 1.f) * mm);
+  const float cs = c1 + c2;
+  if (!(fabsf(cs) > 1e-3f * (fabsf(c1) + fabsf(c2)))) return kScreenUnsure;
+  const float A0 = (8.f / (ut * ut)) * cs;
+  const float sw = sqrtf(W);
+  const float P0 = A0, P1 = Y * A1, P2 = Am1 / sw, P3 = Y * Am2 / (W * sw);
+  const float ps = P0 + P1 + P2 + P3;
+  if (!(fabsf(ps) > 1e-2f * (fabsf(P0) + fabsf(P1) + fabsf(P2) + fabsf(P3)))) return kScreenUnsure;
+  const float phi = ps / (8.f * MT * MT);
+  // Gelastic_inelastic_over_tsquared in float32 (all_processes.py:112-133)
+  const float Z = (float)Z_, A = (float)A_;
+  const float cc1 = 111.f * powf(Z, -1.f / 3.f) / (float)kMe, cs1 = cc1 * cc1;
+  const float cc2 = 0.164f * powf(A, -2.f / 3.f);
+  const float g1 = 1.f / (1.f + cs1 * t), g2 = 1.f / (1.f + t / cc2);
+  const float ap = 773.f * powf(Z, -2.f / 3.f) / (float)kMe, ap2 = ap * ap;
+  const float g3 = ap2 / (1.f + ap2 * t), g4 = 1.f + t / 0.71f;
+  const float Ginel = Z / (cs1 * cs1 * Z * Z) * (g3 * g3) *
+                      ((1.f + (2.79f * 2.79f - 1.f) * t / (4.f * (float)(kMproton * kMproton))) / (g4 * g4 * g4 * g4));
+  const float ff = Z * Z * cs1 * cs1 * (g1 * g1 * g2 * g2 + Ginel);
+  const float al = (float)kAlpha;
+  const float ans = ff * (al * al * al) * k * E * phi / (p * V);
+  out = ans * tconv * (omc * tt * (float)(kLn10 * kLn10));
+  return (out > 0.f && out < 3.0e38f) ? kScreenValue : kScreenUnsure;
+}
+
 // ----------------------------------------------------------- dark Compton
 // dsigma_compton_dCT.__call__ with mV > 0 (all_processes.py:639-742)
 template <class T>
