@@ -466,10 +466,12 @@ class DarkOracle:
     """GetBSMWeights, draw_dark_sample and produce_bsm_particle on one SM
     particle record (fields of :class:`oracle.shower.Rec`)."""
 
-    def __init__(self, dark: DarkTables, sm_tables, seed, max_n_integrators=10000, rescale=1.0):
+    def __init__(self, dark: DarkTables, sm_tables, seed, max_n_integrators=10000, rescale=1.0,
+                 fast_MCS_mode=True):
         self.d, self.sm, self.seed = dark, sm_tables, seed
         self.max_n_integrators = max_n_integrators
         self.rescale = rescale
+        self.fast_mcs = fast_MCS_mode              # dark_shower.py:134-138
 
     # dark_shower.py:595-647 (bound-electron form)
     def weight(self, pid, E, process):
@@ -547,7 +549,9 @@ class DarkOracle:
             E_int = en[idx] + (E0 - Ei_all[j])
             dist = (r.p0[0] - E_int) / (d.dEdx * 0.1)
             ps = tuple(r.p0)
-            if P.norm3(ps[1], ps[2], ps[3]) > 0:
+            if P.norm3(ps[1], ps[2], ps[3]) > 0 and not self.fast_mcs:
+                ps = P.scattered_momentum_bethe(ps, d.rho * (dist / P.cmtom), d.A, d.Z, self.rescale, s.next)
+            elif P.norm3(ps[1], ps[2], ps[3]) > 0:
                 u1, u2, u3, u4 = s.next(), s.next(), s.next(), s.next()
                 ps = P.scattered_momentum_fast(ps, d.rho * (dist / P.cmtom), d.A, d.Z, self.rescale,
                                                P.m_electron, u1, u2, u3, u4)

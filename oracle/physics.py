@@ -462,27 +462,14 @@ def rotation_to_z(vx, vy, vz):
             (-sb * ca, sb * sa, cb))
 
 
-def scattered_momentum_fast(p4, t, A, Z, rescale, m_lepton, u_sign, u_ang, u_rad, u_phi):
-    """get_scattered_momentum_fast, moliere.py:350-400, with its four draws:
-    sign (random.choice), the Gaussian pair (random.gauss twice; Box-Muller
-    from an angle uniform and a radius uniform), and phi (random.uniform).
-    """
+def _scatter_to_lab(p4, pn, theta, phi):
+    """The rotation of moliere.py:384-398 (and :427-445): the scattered
+    direction (theta, phi) about z, taken to the lab by the transpose of
+    get_rotation_matrix."""
     E, px, py, pz = p4
-    pn = norm3(px, py, pz)
-    if not pn > 0:
-        return tuple(p4)
-    beta = pn / E
-    th0 = theta0_lynch_dahl(t, beta, A, Z, m_lepton)
-    sign = -1.0 if u_sign < 0.5 else 1.0
-    r = math.sqrt(-2.0 * math.log(1.0 - u_rad))
-    ang = 2.0 * PI * u_ang
-    g1 = th0 * (r * math.cos(ang))
-    g2 = th0 * (r * math.sin(ang))
-    theta = sign * math.sqrt(g1 ** 2 + g2 ** 2) * rescale
-    phi = 2. * PI * u_phi
     cth, sth = math.cos(theta), math.sin(theta)
     cph, sph = math.cos(phi), math.sin(phi)
-    # Rphi @ Rtheta @ z_hat = (-sph*(-sth)... ) : Rtheta z = (0,-sth,cth); Rphi (0,-sth,cth) = (sph*sth, -cph*sth, cth)
+    # Rphi @ Rtheta @ z_hat: Rtheta z = (0,-sth,cth); Rphi (0,-sth,cth) = (sph*sth, -cph*sth, cth)
     n = (pn * (sph * sth), pn * (-cph * sth), pn * cth)
     R = rotation_to_z(px, py, pz)
     # lab = R^T n
@@ -490,6 +477,249 @@ def scattered_momentum_fast(p4, t, A, Z, rescale, m_lepton, u_sign, u_ang, u_rad
     ly = R[0][1] * n[0] + R[1][1] * n[1] + R[2][1] * n[2]
     lz = R[0][2] * n[0] + R[1][2] * n[1] + R[2][2] * n[2]
     return (E, lx, ly, lz)
+
+
+def _lynch_dahl_theta(t, beta, A, Z, m_lepton, u_sign, u_ang, u_rad):
+    """generate_moliere_angle_simplified_alt, moliere.py:265-284, on its
+    draws: sign (random.choice), the Gaussian pair (random.gauss twice;
+    Box-Muller from an angle uniform and a radius uniform)."""
+    th0 = theta0_lynch_dahl(t, beta, A, Z, m_lepton)
+    sign = -1.0 if u_sign < 0.5 else 1.0
+    r = math.sqrt(-2.0 * math.log(1.0 - u_rad))
+    ang = 2.0 * PI * u_ang
+    g1 = th0 * (r * math.cos(ang))
+    g2 = th0 * (r * math.sin(ang))
+    return sign * math.sqrt(g1 ** 2 + g2 ** 2)
+
+
+def scattered_momentum_fast(p4, t, A, Z, rescale, m_lepton, u_sign, u_ang, u_rad, u_phi):
+    """get_scattered_momentum_fast, moliere.py:350-400, with its four draws:
+    sign, the Gaussian pair (angle, radius), and phi (random.uniform).
+    """
+    E, px, py, pz = p4
+    pn = norm3(px, py, pz)
+    if not pn > 0:
+        return tuple(p4)
+    beta = pn / E
+    theta = _lynch_dahl_theta(t, beta, A, Z, m_lepton, u_sign, u_ang, u_rad) * rescale
+    phi = 2. * PI * u_phi
+    return _scatter_to_lab(p4, pn, theta, phi)
+
+
+# ------------------------------------ Bethe-Moliere multiple scattering
+# moliere.py:33-174,221-247,403-453 (fast_MCS_mode=False).  The reference's
+# inverse CDF integrates the Moliere density with scipy.integrate.quad inside
+# a Ridder root search; here the integral is in closed form:
+#   F(x, B) = (1 - e^-x)(1 + 1/B) - x e^-x g(x) / B,  g(x) = Ei(x) - ln x,
+# from f1 = -2 d/dx[x e^-x g(x)] + 2 e^-x (g' = (e^x - 1)/x), which also
+# shows that f1 integrates to 0.  With h(x) = x e^-x g(x) - 1 the tail is
+#   Q(x) = 1 - F(x, B) = e^-x (1 + 1/B) + h(x) / B.
+EULER_GAMMA = 0.57721566490153286061
+
+
+def moliere_h(x, series_below=40.0, eps=1e-17):
+    """x e^-x (Ei(x) - ln x) - 1.  Below ``series_below``: the power series
+    g(x) = gamma + sum_k x^k / (k k!) (all terms positive); above it the
+    asymptotic series x e^-x Ei(x) ~ sum_k k! / x^k, stopped at its smallest
+    term (k ~ x), whose size sqrt(2 pi x) e^-x is below 3e-15 of h there."""
+    if x < series_below:
+        term, s, k = 1.0, 0.0, 1
+        while True:
+            term *= x / k
+            d = term / k
+            s += d
+            if d <= eps * s or k >= 400:
+                break
+            k += 1
+        return x * math.exp(-x) * (EULER_GAMMA + s) - 1.0
+    term, s, k = 1.0, 0.0, 1
+    while True:
+        nxt = term * (k / x)
+        if nxt >= term:
+            break
+        term = nxt
+        s += term
+        if term <= eps * s:
+            break
+        k += 1
+    return s - x * math.exp(-x) * math.log(x)
+
+
+def moliere_tail(x, B):
+    """1 - moliere_cdf(x, B) in closed form (moliere.py:62-81 without quad)."""
+    return math.exp(-x) * (1.0 + 1.0 / B) + moliere_h(x) / B
+
+
+def moliere_density(x, B):
+    """moliere_f(x, B) = (f0 + f1/B)/2 (moliere.py:33-59) in terms of h:
+    f1 = 2((x-1) h - 1)/x + 4 e^-x."""
+    e = math.exp(-x)
+    f1 = 2.0 * ((x - 1.0) * moliere_h(x) - 1.0) / x + 4.0 * e
+    return e + 0.5 * f1 / B
+
+
+def moliere_f1_at_zero():
+    """moliere_f1(0): the reference evaluates x <= 1e-6 at x = 1e-6 (moliere.py:45-50)."""
+    x = 1e-6
+    g = (moliere_h(x) + 1.0) / (x * math.exp(-x))
+    return 2. * math.exp(-x) * (x - 1.) * g - 2. * (1. - 2. * math.exp(-x))
+
+
+def moliere_cdf_pieces(x, B, f00):
+    """moliere_cdf, moliere.py:62-81: f(0,B) x below 0.01, the integral (here
+    closed form) up to 100, a three-term asymptote above."""
+    if x > 100:
+        return 1.0 - (1.0 / B / x + 2.0 / B / x ** 2 + 6.0 / B / x ** 3)
+    if x < 0.01:
+        return f00 * x
+    return 1.0 - moliere_tail(x, B)
+
+
+def ridders_root(f, a, b, xtol=2e-12, rtol=4 * 2.220446049250313e-16, max_iter=100):
+    """Ridders' method (C. Ridders, IEEE Trans. Circuits Syst. 26 (1979) 979):
+    the bracket's midpoint m, then the root of the exponentially scaled line
+    through the three points, x = m - sign(f(b) - f(a)) (b - a)/2 f(m) /
+    sqrt(f(m)^2 - f(a) f(b)); the sub-bracket with a sign change is kept.  The
+    stopping rule |b - a| < xtol + rtol x is scipy's default for
+    root_scalar(method='ridder')."""
+    fa, fb = f(a), f(b)
+    if fa == 0:
+        return a
+    if fb == 0:
+        return b
+    x = a
+    for _ in range(max_iter):
+        dm = 0.5 * (b - a)
+        m = a + dm
+        fm = f(m)
+        x = m - math.copysign(1.0, fb - fa) * dm * fm / math.sqrt(fm * fm - fa * fb)
+        fx = f(x)
+        if fx * fm < 0:
+            a, fa, b, fb = x, fx, m, fm
+        elif fx * fa < 0:
+            b, fb = x, fx
+        else:
+            a, fa = x, fx
+        if fx == 0 or abs(b - a) < xtol + rtol * x:
+            break
+    return x
+
+
+def moliere_x(u, B, tol=1e-10, max_iter=60):
+    """inverse_moliere_cdf, moliere.py:84-120.  The explicit branches are the
+    reference's.  Otherwise the root of the reference's piecewise CDF
+    (moliere_cdf_pieces): the integral piece is solved by Newton steps on the
+    closed-form tail, kept inside a bracket (bisection when a step leaves
+    it); a root below 0.01 or above 100 falls on the other pieces.  At x =
+    0.01 the pieces step down by ~5e-5; for u inside that step there are two
+    roots about 1 % apart, and the reference's choice is reproduced by its
+    own search: the bracket expansion of moliere.py:102-115 from [0.5, 2],
+    then Ridders' method."""
+    if 1 - u < 1 / B / 100:
+        return 1 / (1 - u) / B
+    if u < 0.01:
+        return u
+    f00 = 0.5 * (2. * math.exp(-0.) + moliere_f1_at_zero() / B)
+    if 1.0 - moliere_tail(0.01, B) < u < f00 * 0.01:
+        f = lambda xx: moliere_cdf_pieces(xx, B, f00) - u
+        a, b, it = 0.5, 2.0, 0
+        while f(a) * f(b) > 0 and it <= 20:
+            if f(b) < 0:
+                b *= 2
+            if f(a) > 0:
+                a *= 0.5
+            it += 1
+        return ridders_root(f, a, b)
+    q = 1.0 - u
+    lo, hi = 0.0, 200.0
+    x = max(math.log((1.0 + 1.0 / B) / q), 1.0 / (B * q))
+    if not lo < x < hi:
+        x = 0.5 * (lo + hi)
+    for _ in range(max_iter):
+        Q = moliere_tail(x, B)
+        if Q > q:
+            lo = x
+        else:
+            hi = x
+        xn = x + (Q - q) / moliere_density(x, B)
+        if not lo < xn < hi:
+            xn = 0.5 * (lo + hi)
+        done = abs(xn - x) <= tol * xn
+        x = xn
+        if done:
+            break
+    if x < 0.01:
+        return u / f00
+    if x > 100.0:
+        # 1 - (1/B/x + 2/B/x**2 + 6/B/x**3) = u, in y = 1/x; below x = 100
+        # the pieces step up past u and the reference's search ends at 100
+        c = B * q
+        y = c
+        for _ in range(max_iter):
+            yn = y - (y + 2.0 * y * y + 6.0 * y * y * y - c) / (1.0 + 4.0 * y + 18.0 * y * y)
+            done = abs(yn - y) <= 1e-15 * yn
+            y = yn
+            if done:
+                break
+        return max(1.0 / y, 100.0)
+    return x
+
+
+def moliere_b(t, beta, A, Z, z=1.):
+    """get_b, moliere.py:139-155 (Bethe 1953 eq. 22)."""
+    alpha = z * Z * alpha_em / beta
+    expb = 6700. * t * (Z + 1.) * Z ** (1. / 3.) * z ** 2. / (beta * beta * A * (1. + 3.34 * alpha ** 2))
+    return math.log(expb)
+
+
+def moliere_B(b):
+    """get_capital_B, moliere.py:157-174: B = b + ln B by fixed-point steps
+    from b + ln b, stopped at |B - (b + ln B)| <= 1e-3."""
+    B = b + math.log(b)
+    B = b + math.log(B)
+    while abs(B - (b + math.log(B))) > 1e-3:
+        B = b + math.log(B)
+    return B
+
+
+n_avogadro = 6.0221409e+23                      # physical_constants.py:24
+
+
+def chic2_bethe(t, beta, A, Z, z=1.):
+    """get_chic_squared, moliere.py:180-192 (Bethe 1953 eq. 10); its momentum
+    uses the electron mass for every lepton."""
+    me_in_inv_cm = m_electron / hbarc
+    p = me_in_inv_cm * beta / math.sqrt(1. - beta * beta)
+    return 4. * PI * n_avogadro * alpha_em ** 2 * t * Z * (Z + 1.) * z ** 2 / (A * (p * p) * (beta * beta))
+
+
+def scattered_momentum_bethe(p4, t, A, Z, rescale, draw):
+    """get_scattered_momentum_Bethe, moliere.py:403-453, with
+    generate_moliere_angle (moliere.py:221-247).  ``draw()`` returns the next
+    uniform.  b < 2: the Lynch-Dahl angle with its default (electron) mass,
+    four draws with phi.  Otherwise three: the inverse-CDF uniform
+    (random.random in generate_moliere_x), the sign (random.choice) and phi.
+    The reference passes m_lepton on to get_chic_squared (moliere.py:244),
+    which does not take it (a TypeError); the momentum there is the electron's
+    as that function defines it."""
+    E, px, py, pz = p4
+    pn = norm3(px, py, pz)
+    if not pn > 0:
+        return tuple(p4)
+    beta = pn / E
+    b = moliere_b(t, beta, A, Z)
+    if b < 2:
+        u_sign, u_ang, u_rad = draw(), draw(), draw()
+        theta = _lynch_dahl_theta(t, beta, A, Z, m_electron, u_sign, u_ang, u_rad)
+    else:
+        B = moliere_B(b)
+        x = moliere_x(draw(), B)
+        chic2 = chic2_bethe(t, beta, A, Z)
+        sign = -1 if draw() < 0.5 else 1
+        theta = sign * math.sqrt(x * chic2 * B)
+    theta = theta * rescale
+    phi = 2. * PI * draw()
+    return _scatter_to_lab(p4, pn, theta, phi)
 
 
 def rotation_matrix_from(pf):

@@ -160,8 +160,9 @@ def invariant_mass(p):
 
 class OracleShower:
     def __init__(self, tables: OracleTables, min_energy: float, seed: int = 0,
-                 max_n_integrators: int = 10000, rescale_MCS: float = 1.0):
+                 max_n_integrators: int = 10000, rescale_MCS: float = 1.0, fast_MCS_mode: bool = True):
         self.t = tables
+        self.fast_mcs = fast_MCS_mode              # shower.py:147-151
         self.min_energy = min_energy
         self.seed = seed
         self.max_n_integrators = max_n_integrators
@@ -191,6 +192,8 @@ class OracleShower:
         E, px, py, pz = pf
         if not P.norm3(px, py, pz) > 0:
             return pf
+        if not self.fast_mcs:
+            return P.scattered_momentum_bethe(pf, t, self.t.A, self.t.Z, self.rescale, s.next)
         u1, u2, u3, u4 = s.next(), s.next(), s.next(), s.next()
         return P.scattered_momentum_fast(pf, t, self.t.A, self.t.Z, self.rescale, m_lepton, u1, u2, u3, u4)
 

@@ -19,7 +19,7 @@ The particle being processed is tracked by wrapping the Shower instance's
 ``propagate_particle`` and ``sample_scattering``; daughters get the keys of
 ``oracle.philox.daughter_key``.
 
-Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|all]
+Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|moliere|all]
 (DICT_DIR from rebuild_maps.py; for ``dark`` it must also hold the output of
 ``rebuild_maps.py --dark``)
 """
@@ -495,6 +495,121 @@ def gen_dark(dict_dir, out_path):
     print("dark golden written", out_path)
 
 
+def install_bethe(router):
+    """fast_MCS_mode=False draws its inverse-CDF uniform with random.random
+    (moliere.py:132).  The reference's generate_moliere_angle passes
+    m_lepton to get_chic_squared (moliere.py:244), which has no such
+    parameter, so every call with b >= 2 raises TypeError; the wrapper drops
+    the keyword (the function's momentum is the electron's by definition).
+    Nothing else is changed."""
+    from PETITE import moliere
+    saved = dict(rrandom=random.random, chic=moliere.get_chic_squared)
+    orig = moliere.get_chic_squared
+
+    def chic(t, beta, A, Z, z, m_lepton=None):
+        return orig(t, beta, A, Z, z)
+
+    random.random = router.u
+    moliere.get_chic_squared = chic
+    return saved
+
+
+def uninstall_bethe(saved):
+    from PETITE import moliere
+    random.random = saved["rrandom"]
+    moliere.get_chic_squared = saved["chic"]
+
+
+def gen_moliere(dict_dir, out_path):
+    """Bethe-Moliere multiple scattering (fast_MCS_mode=False): its pieces,
+    the routed get_scattered_momentum_Bethe, and showers in that mode."""
+    refimport.setup()
+    from PETITE import moliere
+    from PETITE.shower import Shower
+    from PETITE.particle import Particle
+    rng = np.random.default_rng(777)
+    out = {}
+    targets = {"graphite": (6, 12), "lead": (82, 207), "iron": (26, 56)}
+    # b, B and chi_c^2 over thickness and velocity
+    rows = []
+    for tname, (Z, A) in targets.items():
+        for t in np.logspace(-4, 1.5, 12):
+            for beta in (0.3, 0.8, 0.99, 0.99999, 1 - 1e-9):
+                b = moliere.get_b(t, beta, A, Z, 1.)
+                B = moliere.get_capital_B(t, beta, A, Z, 1.) if b >= 2 else np.nan
+                chic2 = moliere.get_chic_squared(t, beta, A, Z, 1.)
+                rows.append([Z, A, t, beta, b, B, chic2])
+    out["params/rows"] = np.array(rows)
+    # inverse CDF: uniform u, the far tail, both explicit branches and the
+    # step of the piecewise CDF at x = 0.01
+    rows = []
+    for B in (3.15, 3.6, 4.5, 6.0, 8.0, 11.0, 15.0, 20.0):
+        f00 = moliere.moliere_f(0, B)
+        band = (moliere.moliere_cdf(0.0100000000001, B), 0.01 * f00)
+        us = np.concatenate([rng.uniform(0, 1, 40), 1 - 10 ** rng.uniform(-7, -1, 12),
+                             rng.uniform(0.005, 0.0125, 8), np.linspace(band[0], band[1], 4)[1:-1],
+                             [0.0, 0.5, 1 - 1 / B / 100 * 1.0001]])
+        for u in us:
+            rows.append([B, u, moliere.inverse_moliere_cdf(u, B), float(band[0] < u < band[1])])
+    out["icdf/rows"] = np.array(rows)
+    # get_scattered_momentum_Bethe on fixed streams
+    router = StreamRouter(SEED)
+    saved = install(router)
+    saved_b = install_bethe(router)
+    rows = []
+    try:
+        case = 0
+        for tname, (Z, A) in targets.items():
+            for t in (3e-4, 1e-3, 4e-3, 0.03, 0.3, 3.0):
+                for E, m in ((0.02, 0.000511), (1.0, 0.000511), (30.0, 0.000511), (2.0, 0.1056583755)):
+                    d = rng.normal(size=3)
+                    d /= np.linalg.norm(d)
+                    pn = math.sqrt(E * E - m * m)
+                    p4 = np.array([E, *(pn * d)])
+                    router.set_current(70_000 + case)
+                    outp = moliere.get_scattered_momentum_Bethe(p4, t, A, Z, 1.0, m_lepton=m)
+                    rows.append([E, t, A, Z, m, *p4, *outp, router.cur.n])
+                    case += 1
+    finally:
+        uninstall_bethe(saved_b)
+        uninstall(saved)
+    out["scatter/rows"] = np.array(rows)
+    # showers with fast_MCS_mode=False
+    for name, target, cut, pid, E0, n, mass in BETHE_CASES:
+        t0 = time.time()
+        router = StreamRouter(SEED)
+        shower = Shower(dict_dir, target, cut, fast_MCS_mode=False)
+        wrap_shower(shower, router)
+        saved = install(router)
+        saved_b = install_bethe(router)
+        F, I, K, D = [], [], [], []
+        try:
+            for j in range(n):
+                m = 0.0 if pid == 22 else mass
+                part = Particle([E0, 0.0, 0.0, math.sqrt(E0 * E0 - m * m)], [0.0, 0.0, 0.0], {"PID": pid})
+                part._pkey = primary_key(j)
+                f, i, _, k, d = shower_arrays(shower.generate_shower(part), router, j)
+                F.append(f); I.append(i); K.append(k); D.append(d)
+        finally:
+            uninstall_bethe(saved_b)
+            uninstall(saved)
+        out[f"shower/{name}/f64"] = np.concatenate(F)
+        out[f"shower/{name}/i64"] = np.concatenate(I)
+        out[f"shower/{name}/pkey"] = np.concatenate(K)
+        out[f"shower/{name}/draws"] = np.concatenate(D)
+        out[f"shower/{name}/meta"] = np.array([SEED, pid, n], np.int64)
+        out[f"shower/{name}/params"] = np.array([E0, cut, mass])
+        out[f"shower/{name}/target"] = np.array(target)
+        print(f"bethe {name}: {n} primaries, {sum(len(x) for x in F)} particles, {time.time() - t0:.1f} s")
+    np.savez_compressed(out_path, **out)
+
+
+BETHE_CASES = [
+    ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 6, 0.000511),
+    ("pos3_lead", "lead", 0.010, -11, 3.0, 2, 0.000511),
+    ("mu5_graphite", "graphite", 0.010, 13, 5.0, 2, 0.1056583755),
+]
+
 CASES = [
     # name, target, cut, pid, E0, n primaries, primary mass for the momentum
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 12, 0.000511),
@@ -512,3 +627,5 @@ if __name__ == "__main__":
         gen_showers(d, os.path.join(HERE, "showers.npz"), CASES)
     if which in ("all", "dark"):
         gen_dark(d, os.path.join(HERE, "dark.npz"))
+    if which in ("all", "moliere"):
+        gen_moliere(d, os.path.join(HERE, "moliere.npz"))
