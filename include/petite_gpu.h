@@ -89,6 +89,7 @@ typedef struct pt_tables {
   double a0sq;                    /* a0**2 */
   double Z2a04;                   /* Z**2 * a0**4  (g2_elastic, all_processes.py:99-103) */
   double Z23;                     /* Z**(2/3)      (moliere.py:219) */
+  double Z13;                     /* Z**(1/3)      (moliere.py:152) */
 } pt_tables;
 
 typedef struct pt_handle pt_handle;
@@ -130,6 +131,9 @@ typedef struct pt_opts {
   int32_t precision;             /* 0 = float64 throughout, 1 = float32 sampling + float64 kinematics */
   uint64_t seed;                 /* Philox key */
   int64_t primary_offset;        /* primary i draws from the stream of index primary_offset + i */
+  int32_t mcs_mode;              /* 0 = Shower(fast_MCS_mode=True): Lynch-Dahl Gaussian (moliere.py:350-400);
+                                    1 = fast_MCS_mode=False: Bethe-Moliere (moliere.py:403-453) */
+  int32_t reserved0;             /* 0 */
 } pt_opts;
 
 /* Shower.generate_shower (shower.py:603-708) for n_primaries independent
@@ -225,6 +229,13 @@ pt_status pt_sample_only(pt_handle* h, int32_t process, const double* energy,
  * classes) at n points x[i*4 + d] and energies energy[i]: value[i]. */
 pt_status pt_dsigma(pt_handle* h, int32_t process, const double* x, const double* energy,
                     int64_t n, int32_t precision, double* value, void* stream);
+
+/* inverse_moliere_cdf(u, B) (moliere.py:84-120), the sampler of
+ * fast_MCS_mode=False, for n device pairs: x[i] with Moliere's
+ * x = theta^2 / (chi_c^2 B).  precision 0 = float64 (the engines' form),
+ * 1 = float32 (the mixed engine's).  Needs no handle. */
+pt_status pt_moliere_inverse_cdf(const double* u, const double* B, int64_t n, int32_t precision, double* x,
+                                 void* stream);
 
 /* ------------------------------------------------------------------------
  * Dark-vector production on an SM shower (DarkShower, dark_shower.py).

@@ -637,14 +637,20 @@ def moliere_x(u, B, tol=1e-10, max_iter=60):
         x = 0.5 * (lo + hi)
     for _ in range(max_iter):
         Q = moliere_tail(x, B)
+        if Q == q:
+            break
         if Q > q:
             lo = x
         else:
             hi = x
         xn = x + (Q - q) / moliere_density(x, B)
-        if not lo < xn < hi:
+        if xn == x:                      # the step is below one ulp of x
+            break
+        if lo < xn < hi:                 # a Newton step: the next error is ~ its square
+            done = abs(xn - x) <= tol * xn
+        else:                            # bisection ends only on a closed bracket
             xn = 0.5 * (lo + hi)
-        done = abs(xn - x) <= tol * xn
+            done = hi - lo <= 4.5e-16 * xn
         x = xn
         if done:
             break
@@ -657,7 +663,7 @@ def moliere_x(u, B, tol=1e-10, max_iter=60):
         y = c
         for _ in range(max_iter):
             yn = y - (y + 2.0 * y * y + 6.0 * y * y * y - c) / (1.0 + 4.0 * y + 18.0 * y * y)
-            done = abs(yn - y) <= 1e-15 * yn
+            done = abs(yn - y) <= tol * yn
             y = yn
             if done:
                 break

@@ -19,7 +19,7 @@ PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG =
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
            "pt_last_kernel_times", "pt_set_batch_tuning", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch",
-           "pt_sample_only", "pt_dsigma",
+           "pt_sample_only", "pt_dsigma", "pt_moliere_inverse_cdf",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
            "pt_dark_yield", "pt_dark_yield_adjoint")
 
@@ -42,7 +42,7 @@ class PtTables(C.Structure):
         ("Eg_min", C.c_double), ("Ee_min", C.c_double),
         ("min_calc_electron", C.c_double), ("min_calc_positron", C.c_double),
         ("min_calc_muon", C.c_double), ("min_calc_photon", C.c_double),
-        ("a0sq", C.c_double), ("Z2a04", C.c_double), ("Z23", C.c_double),
+        ("a0sq", C.c_double), ("Z2a04", C.c_double), ("Z23", C.c_double), ("Z13", C.c_double),
     ]
 
 
@@ -64,7 +64,7 @@ class PtTally(C.Structure):
 class PtOpts(C.Structure):
     _fields_ = [("min_energy", C.c_double), ("max_n_integrators", C.c_int64), ("rescale_MCS", C.c_double),
                 ("multiple_scattering", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64),
-                ("primary_offset", C.c_int64)]
+                ("primary_offset", C.c_int64), ("mcs_mode", C.c_int32), ("reserved0", C.c_int32)]
 
 
 N_DARK = 4
@@ -163,6 +163,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_sample_only.restype = C.c_int
     lib.pt_dsigma.argtypes = [vp, i32, vp, vp, i64, i32, vp, vp]
     lib.pt_dsigma.restype = C.c_int
+    lib.pt_moliere_inverse_cdf.argtypes = [vp, vp, i64, i32, vp, vp]
+    lib.pt_moliere_inverse_cdf.restype = C.c_int
     _LIB = lib
     return lib
 

@@ -68,7 +68,7 @@ template <int PREC> struct WaveCtx {
   Tabs T;
   double min_energy, rescale;
   int64_t max_n_integrators;
-  int ms;
+  int ms, mcs_mode;
   uint64_t seed;
   RingT<PREC> q;
   uint64_t mask;                      // ring capacity - 1
@@ -358,6 +358,7 @@ __device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf],
 
 // ------------------------------------------------------------ phase 1, float64
 // Same device functions and operation order as the record engine (pt_run_sm).
+template <int BETHE>
 __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
@@ -434,8 +435,8 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
             double pf[4] = {E, px, py, pz}, rf[3] = {x, y, z};
             lose_energy(pf, mass, (S(losses) * S(dz)).v);
             move_along(pf, rf, dz);
-            if (c.ms) mcs_fast(pf, (S(T.t.rho) * (S(dz) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, c.rescale,
-                               table_mass(pid), rng);
+            if (c.ms) mcs_apply(BETHE, pf, (S(T.t.rho) * (S(dz) / S(kCmToM))).v, T.t, c.rescale,
+                                table_mass(pid), rng);
             E = pf[0]; px = pf[1]; py = pf[2]; pz = pf[3]; x = rf[0]; y = rf[1]; z = rf[2];
           }
         }
@@ -452,7 +453,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
           double pf[4] = {E, px, py, pz}, rf[3] = {x, y, z};
           lose_energy(pf, mass, (S(losses) * S(last)).v);
           move_along(pf, rf, last);
-          if (c.ms) mcs_fast(pf, (S(T.t.rho) * (S(last) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, c.rescale, kMe, rng);
+          if (c.ms) mcs_apply(BETHE, pf, (S(T.t.rho) * (S(last) / S(kCmToM))).v, T.t, c.rescale, kMe, rng);
           E = pf[0]; px = pf[1]; py = pf[2]; pz = pf[3]; x = rf[0]; y = rf[1]; z = rf[2];
           active = false;
           finish = true;
@@ -540,6 +541,9 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
   publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
 }
 
+// BETHE: Shower(fast_MCS_mode=False); a separate instantiation keeps the
+// Bethe-Moliere inverse CDF out of the fast mode's registers.
+template <int BETHE>
 __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
   __shared__ unsigned int sh_hist[kHist];
   __shared__ int32_t sh_buf[kWarps][8][kBuf];
@@ -559,6 +563,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
   const float minE = (float)c.min_energy;
   const float lossesf = (float)T.t.dEdx_GeV_per_m;
   const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
+  const float Z13 = (float)T.t.Z13;
   const float rescale = (float)c.rescale;
   const float me = (float)kMe;
   LocalTally L;
@@ -661,10 +666,19 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
       // Lynch-Dahl momentum p = m_lepton * beta * gamma = |p| m_lepton / m;
       // a particle at rest draws nothing (moliere.py:359-363)
       const bool scat = charged && c.ms && pmag > 0.f;
-      if (scat)
-        mcs32_u(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, pick(dr.u, base),
-                pick(dr.u, base + 2), pick(dr.u, base + 3), pmag / Ef);
-      const int after = base + (scat ? 4 : 0);
+      int used = 0;
+      if (scat) {
+        if constexpr (BETHE) {
+          // the electron's momentum throughout (moliere.py:237,244)
+          used = mcs32_bethe(dir, pmag * (me / mf), pmag / Ef, rho_cm * step, A, Z, Z13, Z23, rescale,
+                             pick(dr.u, base), pick(dr.u, base + 1), pick(dr.u, base + 2), pick(dr.u, base + 3));
+        } else {
+          mcs32_u(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, pick(dr.u, base),
+                  pick(dr.u, base + 2), pick(dr.u, base + 3), pmag / Ef);
+          used = 4;
+        }
+      }
+      const int after = base + used;
       if (last) uc = pick(dr.u, after);                  // the process-choice draw
       rng.advance(dr, after + (last ? 1 : 0));
       have_uc = last;
@@ -1176,6 +1190,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.rescale = o->rescale_MCS;
   c.max_n_integrators = o->max_n_integrators;
   c.ms = o->multiple_scattering;
+  c.mcs_mode = o->mcs_mode;
   c.seed = o->seed;
   c.q = carve_ring<PREC>(S);
   c.mask = (uint64_t)S->cap - 1;
@@ -1192,7 +1207,8 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.refill_min[1] = tu[1] ? tu[1] : kRefillMinSample;
   c.chunk[0] = tu[2] ? tu[2] : kChunkPropagate;
   c.chunk[1] = tu[3] ? tu[3] : kChunkSample;
-  const void* kp = PREC ? (const void*)k_propagate_mixed : (const void*)k_propagate_fp64;
+  const void* kp = PREC ? (c.mcs_mode ? (const void*)k_propagate_mixed<1> : (const void*)k_propagate_mixed<0>)
+                       : (c.mcs_mode ? (const void*)k_propagate_fp64<1> : (const void*)k_propagate_fp64<0>);
   const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);
   const int rb_s = resident_blocks(ks);
@@ -1243,8 +1259,12 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
     PT_CUDA(cudaEventRecord(S->ev[0], st));
-    if constexpr (PREC == 1) k_propagate_mixed<<<gp, kThreads, 0, st>>>(c);
-    else k_propagate_fp64<<<gp, kThreads, 0, st>>>(c);
+    if constexpr (PREC == 1) {
+      if (c.mcs_mode) k_propagate_mixed<1><<<gp, kThreads, 0, st>>>(c);
+      else k_propagate_mixed<0><<<gp, kThreads, 0, st>>>(c);
+    }
+    else if (c.mcs_mode) k_propagate_fp64<1><<<gp, kThreads, 0, st>>>(c);
+    else k_propagate_fp64<0><<<gp, kThreads, 0, st>>>(c);
     PT_CUDA(cudaEventRecord(S->ev[1], st));
     k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
     PT_CUDA(cudaEventRecord(S->ev[2], st));

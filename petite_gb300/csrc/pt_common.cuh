@@ -16,6 +16,8 @@ constexpr double kAlpha = 1 / 137.035999;
 constexpr double kMe = 510.998950 * kkeV;
 constexpr double kMmu = 105.6583755 * kMeV;
 constexpr double kCmToM = 0.01;
+constexpr double kHbarc = 0.1973269804E-13;       // GeV cm
+constexpr double kNAvogadro = 6.0221409e+23;
 
 // ------------------------------------------------------------ random stream
 // Philox4x32-10 (Salmon et al., SC'11).  Counter = (draw block lo, hi,

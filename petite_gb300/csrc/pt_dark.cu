@@ -217,7 +217,7 @@ __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_
     const double dEdx = T.t.dEdx_GeV_per_m;
     const double dist = ((S(E0) - S(E_int)) / S(dEdx)).v;
     double ps[4] = {r.p0[0], r.p0[1], r.p0[2], r.p0[3]};
-    mcs_fast(ps, (S(T.t.rho) * (S(dist) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, o.rescale_MCS, kMe, rng);
+    mcs_apply(o.mcs_mode, ps, (S(T.t.rho) * (S(dist) / S(kCmToM))).v, T.t, o.rescale_MCS, kMe, rng);
     pf[0] = ps[0]; pf[1] = ps[1]; pf[2] = ps[2]; pf[3] = ps[3];
     lose_energy(pf, r.mass, (S(E0) - S(E_int)).v);
   }

@@ -22,7 +22,7 @@ struct RunCtx {
   Tabs T;
   double min_energy, rescale;
   int64_t max_n_integrators;
-  int ms;
+  int ms, mcs_mode;
   uint64_t seed;
   pt_particles P;
   const int64_t* live_in;
@@ -113,6 +113,8 @@ __global__ void k_iota(int64_t* a, int64_t n) {
   if (i < n) a[i] = i;
 }
 
+// BETHE: Shower(fast_MCS_mode=False), instantiated apart from the fast mode.
+template <int BETHE>
 __global__ void __launch_bounds__(128) k_transport_fp64(RunCtx c) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= c.n_in) return;
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(128) k_transport_fp64(RunCtx c) {
         } else {
           lose_energy(pf, mass, (S(losses) * S(dz)).v);
           move_along(pf, rf, dz);
-          if (c.ms) mcs_fast(pf, (S(T.t.rho) * (S(dz) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, c.rescale, m_tab, rng);
+          if (c.ms) mcs_apply(BETHE, pf, (S(T.t.rho) * (S(dz) / S(kCmToM))).v, T.t, c.rescale, m_tab, rng);
         }
       }
       const double distC = rng.u();
@@ -172,7 +174,7 @@ __global__ void __launch_bounds__(128) k_transport_fp64(RunCtx c) {
       lose_energy(pf, mass, (S(losses) * S(last)).v);
       move_along(pf, rf, last);
       // shower.py:596-598 passes no m_lepton: the electron mass applies
-      if (c.ms) mcs_fast(pf, (S(T.t.rho) * (S(last) / S(kCmToM))).v, T.t.A, T.t.Z, T.t.Z23, c.rescale, kMe, rng);
+      if (c.ms) mcs_apply(BETHE, pf, (S(T.t.rho) * (S(last) / S(kCmToM))).v, T.t, c.rescale, kMe, rng);
     }
   }
 
@@ -406,6 +408,7 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
   c.rescale = o->rescale_MCS;
   c.max_n_integrators = o->max_n_integrators;
   c.ms = o->multiple_scattering;
+  c.mcs_mode = o->mcs_mode;
   c.seed = o->seed;
   c.P = *P;
   c.n_out = h->counters + 0;
@@ -425,7 +428,8 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
     c.n_in = n_in;
     c.live_out = h->live[cur ^ 1];
     c.live_cap = h->scratch_cap;
-    k_transport_fp64<<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
+    if (c.mcs_mode) k_transport_fp64<1><<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
+    else k_transport_fp64<0><<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
     PT_CUDA(cudaGetLastError());
     PT_CUDA(cudaMemcpyAsync(h->h_counters, h->counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     s = read_status(h, st);
@@ -518,6 +522,7 @@ extern "C" pt_status pt_run_sm_noalloc(pt_handle* h, pt_particles* P, int64_t n_
   c.rescale = o->rescale_MCS;
   c.max_n_integrators = o->max_n_integrators;
   c.ms = o->multiple_scattering;
+  c.mcs_mode = o->mcs_mode;
   c.seed = o->seed;
   c.P = *P;
   c.n_out = counters + 0;
@@ -537,7 +542,8 @@ extern "C" pt_status pt_run_sm_noalloc(pt_handle* h, pt_particles* P, int64_t n_
     c.n_in = n_in;
     c.live_out = live[cur ^ 1];
     c.live_cap = kNoAllocMaxRows;
-    k_transport_fp64<<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
+    if (c.mcs_mode) k_transport_fp64<1><<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
+    else k_transport_fp64<0><<<(unsigned)((n_in + tbt - 1) / tbt), tbt, 0, st>>>(c);
     PT_CUDA(cudaGetLastError());
     PT_CUDA(cudaMemcpyAsync(h->h_counters, counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     PT_CUDA(cudaMemcpyAsync(h->h_status, status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -599,6 +605,25 @@ extern "C" pt_status pt_sample_only(pt_handle* h, int32_t process, const double*
                                                               h->status, h->err_info);
   PT_CUDA(cudaGetLastError());
   return read_status(h, st);
+}
+
+static __global__ void k_moliere_x(const double* u, const double* B, int64_t n, int prec, double* x) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  x[i] = prec ? (double)moliere_x<float>((float)u[i], (float)B[i]) : moliere_x<double>(u[i], B[i]);
+}
+
+extern "C" pt_status pt_moliere_inverse_cdf(const double* u, const double* B, int64_t n, int32_t precision,
+                                            double* x, void* stream) {
+  if (n < 0 || precision < 0 || precision > 1) return PT_BAD_ARG;
+  if (n == 0) return PT_OK;
+  if (!u || !B || !x) return PT_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int tb = 128;
+  k_moliere_x<<<(unsigned)((n + tb - 1) / tb), tb, 0, st>>>(u, B, n, precision, x);
+  PT_CUDA(cudaGetLastError());
+  PT_CUDA(cudaStreamSynchronize(st));
+  return PT_OK;
 }
 
 extern "C" pt_status pt_dsigma(pt_handle* h, int32_t process, const double* x, const double* energy, int64_t n,

@@ -6,6 +6,7 @@
 // (pt_common.cuh) because their formulas are ill-conditioned.
 #pragma once
 #include "pt_common.cuh"
+#include "pt_moliere.cuh"
 #include "petite_gpu.h"
 
 namespace pt {
@@ -370,14 +371,10 @@ __device__ __forceinline__ V4 to_lab(const Rot& R, const V4& v) {
 }
 
 // ----------------------------------------------- multiple Coulomb scattering
-// get_scattered_momentum_fast (moliere.py:350-400) with the Lynch-Dahl width
-// of moliere.py:196-219,265-284.  Draw order: sign, Gaussian pair (angle,
-// radius; the pair shares one Box-Muller evaluation), phi.
-static __device__ void mcs_fast(double* p4, double t_, double A_, double Z_, double Z23, double rescale, double m_lep,
-                         Rng& rng) {
-  const double pn = norm3_np(p4[1], p4[2], p4[3]);
-  if (!(pn > 0)) return;
-  const S beta = S(pn) / S(p4[0]);
+// generate_moliere_angle_simplified_alt (moliere.py:265-284): the Lynch-Dahl
+// width (moliere.py:196-219) and the space angle from a Gaussian pair.  Draw
+// order: sign, the pair (angle, radius; one Box-Muller evaluation).
+static __device__ S lynch_dahl_theta(S beta, double t_, double A_, double Z_, double Z23, double m_lep, Rng& rng) {
   const S Z(Z_), A(A_), t(t_);
   const S p = S(m_lep / kMeV) * beta / ssqrt(S(1.0) - sq(beta));       // moliere.py:206
   const S pb = p * beta;
@@ -388,14 +385,18 @@ static __device__ void mcs_fast(double* p4, double t_, double A_, double Z_, dou
   const S v = S(0.5) * omega / (S(1.0) - S(0.98));
   const S onev = S(1.0) + v;
   const S th0 = ssqrt(chic2 * (onev * S(log(onev.v)) / v - S(1.0)) / (S(1.0) + sq(S(0.98))));
-  const double u_sign = rng.u(), u_ang = rng.u(), u_rad = rng.u(), u_phi = rng.u();
+  const double u_sign = rng.u(), u_ang = rng.u(), u_rad = rng.u();
   const S sign = (u_sign < 0.5) ? S(-1.0) : S(1.0);
   const S x2pi = S(u_ang) * S(2.0 * kPi);
   const S g2rad = ssqrt(S(-2.0) * S(log((S(1.0) - S(u_rad)).v)));
   const S g1 = S(0.0) + (S(cos(x2pi.v)) * g2rad) * th0;
   const S g2 = S(0.0) + (S(sin(x2pi.v)) * g2rad) * th0;
-  const S theta = sign * ssqrt(sq(g1) + sq(g2)) * S(rescale);
-  const S phi = S(0.0) + S(2.0 * kPi) * S(u_phi);
+  return sign * ssqrt(sq(g1) + sq(g2));
+}
+
+// The rotation of moliere.py:384-398 (and :427-445): the direction (theta,
+// phi) about z taken to the lab with the transpose of get_rotation_matrix.
+static __device__ void mcs_rotate(double* p4, double pn, S theta, S phi) {
   const S cth(cos(theta.v)), sth(sin(theta.v)), cph(cos(phi.v)), sph(sin(phi.v));
   const S n0 = S(pn) * (sph * sth), n1 = S(pn) * (-cph * sth), n2 = S(pn) * cth;
   // get_rotation_matrix, moliere.py:287-348 (the repeated branch at :331 kept)
@@ -428,6 +429,58 @@ static __device__ void mcs_fast(double* p4, double t_, double A_, double Z_, dou
   p4[1] = (R00 * n0 + R10 * n1 + R20 * n2).v;
   p4[2] = (R01 * n0 + R11 * n1 + R21 * n2).v;
   p4[3] = (R02 * n0 + R12 * n1 + R22 * n2).v;
+}
+
+// get_scattered_momentum_fast (moliere.py:350-400): four draws with phi.
+static __device__ void mcs_fast(double* p4, double t_, double A_, double Z_, double Z23, double rescale, double m_lep,
+                                Rng& rng) {
+  const double pn = norm3_np(p4[1], p4[2], p4[3]);
+  if (!(pn > 0)) return;
+  const S beta = S(pn) / S(p4[0]);
+  const S theta = lynch_dahl_theta(beta, t_, A_, Z_, Z23, m_lep, rng) * S(rescale);
+  const S phi = S(0.0) + S(2.0 * kPi) * S(rng.u());
+  mcs_rotate(p4, pn, theta, phi);
+}
+
+// get_scattered_momentum_Bethe (moliere.py:403-453) with
+// generate_moliere_angle (moliere.py:221-247).  b < 2: the Lynch-Dahl angle
+// with its default (electron) mass, four draws with phi.  Otherwise three:
+// the inverse-CDF uniform (generate_moliere_x, moliere.py:124-136), the sign,
+// phi.  The reference passes m_lepton on to get_chic_squared (moliere.py:244),
+// which takes none (a TypeError there); its momentum is the electron's.
+static __device__ void mcs_bethe(double* p4, double t_, double A_, double Z_, double Z13, double Z23, double rescale,
+                                 Rng& rng) {
+  const double pn = norm3_np(p4[1], p4[2], p4[3]);
+  if (!(pn > 0)) return;
+  const S beta = S(pn) / S(p4[0]);
+  const S Z(Z_), A(A_), t(t_);
+  // get_b, moliere.py:139-155 (z = 1)
+  const S alpha = Z * S(kAlpha) / beta;
+  const S expb = S(6700.0) * t * (Z + S(1.0)) * S(Z13) * S(1.0) / (sq(beta) * A * (S(1.0) + S(3.34) * sq(alpha)));
+  const double b = log(expb.v);
+  S theta;
+  if (b < 2.0) {
+    theta = lynch_dahl_theta(beta, t_, A_, Z_, Z23, kMe, rng);
+  } else {
+    const double B = moliere_B(b);
+    const double x = moliere_x(rng.u(), B);
+    // get_chic_squared, moliere.py:180-192
+    const S p = S(kMe) / S(kHbarc) * beta / ssqrt(S(1.0) - sq(beta));
+    const S chic2 = S(4.0) * S(kPi) * S(kNAvogadro) * sq(S(kAlpha)) * t * Z * (Z + S(1.0)) * S(1.0) /
+                    (A * sq(p) * sq(beta));
+    const S sign = rng.u() < 0.5 ? S(-1.0) : S(1.0);
+    theta = sign * ssqrt(S(x) * chic2 * S(B));
+  }
+  theta = theta * S(rescale);
+  const S phi = S(0.0) + S(2.0 * kPi) * S(rng.u());
+  mcs_rotate(p4, pn, theta, phi);
+}
+
+// Shower._get_MCS_p (shower.py:147-151): mode 0 = fast (Lynch-Dahl), 1 = Bethe-Moliere.
+__device__ __forceinline__ void mcs_apply(int mode, double* p4, double t, const pt_tables& tb, double rescale,
+                                          double m_lep, Rng& rng) {
+  if (mode) mcs_bethe(p4, t, tb.A, tb.Z, tb.Z13, tb.Z23, rescale, rng);
+  else mcs_fast(p4, t, tb.A, tb.Z, tb.Z23, rescale, m_lep, rng);
 }
 
 // Particle.lose_energy, particle.py:143-153

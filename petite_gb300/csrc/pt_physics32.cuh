@@ -208,25 +208,23 @@ __device__ __forceinline__ float lynch_dahl_g(float v) {
   return (1.f + v) * log1pf(v) / v - 1.f;
 }
 
-// The scattering with its three used draws given (sign, Gaussian radius, phi;
-// the pair's angle draw cancels in the space angle).
-__device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
-                                        float rescale, float u_sign, float u_rad, float u_phi, float beta_p);
-
-
-__device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
-                                        float rescale, float u_sign, float u_rad, float u_phi, float beta_p) {
-  const float beta = beta_p >= 0.f ? beta_p : pmag / E;
-  const float p = pmag * 1000.f;                         // MeV
+// Lynch-Dahl space angle (sign and Gaussian radius draws given; the pair's
+// angle draw cancels in the space angle).  p = m_lepton beta gamma (GeV).
+__device__ __forceinline__ float lynch_dahl_theta32(float p_gev, float beta, float t, float A, float Z, float Z23,
+                                                    float u_sign, float u_rad) {
+  const float p = p_gev * 1000.f;                       // MeV
   const float pb = p * beta;
   const float chic2 = 0.157f * Z * (Z + 1.f) * (t / A) / (pb * pb);
   const float zab = Z * (float)kAlpha / beta;
   const float chia2 = 2.007e-5f * Z23 * (1.f + 3.34f * zab * zab) / (p * p);
   const float v = 0.5f * (chic2 / chia2) / (1.f - 0.98f);
   const float th0 = sqrtf(chic2 * lynch_dahl_g(v) / (1.f + 0.98f * 0.98f));
-  const float r = sqrtf(-2.f * __logf(1.f - u_rad));
-  float theta = th0 * r * rescale;
-  if (u_sign < 0.5f) theta = -theta;
+  const float theta = th0 * sqrtf(-2.f * __logf(1.f - u_rad));
+  return u_sign < 0.5f ? -theta : theta;
+}
+
+// The direction turned by (theta, phi) about itself.
+__device__ __forceinline__ void mcs32_rotate(float3& dir, float theta, float u_phi) {
   float sth, cth, sph, cph;
   sincosf(theta, &sth, &cth);
   sincospif(2.f * u_phi, &sph, &cph);
@@ -242,6 +240,37 @@ __device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float 
   float3 o = make_float3(ca * w0 + sa * w1, -sa * w0 + ca * w1, w2);
   const float inv = rsqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
   dir = make_float3(o.x * inv, o.y * inv, o.z * inv);
+}
+
+// get_scattered_momentum_fast with its used draws given (sign, radius, phi).
+__device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float t, float A, float Z, float Z23,
+                                        float rescale, float u_sign, float u_rad, float u_phi, float beta_p) {
+  const float beta = beta_p >= 0.f ? beta_p : pmag / E;
+  mcs32_rotate(dir, lynch_dahl_theta32(pmag, beta, t, A, Z, Z23, u_sign, u_rad) * rescale, u_phi);
+}
+
+// get_scattered_momentum_Bethe (moliere.py:403-453) on the next four draws
+// u[0..3]; returns how many it used.  b < 2: the Lynch-Dahl angle with the
+// electron mass, draws sign, (pair angle), radius, phi.  Otherwise the
+// inverse-CDF draw, the sign and phi.  pe = m_e beta gamma (GeV): the
+// reference's momentum m_e beta / sqrt(1 - beta^2) in a well-conditioned form.
+__device__ __forceinline__ int mcs32_bethe(float3& dir, float pe, float beta, float t, float A, float Z, float Z13,
+                                           float Z23, float rescale, float u0, float u1, float u2, float u3) {
+  const float alpha = Z * (float)kAlpha / beta;        // get_b, moliere.py:139-155
+  const float expb = 6700.f * t * (Z + 1.f) * Z13 / (beta * beta * A * (1.f + 3.34f * alpha * alpha));
+  const float b = __logf(expb);
+  if (b < 2.f) {
+    mcs32_rotate(dir, lynch_dahl_theta32(pe, beta, t, A, Z, Z23, u0, u2) * rescale, u3);
+    return 4;
+  }
+  const float B = moliere_B(b);
+  const float x = moliere_x(u0, B);
+  const float pb = pe * (float)(1.0 / kHbarc) * beta;  // get_chic_squared, moliere.py:180-192 (1/cm)
+  const float chic2 = (float)(4.0 * kPi * kNAvogadro * kAlpha * kAlpha) * t * Z * (Z + 1.f) / (A * pb * pb);
+  float theta = sqrtf(x * chic2 * B);
+  if (u1 < 0.5f) theta = -theta;
+  mcs32_rotate(dir, theta * rescale, u2);
+  return 3;
 }
 
 // Lab frame from the parent's unit direction: Particle.rotation_matrix

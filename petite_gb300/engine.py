@@ -191,6 +191,7 @@ class SMEngine:
         pt.a0sq = a0 ** 2
         pt.Z2a04 = Z ** 2 * a0 ** 4
         pt.Z23 = Z ** (2. / 3.)
+        pt.Z13 = Z ** (1. / 3.)
         self._pt = pt
         h = C.c_void_p()
         _lib.check(self.lib.pt_create(C.byref(pt), C.byref(h)), "pt_create")
@@ -239,7 +240,7 @@ class SMEngine:
 
     @staticmethod
     def opts(min_energy, max_n_integrators=10000, rescale_MCS=1.0, ms=True, precision="fp64", seed=0,
-             primary_offset=0):
+             primary_offset=0, fast_MCS_mode=True):
         o = _lib.PtOpts()
         o.min_energy = float(min_energy)
         o.max_n_integrators = int(max_n_integrators)
@@ -248,6 +249,7 @@ class SMEngine:
         o.precision = PRECISIONS[precision]
         o.seed = int(seed) & ((1 << 64) - 1)
         o.primary_offset = int(primary_offset)
+        o.mcs_mode = 0 if fast_MCS_mode else 1
         return o
 
     def run_sm(self, p0, r0, pid, mass, weight, opts: _lib.PtOpts, capacity: int | None = None):

@@ -77,8 +77,6 @@ class Shower:
     def __init__(self, dict_dir, target_material, min_energy, maxF_fudge_global=1,
                  max_n_integrators=int(1e4), fast_MCS_mode=True, seed=None, rescale_MCS=1,
                  precision="fp64", device="cuda"):
-        if not fast_MCS_mode:
-            raise NotImplementedError("fast_MCS_mode=False (Bethe-Moliere scattering) is not implemented")
         if dict_dir is None:
             dict_dir = T.BUNDLED_DIR
         self._dict_dir = dict_dir
@@ -91,6 +89,7 @@ class Shower:
         self._maxF_fudge_global = maxF_fudge_global
         self._max_n_integrators = max_n_integrators
         self._MCS_rescale_factor = rescale_MCS
+        self._fast_MCS_mode = bool(fast_MCS_mode)     # shower.py:147-151
         self._precision = precision
         if seed is None:
             seed = int.from_bytes(os.urandom(8), "little")
@@ -113,7 +112,8 @@ class Shower:
 
     def _opts(self, GlobalMS=True, precision=None):
         return SMEngine.opts(self.min_energy, self._max_n_integrators, self._MCS_rescale_factor,
-                             ms=GlobalMS, precision=precision or self._precision, seed=self._seed)
+                             ms=GlobalMS, precision=precision or self._precision, seed=self._seed,
+                             fast_MCS_mode=self._fast_MCS_mode)
 
     # ------------------------------------------------------------- n*sigma
     def _ns(self, slot, E):

@@ -42,6 +42,29 @@ def test_closed_form_cdf_is_the_integral():
             assert abs((1.0 - P.moliere_tail(x, B)) - q) <= 1e-12, (B, x)
 
 
+def test_inverse_cdf_root_is_accurate():
+    """The Newton root of the closed-form tail against a 30-digit root of the
+    same equation (mpmath's Ei)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 30
+    rng = np.random.default_rng(3)
+
+    def tail(x, B):
+        x, B = mp.mpf(x), mp.mpf(B)
+        return mp.e ** (-x) * (1 + 1 / B) + (x * mp.e ** (-x) * (mp.ei(x) - mp.log(x)) - 1) / B
+    n = 0
+    for k in range(80):
+        B = rng.uniform(3.15, 20.0)
+        u = rng.uniform(0.011, 0.999) if k % 3 else 1 - 10 ** rng.uniform(-3, -0.5)
+        x = P.moliere_x(u, B)
+        if not 0.01 < x < 100 or 1 - u < 1 / B / 100:
+            continue
+        root = mp.findroot(lambda t: tail(t, B) - (1 - mp.mpf(u)), x)
+        assert abs(float(root) - x) <= 1e-13 * x, (u, B)
+        n += 1
+    assert n > 60
+
+
 def test_b_B_and_chic2_match_reference():
     for Z, A, t, beta, b, B, chic2 in G["params/rows"]:
         assert P.moliere_b(t, beta, A, int(Z)) == pytest.approx(b, rel=0, abs=1e-13 * max(1.0, abs(b)))
