@@ -245,6 +245,11 @@ enum { PT_N_DARK = 4, PT_DARK_MAX_MASSES = 8 };
  * output process code when the bound-electron form produced the vector
  * ("DarkAnn_bound", "DarkComp_bound", dark_shower.py:799-802). */
 enum { PT_DARKBREM = 0, PT_DARKANN = 1, PT_DARKCOMP = 2, PT_DARKMUONBREM = 3, PT_DARK_BOUND = 4 };
+/* TwoBody_BSMDecay (dark_shower.py:633-638,836-844; Particle.two_body_decay,
+ * particle.py:209-256): a pi0 row decays to gamma + V.  PT_TWOBODY is its bit
+ * in pt_dark_params.active and its yield slot; its vectors carry process
+ * code PT_TWOBODY_CODE. */
+enum { PT_TWOBODY = 4, PT_TWOBODY_CODE = 8 };
 
 /* VEGAS maps of the dark processes for one target, for up to
  * PT_DARK_MAX_MASSES vector masses (dark_maps.pkl, dark_shower.py:148-201):
@@ -273,7 +278,7 @@ typedef struct pt_dark_maps {
 typedef struct pt_dark_params {
   int32_t mass_index;             /* map block sampled (the mV estimator) */
   int32_t bound_electron;         /* 1: bound-electron DarkAnn/DarkComp (the reference default) */
-  int32_t active;                 /* bit p: dark process p active */
+  int32_t active;                 /* bit p: dark process p active; bit PT_TWOBODY: TwoBody_BSMDecay */
   double mV;                      /* vector mass used in the cross sections and kinematics */
   double coupling;                /* g_e^2 / (4 pi alpha_em) */
   double Zeff;
@@ -291,6 +296,7 @@ typedef struct pt_dark_params {
   const double* nsc_lx;           /* DarkComp n*sigma, log10 energies and log10 values */
   const double* nsc_ly;
   int32_t nsc_n;
+  double kinetic_mixing;          /* DarkShower(kinetic_mixing): the TwoBody_BSMDecay weight */
 } pt_dark_params;
 
 /* Vectors produced by pt_run_dark (device pointers; SoA like pt_particles). */
@@ -299,11 +305,11 @@ typedef struct pt_dark_out {
   double* r;           /* [3][capacity] production point (the parent's final position) */
   double* weight;      /* [capacity] */
   int64_t* parent;     /* [capacity] SM row */
-  int32_t* process;    /* [capacity] dark process code (+PT_DARK_BOUND) */
+  int32_t* process;    /* [capacity] dark process code (+PT_DARK_BOUND), or PT_TWOBODY_CODE */
   int32_t* draws;      /* [capacity] uniforms used (diagnostic) */
   int64_t capacity;
-  double* yield;       /* [PT_N_DARK] summed weights per process (accumulated) */
-  double* yield_E;     /* [PT_N_DARK] summed weight * E_V per process (accumulated) */
+  double* yield;       /* [PT_N_DARK + 1] summed weights per process, PT_TWOBODY last (accumulated) */
+  double* yield_E;     /* [PT_N_DARK + 1] summed weight * E_V per process (accumulated) */
 } pt_dark_out;
 
 typedef struct pt_dark pt_dark;

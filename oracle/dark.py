@@ -114,12 +114,51 @@ DARK_PROCESSES = ("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")
 DARK_CODE = {p: i for i, p in enumerate(DARK_PROCESSES)}
 DARK_DIM = {"DarkComp": 1, "DarkBrem": 3, "DarkAnn": 1, "DarkMuonBrem": 3}   # dark_shower.py:67
 V_PID = 4900022
+TWOBODY = "TwoBody_BSMDecay"
+MESON_TWOBODY_BR = {111: 0.98823}       # meson_twobody_branchingratios, particle.py:39-48
 
 
 def dark_key(pkey: int, process: str) -> int:
     """Stream key of dark process `process` produced by the particle `pkey`
-    (daughters use multipliers 1 and 2; dark processes 3..6)."""
-    return mix64((int(pkey) + 0x9E3779B97F4A7C15 * (3 + DARK_CODE[process])) & 0xFFFFFFFFFFFFFFFF)
+    (daughters use multipliers 1 and 2; dark processes 3..6, the two-body
+    meson decay 7)."""
+    idx = 4 if process == TWOBODY else DARK_CODE[process]
+    return mix64((int(pkey) + 0x9E3779B97F4A7C15 * (3 + idx)) & 0xFFFFFFFFFFFFFFFF)
+
+
+def boost_matrix(pf, m0):
+    """Particle.boost_matrix, particle.py:187-207: rest frame -> lab for a
+    particle of final momentum pf and mass m0."""
+    E0, px0, py0, pz0 = pf
+    gamma = E0 / m0
+    beta = 1.0 if gamma == 1.0 else math.sqrt(1.0 - 1.0 / gamma ** 2)
+    pmag = P.norm3(px0, py0, pz0)
+    if pmag == 0.0:
+        return [[1.0 if i == j else 0.0 for j in range(4)] for i in range(4)]
+    bx, by, bz = beta * px0 / pmag, beta * py0 / pmag, beta * pz0 / pmag
+    return [[gamma, gamma * bx, gamma * by, gamma * bz],
+            [gamma * bx, 1 + (gamma - 1) * bx ** 2 / beta ** 2, (gamma - 1) * bx * by / beta ** 2,
+             (gamma - 1) * bx * bz / beta ** 2],
+            [gamma * by, (gamma - 1) * by * bx / beta ** 2, 1 + (gamma - 1) * by ** 2 / beta ** 2,
+             (gamma - 1) * by * bz / beta ** 2],
+            [gamma * bz, (gamma - 1) * bz * bx / beta ** 2, (gamma - 1) * bz * by / beta ** 2,
+             1 + (gamma - 1) * bz ** 2 / beta ** 2]]
+
+
+def two_body_V(pf, mX, mV, u_ct, u_phi):
+    """Particle.two_body_decay (particle.py:209-256) into (gamma, V) with its
+    two draws (np.random.uniform(-1, 1) for cos theta, (0, 2 pi) for phi):
+    the V four-momentum in the lab."""
+    m1, m2 = 0.0, mV
+    E1 = (mX ** 2 - m2 ** 2 + m1 ** 2) / (2 * mX)
+    E2 = (mX ** 2 - m1 ** 2 + m2 ** 2) / (2 * mX)
+    pF = math.sqrt(E1 ** 2 - m1 ** 2)
+    cos_theta = -1.0 + (1.0 - -1.0) * u_ct
+    phi = 0.0 + (2.0 * math.pi - 0.0) * u_phi
+    sin_theta = math.sqrt(1 - cos_theta ** 2)
+    q = (E2, pF * sin_theta * math.sin(phi), pF * sin_theta * math.cos(phi), pF * cos_theta)
+    M = boost_matrix(pf, mX)
+    return tuple(M[i][0] * q[0] + M[i][1] * q[1] + M[i][2] * q[2] + M[i][3] * q[3] for i in range(4))
 
 
 # ------------------------------------------------------------ cross sections
@@ -467,15 +506,24 @@ class DarkOracle:
     particle record (fields of :class:`oracle.shower.Rec`)."""
 
     def __init__(self, dark: DarkTables, sm_tables, seed, max_n_integrators=10000, rescale=1.0,
-                 fast_MCS_mode=True):
+                 fast_MCS_mode=True, kinetic_mixing=1.0):
         self.d, self.sm, self.seed = dark, sm_tables, seed
+        self.kinetic_mixing = kinetic_mixing
         self.max_n_integrators = max_n_integrators
         self.rescale = rescale
         self.fast_mcs = fast_MCS_mode              # dark_shower.py:134-138
 
     # dark_shower.py:595-647 (bound-electron form)
-    def weight(self, pid, E, process):
+    def weight(self, pid, E, process, mass=None):
         d = self.d
+        if process == TWOBODY:
+            # dark_shower.py:633-638 (pi0; eta and eta' raise KeyError at :604)
+            if pid != 111:
+                return 0.0
+            mass_ratio = d.mV / mass
+            if mass_ratio >= 1.0:
+                return 0.0
+            return 2 * self.kinetic_mixing ** 2 * (1.0 - mass_ratio ** 2) ** 3 * MESON_TWOBODY_BR[111]
         key = (pid, process)
         if key not in d.min_dark:
             return 0.0
@@ -593,8 +641,12 @@ class DarkOracle:
         out = []
         for k, r in enumerate(records):
             for p in processes:
-                wg = self.weight(r.pid, r.p0[0], p)
-                if wg > 0.0:
+                wg = self.weight(r.pid, r.p0[0], p, r.mass)
+                if wg > 0.0 and p == TWOBODY:
+                    s = Stream(self.seed, dark_key(r.pkey, p))
+                    v = two_body_V(tuple(r.pf), r.mass, self.d.mV, s.next(), s.next())
+                    out.append((k, p, wg * r.weight, v, tuple(r.rf)))
+                elif wg > 0.0:
                     s = Stream(self.seed, dark_key(r.pkey, p))
                     res = self.produce(r, p, wg, s)
                     if res is not None:

@@ -70,6 +70,8 @@ class PtOpts(C.Structure):
 N_DARK = 4
 DARK_MAX_MASSES = 8
 DARK_BOUND = 4
+TWOBODY = 4            # TwoBody_BSMDecay: active bit and yield slot
+TWOBODY_CODE = 8       # its vectors' process code
 
 
 class PtDarkMaps(C.Structure):
@@ -88,7 +90,8 @@ class PtDarkParams(C.Structure):
                 ("w_x", C.c_void_p * 4), ("w_y", C.c_void_p * 4), ("w_n", C.c_int32 * 4),
                 ("dr_Ei", C.c_void_p * 4), ("dr_bins", C.c_void_p * 4), ("dr_nbins", C.c_void_p * 4),
                 ("dr_n", C.c_int32 * 4), ("dr_nbmax", C.c_int32 * 4),
-                ("nsc_lx", C.c_void_p), ("nsc_ly", C.c_void_p), ("nsc_n", C.c_int32)]
+                ("nsc_lx", C.c_void_p), ("nsc_ly", C.c_void_p), ("nsc_n", C.c_int32),
+                ("kinetic_mixing", C.c_double)]
 
 
 class PtDarkOut(C.Structure):

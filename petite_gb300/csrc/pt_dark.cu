@@ -184,6 +184,50 @@ struct DarkRow {
   uint64_t key;
 };
 
+// GetBSMWeights for TwoBody_BSMDecay (dark_shower.py:633-638): pi0 rows,
+// 2 kappa^2 (1 - (mV/m)^2)^3 Br(pi0 -> gamma gamma) (particle.py:39-48), zero
+// once mV >= m.  (The reference raises KeyError for eta and eta' rows, whose
+// PIDs its threshold table lacks; the host refuses them before the launch.)
+__device__ double twobody_weight(const pt_dark_params& P, int pid, double mass) {
+  if (pid != 111) return 0.0;
+  const S ratio = S(P.mV) / S(mass);
+  if (!(ratio.v < 1.0)) return 0.0;
+  const S omr = S(1.0) - sq(ratio);
+  return (S(2.0) * sq(S(P.kinetic_mixing)) * (omr * omr * omr) * S(0.98823)).v;
+}
+
+// Particle.two_body_decay (particle.py:209-256) into (gamma, V), V kept: the
+// rest-frame momenta, its two draws (cos theta on [-1, 1), phi on [0, 2 pi))
+// and boost_matrix (particle.py:187-207) from the parent's final momentum and
+// its mass.
+__device__ void two_body_V(const DarkRow& r, double mV, Rng& rng, double* V) {
+  const S mX(r.mass), m1(0.0), m2(mV);
+  const S E1 = (sq(mX) - sq(m2) + sq(m1)) / (S(2.0) * mX);
+  const S E2 = (sq(mX) - sq(m1) + sq(m2)) / (S(2.0) * mX);
+  const S pF = ssqrt(sq(E1) - sq(m1));
+  const S ct = S(-1.0) + (S(1.0) - S(-1.0)) * S(rng.u());
+  const S phi = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+  const S st = ssqrt(S(1.0) - sq(ct));
+  const S q[4] = {E2, pF * st * S(sin(phi.v)), pF * st * S(cos(phi.v)), pF * ct};
+  const double px = r.pf[1], py = r.pf[2], pz = r.pf[3];
+  const double pmag = norm3_np(px, py, pz);
+  if (pmag == 0.0) {                              // np.identity(4)
+    for (int i = 0; i < 4; ++i) V[i] = q[i].v;
+    return;
+  }
+  const S gamma = S(r.pf[0]) / mX;
+  const S beta = gamma.v == 1.0 ? S(1.0) : ssqrt(S(1.0) - S(1.0) / sq(gamma));
+  const S b[3] = {beta * S(px) / S(pmag), beta * S(py) / S(pmag), beta * S(pz) / S(pmag)};
+  const S g1 = gamma - S(1.0), b2 = sq(beta);
+  S M[4][4];
+  M[0][0] = gamma;
+  for (int i = 0; i < 3; ++i) { M[0][i + 1] = gamma * b[i]; M[i + 1][0] = gamma * b[i]; }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      M[i + 1][j + 1] = i == j ? S(1.0) + g1 * sq(b[i]) / b2 : g1 * b[i] * b[j] / b2;
+  for (int i = 0; i < 4; ++i) V[i] = (M[i][0] * q[0] + M[i][1] * q[1] + M[i][2] * q[2] + M[i][3] * q[3]).v;
+}
+
 // produce_bsm_particle (dark_shower.py:721-804).  Returns false when the
 // reference returns None; on true, V and wg hold the vector and its weight.
 __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
@@ -329,26 +373,36 @@ __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_
 }
 
 __global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, pt_particles sm, int64_t n_rows,
-                           pt_dark_out out, unsigned long long* counter, int* status, double* info) {
+                           int ncol, pt_dark_out out, unsigned long long* counter, int* status, double* info) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_rows * PT_N_DARK) return;
-  // process-major: a warp works on one dark process for 32 consecutive rows
+  if (t >= n_rows * ncol) return;
+  // process-major: a warp works on one dark process for 32 consecutive rows;
+  // column PT_TWOBODY (launched when active) decays the pi0 rows
   const int p = (int)(t / n_rows);
   const int64_t row = t - (int64_t)p * n_rows;
   DarkRow r;
   r.pid = sm.pid[row];
+  if (p == PT_TWOBODY && r.pid != 111) return;
   const int64_t cap = sm.capacity;
   for (int c = 0; c < 4; ++c) { r.p0[c] = sm.p0[c * cap + row]; r.pf[c] = sm.pf[c * cap + row]; }
   for (int c = 0; c < 3; ++c) r.rf[c] = sm.rf[c * cap + row];
   r.mass = sm.mass[row];
   r.weight = sm.weight[row];
   r.key = sm.pkey[row];
-  double wg = bsm_weight(T, P, r.pid, r.p0[0], p);
-  if (!(wg > 0.0)) return;
   Rng rng;
-  rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
   double V[4];
-  if (!produce_bsm(T, M, P, o, r, p, wg, V, rng, status, info)) return;
+  double wg;
+  if (p == PT_TWOBODY) {
+    wg = twobody_weight(P, r.pid, r.mass);
+    if (!(wg > 0.0)) return;
+    rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
+    two_body_V(r, P.mV, rng, V);
+  } else {
+    wg = bsm_weight(T, P, r.pid, r.p0[0], p);
+    if (!(wg > 0.0)) return;
+    rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
+    if (!produce_bsm(T, M, P, o, r, p, wg, V, rng, status, info)) return;
+  }
   const double w = (S(wg) * S(r.weight)).v;
   if (out.yield) atomicAdd(out.yield + p, w);
   if (out.yield_E) atomicAdd(out.yield_E + p, w * V[0]);
@@ -360,7 +414,8 @@ __global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, 
   for (int c = 0; c < 3; ++c) out.r[c * oc + slot] = r.rf[c];
   out.weight[slot] = w;
   out.parent[slot] = row;
-  out.process[slot] = p + ((P.bound_electron && (p == PT_DARKANN || p == PT_DARKCOMP)) ? PT_DARK_BOUND : 0);
+  out.process[slot] = p == PT_TWOBODY ? PT_TWOBODY_CODE
+                                      : p + ((P.bound_electron && (p == PT_DARKANN || p == PT_DARKCOMP)) ? PT_DARK_BOUND : 0);
   out.draws[slot] = (int32_t)rng.n;
 }
 
@@ -576,10 +631,11 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
   cudaStream_t st = (cudaStream_t)stream;
   PT_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
   PT_CUDA(cudaMemsetAsync(d->counter, 0, sizeof(unsigned long long), st));
-  const int64_t work = n_rows * PT_N_DARK;
+  const int ncol = PT_N_DARK + ((prm->active >> PT_TWOBODY) & 1);
+  const int64_t work = n_rows * ncol;
   const int tb = 128;
-  k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(d->T, d->M, *prm, *o, *sm, n_rows, *out, d->counter,
-                                                             d->status, d->err_info);
+  k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(d->T, d->M, *prm, *o, *sm, n_rows, ncol, *out,
+                                                             d->counter, d->status, d->err_info);
   PT_CUDA(cudaGetLastError());
   PT_CUDA(cudaMemcpyAsync(d->h_counter, d->counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   const pt_status s = read_dark_status(d, st);

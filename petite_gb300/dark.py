@@ -33,6 +33,8 @@ DARK_CODE = {p: i for i, p in enumerate(DARK_PROCESSES)}
 DARK_PROCESS_CODES = ["DarkBrem", "DarkAnn", "DarkComp", "TwoBody_BSMDecay", "DarkMuonBrem"]   # dark_shower.py:49
 DIMENSIONALITIES_DARK = {"DarkComp": 1, "DarkBrem": 3, "DarkAnn": 1, "DarkMuonBrem": 3}     # dark_shower.py:67
 V_PID = 4900022
+TWOBODY = "TwoBody_BSMDecay"
+MESON_TWOBODY_BR_PI0 = 0.98823                  # meson_twobody_branchingratios[111], particle.py:39-48
 DARK_NPZ = os.path.join(T.BUNDLED_DIR, "dark_tables.npz")
 _TABLES = ("brem_elec", "brem_positron", "ann", "muon_brem")
 
@@ -184,8 +186,8 @@ class DarkEngine:
         arrays (p4, r, weight, parent, process, draws) and the yields."""
         import torch
         dev = self.device
-        yld = torch.zeros(_lib.N_DARK, dtype=torch.float64, device=dev)
-        yldE = torch.zeros(_lib.N_DARK, dtype=torch.float64, device=dev)
+        yld = torch.zeros(_lib.N_DARK + 1, dtype=torch.float64, device=dev)
+        yldE = torch.zeros(_lib.N_DARK + 1, dtype=torch.float64, device=dev)
         if capacity is None:
             capacity = max(16, 4 * n_rows)
         while True:
@@ -247,6 +249,12 @@ class DarkEngine:
         return g
 
 
+def _active_bits(processes) -> int:
+    """pt_dark_params.active: bit p for engine process p, bit TWOBODY for the meson decay."""
+    bits = sum(1 << DARK_CODE[p] for p in processes if p in DARK_CODE)
+    return bits | ((1 << _lib.TWOBODY) if TWOBODY in processes else 0)
+
+
 def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, active, coupling, Zeff):
     """pt_dark_params for one DarkShower (tables kept alive on the engine)."""
     import torch
@@ -256,8 +264,9 @@ def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, 
     prm = _lib.PtDarkParams()
     prm.mass_index = engine.mass_index(mV_est)
     prm.bound_electron = 1 if bound else 0
-    prm.active = sum(1 << DARK_CODE[p] for p in active if p in DARK_CODE)
+    prm.active = _active_bits(active)
     prm.mV, prm.coupling, prm.Zeff = float(mV), float(coupling), float(Zeff)
+    prm.kinetic_mixing = float(sh.kinetic_mixing)
     prm.E_res, prm.E_compth = d["E_res"], d["E_compth"]
     for i in range(5):
         prm.min_dark[i] = float(d["min_dark"][i])
@@ -331,9 +340,24 @@ class DarkShower(Shower):
             part = Particle([E, 0, 0, 0], [0, 0, 0], {"PID": int(PID), "mass": 0.0})
         else:
             part = particle
-        if process not in DARK_CODE or process not in self.active_processes:
+        pid = part.get_ids()["PID"]
+        if pid in (221, 331):
+            # dark_shower.py:604: _minimum_calculable_dark_energy has no entry for eta, eta'
+            raise KeyError(pid)
+        if process == TWOBODY:
+            return self._twobody_weight(pid, part.get_ids()["mass"])
+        if process not in DARK_CODE:
             return 0.0
         return float(self._weights_of([part])[0, DARK_CODE[process]])
+
+    def _twobody_weight(self, pid, mass):
+        """dark_shower.py:633-638 for a pi0 (the pt_run_dark column PT_TWOBODY)."""
+        if pid != 111:
+            return 0.0
+        mass_ratio = self._mV / mass
+        if mass_ratio >= 1.0:
+            return 0.0
+        return 2 * self.kinetic_mixing ** 2 * (1.0 - mass_ratio ** 2) ** 3 * MESON_TWOBODY_BR_PI0
 
     def draw_dark_sample(self, Einc, LU_Key=-1, process="DarkBrem", VB=False, pkey=None):
         """dark_shower.py:649-704 (LU_Key chosen from Einc)."""
@@ -380,7 +404,7 @@ class DarkShower(Shower):
         prm = self._prm
         if processes is not None:
             prm = _lib.PtDarkParams.from_buffer_copy(self._prm)
-            prm.active = sum(1 << DARK_CODE[p] for p in processes if p in DARK_CODE)
+            prm.active = _active_bits(processes)
         return self._dark_engine.run_dark(prm, st, n, self._opts(), keep_records=records)
 
     def _weights_of(self, parts):
@@ -399,7 +423,7 @@ class DarkShower(Shower):
         for i, p in enumerate(parts):
             pid, E = p.get_ids()["PID"], p.get_p0()[0]
             for c, proc in enumerate(DARK_PROCESSES):
-                if proc not in self.active_processes or (pid, proc) not in slots:
+                if (pid, proc) not in slots:
                     continue
                 k = slots[(pid, proc)]
                 if E < md[k]:
@@ -426,15 +450,21 @@ class DarkShower(Shower):
     def _v_particle(self, parent, res, j, weight=None):
         ids = parent.get_ids()
         code = int(res["process"][j])
+        w = float(res["weight"][j])
+        if code == _lib.TWOBODY_CODE:
+            # dark_shower.py:836-843: ID 2*ID+1, the vector mass given
+            v = {"mass": self._mV, "PID": V_PID, "weight": w, "parent_PID": ids["PID"], "parent_ID": ids["ID"],
+                 "ID": 2 * ids["ID"] + 1, "generation_number": ids["generation_number"] + 1,
+                 "generation_process": TWOBODY}
+            return Particle(list(res["p4"][j]), list(res["r"][j]), v)
         name = DARK_PROCESSES[code % _lib.DARK_BOUND]
         if code >= _lib.DARK_BOUND:
             name += "_bound"
-        w = float(res["weight"][j])
         if weight is not None and w != 0.0:
             w = weight * ids["weight"]       # dark_shower.py:723-726,795: the given weight times the parent's
+        # dark_shower.py:789-804: no mass given, so Particle takes the invariant's
         v = {"PID": V_PID, "parent_PID": ids["PID"], "ID": 2 * ids["ID"] + 0, "parent_ID": ids["ID"],
-             "generation_number": ids["generation_number"] + 1, "generation_process": name, "weight": w,
-             "mass": self._mV}
+             "generation_number": ids["generation_number"] + 1, "generation_process": name, "weight": w}
         return Particle(list(res["p4"][j]), list(res["r"][j]), v)
 
     def generate_dark_shower(self, ExDir=None, SParams=None):
@@ -450,12 +480,18 @@ class DarkShower(Shower):
             ShowerToSamp = self.generate_shower(SParams)
         else:
             raise ValueError("Provided SParams must be a `Particle' class object")
-        parts = [p for p in ShowerToSamp if p.get_ids()["PID"] in (11, -11, 22, 13, -13)]
-        active = [p for p in self.active_processes if p in DARK_CODE]
+        active = [p for p in self.active_processes if p in DARK_CODE or p == TWOBODY]
+        if active:
+            for p in ShowerToSamp:
+                if p.get_ids()["PID"] in (221, 331):
+                    # GetBSMWeights, dark_shower.py:604: no threshold entry for eta, eta'
+                    raise KeyError(p.get_ids()["PID"])
+        parts = [p for p in ShowerToSamp if p.get_ids()["PID"] in (11, -11, 22, 13, -13, 111)]
         res = self._run_particles(parts, processes=active)
         # the reference's order: particle by particle, processes in active order
-        rank = np.array([active.index(p) if p in active else 0 for p in DARK_PROCESSES])
-        order = np.lexsort((rank[res["process"] % _lib.DARK_BOUND], res["parent"]))
+        rank = np.array([active.index(p) if p in active else 0 for p in (*DARK_PROCESSES, TWOBODY)])
+        col = np.where(res["process"] == _lib.TWOBODY_CODE, _lib.TWOBODY, res["process"] % _lib.DARK_BOUND)
+        order = np.lexsort((rank[col], res["parent"]))
         NewShower = [self._v_particle(parts[int(res["parent"][j])], res, j) for j in order]
         return ShowerToSamp, NewShower
 

@@ -19,7 +19,7 @@ The particle being processed is tracked by wrapping the Shower instance's
 ``propagate_particle`` and ``sample_scattering``; daughters get the keys of
 ``oracle.philox.daughter_key``.
 
-Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|moliere|all]
+Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|moliere|mesons|all]
 (DICT_DIR from rebuild_maps.py; for ``dark`` it must also hold the output of
 ``rebuild_maps.py --dark``)
 """
@@ -604,6 +604,88 @@ def gen_moliere(dict_dir, out_path):
     np.savez_compressed(out_path, **out)
 
 
+def gen_mesons(dict_dir, out_path, beam_path):
+    """TwoBody_BSMDecay (dark_shower.py:633-638,836-844; particle.py:209-256):
+    generate_dark_shower on lists of pi0s from the reference's own beam file
+    (examples/beams, four-momenta) mixed with SM particles, with the decay's
+    np.random.uniform draws routed to the decaying particle's stream; and the
+    KeyError the reference raises for an eta."""
+    refimport.setup()
+    from PETITE.dark_shower import DarkShower
+    from PETITE.particle import Particle
+    from oracle.dark import dark_key
+    beam = np.load(beam_path)[:40]
+    out = {"beam/p4": beam}
+    router = StreamRouter(SEED)
+    saved = install(router)
+    saved_d = install_dark(router)
+    orig_tbd = Particle.two_body_decay
+
+    def tbd(self, p1_dict, p2_dict, angular_information="Isotropic"):
+        router.set_current(dark_key(self._pkey, "TwoBody_BSMDecay"))
+        return orig_tbd(self, p1_dict, p2_dict, angular_information)
+
+    Particle.two_body_decay = tbd
+    # set_dark_samples (dark_shower.py:196-201) loads a map entry for every
+    # active process, TwoBody_BSMDecay included, which is never sampled; the
+    # rebuilt dark_maps.pkl holds the four sampled processes only
+    orig_lds = DarkShower.load_dark_sample
+
+    def lds(self, dict_dir, process):
+        return [] if process == "TwoBody_BSMDecay" else orig_lds(self, dict_dir, process)
+
+    DarkShower.load_dark_sample = lds
+    try:
+        for mV in (0.01, 0.03, 0.1, 0.3):
+            router.streams.clear()
+            ds = DarkShower(dict_dir, "graphite", 0.010, mV)
+            orig_pb = ds.produce_bsm_particle
+
+            def pb(p_original, process, weight=None, VB=False, _orig=orig_pb):
+                router.set_current(dark_key(p_original._pkey, process))
+                return _orig(p_original, process, weight=weight, VB=VB)
+
+            ds.produce_bsm_particle = pb
+            parts = []
+            for j, p4 in enumerate(beam):
+                part = Particle(list(p4), [0.0, 0.0, 0.01 * j], {"PID": 111, "weight": 1.0 / len(beam), "ID": j + 1})
+                part._pkey = primary_key(j)
+                parts.append(part)
+                if j % 13 == 5:          # SM particles in between
+                    sm = Particle([3.0 + j, 0.0, 0.0, 3.0 + j], [0.0, 0.0, 0.0], {"PID": 22, "ID": 100 + j})
+                    sm._pkey = primary_key(1000 + j)
+                    parts.append(sm)
+            _, vs = ds.generate_dark_shower(ExDir=list(parts))
+            index = {id(p): k for k, p in enumerate(parts)}
+            rows = []
+            for v in vs:
+                d = v.get_ids()
+                src = next(k for k, p in enumerate(parts) if p.get_ids()["ID"] == d["parent_ID"]
+                           and p.get_ids()["PID"] == d["parent_PID"])
+                rows.append([src, V_PROC_CODE.get(d["generation_process"], 8), d["weight"], *v.get_p0(),
+                             *v.get_r0(), d["ID"], d["parent_ID"], d["mass"] if d["mass"] is not None else -1.0])
+            out[f"m{mV}/V"] = np.array(rows).reshape(-1, 13)
+            out[f"m{mV}/parts_f64"] = np.array([[*p.get_p0(), *p.get_r0(), p.get_ids()["weight"],
+                                                  p.get_ids()["mass"]] for p in parts])
+            out[f"m{mV}/parts_i64"] = np.array([[p.get_ids()["PID"], p.get_ids()["ID"]] for p in parts])
+            out[f"m{mV}/parts_pkey"] = np.array([p._pkey for p in parts], np.uint64)
+            out[f"m{mV}/weights"] = np.array([ds.GetBSMWeights(p, "TwoBody_BSMDecay") for p in parts])
+            print(f"mesons mV={mV}: {len(parts)} inputs, {len(vs)} V")
+        eta = Particle([5.0, 0.0, 0.0, math.sqrt(25.0 - 0.547862 ** 2)], [0, 0, 0], {"PID": 221})
+        eta._pkey = primary_key(7)
+        try:
+            ds.generate_dark_shower(ExDir=[eta])
+            out["eta/raises"] = np.array(0)
+        except KeyError:
+            out["eta/raises"] = np.array(1)
+    finally:
+        Particle.two_body_decay = orig_tbd
+        DarkShower.load_dark_sample = orig_lds
+        uninstall_dark(saved_d)
+        uninstall(saved)
+    np.savez_compressed(out_path, **out)
+
+
 BETHE_CASES = [
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 6, 0.000511),
     ("pos3_lead", "lead", 0.010, -11, 3.0, 2, 0.000511),
@@ -629,3 +711,6 @@ if __name__ == "__main__":
         gen_dark(d, os.path.join(HERE, "dark.npz"))
     if which in ("all", "moliere"):
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
+    if which in ("all", "mesons"):
+        gen_mesons(d, os.path.join(HERE, "mesons.npz"),
+                   os.path.join(refimport.REFERENCE, "examples", "beams", "Pi0_8GeVProtons_1000POT.npy"))

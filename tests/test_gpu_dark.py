@@ -257,3 +257,55 @@ def test_dark_on_gpu_showers_matches_oracle(showers):
     np.testing.assert_allclose(res["p4"][o][:, 0], want[:, 3], rtol=1e-12, atol=0)
     for p_ in range(3):
         np.testing.assert_allclose(res["yield"][p_], want[want[:, 1] == p_, 2].sum(), rtol=1e-12)
+
+
+MESONS = np.load(os.path.join(GOLDEN, "mesons.npz"))
+
+
+@pytest.mark.parametrize("mV", [0.01, 0.1, 0.3])
+def test_two_body_meson_decay_dropin(mV):
+    """generate_dark_shower(ExDir=[Particle, ...]) with pi0s from the
+    reference's beam file and photons in between, default active processes
+    (TwoBody_BSMDecay included): the reference's vectors, in its order, with
+    its IDs, weights, masses and momenta."""
+    from petite_gb300 import Particle
+    from petite_gb300.dark import DarkShower
+    pre = f"m{mV}"
+    F, I, K = MESONS[f"{pre}/parts_f64"], MESONS[f"{pre}/parts_i64"], MESONS[f"{pre}/parts_pkey"]
+    parts = []
+    for k in range(len(F)):
+        ids = {"PID": int(I[k, 0]), "ID": int(I[k, 1]), "weight": float(F[k, 7])}
+        p = Particle(list(F[k, 0:4]), list(F[k, 4:7]), ids)
+        assert p.get_ids()["mass"] == F[k, 8]     # the invariant, rounded as the reference rounds it
+        p._pkey = int(K[k])
+        parts.append(p)
+    ds = DarkShower(None, "graphite", 0.010, mV, seed=SEED)
+    w = np.array([ds.GetBSMWeights(p, "TwoBody_BSMDecay") for p in parts])
+    np.testing.assert_allclose(w, MESONS[f"{pre}/weights"], rtol=1e-15, atol=0)
+    _, vs = ds.generate_dark_shower(ExDir=parts)
+    V = MESONS[f"{pre}/V"]
+    assert len(vs) == len(V)
+    for v, row in zip(vs, V):
+        d = v.get_ids()
+        assert d["parent_ID"] == parts[int(row[0])].get_ids()["ID"]
+        assert (d["generation_process"] == "TwoBody_BSMDecay") == (row[1] == 8)
+        assert (d["ID"], d["parent_ID"]) == (int(row[10]), int(row[11]))
+        assert d["weight"] == pytest.approx(row[2], rel=1e-14)
+        np.testing.assert_allclose(v.get_p0(), row[3:7], rtol=0, atol=1e-12 * np.abs(row[3:7]).max())
+        np.testing.assert_array_equal(v.get_r0(), row[7:10])
+        if row[1] == 8:
+            assert d["mass"] == row[12]
+
+
+def test_eta_input_raises_like_the_reference():
+    """The reference's GetBSMWeights has no threshold entry for eta and eta'
+    (dark_shower.py:604) and raises KeyError."""
+    from petite_gb300 import Particle
+    from petite_gb300.dark import DarkShower
+    assert int(MESONS["eta/raises"]) == 1
+    ds = DarkShower(None, "graphite", 0.010, 0.03, seed=SEED)
+    eta = Particle([5.0, 0.0, 0.0, math.sqrt(25.0 - 0.547862 ** 2)], [0, 0, 0], {"PID": 221})
+    with pytest.raises(KeyError):
+        ds.generate_dark_shower(ExDir=[eta])
+    with pytest.raises(KeyError):
+        ds.GetBSMWeights(eta, "DarkBrem")

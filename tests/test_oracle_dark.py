@@ -121,3 +121,43 @@ def test_reference_gradient_matches_finite_differences(proc):
         assert gy != 0.0
         assert abs(gy - (yp - ym) / (2 * h)) <= 1e-5 * abs(gy)
         assert abs(gm - (mp - mm) / (2 * h)) <= 1e-5 * abs(gm)
+
+
+MESONS = np.load(os.path.join(GOLDEN, "mesons.npz"))
+REF_ORDER = ("DarkBrem", "DarkAnn", "DarkComp", "TwoBody_BSMDecay", "DarkMuonBrem")   # dark_shower.py:49
+
+
+class _In:
+    """An input Particle of generate_dark_shower(ExDir=list): pf = p0, rf = r0."""
+    def __init__(self, f, i, key):
+        self.p0 = self.pf = tuple(f[0:4])
+        self.r0 = self.rf = tuple(f[4:7])
+        self.weight, self.mass = f[7], f[8]
+        self.pid = int(i[0])
+        self.pkey = int(key)
+
+
+@pytest.mark.parametrize("mV", [0.01, 0.03, 0.1, 0.3])
+def test_two_body_meson_decay_matches_reference(mV):
+    """pi0 inputs from the reference's beam file (with photons in between)
+    through generate_dark_shower: TwoBody_BSMDecay weights and V momenta."""
+    pre = f"m{mV}"
+    F, I, K = MESONS[f"{pre}/parts_f64"], MESONS[f"{pre}/parts_i64"], MESONS[f"{pre}/parts_pkey"]
+    recs = [_In(F[k], I[k], K[k]) for k in range(len(F))]
+    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, "graphite", mV), OracleTables(BUNDLED_NPZ, "graphite"), SEED)
+    w = np.array([orc.weight(r.pid, r.p0[0], D.TWOBODY, r.mass) for r in recs])
+    np.testing.assert_allclose(w, MESONS[f"{pre}/weights"], rtol=1e-15, atol=0)
+    out = orc.dark_shower(recs, processes=REF_ORDER)
+    V = MESONS[f"{pre}/V"]
+    assert len(out) == len(V)
+    code = {"TwoBody_BSMDecay": 8, "DarkComp": 2}
+    got = np.array([[k, code[p], wt, *v, *r] for k, p, wt, v, r in out])
+    np.testing.assert_array_equal(got[:, :2], V[:, :2])
+    np.testing.assert_allclose(got[:, 2], V[:, 2], rtol=1e-14, atol=0)
+    np.testing.assert_array_equal(got[:, 7:10], V[:, 7:10])
+    scale = np.abs(V[:, 3:7]).max(1)
+    assert (np.abs(got[:, 3:7] - V[:, 3:7]).max(1) <= 1e-13 * scale).all()
+    if mV >= 0.135:
+        assert not (V[:, 1] == 8).any()          # above the pi0 mass: no decay
+    else:
+        assert (V[:, 1] == 8).sum() == 40
