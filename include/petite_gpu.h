@@ -277,7 +277,7 @@ typedef struct pt_dark_maps {
  * 3 = muon DarkMuonBrem. */
 typedef struct pt_dark_params {
   int32_t mass_index;             /* map block sampled (the mV estimator) */
-  int32_t bound_electron;         /* 1: bound-electron DarkAnn/DarkComp (the reference default) */
+  int32_t bound_electron;         /* 1: bound-electron DarkAnn/DarkComp (the reference default); 0: free */
   int32_t active;                 /* bit p: dark process p active; bit PT_TWOBODY: TwoBody_BSMDecay */
   double mV;                      /* vector mass used in the cross sections and kinematics */
   double coupling;                /* g_e^2 / (4 pi alpha_em) */
@@ -297,6 +297,13 @@ typedef struct pt_dark_params {
   const double* nsc_ly;
   int32_t nsc_n;
   double kinetic_mixing;          /* DarkShower(kinetic_mixing): the TwoBody_BSMDecay weight */
+  /* bound_electron = 0 (free electrons): the DarkAnn weight adds a closed-form
+   * resonant part (dark_shower.py:619-630) */
+  double ann_E0;                  /* first energy of the free DarkAnn cross section (get_DarkAnnXSec()[0][0]) */
+  double ann_K;                   /* (1/dEdx[GeV/cm]) (2 pi^2 alpha/m_e) n_e GeVsqcm2, the reference's order */
+  const double* ii_x[3];          /* interaction integrals of Brem, Ann, Bhabha (shower.py:296-314): */
+  const double* ii_y[3];          /*   interp1d(fill 0) tables behind _positron_exponential_factor */
+  int32_t ii_n[3];
 } pt_dark_params;
 
 /* Vectors produced by pt_run_dark (device pointers; SoA like pt_particles). */

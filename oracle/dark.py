@@ -431,8 +431,9 @@ class DarkTables:
     ``dark_tables.npz`` (maps rebuilt with PETITE's find_maxes; weight, dR/dE
     and bound-electron tables as PETITE's DarkShower constructor builds them)."""
 
-    def __init__(self, npz_path, target, mV, maxF_fudge=1.0, Zeff=29.508, kinetic_mixing=1.0):
+    def __init__(self, npz_path, target, mV, maxF_fudge=1.0, Zeff=29.508, kinetic_mixing=1.0, bound_electron=True):
         z = np.load(npz_path, allow_pickle=False)
+        self.bound = bound_electron
         masses = [float(m) for m in z["masses"]]
         targets = [str(t) for t in z["targets"]]
         if target not in targets:
@@ -470,6 +471,23 @@ class DarkTables:
         DCS = z[f"{pre}/xsec/DarkComp_bound"]
         nZ = self.rho / P.m_proton_grams / self.A
         ne = nZ * self.Z
+        self.ne = ne
+        if not bound_electron:
+            # free electrons (bound_electron=False): dark_xsec.pkl's DarkAnn and
+            # DarkComp, the annihilation weights and dR/dE with the resonant bin,
+            # the thresholds (dark_shower.py:229-245,254-309,382-452,495-593)
+            fpre = f"{pre}/free"
+            DCS = z[f"{fpre}/xsec/DarkComp"]
+            self.ann_E0 = float(z[f"{fpre}/xsec/DarkAnn"][0, 0])
+            md = z[f"{fpre}/min_dark"]
+            self.min_dark = {(11, "DarkBrem"): md[0], (-11, "DarkBrem"): md[1], (-11, "DarkAnn"): md[2],
+                             (22, "DarkComp"): md[3], (13, "DarkMuonBrem"): md[4], (-13, "DarkMuonBrem"): md[4]}
+            w = z[f"{fpre}/weights/ann"]
+            self.weights["ann"] = (w[:, 0].tolist(), w[:, 1].tolist())
+            self.drate["ann"] = (z[f"{fpre}/drate/ann/Ei"], z[f"{fpre}/drate/ann/bins"], z[f"{fpre}/drate/ann/nbins"])
+            # the positron interaction integrals of Shower.set_NSigmas (shower.py:296-314)
+            self.ii = {k: (z[f"{target}/ii/{k}"][:, 0].tolist(), z[f"{target}/ii/{k}"][:, 1].tolist())
+                       for k in ("Brem", "Ann", "Bhabha")}
         self.nsc = (np.log10(DCS[:, 0] + 1e-20).tolist(), np.log10(ne * P.GeVsqcm2 * DCS[:, 1] + 1e-20).tolist())
 
 
@@ -536,7 +554,32 @@ class DarkOracle:
             return d.coupling * nd / (interp(E, self.sm.ns["PairProd"]) + interp(E, self.sm.ns["Comp"]))
         name = {(11, "DarkBrem"): "brem_elec", (-11, "DarkBrem"): "brem_positron", (-11, "DarkAnn"): "ann",
                 (13, "DarkMuonBrem"): "muon_brem", (-13, "DarkMuonBrem"): "muon_brem"}[key]
+        if key == (-11, "DarkAnn") and not d.bound:
+            # dark_shower.py:619-630: the tabulated part above the first saved
+            # energy plus the resonant part in closed form
+            me = P.m_electron
+            E0s = d.ann_E0
+            sMAX = 2 * (me * min(E0s, E) + me ** 2)
+            beta = (2. * P.alpha_em / math.pi) * (math.log(sMAX / me ** 2) - 1.)
+            dEdxT_GeVpercm = d.dEdx * (0.1) * P.cmtom
+            base = np.float64(sMAX - d.mV ** 2)
+            with np.errstate(invalid="ignore"):
+                wa = (1 / dEdxT_GeVpercm) * (2 * math.pi ** 2 * P.alpha_em / me) * d.ne * P.GeVsqcm2 * float(base ** beta) \
+                    * self.positron_exponential_factor(d.E_res, E)
+            wn = interp(E, d.weights[name]) if E > E0s else 0.0
+            return d.coupling * (wn + wa)
         return d.coupling * interp(E, d.weights[name])
+
+    def positron_exponential_factor(self, E, Ei):
+        """Shower._positron_exponential_factor, shower.py:322-334."""
+        ii = self.d.ii
+        n_sigma_diff = (interp(Ei, ii["Brem"]) - interp(E, ii["Brem"])) \
+            + (interp(Ei, ii["Ann"]) - interp(E, ii["Ann"])) \
+            + (interp(Ei, ii["Bhabha"]) - interp(E, ii["Bhabha"]))
+        if n_sigma_diff < 0.0 or E > Ei:
+            return 0.0
+        dEdxT = self.d.dEdx * (0.1)
+        return math.exp(-n_sigma_diff / dEdxT / P.cmtom)
 
     # dark_shower.py:649-704
     def draw(self, E, process, s: Stream, count=None):
@@ -606,15 +649,21 @@ class DarkOracle:
             pf = P.lose_energy(ps, r.mass, E0 - E_int)
         E0 = pf[0]
         RM = P.rotation_matrix_from(pf)
-        if process == "DarkAnn" and E0 <= d.E_res:
+        if process == "DarkAnn" and E0 <= d.E_res and d.bound:
             v = (math.sqrt(E0 ** 2 - me ** 2 + mV ** 2), 0, 0, math.sqrt(E0 ** 2 - me ** 2))
-        elif process == "DarkComp" and E0 <= d.E_compth:
+        elif process == "DarkComp" and E0 <= d.E_compth and d.bound:
             v = (math.sqrt(E0 ** 2 + mV ** 2), 0, 0, E0)
+        elif process == "DarkAnn" and not d.bound and E0 <= d.ann_E0:
+            # dark_shower.py:767-768
+            v = (d.E_res, 0, 0, math.sqrt(d.E_res ** 2 - mV ** 2))
         else:
             x, _ = self.draw(E0, process, s)
             if x is None:
                 return None
-            if process == "DarkComp":
+            if process == "DarkComp" and not d.bound:
+                # compton_fourvecs with mV (kinematics.py:104-132)
+                v = P.compton(E0, x[0], 0 + (2.0 * math.pi - 0) * s.next(), mV)[1]
+            elif process == "DarkComp":
                 pe = draw_pe_sample(d.Zeff, s)
                 c0 = -1 + (1 - -1) * s.next()
                 ss = me ** 2 + 2 * E0 * (math.sqrt(me ** 2 + pe ** 2) - c0 * pe)

@@ -91,7 +91,8 @@ class PtDarkParams(C.Structure):
                 ("dr_Ei", C.c_void_p * 4), ("dr_bins", C.c_void_p * 4), ("dr_nbins", C.c_void_p * 4),
                 ("dr_n", C.c_int32 * 4), ("dr_nbmax", C.c_int32 * 4),
                 ("nsc_lx", C.c_void_p), ("nsc_ly", C.c_void_p), ("nsc_n", C.c_int32),
-                ("kinetic_mixing", C.c_double)]
+                ("kinetic_mixing", C.c_double), ("ann_E0", C.c_double), ("ann_K", C.c_double),
+                ("ii_x", C.c_void_p * 3), ("ii_y", C.c_void_p * 3), ("ii_n", C.c_int32 * 3)]
 
 
 class PtDarkOut(C.Structure):

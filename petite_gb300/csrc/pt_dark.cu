@@ -143,6 +143,24 @@ __device__ double bsm_weight(const Tabs& T, const pt_dark_params& P, int pid, do
     return P.coupling * nd / (nsig(T, 1, E) + nsig(T, 3, E));
   }
   const int w = (k == 4) ? 3 : k;
+  if (k == 2 && !P.bound_electron) {
+    // free electrons (dark_shower.py:619-630): the tabulated weight above the
+    // first saved energy plus the resonant weight in closed form,
+    // K (sMAX - mV^2)^beta exp(-(dII)/dEdx/cmtom) (shower.py:322-334)
+    const double me = kMe;
+    const double E0s = P.ann_E0;
+    const S sMAX = S(2.0) * (S(me) * S(E0s < E ? E0s : E) + S(me) * S(me));
+    const S beta = S(2.0) * S(kAlpha) / S(kPi) * (S(log((sMAX / (S(me) * S(me))).v)) - S(1.0));
+    double pef = 0.0;
+    const double Er = P.E_res;
+    const double ds = ((S(interp_tab(P.ii_x[0], P.ii_y[0], P.ii_n[0], E)) - S(interp_tab(P.ii_x[0], P.ii_y[0], P.ii_n[0], Er))) +
+                       (S(interp_tab(P.ii_x[1], P.ii_y[1], P.ii_n[1], E)) - S(interp_tab(P.ii_x[1], P.ii_y[1], P.ii_n[1], Er))) +
+                       (S(interp_tab(P.ii_x[2], P.ii_y[2], P.ii_n[2], E)) - S(interp_tab(P.ii_x[2], P.ii_y[2], P.ii_n[2], Er)))).v;
+    if (!(ds < 0.0 || Er > E)) pef = exp((S(-ds) / S(T.t.dEdx_GeV_per_m) / S(kCmToM)).v);
+    const double wa = (S(P.ann_K) * S(pow((sMAX - S(P.mV) * S(P.mV)).v, beta.v)) * S(pef)).v;
+    const double wn = E > E0s ? interp_tab(P.w_x[w], P.w_y[w], P.w_n[w], E) : 0.0;
+    return (S(P.coupling) * (S(wn) + S(wa))).v;
+  }
   return P.coupling * interp_tab(P.w_x[w], P.w_y[w], P.w_n[w], E);
 }
 
@@ -275,6 +293,9 @@ __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_
     v = {sqrt((S(E0) * S(E0) - S(me) * S(me) + S(mV) * S(mV)).v), 0.0, 0.0, pz};
   } else if (p == PT_DARKCOMP && bound && E0 <= P.E_compth) {
     v = {sqrt((S(E0) * S(E0) + S(mV) * S(mV)).v), 0.0, 0.0, E0};
+  } else if (p == PT_DARKANN && !bound && E0 <= P.ann_E0) {
+    // free electrons below the first saved energy (dark_shower.py:767-768)
+    v = {P.E_res, 0.0, 0.0, sqrt((S(P.E_res) * S(P.E_res) - S(mV) * S(mV)).v)};
   } else {
     double x[4] = {0, 0, 0, 0};
     int key;

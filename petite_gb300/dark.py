@@ -93,7 +93,10 @@ class DarkData:
                     offset=np.concatenate(offs), ninc=np.concatenate(ninc), nodes=np.concatenate(nodes),
                     base=base, rows=rows)
 
-    def params_for(self, mV_est: float, target: str) -> dict:
+    def params_for(self, mV_est: float, target: str, bound_electron: bool = True) -> dict:
+        """The tables of one (mass, target).  bound_electron=False swaps in the
+        free-electron DarkAnn/DarkComp cross sections, annihilation weights and
+        dR/dE, thresholds, and the positron interaction integrals."""
         pre = f"m{mV_est}/{target}"
         z = self.z
         out = {"E_res": float(z[f"{pre}/E_res"]), "E_compth": float(z[f"{pre}/E_compth"]),
@@ -104,6 +107,17 @@ class DarkData:
             out[f"dr/{k}/Ei"] = z[f"{pre}/drate/{k}/Ei"]
             out[f"dr/{k}/bins"] = z[f"{pre}/drate/{k}/bins"]
             out[f"dr/{k}/nbins"] = z[f"{pre}/drate/{k}/nbins"].astype(np.int32)
+        if not bound_electron:
+            f = f"{pre}/free"
+            out["min_dark"] = z[f"{f}/min_dark"].astype(np.float64)
+            out["xsec_DarkComp"] = z[f"{f}/xsec/DarkComp"]
+            out["ann_E0"] = float(z[f"{f}/xsec/DarkAnn"][0, 0])
+            out["w/ann"] = z[f"{f}/weights/ann"]
+            out["dr/ann/Ei"] = z[f"{f}/drate/ann/Ei"]
+            out["dr/ann/bins"] = z[f"{f}/drate/ann/bins"]
+            out["dr/ann/nbins"] = z[f"{f}/drate/ann/nbins"].astype(np.int32)
+            for k in ("Brem", "Ann", "Bhabha"):
+                out[f"ii/{k}"] = z[f"{target}/ii/{k}"]
         return out
 
 
@@ -249,6 +263,13 @@ class DarkEngine:
         return g
 
 
+def _ann_K(sh) -> float:
+    """(1/dEdxT_GeVpercm) (2 pi^2 alpha/m_e) n_e GeVsqcm2 in the order of
+    dark_shower.py:627 (the free-electron resonant DarkAnn weight's prefactor)."""
+    dEdxT_GeVpercm = sh.get_material_properties()[3] * (0.1) * T.CMTOM
+    return (1 / dEdxT_GeVpercm) * (2 * np.pi ** 2 * T.ALPHA_EM / T.M_ELECTRON) * (sh.get_n_targets()[1]) * T.GEVSQCM2
+
+
 def _active_bits(processes) -> int:
     """pt_dark_params.active: bit p for engine process p, bit TWOBODY for the meson decay."""
     bits = sum(1 << DARK_CODE[p] for p in processes if p in DARK_CODE)
@@ -258,7 +279,7 @@ def _active_bits(processes) -> int:
 def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, active, coupling, Zeff):
     """pt_dark_params for one DarkShower (tables kept alive on the engine)."""
     import torch
-    d = engine.data.params_for(mV_est, sh.get_target_material())
+    d = engine.data.params_for(mV_est, sh.get_target_material(), bound)
     dev = engine.device
     keep = {}
     prm = _lib.PtDarkParams()
@@ -267,6 +288,14 @@ def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, 
     prm.active = _active_bits(active)
     prm.mV, prm.coupling, prm.Zeff = float(mV), float(coupling), float(Zeff)
     prm.kinetic_mixing = float(sh.kinetic_mixing)
+    if not bound:
+        prm.ann_E0 = d["ann_E0"]
+        prm.ann_K = _ann_K(sh)
+        for k, name in enumerate(("Brem", "Ann", "Bhabha")):
+            t = d[f"ii/{name}"]
+            keep[f"iix{k}"] = torch.as_tensor(np.ascontiguousarray(t[:, 0]), device=dev)
+            keep[f"iiy{k}"] = torch.as_tensor(np.ascontiguousarray(t[:, 1]), device=dev)
+            prm.ii_x[k], prm.ii_y[k], prm.ii_n[k] = keep[f"iix{k}"].data_ptr(), keep[f"iiy{k}"].data_ptr(), len(t)
     prm.E_res, prm.E_compth = d["E_res"], d["E_compth"]
     for i in range(5):
         prm.min_dark[i] = float(d["min_dark"][i])
@@ -304,8 +333,6 @@ class DarkShower(Shower):
         super().__init__(dict_dir, target_material, min_energy, maxF_fudge_global=maxF_fudge_global,
                          max_n_integrators=max_n_integrators, fast_MCS_mode=fast_MCS_mode, seed=seed,
                          rescale_MCS=rescale_MCS, device=device)
-        if not bound_electron:
-            raise NotImplementedError("bound_electron=False (free-electron DarkAnn/DarkComp) is not implemented")
         self.active_processes = list(DARK_PROCESS_CODES if active_processes is None else active_processes)
         self.kinetic_mixing = kinetic_mixing
         self.bound_electron = bound_electron
@@ -412,7 +439,7 @@ class DarkShower(Shower):
         arithmetic of the device's weight (the single-particle API; the
         shower path evaluates the weights in pt_run_dark)."""
         W = np.zeros((len(parts), len(DARK_PROCESSES)))
-        pd = self._dark.params_for(self._mV_estimator, self.get_target_material())
+        pd = self._dark.params_for(self._mV_estimator, self.get_target_material(), self.bound_electron)
         md = pd["min_dark"]
         slots = {(11, "DarkBrem"): 0, (-11, "DarkBrem"): 1, (-11, "DarkAnn"): 2, (22, "DarkComp"): 3,
                  (13, "DarkMuonBrem"): 4, (-13, "DarkMuonBrem"): 4}
@@ -437,8 +464,26 @@ class DarkShower(Shower):
                 else:
                     w = pd[f"w/{_TABLES[3 if k == 4 else k]}"]
                     v = 0.0 if (E < w[0, 0] or E > w[-1, 0]) else np.interp(E, w[:, 0], w[:, 1])
+                    if k == 2 and not self.bound_electron:
+                        v = (v if E > pd["ann_E0"] else 0.0) + self._ann_resonant_weight(pd, E)
                     W[i, c] = self._coupling * v
         return W
+
+    def _ann_resonant_weight(self, pd, E):
+        """The closed-form resonant DarkAnn weight of free electrons
+        (dark_shower.py:621-627), as pt_run_dark evaluates it."""
+        me = T.M_ELECTRON
+        sMAX = 2 * (me * min(pd["ann_E0"], E) + me ** 2)
+        beta = (2. * T.ALPHA_EM / np.pi) * (np.log(sMAX / me ** 2) - 1.)
+        Er = self._resonant_annihilation_energy
+
+        def ii(name, x):
+            t = pd[f"ii/{name}"]
+            return 0.0 if (x < t[0, 0] or x > t[-1, 0]) else float(np.interp(x, t[:, 0], t[:, 1]))
+        ds = (ii("Brem", E) - ii("Brem", Er)) + (ii("Ann", E) - ii("Ann", Er)) + (ii("Bhabha", E) - ii("Bhabha", Er))
+        pef = 0.0 if (ds < 0.0 or Er > E) else np.exp(-ds / (self.get_material_properties()[3] * 0.1) / T.CMTOM)
+        with np.errstate(invalid="ignore"):
+            return _ann_K(self) * np.float64(sMAX - self._mV ** 2) ** beta * pef
 
     def produce_bsm_particle(self, p_original, process, weight=None, VB=False):
         """dark_shower.py:721-804 for one particle; returns a Particle or None."""

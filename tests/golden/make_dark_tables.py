@@ -11,6 +11,7 @@ The arrays are read back from the constructed object.  The VEGAS maps and
 max_F come from ``dark_maps.pkl`` rebuilt by ``rebuild_maps.py --dark``.
 
 Usage: python tests/golden/make_dark_tables.py DARK_DICT_DIR SM_DICT_DIR [OUT.npz]
+       python tests/golden/make_dark_tables.py --add-free DARK_DICT_DIR SM_DICT_DIR [OUT.npz]
 (SM_DICT_DIR: the output of rebuild_maps.py, which DarkShower's Shower base reads)
 """
 import multiprocessing as mp
@@ -84,7 +85,72 @@ def one(args):
     return mV, target, out
 
 
+def one_free(args):
+    """The free-electron tables (DarkShower(bound_electron=False)): the
+    DarkAnn/DarkComp cross sections of dark_xsec.pkl, the annihilation weights
+    and dR/dE with the resonant bin (dark_shower.py:382-400,495-517), the
+    thresholds, and the positron interaction integrals (shower.py:296-314)
+    behind the analytic resonant weight (dark_shower.py:621-629).  The private
+    directory has no dark_weights.pkl or dark_drate.pkl: with a cached entry
+    for the mass and target, set_drate_dE indexes a float with a string
+    (dark_shower.py:550) and raises TypeError in this mode."""
+    dict_dir, sm_dir, mV, target = args
+    refimport.setup()
+    from PETITE.dark_shower import DarkShower
+    work = tempfile.mkdtemp(prefix="darkfree_")
+    for d in (dict_dir, sm_dir):
+        for f in os.listdir(d):
+            if f in ("dark_weights.pkl", "dark_drate.pkl") or os.path.exists(os.path.join(work, f)):
+                continue
+            os.symlink(os.path.realpath(os.path.join(d, f)), os.path.join(work, f))
+    t0 = time.time()
+    sh = DarkShower(work + "/", target, 0.010, mV, active_processes=list(PROCS), bound_electron=False)
+    out = {"free/xsec/DarkAnn": np.asarray(sh.get_DarkAnnXSec(), float),
+           "free/xsec/DarkComp": np.asarray(sh.get_DarkCompXSec(), float)}
+    f = sh._annihilation_numerical_weight
+    out["free/weights/ann"] = np.c_[np.asarray(f.x, float), np.asarray(f.y, float)]
+    d = sh._d_rate_dict_positron_ann
+    Ei = np.array(sorted(d.keys()), float)
+    bins = [np.asarray(d[e], float).reshape(-1, 2) for e in Ei]
+    nb = max(len(b) for b in bins)
+    arr = np.zeros((len(Ei), nb, 2))
+    cnt = np.zeros(len(Ei), np.int32)
+    for i, b in enumerate(bins):
+        arr[i, :len(b)] = b
+        cnt[i] = len(b)
+    out["free/drate/ann/Ei"], out["free/drate/ann/bins"], out["free/drate/ann/nbins"] = Ei, arr, cnt
+    mc = sh._minimum_calculable_dark_energy
+    out["free/min_dark"] = np.array([mc[11]["DarkBrem"], mc[-11]["DarkBrem"], mc[-11]["DarkAnn"], mc[22]["DarkComp"],
+                                     mc[13]["DarkMuonBrem"]])
+    ii = {}
+    for name in ("Brem", "Ann", "Bhabha"):
+        g = getattr(sh, f"_interaction_integral_{name}")
+        ii[f"ii/{name}"] = np.c_[np.asarray(g.x, float), np.asarray(g.y, float)]
+    shutil.rmtree(work, ignore_errors=True)
+    print(f"free mV={mV} {target}: {time.time() - t0:.0f} s", flush=True)
+    return mV, target, out, ii
+
+
+def add_free(dict_dir, sm_dir, path):
+    """Adds the free-electron tables to an existing bundle."""
+    res = dict(np.load(path))
+    jobs = [(dict_dir, sm_dir, mV, t) for mV in MASSES for t in TARGETS]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 1)) as pool:
+        for mV, t, out, ii in pool.imap_unordered(one_free, jobs):
+            for k, v in out.items():
+                res[f"m{mV}/{t}/{k}"] = v
+            for k, v in ii.items():
+                res[f"{t}/{k}"] = v
+    np.savez_compressed(path, **res)
+    print("wrote", path, os.path.getsize(path) // 1024, "KB")
+
+
 def main():
+    if sys.argv[1] == "--add-free":
+        refimport.setup()
+        add_free(os.path.abspath(sys.argv[2]), os.path.abspath(sys.argv[3]), sys.argv[4] if len(sys.argv) > 4 else
+                 os.path.join(os.path.dirname(os.path.dirname(HERE)), "petite_gb300", "data", "dark_tables.npz"))
+        return
     dict_dir = os.path.abspath(sys.argv[1])
     sm_dir = os.path.abspath(sys.argv[2])
     out_path = sys.argv[3] if len(sys.argv) > 3 else os.path.join(
@@ -119,6 +185,7 @@ def main():
                 res[f"m{mV}/{t}/{k}"] = v
     np.savez_compressed(out_path, **res)
     print("wrote", out_path, os.path.getsize(out_path) // 1024, "KB")
+    add_free(dict_dir, sm_dir, out_path)
 
 
 if __name__ == "__main__":

@@ -19,7 +19,7 @@ The particle being processed is tracked by wrapping the Shower instance's
 ``propagate_particle`` and ``sample_scattering``; daughters get the keys of
 ``oracle.philox.daughter_key``.
 
-Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|moliere|mesons|all]
+Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|darkfree|moliere|mesons|all]
 (DICT_DIR from rebuild_maps.py; for ``dark`` it must also hold the output of
 ``rebuild_maps.py --dark``)
 """
@@ -686,6 +686,83 @@ def gen_mesons(dict_dir, out_path, beam_path):
     np.savez_compressed(out_path, **out)
 
 
+def gen_dark_free(dict_dir, out_path):
+    """DarkShower(bound_electron=False): GetBSMWeights of DarkAnn (with the
+    closed-form resonant part, dark_shower.py:619-630) and DarkComp over
+    energy, and generate_dark_shower on routed SM showers.  Each shower is
+    built in a private directory without dark_weights.pkl and
+    dark_drate.pkl: with a cached entry for its mass and target,
+    set_drate_dE raises TypeError in this mode (dark_shower.py:550)."""
+    import shutil
+    import tempfile
+    refimport.setup()
+    from PETITE.dark_shower import DarkShower
+    from PETITE.particle import Particle
+    from oracle.dark import dark_key
+    out = {}
+    router = StreamRouter(SEED)
+    saved = install(router)
+    saved_d = install_dark(router)
+    try:
+        for name, mV, t, pid, E0, n in (("e10_graphite_m0.01", 0.01, "graphite", 11, 10.0, 2),
+                                        ("e5_lead_m0.03", 0.03, "lead", 11, 5.0, 2),
+                                        ("g5_lead_m0.01", 0.01, "lead", 22, 5.0, 2)):
+            work = tempfile.mkdtemp(prefix="darkfree_")
+            for f in os.listdir(dict_dir):
+                if f not in ("dark_weights.pkl", "dark_drate.pkl"):
+                    os.symlink(os.path.realpath(os.path.join(dict_dir, f)), os.path.join(work, f))
+            ds = DarkShower(work + "/", t, 0.010, mV, active_processes=list(DARK_PROCS), bound_electron=False)
+            shutil.rmtree(work, ignore_errors=True)
+            E_res = ds._resonant_annihilation_energy
+            Es = np.concatenate([E_res * np.array([0.999, 1.0, 1.0 + 1e-6, 1.0001, 1.001, 1.01]),
+                                 np.geomspace(E_res * 1.02, 100.0, 30)])
+            out[f"{name}/ann_weights"] = np.c_[Es, [ds.GetBSMWeights([-11, e], "DarkAnn") for e in Es]]
+            Ec = np.geomspace(1e-3, 100.0, 40)
+            out[f"{name}/comp_weights"] = np.c_[Ec, [ds.GetBSMWeights([22, e], "DarkComp") for e in Ec]]
+            router.streams.clear()
+            wrap_shower(ds, router)
+            orig_pb = ds.produce_bsm_particle
+            where = {}
+
+            def pb(p_original, process, weight=None, VB=False, _orig=orig_pb, _where=where):
+                router.set_current(dark_key(p_original._pkey, process))
+                v = _orig(p_original, process, weight=weight, VB=VB)
+                if v is not None:
+                    _where[id(v)] = (id(p_original), process)
+                return v
+
+            ds.produce_bsm_particle = pb
+            SMF, SMI, SMK, VV = [], [], [], []
+            for j in range(n):
+                m = 0.0 if pid == 22 else 0.000511
+                part = Particle([E0, 0.0, 0.0, math.sqrt(E0 * E0 - m * m)], [0.0, 0.0, 0.0], {"PID": pid})
+                part._pkey = primary_key(j)
+                sm = ds.generate_shower(part)
+                f, i, _, k, _ = shower_arrays(sm, router, j)
+                base = sum(len(x) for x in SMF)
+                index = {id(p): base + r for r, p in enumerate(sm)}
+                _, vs = ds.generate_dark_shower(ExDir=list(sm))
+                for v in vs:
+                    src, pc = where[id(v)]
+                    d = v.get_ids()
+                    VV.append(np.concatenate([[index[src], V_PROC_CODE[d["generation_process"]],
+                                               DARK_PROCS.index(pc), d["weight"]], v.get_p0(), v.get_r0()]))
+                SMF.append(f); SMI.append(i); SMK.append(k)
+            out[f"{name}/sm_f64"] = np.concatenate(SMF)
+            out[f"{name}/sm_i64"] = np.concatenate(SMI)
+            out[f"{name}/sm_pkey"] = np.concatenate(SMK)
+            out[f"{name}/V"] = np.array(VV).reshape(-1, 11)
+            out[f"{name}/params"] = np.array([mV, E0, pid, n])
+            out[f"{name}/target"] = np.array(t)
+            procs = np.array(VV).reshape(-1, 11)[:, 2] if VV else np.array([])
+            print(f"dark free {name}: {len(out[f'{name}/sm_f64'])} SM rows, {len(VV)} V, "
+                  f"per process {np.bincount(procs.astype(int), minlength=4) if len(procs) else []}")
+    finally:
+        uninstall_dark(saved_d)
+        uninstall(saved)
+    np.savez_compressed(out_path, **out)
+
+
 BETHE_CASES = [
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 6, 0.000511),
     ("pos3_lead", "lead", 0.010, -11, 3.0, 2, 0.000511),
@@ -711,6 +788,8 @@ if __name__ == "__main__":
         gen_dark(d, os.path.join(HERE, "dark.npz"))
     if which in ("all", "moliere"):
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
+    if which in ("all", "darkfree"):
+        gen_dark_free(d, os.path.join(HERE, "dark_free.npz"))
     if which in ("all", "mesons"):
         gen_mesons(d, os.path.join(HERE, "mesons.npz"),
                    os.path.join(refimport.REFERENCE, "examples", "beams", "Pi0_8GeVProtons_1000POT.npy"))

@@ -64,10 +64,12 @@ def test_draw_dark_sample_matches_reference(showers):
         np.testing.assert_allclose(x[0, :D.DARK_DIM[proc]], row[3:3 + D.DARK_DIM[proc]], rtol=1e-12, atol=0)
 
 
-def _store_from_golden(sh, name):
+def _store_from_golden(sh, name, g=None, pre=None):
     import torch
     from petite_gb300.engine import ParticleStore
-    F, I, K = G[f"shower/{name}/sm_f64"], G[f"shower/{name}/sm_i64"], G[f"shower/{name}/sm_pkey"]
+    g = G if g is None else g
+    pre = f"shower/{name}" if pre is None else pre
+    F, I, K = g[f"{pre}/sm_f64"], g[f"{pre}/sm_i64"], g[f"{pre}/sm_pkey"]
     n = len(F)
     st = ParticleStore(n, sh._engine.device)
     dev = sh._engine.device
@@ -309,3 +311,53 @@ def test_eta_input_raises_like_the_reference():
         ds.generate_dark_shower(ExDir=[eta])
     with pytest.raises(KeyError):
         ds.GetBSMWeights(eta, "DarkBrem")
+
+
+FREE = np.load(os.path.join(GOLDEN, "dark_free.npz"))
+FREE_CASES = ["e10_graphite_m0.01", "e5_lead_m0.03", "g5_lead_m0.01"]
+
+
+@pytest.fixture(scope="module")
+def free_showers():
+    from petite_gb300.dark import DarkShower
+    out = {}
+    for name in FREE_CASES:
+        mV, t = float(FREE[f"{name}/params"][0]), str(FREE[f"{name}/target"])
+        out[name] = DarkShower(None, t, 0.010, mV, seed=SEED, bound_electron=False,
+                               active_processes=["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"])
+    return out
+
+
+@pytest.mark.parametrize("name", FREE_CASES)
+def test_free_electron_weights_match_reference(free_showers, name):
+    """GetBSMWeights with bound_electron=False across the annihilation
+    resonance (tabulated plus closed-form parts) and for DarkComp."""
+    sh = free_showers[name]
+    A, Cw = FREE[f"{name}/ann_weights"], FREE[f"{name}/comp_weights"]
+    np.testing.assert_allclose([sh.GetBSMWeights([-11, e], "DarkAnn") for e in A[:, 0]], A[:, 1], rtol=1e-12, atol=0)
+    np.testing.assert_allclose([sh.GetBSMWeights([22, e], "DarkComp") for e in Cw[:, 0]], Cw[:, 1], rtol=1e-12,
+                               atol=0)
+
+
+@pytest.mark.parametrize("name", FREE_CASES)
+def test_free_electron_run_dark_matches_reference(free_showers, name):
+    """pt_run_dark with free electrons on the reference's routed SM showers:
+    its vectors exactly in integers, weights (the device's resonant DarkAnn
+    weight included) and energies to 1e-12."""
+    sh = free_showers[name]
+    st, n = _store_from_golden(sh, name, FREE, name)
+    res = sh._dark_engine.run_dark(sh._prm, st, n, sh._opts())
+    V = FREE[f"{name}/V"]
+    want = V[np.lexsort((V[:, 2], V[:, 0]))]
+    proc = res["process"]
+    o = np.lexsort((proc, res["parent"]))
+    assert res["n"] == len(want) > 300
+    assert (proc < 4).all()                          # no *_bound forms
+    assert np.array_equal(res["parent"][o], want[:, 0].astype(np.int64))
+    assert np.array_equal(proc[o], want[:, 2].astype(np.int64))
+    assert (want[:, 2] == 1).sum() > 0               # free DarkAnn vectors present
+    np.testing.assert_allclose(res["weight"][o], want[:, 3], rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(res["r"][o], want[:, 8:11])
+    np.testing.assert_allclose(res["p4"][o][:, 0], want[:, 4], rtol=1e-12, atol=0)
+    scale = np.abs(want[:, 4:8]).max(1)
+    assert (np.abs(res["p4"][o] - want[:, 4:8]).max(1) <= 1e-9 * scale).all()

@@ -161,3 +161,48 @@ def test_two_body_meson_decay_matches_reference(mV):
         assert not (V[:, 1] == 8).any()          # above the pi0 mass: no decay
     else:
         assert (V[:, 1] == 8).sum() == 40
+
+
+FREE = np.load(os.path.join(GOLDEN, "dark_free.npz"))
+FREE_CASES = ["e10_graphite_m0.01", "e5_lead_m0.03", "g5_lead_m0.01"]
+
+
+def _free_oracle(name):
+    mV = float(FREE[f"{name}/params"][0])
+    target = str(FREE[f"{name}/target"])
+    return D.DarkOracle(D.DarkTables(DARK_NPZ, target, mV, bound_electron=False), OracleTables(BUNDLED_NPZ, target),
+                        SEED)
+
+
+@pytest.mark.parametrize("name", FREE_CASES)
+def test_free_electron_weights_match_reference(name):
+    """GetBSMWeights with bound_electron=False: DarkAnn's tabulated plus
+    closed-form resonant parts across the resonance, and DarkComp over the
+    free cross section."""
+    orc = _free_oracle(name)
+    A = FREE[f"{name}/ann_weights"]
+    got = np.array([orc.weight(-11, e, "DarkAnn") for e in A[:, 0]])
+    assert (A[:, 1] > 0).sum() > 20
+    np.testing.assert_allclose(got, A[:, 1], rtol=1e-12, atol=0)
+    Cw = FREE[f"{name}/comp_weights"]
+    got = np.array([orc.weight(22, e, "DarkComp") for e in Cw[:, 0]])
+    np.testing.assert_allclose(got, Cw[:, 1], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("name", FREE_CASES)
+def test_free_electron_dark_shower_matches_reference(name):
+    orc = _free_oracle(name)
+    F, I, K = FREE[f"{name}/sm_f64"], FREE[f"{name}/sm_i64"], FREE[f"{name}/sm_pkey"]
+    recs = [_Rec(F[k], I[k], K[k]) for k in range(len(F))]
+    out = orc.dark_shower(recs)
+    V = FREE[f"{name}/V"]
+    got = np.array([[k, D.DARK_CODE[p], w, *v, *r] for k, p, w, v, r in out])
+    want = V[np.lexsort((V[:, 2], V[:, 0]))]
+    got = got[np.lexsort((got[:, 1], got[:, 0]))]
+    assert len(got) == len(want)
+    assert np.array_equal(got[:, :2], want[:, [0, 2]])
+    np.testing.assert_allclose(got[:, 2], want[:, 3], rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(got[:, 7:10], want[:, 8:11])
+    np.testing.assert_allclose(got[:, 3], want[:, 4], rtol=1e-12, atol=0)
+    scale = np.abs(want[:, 4:8]).max(1)
+    assert (np.abs(got[:, 3:7] - want[:, 4:8]).max(1) <= 1e-9 * scale).all()
