@@ -203,10 +203,19 @@ pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* wav
  *  refill_min[k]: idle lanes a warp gathers before refilling them, 1..32
  *                 (k = 0 propagation kernel, 1 sampler kernel; default 8)
  *  chunk[k]:      entries a warp claims from the wave's pool per atomic,
- *                 32..4096 (defaults 128 and 64) */
+ *                 32..4096 (defaults 128 and 64)
+ *  loop:          who runs the waves: PT_LOOP_HOST (0, default) launches the
+ *                 two kernels per wave and reads its counters back;
+ *                 PT_LOOP_GRAPH a CUDA graph whose conditional WHILE node
+ *                 repeats the wave with its plan made on the GPU;
+ *                 PT_LOOP_PERSISTENT one cooperative kernel runs every wave
+ *                 between grid barriers.  Results are identical. */
+enum { PT_LOOP_HOST = 0, PT_LOOP_GRAPH = 1, PT_LOOP_PERSISTENT = 2 };
 typedef struct pt_batch_tuning {
   int32_t refill_min[2];
   int32_t chunk[2];
+  int32_t loop;
+  int32_t reserved0;
 } pt_batch_tuning;
 /* Stores the settings on the handle (NULL restores the defaults);
  * PT_BAD_ARG for a value out of range. */
@@ -214,7 +223,8 @@ pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t);
 
 /* Device time of the last pt_run_batch on this handle, summed over its waves
  * and measured with CUDA events on the run's stream: the propagation kernel
- * and the sampler kernel, in milliseconds.  Diagnostic; no reference
+ * and the sampler kernel, in milliseconds (with PT_LOOP_GRAPH or
+ * PT_LOOP_PERSISTENT: the whole run, and 0).  Diagnostic; no reference
  * counterpart. */
 pt_status pt_last_kernel_times(pt_handle* h, double* propagate_ms, double* sample_ms);
 

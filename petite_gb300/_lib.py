@@ -102,7 +102,7 @@ class PtDarkOut(C.Structure):
 
 
 class PtBatchTuning(C.Structure):
-    _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2)]
+    _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class PetiteGPUError(RuntimeError):

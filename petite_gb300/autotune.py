@@ -2,9 +2,11 @@
 
 Picks, for one GPU, target and precision, the settings of
 ``pt_set_batch_tuning`` -- idle lanes gathered before a refill and pool
-entries claimed per atomic, for the propagation and the sampler kernel --
-by timing short calibration transports (CUDA events on the run's stream,
-``pt_last_kernel_times``) over a small grid, one coordinate at a time.
+entries claimed per atomic, for the propagation and the sampler kernel, and
+who runs the waves (the host, a CUDA graph's conditional loop, or one
+persistent kernel) -- by timing short calibration transports (CUDA events
+around the whole run on its stream) over a small grid, one coordinate at a
+time.
 Results are cached in ``$XDG_CACHE_HOME/petite_gb300/tuning.json`` (or
 ``~/.cache/...``) keyed by device name, target and precision.
 """
@@ -16,8 +18,10 @@ import os
 
 import numpy as np
 
-GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128)}
-DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64)}
+GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128),
+        "loop": ("host", "graph", "persistent")}
+DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host"}
+CACHE_VERSION = 2
 
 
 def _cache_path():
@@ -39,7 +43,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     ``{"refill_min": [p, s], "chunk": [p, s], "seconds": t}``."""
     import torch
     eng = shower._engine
-    key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}"
+    key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}|v{CACHE_VERSION}"
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -50,7 +54,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
             cache = {}
     if use_cache and key in cache:
         best = cache[key]
-        eng.set_tuning(best["refill_min"], best["chunk"])
+        eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"))
         return best
 
     p0, pid, m = _calibration_primaries(n, seed)
@@ -61,27 +65,34 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     M = torch.as_tensor(m, device=dev)
     tally = eng.new_tally(n, 1.0)
 
+    stream = torch.cuda.current_stream(dev)
+
     def run(cfg):
-        eng.set_tuning(cfg["refill_min"], cfg["chunk"])
+        eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"])
         opts = shower._opts(True, precision)
         tally.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
         eng.run_batch(None, None, None, None, opts, tally, queue_capacity=ring_capacity,
                       device_inputs=(P0, R0, PID, M))
-        tp, ts = eng.last_kernel_times()
-        return tp + ts
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
 
-    cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"])}
+    cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"]}
     run(cfg)                                            # warm-up (scratch, caches)
     best_t = run(cfg)
     for name, values in GRID.items():
         for v in values:
-            trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"])}
+            trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"]}
             if name == "refill_min":
                 trial["refill_min"] = [v, v]
             elif name == "chunk_propagate":
                 trial["chunk"][0] = v
-            else:
+            elif name == "chunk_sample":
                 trial["chunk"][1] = v
+            else:
+                trial["loop"] = v
             if trial == cfg:
                 continue
             t = run(trial)
@@ -89,8 +100,8 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
                 print("autotune", trial, round(t, 4))
             if t < best_t * 0.99:                       # a change must beat noise
                 best_t, cfg = t, trial
-    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "seconds": best_t}
-    eng.set_tuning(best["refill_min"], best["chunk"])
+    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "loop": cfg["loop"], "seconds": best_t}
+    eng.set_tuning(best["refill_min"], best["chunk"], best["loop"])
     if use_cache:
         cache[key] = best
         try:

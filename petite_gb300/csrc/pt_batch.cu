@@ -64,6 +64,19 @@ struct Tally {
   float z_max;
 };
 
+// The loop state when the GPU plans the waves itself (the graph-captured loop
+// and the persistent kernel): written by plan_step between waves.
+struct WavePlan {
+  unsigned long long head, tail;      // ring positions of the wave's first entry and of the append point
+  unsigned long long feed_at;         // ring position of this wave's fed primaries
+  long long fed;                      // primaries fed so far
+  long long n_in;                     // entries in this wave
+  long long feed_m;                   // primaries this wave feeds
+  long long waves;                    // waves run
+  int out_chunk;                      // as WaveCtx::out_chunk
+  int done;                           // 1: the run has ended (all primaries finished, or an error)
+};
+
 template <int PREC> struct WaveCtx {
   Tabs T;
   double min_energy, rescale;
@@ -84,7 +97,28 @@ template <int PREC> struct WaveCtx {
   int refill_min[2];                  // idle lanes a warp gathers before refilling: [0] propagation, [1] sampler
   int chunk[2];                       // pool entries a warp claims per atomic: [0] propagation, [1] sampler
   PhiloxRK rk;                        // round keys of `seed` (float32 kernels)
+  // device-planned waves (null: the host plans each wave and passes it here)
+  WavePlan* plan;
+  const double* in_p0;                // the run's primaries, for the planned feed
+  const double* in_r0;
+  const int32_t* in_pid;
+  const double* in_mass;
+  int64_t n_prim, prim_offset, cap, feed_max, slack;
 };
+
+// This wave's parameters: from the plan when the GPU plans, else from the launch.
+template <int PREC> __device__ __forceinline__ uint64_t w_head(const WaveCtx<PREC>& c) {
+  return c.plan ? (uint64_t)__ldcg(&c.plan->head) : c.head;
+}
+template <int PREC> __device__ __forceinline__ uint64_t w_tail(const WaveCtx<PREC>& c) {
+  return c.plan ? (uint64_t)__ldcg(&c.plan->tail) : c.tail;
+}
+template <int PREC> __device__ __forceinline__ int64_t w_n(const WaveCtx<PREC>& c) {
+  return c.plan ? (int64_t)__ldcg(&c.plan->n_in) : c.n_in;
+}
+template <int PREC> __device__ __forceinline__ int w_out_chunk(const WaveCtx<PREC>& c) {
+  return c.plan ? __ldcg(&c.plan->out_chunk) : c.out_chunk;
+}
 
 __device__ void raise_status(int* status, double* info, int code, int process, double E, int key) {
   if (atomicCAS(status, 0, code) == 0 && info) {
@@ -358,11 +392,19 @@ __device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf],
 
 // ------------------------------------------------------------ phase 1, float64
 // Same device functions and operation order as the record engine (pt_run_sm).
+struct PropShared64 {
+  unsigned int hist[kHist];
+  int32_t buf[kWarps][8][kBuf];
+  int bcnt[kWarps][8];
+};
+
 template <int BETHE>
-__global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
-  __shared__ unsigned int sh_hist[kHist];
-  __shared__ int32_t sh_buf[kWarps][8][kBuf];
-  __shared__ int sh_bcnt[kWarps][8];
+__device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropShared64& sm) {
+  unsigned int* sh_hist = sm.hist;
+  int32_t (*sh_buf)[8][kBuf] = sm.buf;
+  int (*sh_bcnt)[8] = sm.bcnt;
+  const int64_t wave_n = w_n(c);
+  const uint64_t wave_head = w_head(c);
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
   if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
@@ -382,12 +424,12 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
   for (;;) {
     __syncwarp();
     const bool need = !active;
-    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, c.chunk[0]);
+    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, c.chunk[0]);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool finish = false;
     if (fresh) {
-      i = (c.head + (uint64_t)got) & c.mask;
+      i = (wave_head + (uint64_t)got) & c.mask;
       E0 = c.q.E[i]; px = c.q.px[i]; py = c.q.py[i]; pz = c.q.pz[i];
       x = c.q.x[i]; y = c.q.y[i]; z = c.q.z[i];
       mass = c.q.mass[i]; pid = c.q.pid[i]; prim = c.q.prim[i];
@@ -493,6 +535,12 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
   flush_tally(c.tally, L, sh_hist);
 }
 
+template <int BETHE>
+__global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
+  __shared__ PropShared64 sm;
+  propagate_fp64_body<BETHE>(c, sm);
+}
+
 // ------------------------------------------------ phase 1, mixed precision
 // A particle whose propagation ended, waiting for the process choice and its
 // sampling task.  Finished particles are queued per warp and handled 32 at a
@@ -543,12 +591,21 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
 
 // BETHE: Shower(fast_MCS_mode=False); a separate instantiation keeps the
 // Bethe-Moliere inverse CDF out of the fast mode's registers.
+struct PropSharedMixed {
+  unsigned int hist[kHist];
+  int32_t buf[kWarps][8][kBuf];
+  int bcnt[kWarps][8];
+  FinEntry fin[kWarps][64];
+};
+
 template <int BETHE>
-__global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
-  __shared__ unsigned int sh_hist[kHist];
-  __shared__ int32_t sh_buf[kWarps][8][kBuf];
-  __shared__ int sh_bcnt[kWarps][8];
-  __shared__ FinEntry sh_fin[kWarps][64];
+__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixed& sm) {
+  unsigned int* sh_hist = sm.hist;
+  int32_t (*sh_buf)[8][kBuf] = sm.buf;
+  int (*sh_bcnt)[8] = sm.bcnt;
+  FinEntry (*sh_fin)[64] = sm.fin;
+  const int64_t wave_n = w_n(c);
+  const uint64_t wave_head = w_head(c);
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
   if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
@@ -585,12 +642,12 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
     // loads and set-up run for several lanes at once
     const unsigned idle = __ballot_sync(kFull, !active);
     const bool need = !active && (__popc(idle) >= c.refill_min[0] || idle == kFull);
-    const int64_t got = pool_take(pool, c.ctr + 0, c.n_in, need, c.chunk[0]);
+    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, c.chunk[0]);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool fin = false;
     if (fresh) {
-      i = (uint32_t)((c.head + (uint64_t)got) & c.mask);
+      i = (uint32_t)((wave_head + (uint64_t)got) & c.mask);
       pid = c.q.pid[i];
     }
     // a dead entry (pid 0, left by the sampler's slot pool) is consumed without work
@@ -609,8 +666,10 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
       mtab = sp == 0 ? 0.f : (sp == 3 ? (float)kMmu : me);   // mass_dict[PID] (particle.py:4-13)
       ++L.steps;
       ++L.species[sp];
-      const float pt = sqrtf(px * px + py * py);
-      pmag = sqrtf(pt * pt + pz * pz);
+      // rounded explicitly: the angle tally must not depend on how the
+      // compiler contracts this in each kernel that inlines the body
+      const float pt = sqrtf(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)));
+      pmag = sqrtf(__fadd_rn(__fmul_rn(pt, pt), __fmul_rn(pz, pz)));
       th0 = atan2f(pt, pz);
       dir = pmag > 0.f ? make_float3(px / pmag, py / pmag, pz / pmag) : make_float3(0.f, 0.f, 1.f);
       disp = make_float3(0.f, 0.f, 0.f);
@@ -726,6 +785,12 @@ __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
   if (fcount > 0) run_finish(c, fq, fcount, buf, bcnt, L, sh_hist);
   publish_rest(c, buf, bcnt);
   flush_tally(c.tally, L, sh_hist);
+}
+
+template <int BETHE>
+__global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
+  __shared__ PropSharedMixed sm;
+  propagate_mixed_body<BETHE>(c, sm);
 }
 
 // ------------------------------------------------------------ phase 2
@@ -902,11 +967,11 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
     if (below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
   }
   uint64_t slots[2] = {0, 0};
-  out_take(opool, c.ctr + 2, want, slots, c.out_chunk);
+  out_take(opool, c.ctr + 2, want, slots, w_out_chunk(c));
   int slot = 0;
   for (int j = 0; j < 2; ++j) {
     if (!on || !(dg[j].E > c.min_energy)) continue;
-    const uint64_t q = (c.tail + slots[slot++]) & c.mask;
+    const uint64_t q = (w_tail(c) + slots[slot++]) & c.mask;
     ++L.pushed;
     c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
     c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
@@ -918,13 +983,18 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
   }
 }
 
+template <int PREC> struct SampShared {
+  unsigned long long off[9];
+  KinEntry<PREC> kq[kWarps][kKinQ];
+};
+
 template <int PREC>
-__global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<PREC> c) {
-  __shared__ unsigned long long sh_off[9];
-  __shared__ KinEntry<PREC> sh_kq[kWarps][kKinQ];
+__device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<PREC>& sm) {
+  unsigned long long* sh_off = sm.off;
+  KinEntry<PREC> (*sh_kq)[kKinQ] = sm.kq;
   if (threadIdx.x == 0) {
     unsigned long long acc = 0;
-    for (int p = 0; p < 8; ++p) { sh_off[p] = acc; acc += c.ctr[8 + p]; }
+    for (int p = 0; p < 8; ++p) { sh_off[p] = acc; acc += __ldcg(c.ctr + 8 + p); }
     sh_off[8] = acc;
   }
   __syncthreads();
@@ -1074,8 +1144,15 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<
   }
   if (kcount > 0) run_kinematics<PREC>(c, kq, kcount, opool, L);
   // unused slots of the warp's last output chunk become dead entries
-  for (uint64_t r = opool.next + lane; r < opool.end; r += 32) c.q.pid[(c.tail + r) & c.mask] = 0;
+  const uint64_t wave_tail = w_tail(c);
+  for (uint64_t r = opool.next + lane; r < opool.end; r += 32) c.q.pid[(wave_tail + r) & c.mask] = 0;
   flush_tally(c.tally, L, nullptr);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<PREC> c) {
+  __shared__ SampShared<PREC> sm;
+  sample_body<PREC>(c, sm);
 }
 
 template <int PREC>
@@ -1092,6 +1169,158 @@ __global__ void k_feed(RingT<PREC> q, uint64_t mask, uint64_t tail, const double
   q.key[i] = primary_key((uint64_t)(offset + g));
 }
 
+// ----------------------------------------------- waves planned on the GPU
+constexpr long long kMaxPlannedWaves = 1ll << 20;
+// plan_step: what the host loop of run_batch_impl decides between waves,
+// done by one thread from the device counters: retire the last wave (its
+// entries are consumed, its daughters appended), feed primaries while the
+// ring is less than 1/8 full, size the next wave, clear the counters.
+template <int PREC>
+__device__ void plan_step(const WaveCtx<PREC>& c) {
+  WavePlan& P = *c.plan;
+  P.head += (unsigned long long)P.n_in;
+  P.tail += __ldcg(c.ctr + 2);
+  P.n_in = 0;
+  P.feed_m = 0;
+  for (int k = 0; k < 16; ++k) c.ctr[k] = 0;
+  if (*(volatile int*)c.status != 0) { P.done = 1; return; }
+  if (P.waves >= kMaxPlannedWaves) {              // a bound on the loop, far above any run's need
+    raise_status(c.status, nullptr, PT_TIMEOUT, 0, 0.0, 0);
+    P.done = 1;
+    return;
+  }
+  const int64_t cap = c.cap;
+  int64_t live = (int64_t)(P.tail - P.head);
+  if (P.fed >= c.n_prim && live == 0) { P.done = 1; return; }
+  if (P.fed < c.n_prim && live < cap / 8) {
+    int64_t m = c.n_prim - P.fed;
+    if (m > cap / 8 - live) m = cap / 8 - live;
+    if (m > c.feed_max) m = c.feed_max;
+    P.feed_m = m;
+    P.feed_at = P.tail;
+    P.tail += (unsigned long long)m;
+    P.fed += m;
+    live += m;
+  }
+  int oc = kOutChunk;
+  int64_t k = (cap - live - c.slack) / 2;
+  if (k > live) k = live;
+  if (k > c.list_cap) k = c.list_cap;
+  if (k < 16 * 1024) {
+    oc = 0;
+    k = (cap - live) / 2;
+    if (k > live) k = live;
+    if (k > c.list_cap) k = c.list_cap;
+  }
+  if (k <= 0) {                                   // the live population filled the ring
+    raise_status(c.status, nullptr, PT_OOM, 0, 0.0, 0);
+    P.done = 1;
+    return;
+  }
+  P.n_in = k;
+  P.out_chunk = oc;
+  P.waves += 1;
+}
+
+// The planned wave's primaries into the ring (k_feed's rows), thread j of nthr.
+template <int PREC>
+__device__ __forceinline__ void feed_planned(const WaveCtx<PREC>& c, int64_t j, int64_t nthr) {
+  const int64_t m = __ldcg(&c.plan->feed_m);
+  const uint64_t at = (uint64_t)__ldcg(&c.plan->feed_at);
+  const int64_t first = __ldcg(&c.plan->fed) - m;
+  const int64_t n = c.n_prim;
+  for (; j < m; j += nthr) {
+    const int64_t g = first + j;
+    const uint64_t i = (at + (uint64_t)j) & c.mask;
+    c.q.E[i] = c.in_p0[0 * n + g]; c.q.px[i] = c.in_p0[1 * n + g]; c.q.py[i] = c.in_p0[2 * n + g];
+    c.q.pz[i] = c.in_p0[3 * n + g];
+    c.q.x[i] = c.in_r0[0 * n + g]; c.q.y[i] = c.in_r0[1 * n + g]; c.q.z[i] = c.in_r0[2 * n + g];
+    c.q.mass[i] = c.in_mass[g]; c.q.pid[i] = c.in_pid[g]; c.q.prim[i] = (int32_t)g; c.q.gen[i] = 0;
+    c.q.key[i] = primary_key((uint64_t)(c.prim_offset + g));
+  }
+}
+
+// Graph-captured loop: the body's first node plans the wave and sets the
+// loop's condition (0 once the run has ended; the rest of that last body
+// then finds an empty wave).
+template <int PREC>
+__global__ void k_plan(WaveCtx<PREC> c, cudaGraphConditionalHandle loop) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    plan_step(c);
+    cudaGraphSetConditional(loop, c.plan->done ? 0u : 1u);
+  }
+}
+
+template <int PREC>
+__global__ void k_feed_planned(WaveCtx<PREC> c) {
+  feed_planned(c, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+// Grid-wide barrier of the persistent kernel, whose blocks the cooperative
+// launch makes co-resident: arrivals in bar[0], the generation in bar[1].
+// Bounded: a block that waits longer than kBarrierNs records PT_TIMEOUT and
+// returns false, and every block then leaves the kernel within the same bound.
+constexpr unsigned long long kBarrierNs = 20ull * 1000ull * 1000ull * 1000ull;
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ bool grid_barrier(unsigned int* bar, int* status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = bar + 1;
+    const unsigned int g = *gen;
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (*gen == g) {
+        if (global_ns() - t0 > kBarrierNs) { good = 0; break; }
+        __nanosleep(200);
+      }
+    }
+    __threadfence();
+    if (!good) atomicCAS(status, 0, PT_TIMEOUT);
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <int PREC> struct PropSharedOf;
+template <> struct PropSharedOf<0> { using T = PropShared64; };
+template <> struct PropSharedOf<1> { using T = PropSharedMixed; };
+
+// One persistent kernel for the whole run: each wave is plan, feed,
+// propagation and sampling, separated by grid barriers; the warps pull
+// their work from the same device pools as the separate kernels.
+template <int PREC, int BETHE>
+__global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_persistent(WaveCtx<PREC> c, unsigned int* bar) {
+  union Shared {
+    typename PropSharedOf<PREC>::T p;
+    SampShared<PREC> s;
+  };
+  __shared__ Shared sm;
+  for (;;) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) plan_step(c);
+    if (!grid_barrier(bar, c.status)) break;
+    if (__ldcg(&c.plan->done)) break;
+    feed_planned(c, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+    if (!grid_barrier(bar, c.status)) break;
+    if constexpr (PREC == 1) propagate_mixed_body<BETHE>(c, sm.p);
+    else propagate_fp64_body<BETHE>(c, sm.p);
+    if (!grid_barrier(bar, c.status)) break;
+    sample_body<PREC>(c, sm.s);
+    if (!grid_barrier(bar, c.status)) break;
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- host side
@@ -1104,6 +1333,8 @@ struct BatchScratch {
   unsigned long long* h_ctr = nullptr;
   int* h_status = nullptr;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // around each wave's two kernels
+  WavePlan* plan = nullptr;       // device-planned waves
+  unsigned int* bar = nullptr;    // the persistent kernel's grid barrier
 };
 
 #define PT_CUDA(call)                                                                 \
@@ -1130,6 +1361,7 @@ pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
   if (cudaMalloc(&s->mem, ring_bytes(c2)) != cudaSuccess ||
       cudaMalloc(&s->idx, (size_t)8 * s->list_cap * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&s->ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&s->plan, sizeof(WavePlan)) != cudaSuccess || cudaMalloc(&s->bar, 2 * sizeof(unsigned int)) != cudaSuccess ||
       cudaMallocHost(&s->h_ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&s->h_status, sizeof(int)) != cudaSuccess || cudaEventCreate(&s->ev[0]) != cudaSuccess ||
       cudaEventCreate(&s->ev[1]) != cudaSuccess || cudaEventCreate(&s->ev[2]) != cudaSuccess) {
@@ -1164,6 +1396,8 @@ void batch_scratch_free(BatchScratch* s) {
   cudaFree(s->mem);
   cudaFree(s->idx);
   cudaFree(s->ctr);
+  cudaFree(s->plan);
+  cudaFree(s->bar);
   cudaFreeHost(s->h_ctr);
   cudaFreeHost(s->h_status);
   for (cudaEvent_t e : s->ev)
@@ -1178,6 +1412,120 @@ static int resident_blocks(const void* kernel) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
   if (per < 1) per = 1;
   return sms * per;
+}
+
+// The outcome of a run whose waves the GPU planned: its status and waves.
+static pt_status finish_planned(HandleParts& hp, BatchScratch* S, cudaStream_t st, int64_t launches, float ms) {
+  WavePlan P;
+  PT_CUDA(cudaMemcpyAsync(&P, S->plan, sizeof(WavePlan), cudaMemcpyDeviceToHost, st));
+  PT_CUDA(cudaMemcpyAsync(S->h_status, hp.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PT_CUDA(cudaStreamSynchronize(st));
+  hp.launches[0] = launches;
+  hp.launches[1] = P.waves;
+  hp.kernel_ms[0] = ms;
+  hp.kernel_ms[1] = 0.0;
+  if (*S->h_status != PT_OK) {
+    if (*S->h_status == PT_NO_SAMPLE || *S->h_status == PT_TIMEOUT)
+      PT_CUDA(cudaMemcpy(hp.last_info, hp.err_info, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    return (pt_status)*S->h_status;
+  }
+  return PT_OK;
+}
+
+// PT_LOOP_GRAPH: one CUDA graph whose conditional WHILE node repeats the
+// wave (plan, feed, propagation, sampling) until the plan ends the run; the
+// host waits once.  The kernels run at their resident grids; a wave smaller
+// than that leaves the extra blocks without work.
+template <int PREC>
+static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> c, const void* kp, int rb_p, int rb_s,
+                                cudaStream_t st) {
+  c.plan = S->plan;
+  c.slack = (int64_t)rb_s * kWarps * kOutChunk;
+  PT_CUDA(cudaMemsetAsync(S->plan, 0, sizeof(WavePlan), st));
+  PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
+  cudaGraph_t g = nullptr, body = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  cudaStream_t cs = nullptr;
+  pt_status rs = PT_OK;
+  float ms = 0.f;
+  const unsigned gf = (unsigned)((c.feed_max + 255) / 256);
+#define PT_G(call)                                                                          \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      fprintf(stderr, "petite_gpu: %s failed: %s\n", #call, cudaGetErrorString(e_));         \
+      rs = PT_CUDA_ERR;                                                                     \
+      goto done;                                                                            \
+    }                                                                                       \
+  } while (0)
+  {
+    cudaGraphConditionalHandle loop;
+    alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)] = {};
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(npbuf);   // zeroed, as the API requires
+    cudaGraphNode_t node;
+    PT_G(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    PT_G(cudaGraphCreate(&g, 0));
+    PT_G(cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault));
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    PT_G(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+    body = np.conditional.phGraph_out[0];
+    PT_G(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    k_plan<PREC><<<1, 32, 0, cs>>>(c, loop);
+    k_feed_planned<PREC><<<gf, 256, 0, cs>>>(c);
+    {
+      void* args[] = {&c};
+      cudaLaunchKernel(kp, dim3(rb_p), dim3(kThreads), args, 0, cs);
+    }
+    k_sample<PREC><<<rb_s, kThreads, 0, cs>>>(c);
+    PT_G(cudaStreamEndCapture(cs, &body));
+    PT_G(cudaGraphInstantiate(&ex, g, 0));
+    PT_G(cudaEventRecord(S->ev[0], st));
+    PT_G(cudaGraphLaunch(ex, st));
+    PT_G(cudaEventRecord(S->ev[1], st));
+    PT_G(cudaEventSynchronize(S->ev[1]));
+    PT_G(cudaEventElapsedTime(&ms, S->ev[0], S->ev[1]));
+  }
+done:
+#undef PT_G
+  if (ex) cudaGraphExecDestroy(ex);
+  if (g) cudaGraphDestroy(g);
+  if (cs) cudaStreamDestroy(cs);
+  if (rs != PT_OK) {
+    cudaGetLastError();
+    return rs;
+  }
+  return finish_planned(hp, S, st, 1, ms);
+}
+
+// PT_LOOP_PERSISTENT: one cooperative kernel (all blocks co-resident) runs
+// every wave; its warps pull work from the same device pools.
+template <int PREC, int BETHE>
+static pt_status run_persistent(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> c, cudaStream_t st) {
+  const void* kern = (const void*)k_persistent<PREC, BETHE>;
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  PT_CUDA(cudaGetDevice(&dev));
+  PT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  PT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, 0));
+  if (!coop || per < 1) return PT_CUDA_ERR;
+  const int grid = sms * per;
+  c.plan = S->plan;
+  c.slack = (int64_t)grid * kWarps * kOutChunk;
+  PT_CUDA(cudaMemsetAsync(S->plan, 0, sizeof(WavePlan), st));
+  PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
+  PT_CUDA(cudaMemsetAsync(S->bar, 0, 2 * sizeof(unsigned int), st));
+  unsigned int* bar = S->bar;
+  void* args[] = {&c, &bar};
+  PT_CUDA(cudaEventRecord(S->ev[0], st));
+  PT_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kThreads), args, 0, st));
+  PT_CUDA(cudaEventRecord(S->ev[1], st));
+  PT_CUDA(cudaEventSynchronize(S->ev[1]));
+  float ms = 0.f;
+  PT_CUDA(cudaEventElapsedTime(&ms, S->ev[0], S->ev[1]));
+  return finish_planned(hp, S, st, 1, ms);
 }
 
 template <int PREC>
@@ -1207,12 +1555,22 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.refill_min[1] = tu[1] ? tu[1] : kRefillMinSample;
   c.chunk[0] = tu[2] ? tu[2] : kChunkPropagate;
   c.chunk[1] = tu[3] ? tu[3] : kChunkSample;
+  c.plan = nullptr;
+  c.in_p0 = p0; c.in_r0 = r0; c.in_pid = pid; c.in_mass = mass;
+  c.n_prim = n;
+  c.prim_offset = o->primary_offset;
+  c.cap = S->cap;
+  c.feed_max = S->cap / 1024 > 256 ? S->cap / 1024 : 256;
+  c.slack = 0;
   const void* kp = PREC ? (c.mcs_mode ? (const void*)k_propagate_mixed<1> : (const void*)k_propagate_mixed<0>)
                        : (c.mcs_mode ? (const void*)k_propagate_fp64<1> : (const void*)k_propagate_fp64<0>);
   const void* ks = (const void*)k_sample<PREC>;
   const int rb_p = resident_blocks(kp);
   const int rb_s = resident_blocks(ks);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
+  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, rb_p, rb_s, st);
+  if (tu[4] == PT_LOOP_PERSISTENT)
+    return c.mcs_mode ? run_persistent<PREC, 1>(hp, S, c, st) : run_persistent<PREC, 0>(hp, S, c, st);
   const int64_t cap = S->cap;
   // A fed primary can grow to a few hundred live particles before its shower
   // thins out, so primaries enter in small increments while the ring is

@@ -19,6 +19,6 @@ struct HandleParts {
   double* last_info;
   int64_t* launches;   // [0] kernel launches, [1] waves of the last run
   double* kernel_ms;   // device time of the last batched run: [0] propagation, [1] sampler
-  int32_t* tuning;     // batched engine: refill_min[2], chunk[2] (0 = default)
+  int32_t* tuning;     // batched engine: refill_min[2], chunk[2] (0 = default), loop (PT_LOOP_*)
 };
 HandleParts handle_parts(pt_handle* h);

@@ -283,13 +283,19 @@ class SMEngine:
         _lib.check(self.lib.pt_last_run_stats(self.handle, C.byref(l), C.byref(w)), "pt_last_run_stats")
         return int(l.value), int(w.value)
 
-    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0)):
-        """Work distribution of the batched engine (0 = library default)."""
+    LOOPS = {"host": 0, "graph": 1, "persistent": 2}
+
+    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host"):
+        """Work distribution of the batched engine (0 = library default) and
+        who runs its waves: "host" (two launches per wave, counters read
+        back), "graph" (a CUDA graph's conditional loop, planned on the GPU)
+        or "persistent" (one cooperative kernel)."""
         t = _lib.PtBatchTuning()
         t.refill_min[0], t.refill_min[1] = int(refill_min[0]), int(refill_min[1])
         t.chunk[0], t.chunk[1] = int(chunk[0]), int(chunk[1])
+        t.loop = self.LOOPS[loop]
         _lib.check(self.lib.pt_set_batch_tuning(self.handle, C.byref(t)), "pt_set_batch_tuning")
-        self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk)}
+        self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk), "loop": loop}
 
     def last_kernel_times(self):
         """Device seconds of the last batched run: (propagation, sampler)."""

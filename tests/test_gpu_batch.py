@@ -108,5 +108,51 @@ def test_autotune_picks_valid_settings(lead):
     assert best["refill_min"][0] in (8,) + GRID["refill_min"]
     assert best["chunk"][0] in (128,) + GRID["chunk_propagate"]
     assert best["chunk"][1] in (64,) + GRID["chunk_sample"]
+    assert best["loop"] in GRID["loop"]
     assert best["seconds"] > 0
     lead._engine.set_tuning((0, 0), (0, 0))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("loop", ["graph", "persistent"])
+def test_device_planned_loops_give_identical_results(lead, precision, loop):
+    """The waves planned on the GPU (a CUDA graph's conditional loop, or one
+    persistent cooperative kernel) are the host loop's waves: the same
+    particles, spectra and deposits; only the summation order of the float64
+    deposits differs."""
+    p0, pid, m = primaries(1500, seed=31, emax=50.0)
+    eng = lead._engine
+    a = run_batch(lead, p0, pid, m, precision, cap=1 << 16)
+    eng.set_tuning((0, 0), (0, 0), loop)
+    try:
+        b = run_batch(lead, p0, pid, m, precision, cap=1 << 16)
+    finally:
+        eng.set_tuning((0, 0), (0, 0))
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    assert np.array_equal(a.counts.cpu().numpy(), b.counts.cpu().numpy())
+    ha, hb = a.hist.cpu().numpy().astype(np.int64), b.hist.cpu().numpy().astype(np.int64)
+    if precision == "fp64":
+        assert np.array_equal(ha, hb)
+    else:
+        # the persistent kernel inlines the float32 bodies into another kernel,
+        # where the compiler may contract a product into a fused multiply-add
+        # differently: a last-place difference can move a binned value across
+        # a bin edge, never a particle or a decision
+        for k in range(3):
+            assert ha[k].sum() == hb[k].sum()
+            assert np.abs(ha[k] - hb[k]).sum() <= 1e-5 * ha[k].sum(), k
+    np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-9)
+    np.testing.assert_allclose(a.energy.cpu().numpy(), b.energy.cpu().numpy(), rtol=1e-9)
+
+
+def test_device_planned_loop_in_bethe_mode():
+    from petite_gb300 import Shower
+    sh = Shower(None, "lead", 0.010, seed=SEED, fast_MCS_mode=False)
+    p0, pid, m = primaries(500, seed=33)
+    a = run_batch(sh, p0, pid, m, "mixed", cap=1 << 15)
+    sh._engine.set_tuning((0, 0), (0, 0), "persistent")
+    b = run_batch(sh, p0, pid, m, "mixed", cap=1 << 15)
+    sh._engine.set_tuning((0, 0), (0, 0))
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    ha, hb = a.hist.cpu().numpy().astype(np.int64), b.hist.cpu().numpy().astype(np.int64)
+    assert (np.abs(ha - hb).sum(axis=(1, 2)) <= 1e-5 * ha.sum(axis=(1, 2))).all()
