@@ -38,9 +38,12 @@ def _calibration_primaries(n, seed):
 
 
 def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
-                   verbose=False):
+                   verbose=False, choose_loop=True):
     """Tunes ``shower``'s engine and returns the chosen settings
-    ``{"refill_min": [p, s], "chunk": [p, s], "seconds": t}``."""
+    ``{"refill_min": [p, s], "chunk": [p, s], "loop": l, "seconds": t, "loop_seconds": {...}}``
+    (``loop_seconds``: the calibration run under each loop at the final work
+    distribution).  ``choose_loop=False`` times the loops but keeps the host
+    loop, whose per-kernel event times a roofline needs."""
     import torch
     eng = shower._engine
     key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}|v{CACHE_VERSION}"
@@ -82,6 +85,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"]}
     run(cfg)                                            # warm-up (scratch, caches)
     best_t = run(cfg)
+    loop_seconds = {}
     for name, values in GRID.items():
         for v in values:
             trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"]}
@@ -94,13 +98,20 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
             else:
                 trial["loop"] = v
             if trial == cfg:
+                if name == "loop":
+                    loop_seconds[v] = best_t
                 continue
             t = run(trial)
+            if name == "loop":
+                loop_seconds[v] = t
+                if not choose_loop:
+                    continue
             if verbose:
                 print("autotune", trial, round(t, 4))
             if t < best_t * 0.99:                       # a change must beat noise
                 best_t, cfg = t, trial
-    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "loop": cfg["loop"], "seconds": best_t}
+    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "loop": cfg["loop"], "seconds": best_t,
+            "loop_seconds": loop_seconds}
     eng.set_tuning(best["refill_min"], best["chunk"], best["loop"])
     if use_cache:
         cache[key] = best
