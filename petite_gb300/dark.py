@@ -518,7 +518,8 @@ class DarkShower(Shower):
             print("Need an existing SM shower-file directory or SM incident particle to run dark shower")
             return None
         if ExDir is not None and isinstance(ExDir, str):
-            ShowerToSamp = list(np.load(ExDir, allow_pickle=True))
+            from .io import read_particle_file
+            ShowerToSamp = read_particle_file(ExDir)      # PETITE's files too, without PETITE
         elif ExDir is not None and isinstance(ExDir, list):
             ShowerToSamp = ExDir
         elif isinstance(SParams, Particle):

@@ -270,3 +270,49 @@ def batch_to_particles(b: ShowerBatch, primaries):
         ids_of[r] = (my_id, gen_parent + 1, int(b.pid[r]))
         out[k].append(part)
     return out
+
+
+# ------------------------------------------------------- detector acceptance
+def transverse_position(particle, z):
+    """shower.py:815-823: (x, y) where the particle's initial straight line
+    (r0 along p0) reaches longitudinal position(s) z."""
+    x0, y0, z0 = particle.get_r0()
+    E, px, py, pz = particle.get_p0()
+    T = (np.asarray(z) - z0) / pz
+    return [x0 + T * px, y0 + T * py]
+
+
+def detector_cut(particle_list, detector_positions, detector_radius, method="Sample", energy_cut=None,
+                 detector_inner_radius=0.0):
+    """shower.py:825-865: which particles cross disk detectors at the
+    longitudinal positions ``detector_positions`` (an annulus between
+    ``detector_inner_radius`` and ``detector_radius``, both exclusive), after
+    an optional open energy window ``energy_cut`` = (min, max).  ``method``:
+    "Sample" (the passing particles per detector), "SampleW" (the pass mask,
+    detectors by particles), "Efficiency" (weighted fraction per detector) or
+    "TotalWeight".  Evaluated on arrays of all particles at once."""
+    parts = np.array(particle_list, dtype=object)
+    if energy_cut is not None and len(parts):
+        E = np.array([p.get_p0()[0] for p in parts])
+        parts = parts[(E < energy_cut[1]) & (E > energy_cut[0])]
+    nd = len(detector_positions)
+    if len(parts) == 0:
+        return [[] for _ in range(nd)] if method == "Sample" else [0.0 for _ in range(nd)]
+    r0 = np.array([p.get_r0() for p in parts], dtype=np.float64)
+    p0 = np.array([p.get_p0() for p in parts], dtype=np.float64)
+    z = np.asarray(detector_positions, dtype=np.float64)
+    T = (z[None, :] - r0[:, 2:3]) / p0[:, 3:4]
+    xf, yf = r0[:, 0:1] + T * p0[:, 1:2], r0[:, 1:2] + T * p0[:, 2:3]
+    rT = np.sqrt(xf * xf + yf * yf)                                   # (particles, detectors)
+    passed = ((rT > detector_inner_radius) & (rT < detector_radius)).T
+    if method == "SampleW":
+        return passed
+    cuts = [parts[passed[i]] for i in range(nd)]
+    if method == "Sample":
+        return cuts
+    w = np.array([p.get_ids()["weight"] for p in parts], dtype=np.float64)
+    if method == "Efficiency":
+        return [np.sum(w[passed[i]]) / np.sum(w) for i in range(nd)]
+    if method == "TotalWeight":
+        return [np.sum(w[passed[i]]) for i in range(nd)]
+    return None

@@ -19,7 +19,7 @@ The particle being processed is tracked by wrapping the Shower instance's
 ``propagate_particle`` and ``sample_scattering``; daughters get the keys of
 ``oracle.philox.daughter_key``.
 
-Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|darkfree|moliere|mesons|all]
+Usage: python tests/golden/make_golden.py DICT_DIR [units|showers|dark|darkfree|moliere|mesons|files|particles|all]
 (DICT_DIR from rebuild_maps.py; for ``dark`` it must also hold the output of
 ``rebuild_maps.py --dark``)
 """
@@ -763,6 +763,115 @@ def gen_dark_free(dict_dir, out_path):
     np.savez_compressed(out_path, **out)
 
 
+def gen_files(dict_dir, out_dir):
+    """A shower file as PETITE writes it (np.save of its Particle objects,
+    which generate_dark_shower(ExDir=path) reads), with its content as plain
+    arrays for the test."""
+    refimport.setup()
+    from PETITE.shower import Shower
+    from PETITE.particle import Particle
+    router = StreamRouter(SEED)
+    saved = install(router)
+    try:
+        sh = Shower(dict_dir, "graphite", 0.010)
+        wrap_shower(sh, router)
+        part = Particle([2.0, 0.0, 0.0, math.sqrt(4.0 - 0.000511 ** 2)], [0.0, 0.0, 0.0], {"PID": 11})
+        part._pkey = primary_key(0)
+        parts = sh.generate_shower(part)
+    finally:
+        uninstall(saved)
+    for p in parts:                                  # the routing key is not part of PETITE's objects
+        del p._pkey
+    np.save(os.path.join(out_dir, "petite_shower_file.npy"), np.array(parts, dtype=object), allow_pickle=True)
+    keys = ("PID", "ID", "parent_PID", "parent_ID", "generation_number", "weight", "mass")
+    np.savez_compressed(os.path.join(out_dir, "petite_shower_file_content.npz"),
+                        p0=np.array([p.get_p0() for p in parts]), r0=np.array([p.get_r0() for p in parts]),
+                        pf=np.array([p.get_pf() for p in parts]), rf=np.array([p.get_rf() for p in parts]),
+                        ids=np.array([[p.get_ids()[k] for k in keys] for p in parts], dtype=np.float64),
+                        process=np.array([p.get_ids()["generation_process"] for p in parts]),
+                        ended=np.array([p.get_ended() for p in parts]))
+    print("shower file:", len(parts), "particles")
+
+
+def gen_particles(out_path):
+    """PETITE's Particle utilities on a seeded numpy generator: boost,
+    two- and three-body decays, the meson decay chain (short- and
+    long-lived), decay/interaction sampling, energy loss, detector_cut."""
+    refimport.setup()
+    from PETITE.particle import Particle
+    from PETITE import shower as shmod
+    rng = np.random.default_rng(91)
+    out = {}
+    rows = []
+    for case in range(40):
+        pid = [111, 221, 331, 223, 211, -211, 321][case % 7]
+        m = {111: 0.1349768, 221: 0.547862, 331: 0.95778, 223: 0.78265, 211: 0.13957039, -211: 0.13957039,
+             321: 0.493677}[pid]
+        E = m * float(1.0 + 10 ** rng.uniform(-2, 2))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        pm = math.sqrt(E * E - m * m)
+        p4 = [E, *(pm * d)]
+        seed = 1000 + case
+        # two-body (gamma + V, V of mass 0.01..0.5 m) and the boost
+        par = Particle(list(p4), [0.0, 0.0, 0.1 * case], {"PID": pid, "mass": m, "ID": 3 + case})
+        np.random.seed(seed)
+        mv = m * float(rng.uniform(0.01, 0.5))
+        a, b = par.two_body_decay({"mass": 0, "PID": 22}, {"mass": mv, "PID": 4900022})
+        L = np.array(par.boost_matrix())
+        # three-body (pi0 pi0 + light) where allowed
+        t3 = np.zeros(12)
+        if m > 3 * 0.1349768:
+            np.random.seed(seed + 1)
+            x = par.three_body_decay({"PID": 22, "mass": 0.0}, {"PID": 22, "mass": 0.0}, {"PID": 111})
+            t3 = np.concatenate([q.get_p0() for q in x])
+        # decay chain
+        ch = np.full(12, np.nan)
+        st = "short-lived" if pid in (111, 221, 331, 223) else "long-lived"
+        q = Particle(list(p4), [0.0, 0.0, 0.0], {"PID": pid, "mass": m, "ID": 5, "stability": st, "weight": 0.5})
+        np.random.seed(seed + 2)
+        try:
+            dd = q.decay_particle()
+            ch = np.concatenate([dd[0].get_p0(), dd[1].get_p0(), [dd[0].get_ids()["weight"], dd[1].get_ids()["weight"],
+                                 dd[0].get_ids()["PID"], dd[1].get_ids()["PID"]]])
+        except ValueError:
+            pass
+        rows.append(np.concatenate([[pid, m, seed, mv], p4, a.get_p0(), b.get_p0(), L.ravel(), t3, ch,
+                                    q.get_rf()]))
+    out["decays"] = np.array(rows)
+    # lose_energy
+    le = []
+    for case in range(20):
+        m = [0.000511, 0.1056583755, 0.1349768][case % 3]
+        E = m + float(10 ** rng.uniform(-3, 1))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        par = Particle([E, *(math.sqrt(E * E - m * m) * d)], [0, 0, 0], {"PID": 11, "mass": m})
+        dE = float(rng.uniform(0, 1.2)) * (E - m)
+        par.lose_energy(dE)
+        le.append(np.concatenate([[m, E, dE], d, par.get_pf()]))
+    out["lose"] = np.array(le)
+    # detector_cut on V-like particles
+    parts = []
+    for k in range(300):
+        E = float(10 ** rng.uniform(-1, 1.5))
+        th = float(10 ** rng.uniform(-4, -0.5))
+        ph = float(rng.uniform(0, 2 * math.pi))
+        p4 = [E, E * math.sin(th) * math.cos(ph), E * math.sin(th) * math.sin(ph), E * math.cos(th)]
+        parts.append(Particle(p4, [float(rng.normal(0, 0.01)), float(rng.normal(0, 0.01)), float(rng.uniform(0, 1))],
+                              {"PID": 4900022, "weight": float(rng.uniform(0.1, 2.0)), "mass": 0.01}))
+    out["det/p0"] = np.array([p.get_p0() for p in parts])
+    out["det/r0"] = np.array([p.get_r0() for p in parts])
+    out["det/w"] = np.array([p.get_ids()["weight"] for p in parts])
+    zs, R = [5.0, 50.0, 100.0], 1.0
+    out["det/sampleW"] = np.asarray(shmod.detector_cut(parts, zs, R, method="SampleW"), bool)
+    out["det/eff"] = np.array(shmod.detector_cut(parts, zs, R, method="Efficiency", energy_cut=(1.0, 20.0),
+                                                 detector_inner_radius=0.05))
+    out["det/total"] = np.array(shmod.detector_cut(parts, zs, R, method="TotalWeight"))
+    np.savez_compressed(out_path, **out)
+    print("particle utilities:", len(rows), "decay cases")
+
+
 BETHE_CASES = [
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 6, 0.000511),
     ("pos3_lead", "lead", 0.010, -11, 3.0, 2, 0.000511),
@@ -790,6 +899,10 @@ if __name__ == "__main__":
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
     if which in ("all", "darkfree"):
         gen_dark_free(d, os.path.join(HERE, "dark_free.npz"))
+    if which in ("all", "particles"):
+        gen_particles(os.path.join(HERE, "particles.npz"))
+    if which in ("all", "files"):
+        gen_files(d, HERE)
     if which in ("all", "mesons"):
         gen_mesons(d, os.path.join(HERE, "mesons.npz"),
                    os.path.join(refimport.REFERENCE, "examples", "beams", "Pi0_8GeVProtons_1000POT.npy"))

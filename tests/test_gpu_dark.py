@@ -361,3 +361,20 @@ def test_free_electron_run_dark_matches_reference(free_showers, name):
     np.testing.assert_allclose(res["p4"][o][:, 0], want[:, 4], rtol=1e-12, atol=0)
     scale = np.abs(want[:, 4:8]).max(1)
     assert (np.abs(res["p4"][o] - want[:, 4:8]).max(1) <= 1e-9 * scale).all()
+
+
+def test_generate_dark_shower_reads_petite_shower_files():
+    """generate_dark_shower(ExDir=path) on a shower file written by PETITE
+    itself (pickled PETITE Particle objects), read without PETITE."""
+    from petite_gb300.dark import DarkShower
+    from petite_gb300.io import read_particle_file
+    path = os.path.join(GOLDEN, "petite_shower_file.npy")
+    ds = DarkShower(None, "graphite", 0.010, 0.03, seed=SEED)
+    sm, vs = ds.generate_dark_shower(ExDir=path)
+    assert len(sm) > 100 and len(vs) > 20
+    parts = read_particle_file(path)
+    for p, q in zip(parts, sm):
+        p._pkey = q._pkey                     # the same streams as the first call
+    _, vs2 = ds.generate_dark_shower(ExDir=parts)
+    assert [v.get_ids()["parent_ID"] for v in vs] == [v.get_ids()["parent_ID"] for v in vs2]
+    np.testing.assert_array_equal(np.array([v.get_p0() for v in vs]), np.array([v.get_p0() for v in vs2]))
