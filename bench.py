@@ -47,6 +47,13 @@ WORKLOADS = {
     # the shipped dark masses nearest below {0.01, 0.05, 0.1, 0.3} GeV
     "dark_e10_graphite_1e5": dict(target="graphite", cut=0.010, n=100_000, species=(11,), emin=10.0, emax=10.0,
                                   seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark"),
+    # 10^5 mu- at 400 GeV in lead, cut 0.010 GeV, seed 3 (the SM transport of
+    # the 400 GeV muon configuration): tables with PETITE's data_400GeV cross
+    # sections, its shipped maps and Brem/PairProd/MuonBrem maps trained by
+    # petite_gb300.train (PETITE ships none above 100 GeV)
+    "sm_mu400_lead_1e5": dict(target="lead", cut=0.010, n=100_000, species=(13,), emin=400.0, emax=400.0,
+                              seed=3, precision="mixed", fp64_sample=1000, cpu_sample=1, mode="batch",
+                              tables="400GeV"),
     # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
     # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
@@ -152,12 +159,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def tables_dir(w):
+    """The workload's table directory: the bundled tables, or a bundled
+    variant (``tables``: a subdirectory of petite_gb300/data)."""
+    base = os.path.join(ROOT, "petite_gb300", "data")
+    return os.path.join(base, w["tables"]) if w.get("tables") else base
+
+
 def cpu_oracle_worker(args):
     """Runs the CPU oracle on a slice of primaries (spawned process)."""
     sys.path.insert(0, ROOT)
     from oracle.shower import OracleShower, OracleTables
-    target, cut, seed, p0, pid, mass, first = args
-    npz = os.path.join(ROOT, "petite_gb300", "data", "sm_tables.npz")
+    target, cut, seed, p0, pid, mass, first, tdir = args
+    npz = os.path.join(tdir, "sm_tables.npz")
     sh = OracleShower(OracleTables(npz, target), cut, seed=seed)
     rows = 0
     for i in range(len(p0)):
@@ -171,7 +185,7 @@ def cpu_baseline(w, n_sample, cores=None):
     p0, pid, m = make_primaries(w, n_sample, offset=10_000)
     order = np.argsort(-p0[:, 0])                      # large showers first for balance
     chunks = [order[k::cores * 2] for k in range(cores * 2)]
-    jobs = [(w["target"], w["cut"], w["seed"], p0[c], pid[c], m[c], 0) for c in chunks if len(c)]
+    jobs = [(w["target"], w["cut"], w["seed"], p0[c], pid[c], m[c], 0, tables_dir(w)) for c in chunks if len(c)]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -241,7 +255,7 @@ def bench_batch(args, w, name, dist, rank, ws):
     from petite_gb300 import Shower
     from petite_gb300.engine import ParticleStore  # noqa: F401  (ensures the package imports)
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    sh = Shower(None, w["target"], w["cut"], seed=w["seed"], precision=w["precision"], device=dev)
+    sh = Shower(tables_dir(w), w["target"], w["cut"], seed=w["seed"], precision=w["precision"], device=dev)
     eng = sh._engine
     n = args.primaries or w["n"]
     cap = 1 << args.ring_log2

@@ -248,6 +248,35 @@ pt_status pt_moliere_inverse_cdf(const double* u, const double* B, int64_t n, in
                                  void* stream);
 
 /* ------------------------------------------------------------------------
+ * Map training (utilities/generate_integrators.py, utilities/find_maxes.py):
+ * VEGAS adaptive maps for every energy row of one SM process at once, and
+ * the scan of each map for max_F and the cross section.  All pointers are
+ * device pointers except `target`/`targets` and `ninc` (host; increments
+ * per dimension, 1..1000).  Grids: nodes[row][d][k], k = 0..ninc[d], rows
+ * padded to max_nodes; acc/cnt: [row][d][1000].
+ * ------------------------------------------------------------------------ */
+typedef struct pt_train_target {   /* what the SM cross sections read of a target */
+  double Eg_min, Ee_min;           /* shower.py:214-215 */
+  double a0sq, Z2a04;              /* aa(Z, m_e)^2 and Z^2 aa^4 (all_processes.py:92-103) */
+} pt_train_target;
+/* One training iteration's samples: points_per_row map points per row
+ * (iteration 0..63 selects the draws); accumulates (jac f)^2 and counts per
+ * increment into acc/cnt and (sum w, sum w^2) into sums[row][2]. */
+pt_status pt_vegas_accumulate(int32_t process, const pt_train_target* target, const double* energy,
+                              int32_t n_rows, int32_t dims, const int32_t* ninc, const double* nodes,
+                              int32_t max_nodes, int64_t points_per_row, uint64_t seed, int32_t iteration,
+                              double* acc, uint32_t* cnt, double* sums, void* stream);
+/* The VEGAS adaptation of every row's grid from acc/cnt (damping alpha). */
+pt_status pt_vegas_adapt(int32_t n_rows, int32_t dims, const int32_t* ninc, double* nodes, int32_t max_nodes,
+                         const double* acc, const uint32_t* cnt, double alpha, void* stream);
+/* find_maxes (find_maxes.py:56-115): per row and target, n_trials batches of
+ * neval points weighted jac/neval: max_F[row][t] = the largest weight*f,
+ * xsec[row][t] = the sum of weight*f divided by n_trials. */
+pt_status pt_find_maxes(int32_t process, const pt_train_target* targets, int32_t n_targets, const double* energy,
+                        int32_t n_rows, int32_t dims, const int32_t* ninc, const double* nodes, int32_t max_nodes,
+                        int32_t neval, int32_t n_trials, uint64_t seed, double* max_F, double* xsec, void* stream);
+
+/* ------------------------------------------------------------------------
  * Dark-vector production on an SM shower (DarkShower, dark_shower.py).
  * ------------------------------------------------------------------------ */
 enum { PT_N_DARK = 4, PT_DARK_MAX_MASSES = 8 };

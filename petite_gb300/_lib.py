@@ -20,6 +20,7 @@ PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG =
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
            "pt_last_kernel_times", "pt_set_batch_tuning", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch",
            "pt_sample_only", "pt_dsigma", "pt_moliere_inverse_cdf",
+           "pt_vegas_accumulate", "pt_vegas_adapt", "pt_find_maxes",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
            "pt_dark_yield", "pt_dark_yield_adjoint")
 
@@ -101,6 +102,10 @@ class PtDarkOut(C.Structure):
                 ("yield_", C.c_void_p), ("yield_E", C.c_void_p)]
 
 
+class PtTrainTarget(C.Structure):
+    _fields_ = [("Eg_min", C.c_double), ("Ee_min", C.c_double), ("a0sq", C.c_double), ("Z2a04", C.c_double)]
+
+
 class PtBatchTuning(C.Structure):
     _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("reserved0", C.c_int32)]
 
@@ -169,6 +174,14 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_dsigma.restype = C.c_int
     lib.pt_moliere_inverse_cdf.argtypes = [vp, vp, i64, i32, vp, vp]
     lib.pt_moliere_inverse_cdf.restype = C.c_int
+    i32p = C.POINTER(i32)                    # host arrays of increments per dimension
+    lib.pt_vegas_accumulate.argtypes = [i32, C.POINTER(PtTrainTarget), vp, i32, i32, i32p, vp, i32, i64, C.c_uint64,
+                                        i32, vp, vp, vp, vp]
+    lib.pt_vegas_adapt.argtypes = [i32, i32, i32p, vp, i32, vp, vp, C.c_double, vp]
+    lib.pt_find_maxes.argtypes = [i32, C.POINTER(PtTrainTarget), i32, vp, i32, i32, i32p, vp, i32, i32, i32,
+                                  C.c_uint64, vp, vp, vp]
+    for f in ("pt_vegas_accumulate", "pt_vegas_adapt", "pt_find_maxes"):
+        getattr(lib, f).restype = C.c_int
     _LIB = lib
     return lib
 

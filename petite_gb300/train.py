@@ -1,0 +1,242 @@
+"""The table builder: VEGAS maps and max_F for PETITE's SM processes, on the GPU.
+
+PETITE trains one VEGAS map per (process, incoming energy) with the vegas
+package (all_processes.py:1160-1245, ``vegas_integration(..., mode="Pickle")``
+called by utilities/generate_integrators.py:49-84 with the hydrogen target,
+:118-123), then scans every map with utilities/find_maxes.py:56-115 for
+``max_F`` per target and the cross section.  Here all energy rows of a
+process train together through ``pt_vegas_accumulate``/``pt_vegas_adapt``
+and are scanned through ``pt_find_maxes``; the settings follow the
+reference's: the integration ranges of ``integration_range``
+(all_processes.py:1102-1160), grids of about 1000 increments kept a multiple
+of each dimension's strata (``vegas_integrator_options``, :1085-1096; the
+shipped maps have 960 for 60 strata), 2 x nitn adaptations (the burn-in
+call and the final one), damping alpha = 0.5, and find_maxes' neval = 300,
+100 trials.
+
+``build_raw_tables`` assembles ``RawTables`` (tables.py) from trained or
+shipped maps and a ``sm_xsec.pkl``; ``save_npz`` of it is a dict_dir that
+``Shower`` loads.  ``build_400GeV_tables`` does this for PETITE's
+``data_400GeV`` directory, whose Brem, PairProd and MuonBrem maps are not
+shipped.
+"""
+from __future__ import annotations
+
+import math
+import os
+import pickle
+
+import numpy as np
+
+from . import _lib
+from . import tables as T
+
+NSTRAT = {"PairProd": (60, 50, 40, 50), "Brem": (60, 50, 50, 50), "MuonBrem": (60, 50, 50, 50),
+          "Comp": (1000,), "Moller": (1000,), "MuonE": (1000,), "Bhabha": (1000,), "Ann": (1000,)}
+NITN = {"PairProd": 10, "Brem": 10, "MuonBrem": 10, "Comp": 20, "Moller": 20, "MuonE": 20, "Bhabha": 20, "Ann": 20}
+TRAINING_TARGET = "hydrogen"               # generate_integrators.py:118-123
+FIND_MAXES_TARGETS = ("graphite", "lead", "iron", "aluminum", "molybdenum")
+
+
+def integration_range(process: str, E: float, Eg_min: float = 0.001, Ee_min: float = 0.005, mV: float = 0.0):
+    """integration_range, all_processes.py:1102-1160, SM processes."""
+    me = T.M_ELECTRON
+    if process in ("PairProd", "Brem"):
+        return [[0, 1], [0, 2], [-2, 2], [0, 1]]
+    if process == "MuonBrem":
+        maxdel = np.sqrt(E / np.max([me, mV]))
+        return [[np.max([Eg_min, mV]), E - me], [0., maxdel], [0., maxdel], [0., 2 * np.pi]]
+    if process in ("Comp", "Ann", "MuonE"):
+        return [[-1., 1.0]]
+    d = 2.0 * Ee_min / (E - me)
+    return [[-1.0 + d, 1.0 - d]]
+
+
+def n_increments(process: str):
+    """Increments per dimension: about 1000, a multiple of the strata."""
+    return [(1000 // s) * s for s in NSTRAT[process]]
+
+
+def target_constants(target: str, Eg_min: float = 0.001, Ee_min: float = 0.005) -> _lib.PtTrainTarget:
+    """What the SM cross sections read of a target (the engine's expressions,
+    all_processes.py:92-103)."""
+    Z = T.TARGET_INFORMATION[target]["Z_T"]
+    a0 = 184.15 * (2.718) ** -0.5 * Z ** (-1.0 / 3.0) / T.M_ELECTRON
+    t = _lib.PtTrainTarget()
+    t.Eg_min, t.Ee_min, t.a0sq, t.Z2a04 = Eg_min, Ee_min, a0 ** 2, Z ** 2 * a0 ** 4
+    return t
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class MapSet:
+    """The maps of one process at its energies: nodes (rows, dims, max_nodes)
+    on the device, increments per dimension."""
+
+    def __init__(self, process: str, energies, nodes, ninc):
+        self.process = process
+        self.energies = np.asarray(energies, np.float64)
+        self.nodes = nodes
+        self.ninc = list(ninc)
+
+    @classmethod
+    def uniform(cls, process, energies, device="cuda"):
+        torch = _torch()
+        ninc = n_increments(process)
+        D, mn = len(ninc), max(ninc) + 1
+        g = np.zeros((len(energies), D, mn))
+        for r, E in enumerate(energies):
+            for d, (lo, hi) in enumerate(integration_range(process, float(E))):
+                g[r, d, :ninc[d] + 1] = np.linspace(lo, hi, ninc[d] + 1)
+        return cls(process, energies, torch.as_tensor(g, device=device), ninc)
+
+    @classmethod
+    def from_grids(cls, process, energies, grids, device="cuda"):
+        """Maps given as per-row lists of node arrays (e.g. PETITE's shipped maps)."""
+        torch = _torch()
+        D = len(grids[0])
+        ninc = [len(grids[0][d]) - 1 for d in range(D)]
+        mn = max(ninc) + 1
+        g = np.zeros((len(grids), D, mn))
+        for r, gr in enumerate(grids):
+            for d in range(D):
+                if len(gr[d]) != ninc[d] + 1:
+                    raise ValueError("rows of one process must share the increments per dimension")
+                g[r, d, :len(gr[d])] = gr[d]
+        return cls(process, energies, torch.as_tensor(g, device=device), ninc)
+
+    def grids(self):
+        g = self.nodes.cpu().numpy()
+        return [[g[r, d, :self.ninc[d] + 1].copy() for d in range(len(self.ninc))] for r in range(len(g))]
+
+    def _args(self):
+        """Energies on the device; increments per dimension on the host."""
+        import ctypes as C
+        torch = _torch()
+        E = torch.as_tensor(self.energies, device=self.nodes.device)
+        ninc = (C.c_int32 * len(self.ninc))(*self.ninc)
+        return E, ninc
+
+
+def train(maps: MapSet, points_per_row: int = 1 << 21, iterations: int | None = None, alpha: float = 0.5,
+          seed: int = 20261204, target: str = TRAINING_TARGET, history: list | None = None) -> MapSet:
+    """Adapts ``maps`` in place: ``iterations`` (default 2 x nitn) rounds of
+    accumulate + adapt.  ``history`` receives each round's per-row integral
+    estimates (mean of jac f)."""
+    torch = _torch()
+    lib = _lib.load()
+    dev = maps.nodes.device
+    E, ninc = maps._args()
+    n, D = len(maps.energies), len(maps.ninc)
+    code = T.PROCESS_CODE[maps.process]
+    tgt = target_constants(target)
+    acc = torch.zeros((n, D, 1000), dtype=torch.float64, device=dev)
+    cnt = torch.zeros((n, D, 1000), dtype=torch.int32, device=dev)
+    sums = torch.zeros((n, 2), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    iters = 2 * NITN[maps.process] if iterations is None else iterations
+    if iters > 64:
+        raise ValueError("at most 64 training iterations")
+    import ctypes as C
+    for it in range(iters):
+        acc.zero_()
+        cnt.zero_()
+        sums.zero_()
+        _lib.check(lib.pt_vegas_accumulate(code, C.byref(tgt), E.data_ptr(), n, D, ninc,
+                                           maps.nodes.data_ptr(), maps.nodes.shape[2], int(points_per_row),
+                                           int(seed) & (2 ** 64 - 1), it, acc.data_ptr(), cnt.data_ptr(),
+                                           sums.data_ptr(), C.c_void_p(stream)), "pt_vegas_accumulate")
+        if history is not None:
+            history.append((sums[:, 0] / points_per_row).cpu().numpy())
+        _lib.check(lib.pt_vegas_adapt(n, D, ninc, maps.nodes.data_ptr(), maps.nodes.shape[2],
+                                      acc.data_ptr(), cnt.data_ptr(), float(alpha), C.c_void_p(stream)),
+                   "pt_vegas_adapt")
+    torch.cuda.synchronize(dev)
+    return maps
+
+
+def find_maxes(maps: MapSet, targets=FIND_MAXES_TARGETS, neval: int = 300, n_trials: int = 100,
+               seed: int = 20261205):
+    """find_maxes.py:56-115 on every row: (max_F, xsec), each (rows, targets)."""
+    torch = _torch()
+    lib = _lib.load()
+    dev = maps.nodes.device
+    E, ninc = maps._args()
+    n, D = len(maps.energies), len(maps.ninc)
+    arr = (_lib.PtTrainTarget * len(targets))(*[target_constants(t) for t in targets])
+    mf = torch.zeros((n, len(targets)), dtype=torch.float64, device=dev)
+    xs = torch.zeros_like(mf)
+    import ctypes as C
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    _lib.check(lib.pt_find_maxes(T.PROCESS_CODE[maps.process], arr, len(targets), E.data_ptr(), n, D,
+                                 ninc, maps.nodes.data_ptr(), maps.nodes.shape[2], int(neval), int(n_trials),
+                                 int(seed) & (2 ** 64 - 1), mf.data_ptr(), xs.data_ptr(), C.c_void_p(stream)),
+               "pt_find_maxes")
+    return mf.cpu().numpy(), xs.cpu().numpy()
+
+
+def load_shipped_maps(dict_dir: str, process: str):
+    """PETITE's ``<Process>/<Process>_AdaptiveMaps.npy`` (list of [event_info,
+    AdaptiveMap]) as (energies, grids), without the vegas package."""
+    path = os.path.join(dict_dir, process, f"{process}_AdaptiveMaps.npy")
+    with open(path, "rb") as f:
+        np.lib.format.read_magic(f)
+        np.lib.format.read_array_header_1_0(f)
+        arr = T._MapsUnpickler(f).load()
+    E = [float(ev["E_inc"]) for ev, _ in arr]
+    grids = [[np.asarray(g, np.float64) for g in m.grid] for _, m in arr]
+    return np.array(E), grids
+
+
+def build_raw_tables(xsec: dict, maps: dict, max_F: dict, neval: int = 300, targets=FIND_MAXES_TARGETS,
+                     Eg_min: float = 0.001, Ee_min: float = 0.005) -> T.RawTables:
+    """RawTables from cross sections (``sm_xsec.pkl`` content: process ->
+    target -> (E, sigma) rows), maps (process -> MapSet) and max_F (process
+    -> (rows, targets))."""
+    raw = T.RawTables()
+    for proc in T.PROCESSES:
+        ms = maps[proc]
+        mf = max_F[proc]
+        rows = []
+        for r, (E, g) in enumerate(zip(ms.energies, ms.grids())):
+            rows.append(T.MapRow(float(E), int(neval), {t: float(mf[r, j]) for j, t in enumerate(targets)}, g,
+                                 Eg_min, Ee_min))
+        raw.maps[proc] = rows
+        raw.xsec[proc] = {t: np.asarray(v, np.float64) for t, v in xsec[proc].items()}
+    return raw
+
+
+def build_400GeV_tables(dict_dir: str, out_path: str, points_per_row: int = 1 << 21, device="cuda",
+                        log=print) -> dict:
+    """Tables for PETITE's ``data_400GeV``: its shipped maps (MuonE, Comp,
+    Ann, Moller, Bhabha) and trained maps for Brem, PairProd and MuonBrem at
+    the energies of its sm_xsec.pkl; max_F of every row from find_maxes.
+    Writes ``out_path`` (``save_npz``) and returns a summary."""
+    with open(os.path.join(dict_dir, "sm_xsec.pkl"), "rb") as f:
+        xsec = pickle.load(f)
+    maps, max_F, summary = {}, {}, {}
+    for proc in T.PROCESSES:
+        ship = os.path.join(dict_dir, proc, f"{proc}_AdaptiveMaps.npy")
+        E_x = np.asarray(xsec[proc]["graphite"], np.float64)[:, 0]
+        if os.path.exists(ship):
+            E, grids = load_shipped_maps(dict_dir, proc)
+            ms = MapSet.from_grids(proc, E, grids, device)
+            how = "shipped"
+        else:
+            ms = train(MapSet.uniform(proc, E_x, device), points_per_row=points_per_row)
+            how = "trained"
+        mf, xs = find_maxes(ms)
+        maps[proc], max_F[proc] = ms, mf
+        ref = np.array([np.interp(e, np.asarray(xsec[proc]["graphite"])[:, 0],
+                                  np.asarray(xsec[proc]["graphite"])[:, 1]) for e in ms.energies])
+        ok = ref > 0
+        ratio = xs[ok, 0] / ref[ok]
+        summary[proc] = {"maps": how, "rows": len(ms.energies), "E_max": float(ms.energies.max()),
+                         "xsec_ratio_graphite_median": float(np.median(ratio)) if ok.any() else None}
+        log(proc, summary[proc])
+    raw = build_raw_tables(xsec, maps, max_F)
+    T.save_npz(raw, out_path)
+    return summary

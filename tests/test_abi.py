@@ -58,7 +58,8 @@ def test_struct_layout_matches_header(tmp_path):
     from petite_gb300 import _lib
     structs = {"pt_tables": _lib.PtTables, "pt_particles": _lib.PtParticles, "pt_opts": _lib.PtOpts,
                "pt_tally": _lib.PtTally, "pt_dark_maps": _lib.PtDarkMaps, "pt_dark_params": _lib.PtDarkParams,
-               "pt_dark_out": _lib.PtDarkOut, "pt_batch_tuning": _lib.PtBatchTuning}
+               "pt_dark_out": _lib.PtDarkOut, "pt_batch_tuning": _lib.PtBatchTuning,
+               "pt_train_target": _lib.PtTrainTarget}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "petite_gpu.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
