@@ -209,13 +209,22 @@ pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* wav
  *                 PT_LOOP_GRAPH a CUDA graph whose conditional WHILE node
  *                 repeats the wave with its plan made on the GPU;
  *                 PT_LOOP_PERSISTENT one cooperative kernel runs every wave
- *                 between grid barriers.  Results are identical. */
+ *                 between grid barriers.  Results are identical.
+ *  staging:       where the mixed engine's propagation kernel reads the
+ *                 float32 n*sigma tables: PT_STAGE_SHARED each block's
+ *                 shared memory, filled by TMA bulk copies at block start
+ *                 (used with PT_LOOP_HOST and PT_LOOP_GRAPH when the tables
+ *                 fit PT_STAGE_MAX_NODES entries and are 16-byte aligned;
+ *                 otherwise the cached path runs); PT_STAGE_CACHED through
+ *                 the read-only data cache; PT_STAGE_DEFAULT (0) the shared
+ *                 form.  Results are identical. */
 enum { PT_LOOP_HOST = 0, PT_LOOP_GRAPH = 1, PT_LOOP_PERSISTENT = 2 };
+enum { PT_STAGE_DEFAULT = 0, PT_STAGE_CACHED = 1, PT_STAGE_SHARED = 2, PT_STAGE_MAX_NODES = 2048 };
 typedef struct pt_batch_tuning {
   int32_t refill_min[2];
   int32_t chunk[2];
   int32_t loop;
-  int32_t reserved0;
+  int32_t staging;
 } pt_batch_tuning;
 /* Stores the settings on the handle (NULL restores the defaults);
  * PT_BAD_ARG for a value out of range. */

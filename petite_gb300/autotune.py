@@ -2,8 +2,10 @@
 
 Picks, for one GPU, target and precision, the settings of
 ``pt_set_batch_tuning`` -- idle lanes gathered before a refill and pool
-entries claimed per atomic, for the propagation and the sampler kernel, and
-who runs the waves (the host, a CUDA graph's conditional loop, or one
+entries claimed per atomic, for the propagation and the sampler kernel,
+where the mixed propagation kernel reads its cross-section tables (the
+read-only data cache, or shared memory staged by TMA bulk copies), and who
+runs the waves (the host, a CUDA graph's conditional loop, or one
 persistent kernel) -- by timing short calibration transports (CUDA events
 around the whole run on its stream) over a small grid, one coordinate at a
 time.
@@ -19,9 +21,9 @@ import os
 import numpy as np
 
 GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128),
-        "loop": ("host", "graph", "persistent")}
-DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host"}
-CACHE_VERSION = 2
+        "staging": ("cached", "shared"), "loop": ("host", "graph", "persistent")}
+DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host", "staging": "shared"}
+CACHE_VERSION = 3
 
 
 def _cache_path():
@@ -40,9 +42,10 @@ def _calibration_primaries(n, seed):
 def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
                    verbose=False, choose_loop=True):
     """Tunes ``shower``'s engine and returns the chosen settings
-    ``{"refill_min": [p, s], "chunk": [p, s], "loop": l, "seconds": t, "loop_seconds": {...}}``
-    (``loop_seconds``: the calibration run under each loop at the final work
-    distribution).  ``choose_loop=False`` times the loops but keeps the host
+    ``{"refill_min": [p, s], "chunk": [p, s], "staging": g, "loop": l, "seconds": t,
+    "staging_seconds": {...}, "loop_seconds": {...}}`` (``*_seconds``: the
+    calibration run under each option, the earlier coordinates already
+    chosen).  ``choose_loop=False`` times the loops but keeps the host
     loop, whose per-kernel event times a roofline needs."""
     import torch
     eng = shower._engine
@@ -57,7 +60,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
             cache = {}
     if use_cache and key in cache:
         best = cache[key]
-        eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"))
+        eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"), best.get("staging", "default"))
         return best
 
     p0, pid, m = _calibration_primaries(n, seed)
@@ -71,7 +74,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     stream = torch.cuda.current_stream(dev)
 
     def run(cfg):
-        eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"])
+        eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"], cfg["staging"])
         opts = shower._opts(True, precision)
         tally.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -82,13 +85,15 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
         b.synchronize()
         return a.elapsed_time(b) / 1e3
 
-    cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"]}
+    cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"],
+           "staging": DEFAULT["staging"]}
     run(cfg)                                            # warm-up (scratch, caches)
     best_t = run(cfg)
-    loop_seconds = {}
+    seconds = {"staging": {}, "loop": {}}
     for name, values in GRID.items():
         for v in values:
-            trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"]}
+            trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"],
+                     "staging": cfg["staging"]}
             if name == "refill_min":
                 trial["refill_min"] = [v, v]
             elif name == "chunk_propagate":
@@ -96,23 +101,23 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
             elif name == "chunk_sample":
                 trial["chunk"][1] = v
             else:
-                trial["loop"] = v
+                trial[name] = v
             if trial == cfg:
-                if name == "loop":
-                    loop_seconds[v] = best_t
+                if name in seconds:
+                    seconds[name][v] = best_t
                 continue
             t = run(trial)
-            if name == "loop":
-                loop_seconds[v] = t
-                if not choose_loop:
+            if name in seconds:
+                seconds[name][v] = t
+                if name == "loop" and not choose_loop:
                     continue
             if verbose:
                 print("autotune", trial, round(t, 4))
             if t < best_t * 0.99:                       # a change must beat noise
                 best_t, cfg = t, trial
-    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "loop": cfg["loop"], "seconds": best_t,
-            "loop_seconds": loop_seconds}
-    eng.set_tuning(best["refill_min"], best["chunk"], best["loop"])
+    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "staging": cfg["staging"], "loop": cfg["loop"],
+            "seconds": best_t, "staging_seconds": seconds["staging"], "loop_seconds": seconds["loop"]}
+    eng.set_tuning(best["refill_min"], best["chunk"], best["loop"], best["staging"])
     if use_cache:
         cache[key] = best
         try:

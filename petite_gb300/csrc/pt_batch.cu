@@ -20,6 +20,7 @@
 // PREC = 0 is the float64 engine (same device functions and operation order
 // as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
 // builds directions in float32 and keeps energies in float64.
+#include <algorithm>
 #include <cstdio>
 #include <type_traits>
 
@@ -253,40 +254,58 @@ __device__ __forceinline__ void out_take(OutPool& P, unsigned long long* ctr, in
 }
 
 // ---------------------------------------------- float32 table lookups
+// The float32 n*sigma tables (nodes, values, slopes) read either through the
+// read-only data path (SH = false) or from a block's shared-memory copy
+// (SH = true; staged by TMA bulk copies, stage_ns_tables).
+template <bool SH> struct Ns32 { const float* x; const float* y; const float* s; };
+template <bool SH> __device__ __forceinline__ float ld32(const float* p) {
+  if constexpr (SH) return *p;
+  else return __ldg(p);
+}
+__device__ __forceinline__ Ns32<false> ns_global(const Tabs& T) { return {T.t.ns_x32, T.t.ns_y32, T.t.ns_s32}; }
+
+template <bool SH>
 __device__ __forceinline__ int geo_index(const float* x, int n, float lnx0, float idl, float E) {
   int j = (int)((__logf(E) - lnx0) * idl);
   j = j < 0 ? 0 : (j > n - 2 ? n - 2 : j);
-  while (j > 0 && __ldg(x + j) > E) --j;
-  while (j < n - 2 && __ldg(x + j + 1) <= E) ++j;
+  while (j > 0 && ld32<SH>(x + j) > E) --j;
+  while (j < n - 2 && ld32<SH>(x + j + 1) <= E) ++j;
   return j;
 }
 
 // interp1d(kind='linear', fill_value=0) in float32 (shower.py:280-295)
-__device__ __forceinline__ float nsig32(const Tabs& T, int slot, float E) {
+template <bool SH>
+__device__ __forceinline__ float nsig32(const Tabs& T, const Ns32<SH>& v, int slot, float E) {
   const int b = T.t.ns_base[slot], n = T.t.ns_len[slot];
-  const float* x = T.t.ns_x32 + b;
-  if (!(E >= __ldg(x)) || E > __ldg(x + n - 1)) return 0.f;
-  const int j = geo_index(x, n, T.t.ns_lnx0[slot], T.t.ns_invdlog[slot], E);
-  return fmaf(E - __ldg(x + j), __ldg(T.t.ns_s32 + b + j), __ldg(T.t.ns_y32 + b + j));
+  const float* x = v.x + b;
+  if (!(E >= ld32<SH>(x)) || E > ld32<SH>(x + n - 1)) return 0.f;
+  const int j = geo_index<SH>(x, n, T.t.ns_lnx0[slot], T.t.ns_invdlog[slot], E);
+  return fmaf(E - ld32<SH>(x + j), ld32<SH>(v.s + b + j), ld32<SH>(v.y + b + j));
 }
+__device__ __forceinline__ float nsig32(const Tabs& T, int slot, float E) { return nsig32(T, ns_global(T), slot, E); }
 
-__device__ __forceinline__ float mfp32(const Tabs& T, int pid, float E) {
+template <bool SH>
+__device__ __forceinline__ float mfp32(const Tabs& T, const Ns32<SH>& v, int pid, float E) {
   float ns;
-  if (pid == 22) ns = nsig32(T, 1, E) + nsig32(T, 3, E);
-  else if (pid == 11) ns = nsig32(T, 0, E) + nsig32(T, 4, E);
-  else if (pid == -11) ns = nsig32(T, 0, E) + nsig32(T, 5, E) + nsig32(T, 2, E);
-  else ns = nsig32(T, 7, E) + nsig32(T, 6, E);
+  if (pid == 22) ns = nsig32(T, v, 1, E) + nsig32(T, v, 3, E);
+  else if (pid == 11) ns = nsig32(T, v, 0, E) + nsig32(T, v, 4, E);
+  else if (pid == -11) ns = nsig32(T, v, 0, E) + nsig32(T, v, 5, E) + nsig32(T, v, 2, E);
+  else ns = nsig32(T, v, 7, E) + nsig32(T, v, 6, E);
   return ns > 0.f ? (float)kCmToM / ns : 1.0e12f;
 }
 
 // Process choice in float32 (shower.py:665-698)
-__device__ __forceinline__ int choose32(const Tabs& T, int pid, float E, float u) {
+template <bool SH>
+__device__ __forceinline__ int choose32(const Tabs& T, const Ns32<SH>& v, int pid, float E, float u) {
   float c0, c1, c2 = 0.f;
   int n0, n1, n2 = -1;
-  if (pid == 11) { n0 = PT_BREM; n1 = PT_MOLLER; c0 = nsig32(T, 0, E); c1 = nsig32(T, 4, E); }
-  else if (pid == -11) { n0 = PT_BREM; n1 = PT_ANN; n2 = PT_BHABHA; c0 = nsig32(T, 0, E); c1 = nsig32(T, 2, E); c2 = nsig32(T, 5, E); }
-  else if (pid == 22) { n0 = PT_PAIRPROD; n1 = PT_COMP; c0 = nsig32(T, 1, E); c1 = nsig32(T, 3, E); }
-  else { n0 = PT_MUONE; n1 = PT_MUONBREM; c0 = nsig32(T, 6, E); c1 = nsig32(T, 7, E); }
+  if (pid == 11) { n0 = PT_BREM; n1 = PT_MOLLER; c0 = nsig32(T, v, 0, E); c1 = nsig32(T, v, 4, E); }
+  else if (pid == -11) {
+    n0 = PT_BREM; n1 = PT_ANN; n2 = PT_BHABHA;
+    c0 = nsig32(T, v, 0, E); c1 = nsig32(T, v, 2, E); c2 = nsig32(T, v, 5, E);
+  }
+  else if (pid == 22) { n0 = PT_PAIRPROD; n1 = PT_COMP; c0 = nsig32(T, v, 1, E); c1 = nsig32(T, v, 3, E); }
+  else { n0 = PT_MUONE; n1 = PT_MUONBREM; c0 = nsig32(T, v, 6, E); c1 = nsig32(T, v, 7, E); }
   const float sum = c0 + c1 + c2;
   if (!(sum > 0.f)) return -1;
   const float t = u * sum;
@@ -303,7 +322,7 @@ __device__ __forceinline__ int lu_key32(const Tabs& T, int process, float E) {
   if (!(E > __ldg(Ei))) best = 0;
   else if (E >= __ldg(Ei + n - 1)) best = n - 1;
   else {
-    const int j = geo_index(Ei, n, T.t.map_lnE0[process], T.t.map_invdlog[process], E);  // Ei[j] <= E < Ei[j+1]
+    const int j = geo_index<false>(Ei, n, T.t.map_lnE0[process], T.t.map_invdlog[process], E);  // Ei[j] <= E < Ei[j+1]
     best = (E - __ldg(Ei + j) <= __ldg(Ei + j + 1) - E) ? j : j + 1;
   }
   const int key = best + 1;
@@ -552,8 +571,9 @@ struct FinEntry {
   float px, py, pz, x, y, z, u, pme, th0;   // th0: polar angle of p0 (creation histogram)
 };
 
-__device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t (*buf)[kBuf], volatile int* bcnt,
-                           LocalTally& L, unsigned int* sh_hist) {
+template <bool SH>
+__device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq, int count, int32_t (*buf)[kBuf],
+                           volatile int* bcnt, LocalTally& L, unsigned int* sh_hist) {
   const int lane = threadIdx.x & 31;
   const bool on = lane < count;
   int process = -1, prim = 0;
@@ -571,7 +591,7 @@ __device__ void run_finish(const WaveCtx<1>& c, FinEntry* fq, int count, int32_t
     const double eloss = e.E0 - e.E;
     L.e_cont += eloss;
     const float Ef = (float)e.E;
-    process = choose32(c.T, e.pid, Ef, e.u);             // shower.py:665-698
+    process = choose32(c.T, ns, e.pid, Ef, e.u);         // shower.py:665-698
     emit = process >= 0 && Ef > e.pme;
     if (emit) {                                          // park the state for the sampler
       c.q.E[i] = e.E; c.q.px[i] = e.px; c.q.py[i] = e.py; c.q.pz[i] = e.pz;
@@ -598,8 +618,8 @@ struct PropSharedMixed {
   FinEntry fin[kWarps][64];
 };
 
-template <int BETHE>
-__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixed& sm) {
+template <int BETHE, bool SH>
+__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixed& sm, const Ns32<SH> ns) {
   unsigned int* sh_hist = sm.hist;
   int32_t (*sh_buf)[8][kBuf] = sm.buf;
   int (*sh_bcnt)[8] = sm.bcnt;
@@ -693,13 +713,13 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       rng.peek(dr, c.rk);
       int base = 1;                                       // first multiple-scattering draw
       if (!charged) {
-        step = -mfp32(T, pid, Ef) * log1pf(-dr.u[0]);     // mfp log(1/(1-u))
+        step = -mfp32(T, ns, pid, Ef) * log1pf(-dr.u[0]); // mfp log(1/(1-u))
       } else if (!(Ef >= pmef)) {
         step = dr.u[0] * dzf;                             // shower.py:584-585
         mlep = me;                                        // shower.py:596-598: electron mass
       } else {
         ++L.substeps;
-        const float mfp = mfp32(T, pid, Ef);
+        const float mfp = mfp32(T, ns, pid, Ef);
         const float u_hard = dr.u[0];
         const float q = fmaf(14.f, dr.u[1], 6.f);         // delta_z = mfp / U(6, 20)
         dzf = mfp / q;
@@ -770,7 +790,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       fcount += __popc(fm);
       __syncwarp();
       if (fcount >= 32) {
-        run_finish(c, fq, 32, buf, bcnt, L, sh_hist);
+        run_finish(c, ns, fq, 32, buf, bcnt, L, sh_hist);
         __syncwarp();
         const int rest = fcount - 32;
         FinEntry carry;
@@ -782,15 +802,98 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       }
     }
   }
-  if (fcount > 0) run_finish(c, fq, fcount, buf, bcnt, L, sh_hist);
+  if (fcount > 0) run_finish(c, ns, fq, fcount, buf, bcnt, L, sh_hist);
   publish_rest(c, buf, bcnt);
   flush_tally(c.tally, L, sh_hist);
 }
 
-template <int BETHE>
+// Entries of the float32 n*sigma tables (all slots, one after another).
+__device__ __forceinline__ int ns_total(const Tabs& T) {
+  int n = 0;
+#pragma unroll
+  for (int s = 0; s < PT_N_NSIGMA; ++s) n = max(n, T.t.ns_base[s] + T.t.ns_len[s]);
+  return n;
+}
+
+// PT_STAGE_SHARED: the block copies the float32 n*sigma tables (nodes,
+// values, slopes; each array padded to 16 bytes in shared memory) into its
+// shared memory with three TMA bulk copies (cp.async.bulk) that complete on
+// one mbarrier; the last total % 4 entries of each array, under 16 bytes,
+// are plain loads.  The host selects this only when the sources are 16-byte
+// aligned.  Bounded: copies that have not landed after kStageNs record
+// PT_TIMEOUT, the block waits once more with the same bound for its copies
+// in flight and returns false.
+constexpr unsigned long long kStageNs = 1000ull * 1000ull * 1000ull;
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long bound_ns) {
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (global_ns() - t0 > bound_ns) return false;
+  }
+}
+
+__device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int pad) {
+  __shared__ __align__(8) unsigned long long bar;
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+  const float* src[3] = {c.T.t.ns_x32, c.T.t.ns_y32, c.T.t.ns_s32};
+  const int bulk = total & ~3;
+  const uint32_t bytes = (uint32_t)bulk * 4u;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(b), "r"(3u * bytes)
+                 : "memory");
+    (void)state;
+    if (bytes)
+      for (int a = 0; a < 3; ++a) {
+        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sh + a * pad);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(dst), "l"(src[a]), "r"(bytes), "r"(b)
+                     : "memory");
+      }
+  }
+  const int rest = total - bulk;
+  if (threadIdx.x < 3 * rest) {
+    const int a = threadIdx.x / rest, k = bulk + threadIdx.x % rest;
+    sh[a * pad + k] = __ldg(src[a] + k);
+  }
+  __syncthreads();                                       // the barrier is initialised before any wait
+  const bool landed = __syncthreads_and(mbar_wait(b, 0, kStageNs));
+  if (!landed) {
+    if (threadIdx.x == 0) {
+      atomicCAS(c.status, 0, PT_TIMEOUT);
+      mbar_wait(b, 0, kStageNs);
+    }
+    __syncthreads();
+  }
+  return landed;
+}
+
+template <int BETHE, bool STAGE>
 __global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
   __shared__ PropSharedMixed sm;
-  propagate_mixed_body<BETHE>(c, sm);
+  if constexpr (STAGE) {
+    extern __shared__ __align__(16) float ns_sh[];
+    const int total = ns_total(c.T), pad = (total + 3) & ~3;
+    if (!stage_ns_tables(c, ns_sh, total, pad)) return;
+    propagate_mixed_body<BETHE, true>(c, sm, Ns32<true>{ns_sh, ns_sh + pad, ns_sh + 2 * pad});
+  } else {
+    propagate_mixed_body<BETHE, false>(c, sm, ns_global(c.T));
+  }
 }
 
 // ------------------------------------------------------------ phase 2
@@ -1261,11 +1364,6 @@ __global__ void k_feed_planned(WaveCtx<PREC> c) {
 // Bounded: a block that waits longer than kBarrierNs records PT_TIMEOUT and
 // returns false, and every block then leaves the kernel within the same bound.
 constexpr unsigned long long kBarrierNs = 20ull * 1000ull * 1000ull * 1000ull;
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 __device__ bool grid_barrier(unsigned int* bar, int* status) {
   __shared__ int ok;
   __syncthreads();
@@ -1313,7 +1411,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_persistent(Wave
     if (__ldcg(&c.plan->done)) break;
     feed_planned(c, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
     if (!grid_barrier(bar, c.status)) break;
-    if constexpr (PREC == 1) propagate_mixed_body<BETHE>(c, sm.p);
+    if constexpr (PREC == 1) propagate_mixed_body<BETHE, false>(c, sm.p, ns_global(c.T));
     else propagate_fp64_body<BETHE>(c, sm.p);
     if (!grid_barrier(bar, c.status)) break;
     sample_body<PREC>(c, sm.s);
@@ -1373,6 +1471,28 @@ pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
   return PT_OK;
 }
 
+// Shared memory of the PT_STAGE_SHARED propagation kernel: the three float32
+// n*sigma arrays, each padded to 16 bytes; 0 (the cached path) when the
+// tables exceed PT_STAGE_MAX_NODES entries or a source is not 16-byte
+// aligned, as the bulk copies require.
+static size_t ns_stage_bytes(const pt_tables& t) {
+  int total = 0;
+  for (int s = 0; s < PT_N_NSIGMA; ++s) total = std::max(total, t.ns_base[s] + t.ns_len[s]);
+  if (total <= 0 || total > PT_STAGE_MAX_NODES) return 0;
+  for (const float* a : {t.ns_x32, t.ns_y32, t.ns_s32})
+    if (!a || (reinterpret_cast<uintptr_t>(a) & 15u)) return 0;
+  return (size_t)3 * (size_t)((total + 3) & ~3) * sizeof(float);
+}
+
+template <int PREC>
+static const void* propagate_kernel(int bethe, bool staged) {
+  if constexpr (PREC == 1) {
+    if (staged) return bethe ? (const void*)k_propagate_mixed<1, true> : (const void*)k_propagate_mixed<0, true>;
+    return bethe ? (const void*)k_propagate_mixed<1, false> : (const void*)k_propagate_mixed<0, false>;
+  }
+  return bethe ? (const void*)k_propagate_fp64<1> : (const void*)k_propagate_fp64<0>;
+}
+
 // Lays out the ring arrays for one engine form in the scratch memory.
 template <int PREC>
 static RingT<PREC> carve_ring(BatchScratch* s) {
@@ -1405,11 +1525,11 @@ void batch_scratch_free(BatchScratch* s) {
   delete s;
 }
 
-static int resident_blocks(const void* kernel) {
+static int resident_blocks(const void* kernel, size_t dyn_smem = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, dyn_smem);
   if (per < 1) per = 1;
   return sms * per;
 }
@@ -1437,8 +1557,8 @@ static pt_status finish_planned(HandleParts& hp, BatchScratch* S, cudaStream_t s
 // host waits once.  The kernels run at their resident grids; a wave smaller
 // than that leaves the extra blocks without work.
 template <int PREC>
-static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> c, const void* kp, int rb_p, int rb_s,
-                                cudaStream_t st) {
+static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> c, const void* kp, size_t smem_p,
+                                int rb_p, int rb_s, cudaStream_t st) {
   c.plan = S->plan;
   c.slack = (int64_t)rb_s * kWarps * kOutChunk;
   PT_CUDA(cudaMemsetAsync(S->plan, 0, sizeof(WavePlan), st));
@@ -1477,7 +1597,7 @@ static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> 
     k_feed_planned<PREC><<<gf, 256, 0, cs>>>(c);
     {
       void* args[] = {&c};
-      cudaLaunchKernel(kp, dim3(rb_p), dim3(kThreads), args, 0, cs);
+      cudaLaunchKernel(kp, dim3(rb_p), dim3(kThreads), args, smem_p, cs);
     }
     k_sample<PREC><<<rb_s, kThreads, 0, cs>>>(c);
     PT_G(cudaStreamEndCapture(cs, &body));
@@ -1562,13 +1682,13 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.cap = S->cap;
   c.feed_max = S->cap / 1024 > 256 ? S->cap / 1024 : 256;
   c.slack = 0;
-  const void* kp = PREC ? (c.mcs_mode ? (const void*)k_propagate_mixed<1> : (const void*)k_propagate_mixed<0>)
-                       : (c.mcs_mode ? (const void*)k_propagate_fp64<1> : (const void*)k_propagate_fp64<0>);
+  const size_t smem_p = PREC == 1 && tu[5] != PT_STAGE_CACHED ? ns_stage_bytes(c.T.t) : 0;
+  const void* kp = propagate_kernel<PREC>(c.mcs_mode, smem_p > 0);
   const void* ks = (const void*)k_sample<PREC>;
-  const int rb_p = resident_blocks(kp);
+  const int rb_p = resident_blocks(kp, smem_p);
   const int rb_s = resident_blocks(ks);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
-  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, rb_p, rb_s, st);
+  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, rb_p, rb_s, st);
   if (tu[4] == PT_LOOP_PERSISTENT)
     return c.mcs_mode ? run_persistent<PREC, 1>(hp, S, c, st) : run_persistent<PREC, 0>(hp, S, c, st);
   const int64_t cap = S->cap;
@@ -1617,12 +1737,10 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
     PT_CUDA(cudaEventRecord(S->ev[0], st));
-    if constexpr (PREC == 1) {
-      if (c.mcs_mode) k_propagate_mixed<1><<<gp, kThreads, 0, st>>>(c);
-      else k_propagate_mixed<0><<<gp, kThreads, 0, st>>>(c);
+    {
+      void* args[] = {&c};
+      PT_CUDA(cudaLaunchKernel(kp, dim3(gp), dim3(kThreads), args, smem_p, st));
     }
-    else if (c.mcs_mode) k_propagate_fp64<1><<<gp, kThreads, 0, st>>>(c);
-    else k_propagate_fp64<0><<<gp, kThreads, 0, st>>>(c);
     PT_CUDA(cudaEventRecord(S->ev[1], st));
     k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
     PT_CUDA(cudaEventRecord(S->ev[2], st));

@@ -109,6 +109,8 @@ def test_autotune_picks_valid_settings(lead):
     assert best["chunk"][0] in (128,) + GRID["chunk_propagate"]
     assert best["chunk"][1] in (64,) + GRID["chunk_sample"]
     assert best["loop"] in GRID["loop"]
+    assert best["staging"] in GRID["staging"]
+    assert set(best["staging_seconds"]) == set(GRID["staging"])
     assert best["seconds"] > 0
     lead._engine.set_tuning((0, 0), (0, 0))
 
@@ -143,6 +145,34 @@ def test_device_planned_loops_give_identical_results(lead, precision, loop):
             assert np.abs(ha[k] - hb[k]).sum() <= 1e-5 * ha[k].sum(), k
     np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-9)
     np.testing.assert_allclose(a.energy.cpu().numpy(), b.energy.cpu().numpy(), rtol=1e-9)
+
+
+@pytest.mark.parametrize("bethe", [False, True])
+@pytest.mark.parametrize("loop", ["host", "graph"])
+def test_shared_memory_staging_gives_identical_results(loop, bethe):
+    """The propagation kernel that reads the n*sigma tables from shared
+    memory (staged by TMA bulk copies) makes the same decisions as the one
+    that reads them through the read-only cache."""
+    from petite_gb300 import Shower
+    sh = Shower(None, "lead", 0.010, seed=SEED, fast_MCS_mode=not bethe)
+    p0, pid, m = primaries(800, seed=37, emax=50.0)
+    eng = sh._engine
+    eng.set_tuning((0, 0), (0, 0), "host", "cached")
+    a = run_batch(sh, p0, pid, m, "mixed", cap=1 << 16)
+    eng.set_tuning((0, 0), (0, 0), loop, "shared")
+    try:
+        b = run_batch(sh, p0, pid, m, "mixed", cap=1 << 16)
+    finally:
+        eng.set_tuning((0, 0), (0, 0))
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    assert np.array_equal(a.counts.cpu().numpy(), b.counts.cpu().numpy())
+    ha, hb = a.hist.cpu().numpy().astype(np.int64), b.hist.cpu().numpy().astype(np.int64)
+    # another kernel instantiation: a contraction into a fused multiply-add
+    # may differ and move a binned value across a bin edge, never a decision
+    assert (np.abs(ha - hb).sum(axis=(1, 2)) <= 1e-5 * ha.sum(axis=(1, 2))).all()
+    np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-9)
+    with pytest.raises(Exception):
+        eng.set_tuning((0, 0), (0, 0), "host", "tma")
 
 
 def test_device_planned_loop_in_bethe_mode():
