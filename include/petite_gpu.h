@@ -217,7 +217,11 @@ pt_status pt_last_run_stats(pt_handle* h, int64_t* kernel_launches, int64_t* wav
  *                 fit PT_STAGE_MAX_NODES entries and are 16-byte aligned;
  *                 otherwise the cached path runs); PT_STAGE_CACHED through
  *                 the read-only data cache; PT_STAGE_DEFAULT (0) the shared
- *                 form.  Results are identical. */
+ *                 form.  Results are identical.
+ *  threads:       threads per block of the mixed engine's two kernels with
+ *                 PT_LOOP_HOST and PT_LOOP_GRAPH: 64, 128 or 256 (0: 128).
+ *                 The FP64 kernels and the persistent kernel run 128.
+ *                 Results are identical. */
 enum { PT_LOOP_HOST = 0, PT_LOOP_GRAPH = 1, PT_LOOP_PERSISTENT = 2 };
 enum { PT_STAGE_DEFAULT = 0, PT_STAGE_CACHED = 1, PT_STAGE_SHARED = 2, PT_STAGE_MAX_NODES = 2048 };
 typedef struct pt_batch_tuning {
@@ -225,6 +229,8 @@ typedef struct pt_batch_tuning {
   int32_t chunk[2];
   int32_t loop;
   int32_t staging;
+  int32_t threads;
+  int32_t reserved0;
 } pt_batch_tuning;
 /* Stores the settings on the handle (NULL restores the defaults);
  * PT_BAD_ARG for a value out of range. */

@@ -107,7 +107,8 @@ class PtTrainTarget(C.Structure):
 
 
 class PtBatchTuning(C.Structure):
-    _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("staging", C.c_int32)]
+    _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("staging", C.c_int32),
+                ("threads", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class PetiteGPUError(RuntimeError):

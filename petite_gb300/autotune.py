@@ -3,7 +3,8 @@
 Picks, for one GPU, target and precision, the settings of
 ``pt_set_batch_tuning`` -- idle lanes gathered before a refill and pool
 entries claimed per atomic, for the propagation and the sampler kernel,
-where the mixed propagation kernel reads its cross-section tables (the
+the threads per block of the mixed kernels, where the mixed propagation
+kernel reads its cross-section tables (the
 read-only data cache, or shared memory staged by TMA bulk copies), and who
 runs the waves (the host, a CUDA graph's conditional loop, or one
 persistent kernel) -- by timing short calibration transports (CUDA events
@@ -21,9 +22,9 @@ import os
 import numpy as np
 
 GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128),
-        "staging": ("cached", "shared"), "loop": ("host", "graph", "persistent")}
-DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host", "staging": "shared"}
-CACHE_VERSION = 3
+        "threads": (64, 128, 256), "staging": ("cached", "shared"), "loop": ("host", "graph", "persistent")}
+DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host", "staging": "shared", "threads": 128}
+CACHE_VERSION = 4
 
 
 def _cache_path():
@@ -42,8 +43,8 @@ def _calibration_primaries(n, seed):
 def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
                    verbose=False, choose_loop=True):
     """Tunes ``shower``'s engine and returns the chosen settings
-    ``{"refill_min": [p, s], "chunk": [p, s], "staging": g, "loop": l, "seconds": t,
-    "staging_seconds": {...}, "loop_seconds": {...}}`` (``*_seconds``: the
+    ``{"refill_min": [p, s], "chunk": [p, s], "threads": b, "staging": g, "loop": l, "seconds": t,
+    "threads_seconds": {...}, "staging_seconds": {...}, "loop_seconds": {...}}`` (``*_seconds``: the
     calibration run under each option, the earlier coordinates already
     chosen).  ``choose_loop=False`` times the loops but keeps the host
     loop, whose per-kernel event times a roofline needs."""
@@ -60,7 +61,8 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
             cache = {}
     if use_cache and key in cache:
         best = cache[key]
-        eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"), best.get("staging", "default"))
+        eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"), best.get("staging", "default"),
+                       best.get("threads", 0))
         return best
 
     p0, pid, m = _calibration_primaries(n, seed)
@@ -74,7 +76,8 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     stream = torch.cuda.current_stream(dev)
 
     def run(cfg):
-        eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"], cfg["staging"])
+        eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"], cfg["staging"],
+                       cfg["threads"] if precision == "mixed" else 0)
         opts = shower._opts(True, precision)
         tally.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -86,14 +89,16 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
         return a.elapsed_time(b) / 1e3
 
     cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"],
-           "staging": DEFAULT["staging"]}
+           "staging": DEFAULT["staging"], "threads": DEFAULT["threads"]}
     run(cfg)                                            # warm-up (scratch, caches)
     best_t = run(cfg)
-    seconds = {"staging": {}, "loop": {}}
+    seconds = {"threads": {}, "staging": {}, "loop": {}}
     for name, values in GRID.items():
+        if name in ("threads", "staging") and precision != "mixed":
+            continue                                    # float32 kernels only
         for v in values:
             trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"],
-                     "staging": cfg["staging"]}
+                     "staging": cfg["staging"], "threads": cfg["threads"]}
             if name == "refill_min":
                 trial["refill_min"] = [v, v]
             elif name == "chunk_propagate":
@@ -115,9 +120,12 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
                 print("autotune", trial, round(t, 4))
             if t < best_t * 0.99:                       # a change must beat noise
                 best_t, cfg = t, trial
-    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "staging": cfg["staging"], "loop": cfg["loop"],
-            "seconds": best_t, "staging_seconds": seconds["staging"], "loop_seconds": seconds["loop"]}
-    eng.set_tuning(best["refill_min"], best["chunk"], best["loop"], best["staging"])
+    best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "threads": cfg["threads"],
+            "staging": cfg["staging"], "loop": cfg["loop"], "seconds": best_t,
+            "threads_seconds": seconds["threads"], "staging_seconds": seconds["staging"],
+            "loop_seconds": seconds["loop"]}
+    eng.set_tuning(best["refill_min"], best["chunk"], best["loop"], best["staging"],
+                   best["threads"] if precision == "mixed" else 0)
     if use_cache:
         cache[key] = best
         try:

@@ -282,7 +282,6 @@ __device__ __forceinline__ float nsig32(const Tabs& T, const Ns32<SH>& v, int sl
   const int j = geo_index<SH>(x, n, T.t.ns_lnx0[slot], T.t.ns_invdlog[slot], E);
   return fmaf(E - ld32<SH>(x + j), ld32<SH>(v.s + b + j), ld32<SH>(v.y + b + j));
 }
-__device__ __forceinline__ float nsig32(const Tabs& T, int slot, float E) { return nsig32(T, ns_global(T), slot, E); }
 
 template <bool SH>
 __device__ __forceinline__ float mfp32(const Tabs& T, const Ns32<SH>& v, int pid, float E) {
@@ -611,15 +610,17 @@ __device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq
 
 // BETHE: Shower(fast_MCS_mode=False); a separate instantiation keeps the
 // Bethe-Moliere inverse CDF out of the fast mode's registers.
-struct PropSharedMixed {
+// NW: warps per block (the block size is a tuning choice of the float32 kernels).
+template <int NW> struct PropSharedMixedT {
   unsigned int hist[kHist];
-  int32_t buf[kWarps][8][kBuf];
-  int bcnt[kWarps][8];
-  FinEntry fin[kWarps][64];
+  int32_t buf[NW][8][kBuf];
+  int bcnt[NW][8];
+  FinEntry fin[NW][64];
 };
+using PropSharedMixed = PropSharedMixedT<kWarps>;
 
-template <int BETHE, bool SH>
-__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixed& sm, const Ns32<SH> ns) {
+template <int BETHE, bool SH, int NW>
+__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixedT<NW>& sm, const Ns32<SH> ns) {
   unsigned int* sh_hist = sm.hist;
   int32_t (*sh_buf)[8][kBuf] = sm.buf;
   int (*sh_bcnt)[8] = sm.bcnt;
@@ -627,7 +628,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
   const int64_t wave_n = w_n(c);
   const uint64_t wave_head = w_head(c);
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
-  if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
+  if (threadIdx.x < NW * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
   __syncthreads();
   const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
   int32_t (*buf)[kBuf] = sh_buf[w];
@@ -852,12 +853,7 @@ __device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int p
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    unsigned long long state;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
-                 : "=l"(state)
-                 : "r"(b), "r"(3u * bytes)
-                 : "memory");
-    (void)state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(3u * bytes) : "memory");
     if (bytes)
       for (int a = 0; a < 3; ++a) {
         const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sh + a * pad);
@@ -883,9 +879,12 @@ __device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int p
   return landed;
 }
 
-template <int BETHE, bool STAGE>
-__global__ void __launch_bounds__(kThreads, 5) k_propagate_mixed(WaveCtx<1> c) {
-  __shared__ PropSharedMixed sm;
+// 96 registers at 2 and 4 warps per block (20 warps per SM), 128 at 8.
+template <int NW> constexpr int min_blocks32() { return 20 / NW; }
+
+template <int BETHE, bool STAGE, int NW>
+__global__ void __launch_bounds__(NW * 32, min_blocks32<NW>()) k_propagate_mixed(WaveCtx<1> c) {
+  __shared__ PropSharedMixedT<NW> sm;
   if constexpr (STAGE) {
     extern __shared__ __align__(16) float ns_sh[];
     const int total = ns_total(c.T), pad = (total + 3) & ~3;
@@ -1086,13 +1085,13 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
   }
 }
 
-template <int PREC> struct SampShared {
+template <int PREC, int NW = kWarps> struct SampShared {
   unsigned long long off[9];
-  KinEntry<PREC> kq[kWarps][kKinQ];
+  KinEntry<PREC> kq[NW][kKinQ];
 };
 
-template <int PREC>
-__device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<PREC>& sm) {
+template <int PREC, int NW>
+__device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<PREC, NW>& sm) {
   unsigned long long* sh_off = sm.off;
   KinEntry<PREC> (*sh_kq)[kKinQ] = sm.kq;
   if (threadIdx.x == 0) {
@@ -1252,9 +1251,9 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
   flush_tally(c.tally, L, nullptr);
 }
 
-template <int PREC>
-__global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_sample(WaveCtx<PREC> c) {
-  __shared__ SampShared<PREC> sm;
+template <int PREC, int NW>
+__global__ void __launch_bounds__(NW * 32, PREC == 1 ? min_blocks32<NW>() : 1) k_sample(WaveCtx<PREC> c) {
+  __shared__ SampShared<PREC, NW> sm;
   sample_body<PREC>(c, sm);
 }
 
@@ -1414,7 +1413,7 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_persistent(Wave
     if constexpr (PREC == 1) propagate_mixed_body<BETHE, false>(c, sm.p, ns_global(c.T));
     else propagate_fp64_body<BETHE>(c, sm.p);
     if (!grid_barrier(bar, c.status)) break;
-    sample_body<PREC>(c, sm.s);
+    sample_body<PREC, kWarps>(c, sm.s);
     if (!grid_barrier(bar, c.status)) break;
   }
 }
@@ -1484,13 +1483,31 @@ static size_t ns_stage_bytes(const pt_tables& t) {
   return (size_t)3 * (size_t)((total + 3) & ~3) * sizeof(float);
 }
 
+template <int NW>
+static const void* propagate_mixed_kernel(int bethe, bool staged) {
+  if (staged) return bethe ? (const void*)k_propagate_mixed<1, true, NW> : (const void*)k_propagate_mixed<0, true, NW>;
+  return bethe ? (const void*)k_propagate_mixed<1, false, NW> : (const void*)k_propagate_mixed<0, false, NW>;
+}
+
+// The kernels of one wave at nw warps per block (2, 4 or 8 for the float32
+// kernels; the FP64 kernels run at kWarps).
 template <int PREC>
-static const void* propagate_kernel(int bethe, bool staged) {
+static const void* propagate_kernel(int bethe, bool staged, int nw) {
   if constexpr (PREC == 1) {
-    if (staged) return bethe ? (const void*)k_propagate_mixed<1, true> : (const void*)k_propagate_mixed<0, true>;
-    return bethe ? (const void*)k_propagate_mixed<1, false> : (const void*)k_propagate_mixed<0, false>;
+    if (nw == 2) return propagate_mixed_kernel<2>(bethe, staged);
+    if (nw == 8) return propagate_mixed_kernel<8>(bethe, staged);
+    return propagate_mixed_kernel<kWarps>(bethe, staged);
   }
   return bethe ? (const void*)k_propagate_fp64<1> : (const void*)k_propagate_fp64<0>;
+}
+
+template <int PREC>
+static const void* sample_kernel(int nw) {
+  if constexpr (PREC == 1) {
+    if (nw == 2) return (const void*)k_sample<1, 2>;
+    if (nw == 8) return (const void*)k_sample<1, 8>;
+  }
+  return (const void*)k_sample<PREC, kWarps>;
 }
 
 // Lays out the ring arrays for one engine form in the scratch memory.
@@ -1525,11 +1542,11 @@ void batch_scratch_free(BatchScratch* s) {
   delete s;
 }
 
-static int resident_blocks(const void* kernel, size_t dyn_smem = 0) {
+static int resident_blocks(const void* kernel, int threads, size_t dyn_smem = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, dyn_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, dyn_smem);
   if (per < 1) per = 1;
   return sms * per;
 }
@@ -1558,9 +1575,9 @@ static pt_status finish_planned(HandleParts& hp, BatchScratch* S, cudaStream_t s
 // than that leaves the extra blocks without work.
 template <int PREC>
 static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> c, const void* kp, size_t smem_p,
-                                int rb_p, int rb_s, cudaStream_t st) {
+                                const void* ks, int nw, int rb_p, int rb_s, cudaStream_t st) {
   c.plan = S->plan;
-  c.slack = (int64_t)rb_s * kWarps * kOutChunk;
+  c.slack = (int64_t)rb_s * nw * kOutChunk;
   PT_CUDA(cudaMemsetAsync(S->plan, 0, sizeof(WavePlan), st));
   PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
   cudaGraph_t g = nullptr, body = nullptr;
@@ -1597,9 +1614,9 @@ static pt_status run_graph_loop(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> 
     k_feed_planned<PREC><<<gf, 256, 0, cs>>>(c);
     {
       void* args[] = {&c};
-      cudaLaunchKernel(kp, dim3(rb_p), dim3(kThreads), args, smem_p, cs);
+      cudaLaunchKernel(kp, dim3(rb_p), dim3(nw * 32), args, smem_p, cs);
+      cudaLaunchKernel(ks, dim3(rb_s), dim3(nw * 32), args, 0, cs);
     }
-    k_sample<PREC><<<rb_s, kThreads, 0, cs>>>(c);
     PT_G(cudaStreamEndCapture(cs, &body));
     PT_G(cudaGraphInstantiate(&ex, g, 0));
     PT_G(cudaEventRecord(S->ev[0], st));
@@ -1683,12 +1700,14 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.feed_max = S->cap / 1024 > 256 ? S->cap / 1024 : 256;
   c.slack = 0;
   const size_t smem_p = PREC == 1 && tu[5] != PT_STAGE_CACHED ? ns_stage_bytes(c.T.t) : 0;
-  const void* kp = propagate_kernel<PREC>(c.mcs_mode, smem_p > 0);
-  const void* ks = (const void*)k_sample<PREC>;
-  const int rb_p = resident_blocks(kp, smem_p);
-  const int rb_s = resident_blocks(ks);
+  const int wpb = PREC == 1 && tu[6] ? tu[6] / 32 : kWarps;
+  const int nt = wpb * 32;
+  const void* kp = propagate_kernel<PREC>(c.mcs_mode, smem_p > 0, wpb);
+  const void* ks = sample_kernel<PREC>(wpb);
+  const int rb_p = resident_blocks(kp, nt, smem_p);
+  const int rb_s = resident_blocks(ks, nt);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
-  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, rb_p, rb_s, st);
+  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, ks, wpb, rb_p, rb_s, st);
   if (tu[4] == PT_LOOP_PERSISTENT)
     return c.mcs_mode ? run_persistent<PREC, 1>(hp, S, c, st) : run_persistent<PREC, 0>(hp, S, c, st);
   const int64_t cap = S->cap;
@@ -1716,7 +1735,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     // partly used output chunk per sampler warp (bounded with the largest
     // grid); small waves reserve slots exactly and leave no dead entries.
     c.out_chunk = kOutChunk;
-    int64_t k = (cap - live - (int64_t)rb_s * kWarps * kOutChunk) / 2;
+    int64_t k = (cap - live - (int64_t)rb_s * wpb * kOutChunk) / 2;
     if (k > live) k = live;
     if (k > S->list_cap) k = S->list_cap;
     if (k < 16 * 1024) {
@@ -1733,16 +1752,14 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     c.head = head;
     c.tail = tail;
     c.n_in = k;
-    const int64_t want_blocks = (k + kThreads - 1) / kThreads;
+    const int64_t want_blocks = (k + nt - 1) / nt;
     const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
     const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
     PT_CUDA(cudaEventRecord(S->ev[0], st));
-    {
-      void* args[] = {&c};
-      PT_CUDA(cudaLaunchKernel(kp, dim3(gp), dim3(kThreads), args, smem_p, st));
-    }
+    void* args[] = {&c};
+    PT_CUDA(cudaLaunchKernel(kp, dim3(gp), dim3(nt), args, smem_p, st));
     PT_CUDA(cudaEventRecord(S->ev[1], st));
-    k_sample<PREC><<<gs, kThreads, 0, st>>>(c);
+    PT_CUDA(cudaLaunchKernel(ks, dim3(gs), dim3(nt), args, 0, st));
     PT_CUDA(cudaEventRecord(S->ev[2], st));
     PT_CUDA(cudaGetLastError());
     nl += 3;

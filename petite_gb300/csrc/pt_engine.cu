@@ -284,7 +284,7 @@ struct pt_handle {
   double last_info[3] = {0, 0, 0};
   int64_t launches[2] = {0, 0};   // kernel launches, waves of the last run
   double kernel_ms[2] = {0, 0};   // batched run: propagation and sampler device time
-  int32_t tuning[6] = {0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
+  int32_t tuning[7] = {0, 0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
   BatchScratch* batch = nullptr;
 };
 
@@ -570,7 +570,7 @@ extern "C" pt_status pt_last_run_stats(pt_handle* h, int64_t* launches, int64_t*
 extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t) {
   if (!h) return PT_BAD_ARG;
   if (!t) {
-    for (int k = 0; k < 6; ++k) h->tuning[k] = 0;
+    for (int k = 0; k < 7; ++k) h->tuning[k] = 0;
     return PT_OK;
   }
   for (int k = 0; k < 2; ++k) {
@@ -579,12 +579,14 @@ extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t)
   }
   if (t->loop < PT_LOOP_HOST || t->loop > PT_LOOP_PERSISTENT) return PT_BAD_ARG;
   if (t->staging < PT_STAGE_DEFAULT || t->staging > PT_STAGE_SHARED) return PT_BAD_ARG;
+  if (t->threads != 0 && t->threads != 64 && t->threads != 128 && t->threads != 256) return PT_BAD_ARG;
   h->tuning[0] = t->refill_min[0];
   h->tuning[1] = t->refill_min[1];
   h->tuning[2] = t->chunk[0];
   h->tuning[3] = t->chunk[1];
   h->tuning[4] = t->loop;
   h->tuning[5] = t->staging;
+  h->tuning[6] = t->threads;
   return PT_OK;
 }
 

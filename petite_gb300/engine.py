@@ -286,21 +286,24 @@ class SMEngine:
     LOOPS = {"host": 0, "graph": 1, "persistent": 2}
     STAGING = {"default": 0, "cached": 1, "shared": 2}
 
-    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default"):
+    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default", threads=0):
         """Work distribution of the batched engine (0 = library default), who
         runs its waves -- "host" (two launches per wave, counters read back),
         "graph" (a CUDA graph's conditional loop, planned on the GPU) or
         "persistent" (one cooperative kernel) -- and where the mixed
         propagation kernel reads the n*sigma tables: "shared" (each block's
         shared memory, filled by TMA bulk copies; "default"), or "cached"
-        (the read-only data cache)."""
+        (the read-only data cache) -- and the mixed kernels' threads per block
+        (64, 128 or 256; 0 = 128)."""
         t = _lib.PtBatchTuning()
         t.refill_min[0], t.refill_min[1] = int(refill_min[0]), int(refill_min[1])
         t.chunk[0], t.chunk[1] = int(chunk[0]), int(chunk[1])
         t.loop = self.LOOPS[loop]
         t.staging = self.STAGING[staging]
+        t.threads = int(threads)
         _lib.check(self.lib.pt_set_batch_tuning(self.handle, C.byref(t)), "pt_set_batch_tuning")
-        self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk), "loop": loop, "staging": staging}
+        self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk), "loop": loop, "staging": staging,
+                       "threads": int(threads)}
 
     def last_kernel_times(self):
         """Device seconds of the last batched run: (propagation, sampler)."""

@@ -110,6 +110,7 @@ def test_autotune_picks_valid_settings(lead):
     assert best["chunk"][1] in (64,) + GRID["chunk_sample"]
     assert best["loop"] in GRID["loop"]
     assert best["staging"] in GRID["staging"]
+    assert best["threads"] in GRID["threads"]
     assert set(best["staging_seconds"]) == set(GRID["staging"])
     assert best["seconds"] > 0
     lead._engine.set_tuning((0, 0), (0, 0))
@@ -173,6 +174,27 @@ def test_shared_memory_staging_gives_identical_results(loop, bethe):
     np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-9)
     with pytest.raises(Exception):
         eng.set_tuning((0, 0), (0, 0), "host", "tma")
+
+
+@pytest.mark.parametrize("threads,loop", [(64, "host"), (256, "host"), (256, "graph")])
+def test_block_size_gives_identical_results(lead, threads, loop):
+    """The float32 kernels at 64 or 256 threads per block: the same
+    particles, spectra and deposits as at 128."""
+    p0, pid, m = primaries(800, seed=41, emax=50.0)
+    eng = lead._engine
+    a = run_batch(lead, p0, pid, m, "mixed", cap=1 << 16)
+    eng.set_tuning((0, 0), (0, 0), loop, "default", threads)
+    try:
+        b = run_batch(lead, p0, pid, m, "mixed", cap=1 << 16)
+    finally:
+        eng.set_tuning((0, 0), (0, 0))
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    assert np.array_equal(a.counts.cpu().numpy(), b.counts.cpu().numpy())
+    ha, hb = a.hist.cpu().numpy().astype(np.int64), b.hist.cpu().numpy().astype(np.int64)
+    assert (np.abs(ha - hb).sum(axis=(1, 2)) <= 1e-5 * ha.sum(axis=(1, 2))).all()
+    np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-9)
+    with pytest.raises(Exception):
+        eng.set_tuning((0, 0), (0, 0), "host", "default", 96)
 
 
 def test_device_planned_loop_in_bethe_mode():
