@@ -270,10 +270,15 @@ pt_status pt_moliere_inverse_cdf(const double* u, const double* B, int64_t n, in
  * per dimension, 1..1000).  Grids: nodes[row][d][k], k = 0..ninc[d], rows
  * padded to max_nodes; acc/cnt: [row][d][1000].
  * ------------------------------------------------------------------------ */
-typedef struct pt_train_target {   /* what the SM cross sections read of a target */
+typedef struct pt_train_target {   /* what the cross sections read of a target */
   double Eg_min, Ee_min;           /* shower.py:214-215 */
   double a0sq, Z2a04;              /* aa(Z, m_e)^2 and Z^2 aa^4 (all_processes.py:92-103) */
+  double mV;                       /* dark processes: the vector's mass (GeV) */
+  double MT, Z, A;                 /* dark processes: event_info mT, Z_T, A_T (all_processes.py:208-372) */
 } pt_train_target;
+/* Process codes of the table builder: the SM codes (PT_BREM ...), and
+ * PT_TRAIN_DARK + a dark code (PT_DARKBREM ...) for the dark processes. */
+enum { PT_TRAIN_DARK = 16 };
 /* One training iteration's samples: points_per_row map points per row
  * (iteration 0..63 selects the draws); accumulates (jac f)^2 and counts per
  * increment into acc/cnt and (sum w, sum w^2) into sums[row][2]. */

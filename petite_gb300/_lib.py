@@ -103,7 +103,11 @@ class PtDarkOut(C.Structure):
 
 
 class PtTrainTarget(C.Structure):
-    _fields_ = [("Eg_min", C.c_double), ("Ee_min", C.c_double), ("a0sq", C.c_double), ("Z2a04", C.c_double)]
+    _fields_ = [("Eg_min", C.c_double), ("Ee_min", C.c_double), ("a0sq", C.c_double), ("Z2a04", C.c_double),
+                ("mV", C.c_double), ("MT", C.c_double), ("Z", C.c_double), ("A", C.c_double)]
+
+
+TRAIN_DARK = 16
 
 
 class PtBatchTuning(C.Structure):

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdio>
 
+#include "pt_dark.cuh"
 #include "pt_internal.cuh"
 #include "pt_physics.cuh"
 
@@ -41,6 +42,26 @@ __device__ __forceinline__ Tabs train_tabs(const pt_train_target& t) {
   T.a0sq = t.a0sq;
   T.Z2a04 = t.Z2a04;
   return T;
+}
+
+// The differential cross section being trained: an SM process, or a dark one
+// with the target's (mV, mT, Z, A) -- diff_xsection_options,
+// all_processes.py:1067-1083; DarkMuonBrem takes the muon mass
+// (find_maxes.py:94-97).
+__device__ __forceinline__ double train_dsigma(const Tabs& T, const pt_train_target& tg, int process, const double* x,
+                                               double E) {
+  if (process < PT_TRAIN_DARK) return dsigma_any(T, process, x, E);
+  switch (process - PT_TRAIN_DARK) {
+    case PT_DARKBREM: return dsig_dark_brem<double>(x, E, tg.mV, tg.MT, kMe, tg.Z, tg.A);
+    case PT_DARKMUONBREM: return dsig_dark_brem<double>(x, E, tg.mV, tg.MT, kMmu, tg.Z, tg.A);
+    case PT_DARKCOMP: return dsig_dark_compton<double>(x[0], E, tg.mV);
+    default: return dsig_radiative_return<double>(x[0], E, tg.mV);
+  }
+}
+
+__host__ __device__ inline bool train_process_ok(int process) {
+  return (process >= 0 && process < PT_N_PROCESSES) ||
+         (process >= PT_TRAIN_DARK && process < PT_TRAIN_DARK + PT_N_DARK);
 }
 
 struct MapView {
@@ -88,7 +109,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_vegas_accumulate(pt_train_tar
     double x[kMaxDim] = {0.0, 0.0, 0.0, 0.0};
     int inc[kMaxDim] = {0, 0, 0, 0};
     const double jac = map_point(m, g, rng, x, inc);
-    double w = jac * dsigma_any(T, process, x, Er);
+    double w = jac * train_dsigma(T, tgt, process, x, Er);
     if (!(w == w)) w = 0.0;
     s1 += w;
     s2 += w * w;
@@ -185,7 +206,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_find_maxes(const pt_train_tar
     double x[kMaxDim] = {0.0, 0.0, 0.0, 0.0};
     int inc[kMaxDim];
     const double jac = map_point(m, g, rng, x, inc);
-    const double MM = jac / neval * dsigma_any(T, process, x, Er);
+    const double MM = jac / neval * train_dsigma(T, tg[t], process, x, Er);
     if (MM > mx) mx = MM;
     if (MM == MM) sm += MM;
   }
@@ -230,7 +251,7 @@ extern "C" pt_status pt_vegas_accumulate(int32_t process, const pt_train_target*
                                          int32_t max_nodes, int64_t points_per_row, uint64_t seed, int32_t iteration,
                                          double* acc, uint32_t* cnt, double* sums, void* stream) {
   MapView m;
-  if (process < 0 || process >= PT_N_PROCESSES || !target || n_rows < 1 || n_rows > 65535 || points_per_row < 1 ||
+  if (!train_process_ok(process) || !target || n_rows < 1 || n_rows > 65535 || points_per_row < 1 ||
       iteration < 0 || iteration > 63 || !make_view(dims, ninc, max_nodes, m))
     return PT_BAD_ARG;
   if (!energy || !nodes || !acc || !cnt || !sums) return PT_BAD_ARG;
@@ -260,7 +281,7 @@ extern "C" pt_status pt_find_maxes(int32_t process, const pt_train_target* targe
                                    const double* nodes, int32_t max_nodes, int32_t neval, int32_t n_trials,
                                    uint64_t seed, double* max_F, double* xsec, void* stream) {
   MapView m;
-  if (process < 0 || process >= PT_N_PROCESSES || !targets || n_targets < 1 || n_targets > 16 || n_rows < 1 ||
+  if (!train_process_ok(process) || !targets || n_targets < 1 || n_targets > 16 || n_rows < 1 ||
       n_rows > 65535 || neval < 1 || n_trials < 1 || !make_view(dims, ninc, max_nodes, m))
     return PT_BAD_ARG;
   if (!energy || !nodes || !max_F || !xsec) return PT_BAD_ARG;

@@ -4,10 +4,13 @@ differentiable dark-vector yield.
 ``DarkShower`` keeps PETITE's constructor and methods (``GetBSMWeights``,
 ``draw_dark_sample``, ``produce_bsm_particle``, ``generate_dark_shower``);
 the dark-vector production runs in ``pt_run_dark`` over the SM particle
-rows.  Tables come from ``data/dark_tables.npz``: the dark VEGAS maps (the
-shipped ``<Process>/mV_*`` maps with max_F rebuilt by PETITE's find_maxes)
-and, per (mass, target), the weight, dR/dE and bound-electron tables
-PETITE's constructor builds (dark_shower.py:219-593).
+rows.  Tables come from the dict_dir's ``dark_tables.npz`` (bundled:
+``data/dark_tables.npz``, and ``data/400GeV/dark_tables.npz`` for the
+400 GeV tables, mV = 0.1 GeV, lead): the dark VEGAS maps (PETITE's shipped
+``<Process>/mV_*`` maps, or maps trained by ``petite_gb300.train`` where
+PETITE ships none, with max_F from find_maxes) and, per (mass, target), the
+weight, dR/dE and bound-electron tables PETITE's constructor builds
+(dark_shower.py:219-593).
 
 ``dark_yield`` is a ``torch.autograd.Function``: forward = the map estimate
 of a dark cross section and its V-energy moment at fixed Philox uniforms
@@ -338,7 +341,10 @@ class DarkShower(Shower):
         self.bound_electron = bound_electron
         self.Zeff = Zeff
         self.g_e = kinetic_mixing * np.sqrt(4 * np.pi * T.ALPHA_EM) if g_e is None else g_e
-        self._dark = DarkData(dark_tables or DARK_NPZ)
+        # the dict_dir's own dark tables (PETITE reads its dark files from
+        # dict_dir, dark_shower.py:69-130), else the bundled ones
+        own = os.path.join(self.get_dict_dir(), "dark_tables.npz")
+        self._dark = DarkData(dark_tables or (own if os.path.exists(own) else DARK_NPZ))
         self._mV_list = list(self._dark.masses)
         if mode == "exact":
             self._mV = closest_lesser_value(self._mV_list, mV_in_GeV)

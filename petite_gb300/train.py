@@ -31,16 +31,37 @@ import numpy as np
 from . import _lib
 from . import tables as T
 
+# vegas_integrator_options, all_processes.py:1085-1096 (DarkAnn: 1000
+# increments, vegas' default, for its neval-only options)
 NSTRAT = {"PairProd": (60, 50, 40, 50), "Brem": (60, 50, 50, 50), "MuonBrem": (60, 50, 50, 50),
-          "Comp": (1000,), "Moller": (1000,), "MuonE": (1000,), "Bhabha": (1000,), "Ann": (1000,)}
-NITN = {"PairProd": 10, "Brem": 10, "MuonBrem": 10, "Comp": 20, "Moller": 20, "MuonE": 20, "Bhabha": 20, "Ann": 20}
+          "Comp": (1000,), "Moller": (1000,), "MuonE": (1000,), "Bhabha": (1000,), "Ann": (1000,),
+          "DarkBrem": (100, 100, 40), "DarkMuonBrem": (100, 100, 40), "DarkComp": (1000,), "DarkAnn": (1000,)}
+NITN = {"PairProd": 10, "Brem": 10, "MuonBrem": 10, "Comp": 20, "Moller": 20, "MuonE": 20, "Bhabha": 20, "Ann": 20,
+        "DarkBrem": 20, "DarkMuonBrem": 20, "DarkComp": 20, "DarkAnn": 10}
 TRAINING_TARGET = "hydrogen"               # generate_integrators.py:118-123
+# the dark maps train on hydrogen with mT = 200 GeV
+# (script_generateintegrators_400GeV.py:51-55, generate_integrators.py:103-113)
+DARK_TRAINING_MT = 200.0
 FIND_MAXES_TARGETS = ("graphite", "lead", "iron", "aluminum", "molybdenum")
+DARK_PROCESSES = ("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")     # engine dark codes 0..3
+
+
+def process_code(process: str) -> int:
+    """The table builder's code of a process (SM codes; dark: TRAIN_DARK + dark code)."""
+    if process in DARK_PROCESSES:
+        return _lib.TRAIN_DARK + DARK_PROCESSES.index(process)
+    return T.PROCESS_CODE[process]
 
 
 def integration_range(process: str, E: float, Eg_min: float = 0.001, Ee_min: float = 0.005, mV: float = 0.0):
-    """integration_range, all_processes.py:1102-1160, SM processes."""
+    """integration_range, all_processes.py:1102-1160."""
     me = T.M_ELECTRON
+    if process in ("DarkBrem", "DarkMuonBrem"):         # x, log10(1 - cos theta), log10 t~
+        return [[max(0., mV / E), 1. - me / E], [-12.0, np.log10(2.0)], [-20.0, 0.0]]
+    if process == "DarkComp":
+        return [[-1., 1.0]]
+    if process == "DarkAnn":
+        return [[0., 1.0]] if 2.0 * me * (E + me) > mV ** 2 else [[0., 0.]]
     if process in ("PairProd", "Brem"):
         return [[0, 1], [0, 2], [-2, 2], [0, 1]]
     if process == "MuonBrem":
@@ -57,13 +78,20 @@ def n_increments(process: str):
     return [(1000 // s) * s for s in NSTRAT[process]]
 
 
-def target_constants(target: str, Eg_min: float = 0.001, Ee_min: float = 0.005) -> _lib.PtTrainTarget:
-    """What the SM cross sections read of a target (the engine's expressions,
-    all_processes.py:92-103)."""
-    Z = T.TARGET_INFORMATION[target]["Z_T"]
+def target_constants(target: str, Eg_min: float = 0.001, Ee_min: float = 0.005, mV: float = 0.0,
+                     mT: float | None = None) -> _lib.PtTrainTarget:
+    """What the cross sections read of a target: the SM screening constants
+    (the engine's expressions, all_processes.py:92-103) and, for the dark
+    processes, mV and the target's mT, Z_T, A_T (find_maxes.py:85-100; ``mT``
+    overrides the table's, as the dark training does)."""
+    ti = T.TARGET_INFORMATION[target]
+    Z = ti["Z_T"]
     a0 = 184.15 * (2.718) ** -0.5 * Z ** (-1.0 / 3.0) / T.M_ELECTRON
     t = _lib.PtTrainTarget()
     t.Eg_min, t.Ee_min, t.a0sq, t.Z2a04 = Eg_min, Ee_min, a0 ** 2, Z ** 2 * a0 ** 4
+    t.mV = float(mV)
+    t.MT = float(ti["mT"] if mT is None else mT)
+    t.Z, t.A = float(Z), float(ti["A_T"])
     return t
 
 
@@ -76,25 +104,26 @@ class MapSet:
     """The maps of one process at its energies: nodes (rows, dims, max_nodes)
     on the device, increments per dimension."""
 
-    def __init__(self, process: str, energies, nodes, ninc):
+    def __init__(self, process: str, energies, nodes, ninc, mV: float = 0.0):
         self.process = process
         self.energies = np.asarray(energies, np.float64)
         self.nodes = nodes
         self.ninc = list(ninc)
+        self.mV = float(mV)                 # dark processes: the vector's mass
 
     @classmethod
-    def uniform(cls, process, energies, device="cuda"):
+    def uniform(cls, process, energies, device="cuda", mV: float = 0.0):
         torch = _torch()
         ninc = n_increments(process)
         D, mn = len(ninc), max(ninc) + 1
         g = np.zeros((len(energies), D, mn))
         for r, E in enumerate(energies):
-            for d, (lo, hi) in enumerate(integration_range(process, float(E))):
+            for d, (lo, hi) in enumerate(integration_range(process, float(E), mV=mV)):
                 g[r, d, :ninc[d] + 1] = np.linspace(lo, hi, ninc[d] + 1)
-        return cls(process, energies, torch.as_tensor(g, device=device), ninc)
+        return cls(process, energies, torch.as_tensor(g, device=device), ninc, mV)
 
     @classmethod
-    def from_grids(cls, process, energies, grids, device="cuda"):
+    def from_grids(cls, process, energies, grids, device="cuda", mV: float = 0.0):
         """Maps given as per-row lists of node arrays (e.g. PETITE's shipped maps)."""
         torch = _torch()
         D = len(grids[0])
@@ -106,7 +135,7 @@ class MapSet:
                 if len(gr[d]) != ninc[d] + 1:
                     raise ValueError("rows of one process must share the increments per dimension")
                 g[r, d, :len(gr[d])] = gr[d]
-        return cls(process, energies, torch.as_tensor(g, device=device), ninc)
+        return cls(process, energies, torch.as_tensor(g, device=device), ninc, mV)
 
     def grids(self):
         g = self.nodes.cpu().numpy()
@@ -122,17 +151,20 @@ class MapSet:
 
 
 def train(maps: MapSet, points_per_row: int = 1 << 21, iterations: int | None = None, alpha: float = 0.5,
-          seed: int = 20261204, target: str = TRAINING_TARGET, history: list | None = None) -> MapSet:
+          seed: int = 20261204, target: str = TRAINING_TARGET, history: list | None = None,
+          mT: float | None = None) -> MapSet:
     """Adapts ``maps`` in place: ``iterations`` (default 2 x nitn) rounds of
     accumulate + adapt.  ``history`` receives each round's per-row integral
-    estimates (mean of jac f)."""
+    estimates (mean of jac f).  The dark processes train on ``target`` with
+    mT = ``mT`` (default 200 GeV, as PETITE's dark training)."""
     torch = _torch()
     lib = _lib.load()
     dev = maps.nodes.device
     E, ninc = maps._args()
     n, D = len(maps.energies), len(maps.ninc)
-    code = T.PROCESS_CODE[maps.process]
-    tgt = target_constants(target)
+    code = process_code(maps.process)
+    dark = maps.process in DARK_PROCESSES
+    tgt = target_constants(target, mV=maps.mV, mT=(DARK_TRAINING_MT if mT is None else mT) if dark else None)
     acc = torch.zeros((n, D, 1000), dtype=torch.float64, device=dev)
     cnt = torch.zeros((n, D, 1000), dtype=torch.int32, device=dev)
     sums = torch.zeros((n, 2), dtype=torch.float64, device=dev)
@@ -166,22 +198,29 @@ def find_maxes(maps: MapSet, targets=FIND_MAXES_TARGETS, neval: int = 300, n_tri
     dev = maps.nodes.device
     E, ninc = maps._args()
     n, D = len(maps.energies), len(maps.ninc)
-    arr = (_lib.PtTrainTarget * len(targets))(*[target_constants(t) for t in targets])
+    arr = (_lib.PtTrainTarget * len(targets))(*[target_constants(t, mV=maps.mV) for t in targets])
     mf = torch.zeros((n, len(targets)), dtype=torch.float64, device=dev)
     xs = torch.zeros_like(mf)
     import ctypes as C
     stream = torch.cuda.current_stream(dev).cuda_stream
-    _lib.check(lib.pt_find_maxes(T.PROCESS_CODE[maps.process], arr, len(targets), E.data_ptr(), n, D,
+    _lib.check(lib.pt_find_maxes(process_code(maps.process), arr, len(targets), E.data_ptr(), n, D,
                                  ninc, maps.nodes.data_ptr(), maps.nodes.shape[2], int(neval), int(n_trials),
                                  int(seed) & (2 ** 64 - 1), mf.data_ptr(), xs.data_ptr(), C.c_void_p(stream)),
                "pt_find_maxes")
     return mf.cpu().numpy(), xs.cpu().numpy()
 
 
-def load_shipped_maps(dict_dir: str, process: str):
-    """PETITE's ``<Process>/<Process>_AdaptiveMaps.npy`` (list of [event_info,
-    AdaptiveMap]) as (energies, grids), without the vegas package."""
-    path = os.path.join(dict_dir, process, f"{process}_AdaptiveMaps.npy")
+def mass_dir(mV: float) -> str:
+    """The per-mass map directory name (generate_integrators.py:114-117)."""
+    return f"mV_{int(np.floor(mV * 1000.))}MeV"
+
+
+def load_shipped_maps(dict_dir: str, process: str, mV: float | None = None):
+    """PETITE's ``<Process>/<Process>_AdaptiveMaps.npy`` (dark processes:
+    ``<Process>/mV_<n>MeV/...``; a list of [event_info, AdaptiveMap]) as
+    (energies, grids), without the vegas package."""
+    sub = (process,) if mV is None else (process, mass_dir(mV))
+    path = os.path.join(dict_dir, *sub, f"{process}_AdaptiveMaps.npy")
     with open(path, "rb") as f:
         np.lib.format.read_magic(f)
         np.lib.format.read_array_header_1_0(f)
@@ -239,4 +278,49 @@ def build_400GeV_tables(dict_dir: str, out_path: str, points_per_row: int = 1 <<
         log(proc, summary[proc])
     raw = build_raw_tables(xsec, maps, max_F)
     T.save_npz(raw, out_path)
+    return summary
+
+
+def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int = 1 << 21, device="cuda",
+                    targets=FIND_MAXES_TARGETS, log=print) -> dict:
+    """The dark maps of one mass for a PETITE dict_dir whose DarkBrem and
+    DarkMuonBrem maps are not shipped (``data_400GeV``): shipped maps where
+    they exist (DarkAnn, DarkComp), trained maps elsewhere at the energies of
+    the directory's ``dark_xsec.pkl`` (the rows find_maxes wrote for the lost
+    maps), and max_F and the cross section of every row (find_maxes,
+    find_maxes.py:211-305).  Writes ``out_path`` with the map entries of
+    ``dark_tables.npz`` (``m<mV>/<Process>/energy, neval, max_F, grid,
+    nnodes``, plus ``xsec`` from find_maxes) and returns, per process, the
+    median ratio of that cross section to ``dark_xsec.pkl`` (lead)."""
+    with open(os.path.join(dict_dir, "dark_xsec.pkl"), "rb") as f:
+        dx = pickle.load(f)
+    key = [k for k in dx if abs(float(k) - mV) < 1e-12][0]
+    out, summary = {"targets": np.array(targets)}, {}
+    for proc in DARK_PROCESSES:
+        ref = np.asarray(dx[key][proc]["lead"], np.float64)
+        ship = os.path.join(dict_dir, proc, mass_dir(mV), f"{proc}_AdaptiveMaps.npy")
+        if os.path.exists(ship):
+            E, grids = load_shipped_maps(dict_dir, proc, mV)
+            ms = MapSet.from_grids(proc, E, grids, device, mV=mV)
+            how = "shipped"
+        else:
+            ms = train(MapSet.uniform(proc, ref[:, 0], device, mV=mV), points_per_row=points_per_row)
+            how = "trained"
+        mf, xs = find_maxes(ms, targets=targets)
+        g = ms.nodes.cpu().numpy()
+        nn = np.tile(np.array(ms.ninc, np.int32) + 1, (len(ms.energies), 1))
+        pre = f"m{mV}/{proc}"
+        out[f"{pre}/energy"] = ms.energies
+        out[f"{pre}/neval"] = np.full(len(ms.energies), 300, np.int64)
+        out[f"{pre}/max_F"] = mf
+        out[f"{pre}/xsec"] = xs
+        out[f"{pre}/grid"] = g
+        out[f"{pre}/nnodes"] = nn
+        j = list(targets).index("lead")
+        r = np.interp(ms.energies, ref[:, 0], ref[:, 1])
+        ok = r > 0
+        summary[proc] = {"maps": how, "rows": len(ms.energies), "E_max": float(ms.energies.max()),
+                         "xsec_ratio_lead_median": float(np.median(xs[ok, j] / r[ok])) if ok.any() else None}
+        log(proc, summary[proc])
+    np.savez_compressed(out_path, **out)
     return summary

@@ -878,6 +878,21 @@ BETHE_CASES = [
     ("mu5_graphite", "graphite", 0.010, 13, 5.0, 2, 0.1056583755),
 ]
 
+def gen_dark_xsec_400(path, mV=0.1, every=15):
+    """Rows of data_400GeV/dark_xsec.pkl (find_maxes' cross sections with
+    PETITE's own DarkBrem/DarkMuonBrem maps, which it does not ship): the
+    anchor for maps trained by petite_gb300.train."""
+    import pickle
+    with open(os.path.join(refimport.REFERENCE, "data_400GeV", "dark_xsec.pkl"), "rb") as f:
+        dx = pickle.load(f)
+    key = [k for k in dx if abs(float(k) - mV) < 1e-12][0]
+    out = {"mV": np.array(mV)}
+    for p in ("DarkBrem", "DarkMuonBrem"):
+        for t in ("lead", "graphite"):
+            out[f"{p}/{t}"] = np.asarray(dx[key][p][t], float)[::every]
+    np.savez_compressed(path, **out)
+
+
 CASES = [
     # name, target, cut, pid, E0, n primaries, primary mass for the momentum
     ("e1gev_graphite", "graphite", 0.010, 11, 1.0, 12, 0.000511),
@@ -899,6 +914,8 @@ if __name__ == "__main__":
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
     if which in ("all", "darkfree"):
         gen_dark_free(d, os.path.join(HERE, "dark_free.npz"))
+    if which in ("all", "darkxsec400"):
+        gen_dark_xsec_400(os.path.join(HERE, "dark_xsec_400GeV.npz"))
     if which in ("all", "particles"):
         gen_particles(os.path.join(HERE, "particles.npz"))
     if which in ("all", "files"):

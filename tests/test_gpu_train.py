@@ -65,6 +65,28 @@ def test_trained_maps_reproduce_shipped_cross_sections(bundled, process, tol):
     assert ok.sum() >= 5 and rel.max() < tol, rel
 
 
+@pytest.mark.parametrize("process", ["DarkBrem", "DarkMuonBrem"])
+def test_trained_dark_maps_reproduce_400gev_cross_sections(process):
+    """DarkBrem / DarkMuonBrem maps (mV = 0.1 GeV) trained from flat grids on
+    hydrogen with mT = 200 GeV, as PETITE trains them, at energies up to 400
+    GeV: find_maxes' cross sections on lead and graphite against PETITE's
+    data_400GeV/dark_xsec.pkl rows (its find_maxes estimate with the maps it
+    does not ship).  Each row carries both estimates' Monte Carlo error
+    (a few per cent)."""
+    import os
+    from conftest import GOLDEN
+    from petite_gb300.train import MapSet, find_maxes, train
+    dx = np.load(os.path.join(GOLDEN, "dark_xsec_400GeV.npz"))
+    E = dx[f"{process}/lead"][:, 0]
+    ms = train(MapSet.uniform(process, E, mV=float(dx["mV"])), points_per_row=1 << 21)
+    mf, xs = find_maxes(ms, targets=("lead", "graphite"), n_trials=400)
+    assert (mf > 0).all()
+    for j, t in enumerate(("lead", "graphite")):
+        q = xs[:, j] / dx[f"{process}/{t}"][:, 1]
+        print(process, t, np.round(q, 4))
+        assert abs(np.median(q) - 1) < 0.03 and np.abs(q - 1).max() < 0.12, q
+
+
 def test_showers_on_trained_maps_match_shipped(bundled):
     """Lead, 10 GeV electrons: the Brem and PairProd maps replaced by maps
     trained here (max_F from find_maxes); multiplicity, deposited energy
