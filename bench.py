@@ -54,6 +54,16 @@ WORKLOADS = {
     "sm_mu400_lead_1e5": dict(target="lead", cut=0.010, n=100_000, species=(13,), emin=400.0, emax=400.0,
                               seed=3, precision="mixed", fp64_sample=1000, cpu_sample=1, mode="batch",
                               tables="400GeV"),
+    # the dark part of the 400 GeV muon configuration: mu- at 400 GeV in lead,
+    # cut 0.010 GeV, seed 3, mV = 0.1 GeV, DarkMuonBrem on the muon and
+    # DarkBrem/DarkAnn/DarkComp on its cascade, on the 400 GeV dark tables
+    # (DarkBrem/DarkMuonBrem maps trained by petite_gb300.train); 10^3 of the
+    # configuration's 10^5 primaries per step (4.4e7 SM rows), in one chunk:
+    # the record engine runs a generation per launch, and a muon's line is
+    # hundreds of generations deep
+    "dark_mu400_lead_1e3": dict(target="lead", cut=0.010, n=1000, species=(13,), emin=400.0, emax=400.0,
+                                seed=3, masses=(0.1,), chunk=1000, mode="dark", tables="400GeV",
+                                dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")),
     # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
     # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
@@ -504,8 +514,9 @@ def bench_dark(args, w, name, dist, rank, ws):
     from petite_gb300.dark import DarkShower
     n = args.primaries or w["n"]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
-    showers = [DarkShower(None, w["target"], w["cut"], m, seed=w["seed"], device=dev,
-                          active_processes=["DarkBrem", "DarkAnn", "DarkComp"]) for m in w["masses"]]
+    procs = list(w.get("dark_processes", ("DarkBrem", "DarkAnn", "DarkComp")))
+    showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
+                          active_processes=procs) for m in w["masses"]]
     sm = showers[0]
     chunk = min(w["chunk"], n)
 
@@ -555,7 +566,8 @@ def bench_dark(args, w, name, dist, rank, ws):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": name, "primaries_per_step": n, "E0_GeV": w["emin"], "target": w["target"],
                    "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "chunk": chunk,
-                   "processes": ["DarkBrem", "DarkAnn_bound", "DarkComp_bound"]},
+                   "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
+                   "tables": w.get("tables", "bundled")},
         "sm_rows": rows, "sm_rows_per_s": rows / t_sm, "vectors": vecs, "vectors_per_s": vecs / t_dark,
         "yields": per_mass, "clocks": clk.summary()}))
 
