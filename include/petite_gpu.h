@@ -408,6 +408,22 @@ pt_status pt_dark_sample_only(pt_dark* d, const pt_dark_params* prm, int32_t pro
  * Vectors are appended to `out` (any order; parent/process identify them);
  * *n_out returns the count.  PT_OOM if out->capacity is too small.  With
  * out->p4 == NULL only the yields and the count are accumulated. */
+/* pt_run_batch with dark-vector production on every wave: each particle's
+ * row (the record engine's row of that particle: p0 at the start of its
+ * propagation, pf/rf at its end, its stream key) goes through pt_run_dark's
+ * GetBSMWeights and produce_bsm_particle for each of n_params parameter
+ * sets (dark masses, 1..16) on the same showers, so precision 0 gives
+ * pt_run_sm + pt_run_dark's vectors.  Only the yields are kept:
+ * yield/yield_E (device, [n_params][PT_N_DARK + 1], accumulated) and
+ * *n_vectors (all sets).  d must be bound to h.  The waves run on the host
+ * loop; TwoBody_BSMDecay is not applied (SM showers hold no mesons).  No
+ * reference counterpart as one call: PETITE runs generate_shower and then
+ * generate_dark_shower over its list, once per mass. */
+pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_params* prm, int32_t n_params, const double* p0,
+                            const double* r0, const int32_t* pid, const double* mass, int64_t n_primaries,
+                            const pt_opts* opts, pt_tally* tally, int64_t queue_capacity, double* yield,
+                            double* yield_E, int64_t* n_vectors, void* stream);
+
 pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles* sm, int64_t n_rows,
                       const pt_opts* opts, pt_dark_out* out, int64_t* n_out, void* stream);
 

@@ -100,6 +100,7 @@ template <int PREC> struct WaveCtx {
   PhiloxRK rk;                        // round keys of `seed` (float32 kernels)
   // device-planned waves (null: the host plans each wave and passes it here)
   WavePlan* plan;
+  pt_particles rows;                  // per-wave rows for a WaveRowsHook (capacity 0: none)
   const double* in_p0;                // the run's primaries, for the planned feed
   const double* in_r0;
   const int32_t* in_pid;
@@ -408,6 +409,26 @@ __device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf],
   }
 }
 
+// ------------------------------------------------------ per-wave rows
+// A particle's row for a WaveRowsHook (layout of pt_particles): written at
+// the start of its propagation and completed at its end.
+__device__ __forceinline__ void row_start(const pt_particles& r, int64_t s, int pid, double E, double px, double py,
+                                          double pz, double mass, uint64_t key) {
+  const int64_t cap = r.capacity;
+  r.pid[s] = pid;
+  if (pid == 0) return;
+  r.p0[s] = E; r.p0[cap + s] = px; r.p0[2 * cap + s] = py; r.p0[3 * cap + s] = pz;
+  r.mass[s] = mass;
+  r.weight[s] = 1.0;
+  r.pkey[s] = key;
+}
+__device__ __forceinline__ void row_end(const pt_particles& r, int64_t s, double E, double px, double py, double pz,
+                                        double x, double y, double z) {
+  const int64_t cap = r.capacity;
+  r.pf[s] = E; r.pf[cap + s] = px; r.pf[2 * cap + s] = py; r.pf[3 * cap + s] = pz;
+  r.rf[s] = x; r.rf[cap + s] = y; r.rf[2 * cap + s] = z;
+}
+
 // ------------------------------------------------------------ phase 1, float64
 // Same device functions and operation order as the record engine (pt_run_sm).
 struct PropShared64 {
@@ -451,6 +472,7 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
       E0 = c.q.E[i]; px = c.q.px[i]; py = c.q.py[i]; pz = c.q.pz[i];
       x = c.q.x[i]; y = c.q.y[i]; z = c.q.z[i];
       mass = c.q.mass[i]; pid = c.q.pid[i]; prim = c.q.prim[i];
+      if (c.rows.capacity) row_start(c.rows, got, pid, E0, px, py, pz, mass, c.q.key[i]);
     }
     // a dead entry (pid 0, left by the sampler's slot pool) is consumed without work
     if (fresh && pid != 0) {
@@ -526,6 +548,7 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
     double edep = 0.0;
     if (finish) {
       const int sp = species_of(pid);
+      if (c.rows.capacity) row_end(c.rows, (int64_t)((i - wave_head) & c.mask), E, px, py, pz, x, y, z);
       atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of((float)z, 0.f, zmax)], 1u);
       const double eloss = E0 - E;
       L.e_cont += eloss;
@@ -589,6 +612,8 @@ __device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq
     atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of(e.z, 0.f, c.tally.z_max)], 1u);
     const double eloss = e.E0 - e.E;
     L.e_cont += eloss;
+    if (c.rows.capacity)
+      row_end(c.rows, (int64_t)((i - w_head(c)) & c.mask), e.E, e.px, e.py, e.pz, e.x, e.y, e.z);
     const float Ef = (float)e.E;
     process = choose32(c.T, ns, e.pid, Ef, e.u);         // shower.py:665-698
     emit = process >= 0 && Ef > e.pme;
@@ -670,6 +695,8 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
     if (fresh) {
       i = (uint32_t)((wave_head + (uint64_t)got) & c.mask);
       pid = c.q.pid[i];
+      if (c.rows.capacity)
+        row_start(c.rows, got, pid, c.q.E[i], c.q.px[i], c.q.py[i], c.q.pz[i], c.q.mass[i], c.q.key[i]);
     }
     // a dead entry (pid 0, left by the sampler's slot pool) is consumed without work
     if (fresh && pid != 0) {
@@ -1432,6 +1459,7 @@ struct BatchScratch {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // around each wave's two kernels
   WavePlan* plan = nullptr;       // device-planned waves
   unsigned int* bar = nullptr;    // the persistent kernel's grid barrier
+  void* rows_mem = nullptr;       // per-wave rows for a WaveRowsHook (list_cap rows)
 };
 
 #define PT_CUDA(call)                                                                 \
@@ -1535,6 +1563,7 @@ void batch_scratch_free(BatchScratch* s) {
   cudaFree(s->ctr);
   cudaFree(s->plan);
   cudaFree(s->bar);
+  cudaFree(s->rows_mem);
   cudaFreeHost(s->h_ctr);
   cudaFreeHost(s->h_status);
   for (cudaEvent_t e : s->ev)
@@ -1665,9 +1694,34 @@ static pt_status run_persistent(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> 
   return finish_planned(hp, S, st, 1, ms);
 }
 
+// The per-wave rows in the scratch (allocated on first use): pt_particles
+// layout over list_cap rows, the fields a WaveRowsHook reads.
+static pt_status wave_rows(BatchScratch* S, pt_particles* r) {
+  const int64_t L = S->list_cap;
+  const size_t bytes = (size_t)L * (13 * sizeof(double) + sizeof(int32_t) + sizeof(uint64_t)) + 8 * 256;
+  if (!S->rows_mem && cudaMalloc(&S->rows_mem, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    S->rows_mem = nullptr;
+    return PT_OOM;
+  }
+  char* p = (char*)S->rows_mem;
+  auto take = [&](size_t b) { char* q = p; p += (b + 255) & ~size_t(255); return q; };
+  *r = pt_particles{};
+  r->p0 = (double*)take(4 * L * sizeof(double));
+  r->pf = (double*)take(4 * L * sizeof(double));
+  r->rf = (double*)take(3 * L * sizeof(double));
+  r->mass = (double*)take(L * sizeof(double));
+  r->weight = (double*)take(L * sizeof(double));
+  r->pid = (int32_t*)take(L * sizeof(int32_t));
+  r->pkey = (uint64_t*)take(L * sizeof(uint64_t));
+  r->capacity = L;
+  return PT_OK;
+}
+
 template <int PREC>
 static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0, const double* r0, const int32_t* pid,
-                                const double* mass, int64_t n, const pt_opts* o, pt_tally* tally, cudaStream_t st) {
+                                const double* mass, int64_t n, const pt_opts* o, pt_tally* tally, cudaStream_t st,
+                                const WaveRowsHook* hook = nullptr) {
   HandleParts hp = handle_parts(h);
   WaveCtx<PREC> c;
   c.T = *hp.T;
@@ -1693,6 +1747,11 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.chunk[0] = tu[2] ? tu[2] : kChunkPropagate;
   c.chunk[1] = tu[3] ? tu[3] : kChunkSample;
   c.plan = nullptr;
+  c.rows = pt_particles{};
+  if (hook) {
+    const pt_status rs = wave_rows(S, &c.rows);
+    if (rs != PT_OK) return rs;
+  }
   c.in_p0 = p0; c.in_r0 = r0; c.in_pid = pid; c.in_mass = mass;
   c.n_prim = n;
   c.prim_offset = o->primary_offset;
@@ -1707,8 +1766,8 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   const int rb_p = resident_blocks(kp, nt, smem_p);
   const int rb_s = resident_blocks(ks, nt);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
-  if (tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, ks, wpb, rb_p, rb_s, st);
-  if (tu[4] == PT_LOOP_PERSISTENT)
+  if (!hook && tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, ks, wpb, rb_p, rb_s, st);
+  if (!hook && tu[4] == PT_LOOP_PERSISTENT)
     return c.mcs_mode ? run_persistent<PREC, 1>(hp, S, c, st) : run_persistent<PREC, 0>(hp, S, c, st);
   const int64_t cap = S->cap;
   // A fed primary can grow to a few hundred live particles before its shower
@@ -1762,6 +1821,14 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     PT_CUDA(cudaLaunchKernel(ks, dim3(gs), dim3(nt), args, 0, st));
     PT_CUDA(cudaEventRecord(S->ev[2], st));
     PT_CUDA(cudaGetLastError());
+    if (hook) {
+      const pt_status hs = hook->fn(hook->ctx, &c.rows, k, st);
+      if (hs != PT_OK) {
+        hp.launches[0] = nl; hp.launches[1] = nw;
+        return hs;
+      }
+      ++nl;
+    }
     nl += 3;
     ++nw;
     PT_CUDA(cudaMemcpyAsync(S->h_ctr, S->ctr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -1784,6 +1851,21 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   hp.launches[0] = nl;
   hp.launches[1] = nw;
   return PT_OK;
+}
+
+pt_status run_batch_rows(pt_handle* h, const double* p0, const double* r0, const int32_t* pid, const double* mass,
+                         int64_t n, const pt_opts* o, pt_tally* tally, int64_t queue_capacity,
+                         const WaveRowsHook* hook, cudaStream_t st) {
+  if (!h || !o || !tally || n < 0) return PT_BAD_ARG;
+  if (n == 0) return PT_OK;
+  if (!p0 || !r0 || !pid || !mass || !tally->counts || !tally->energy || !tally->hist || !tally->primary_count ||
+      !tally->primary_edep || (o->precision != 0 && o->precision != 1) || n > 0x7fffffff)
+    return PT_BAD_ARG;
+  BatchScratch* S = nullptr;
+  const pt_status s = batch_scratch_get(h, &S, queue_capacity > 0 ? queue_capacity : ((int64_t)1 << 24));
+  if (s != PT_OK) return s;
+  if (o->precision == 1) return run_batch_impl<1>(h, S, p0, r0, pid, mass, n, o, tally, st, hook);
+  return run_batch_impl<0>(h, S, p0, r0, pid, mass, n, o, tally, st, hook);
 }
 
 extern "C" pt_status pt_run_batch(pt_handle* h, const double* p0, const double* r0, const int32_t* pid,

@@ -664,6 +664,76 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
   return s;
 }
 
+// Dark vectors on the batched engine's waves: k_run_dark over each wave's
+// rows (the record engine's rows of those particles), yields only.
+namespace {
+constexpr int kMaxBatchMasses = 16;
+struct BatchDark {
+  pt_dark* d;
+  int n;                                   // parameter sets (masses)
+  pt_dark_params prm[kMaxBatchMasses];
+  pt_opts o;
+  pt_dark_out out[kMaxBatchMasses];
+};
+
+// One k_run_dark per parameter set over the wave's rows.
+pt_status batch_dark_wave(void* ctx, const pt_particles* rows, int64_t n_rows, cudaStream_t st) {
+  BatchDark* b = static_cast<BatchDark*>(ctx);
+  const int64_t work = n_rows * PT_N_DARK;
+  const int tb = 128;
+  if (work > 0)
+    for (int m = 0; m < b->n; ++m)
+      k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(b->d->T, b->d->M, b->prm[m], b->o, *rows, n_rows,
+                                                                 PT_N_DARK, b->out[m], b->d->counter, b->d->status,
+                                                                 b->d->err_info);
+  return cudaGetLastError() == cudaSuccess ? PT_OK : PT_CUDA_ERR;
+}
+}  // namespace
+
+extern "C" pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_params* prm, int32_t n_params,
+                                       const double* p0, const double* r0, const int32_t* pid, const double* mass,
+                                       int64_t n, const pt_opts* o, pt_tally* tally, int64_t queue_capacity,
+                                       double* yield, double* yield_E, int64_t* n_vectors, void* stream) {
+  if (!h || !d || !prm || !o || !tally || !yield || !yield_E || !n_vectors || n < 0 || n_params < 1 ||
+      n_params > kMaxBatchMasses)
+    return PT_BAD_ARG;
+  for (int m = 0; m < n_params; ++m) {
+    const pt_dark_params* q = prm + m;
+    if (q->mass_index < 0 || q->mass_index >= d->M.n_masses) return PT_BAD_TABLE;
+    for (int p = 0; p < PT_N_DARK; ++p)
+      if (((q->active >> p) & 1) && !mass_block_ok(d, q, p)) return PT_BAD_TABLE;
+    for (int k = 0; k < 4; ++k)
+      if (!q->w_x[k] || !q->w_y[k] || q->w_n[k] < 2 || !q->dr_Ei[k] || !q->dr_bins[k] || !q->dr_nbins[k] ||
+          q->dr_n[k] < 1 || q->dr_nbmax[k] < 1)
+        return PT_BAD_TABLE;
+    if (!q->nsc_lx || !q->nsc_ly || q->nsc_n < 2) return PT_BAD_TABLE;
+  }
+  *n_vectors = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  PT_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
+  PT_CUDA(cudaMemsetAsync(d->counter, 0, sizeof(unsigned long long), st));
+  BatchDark* b = new (std::nothrow) BatchDark();
+  if (!b) return PT_OOM;
+  b->d = d;
+  b->n = n_params;
+  b->o = *o;
+  for (int m = 0; m < n_params; ++m) {
+    b->prm[m] = prm[m];
+    b->prm[m].active &= (1 << PT_N_DARK) - 1;        // SM showers hold no mesons
+    b->out[m] = pt_dark_out{};
+    b->out[m].yield = yield + (size_t)m * (PT_N_DARK + 1);
+    b->out[m].yield_E = yield_E + (size_t)m * (PT_N_DARK + 1);
+  }
+  const WaveRowsHook hook{batch_dark_wave, b};
+  const pt_status s = run_batch_rows(h, p0, r0, pid, mass, n, o, tally, queue_capacity, &hook, st);
+  delete b;
+  if (s != PT_OK) return s;
+  PT_CUDA(cudaMemcpyAsync(d->h_counter, d->counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  const pt_status ds = read_dark_status(d, st);
+  *n_vectors = (int64_t)d->h_counter[0];
+  return ds;
+}
+
 template <bool ADJ>
 static pt_status dark_yield_launch(pt_dark* d, int32_t process, const double* energy, const double* mV,
                                    const double* anchor, const int32_t* mass_index, int64_t n_pairs,

@@ -22,3 +22,18 @@ struct HandleParts {
   int32_t* tuning;     // batched engine: refill_min[2], chunk[2] (0 = default), loop (PT_LOOP_*)
 };
 HandleParts handle_parts(pt_handle* h);
+
+// Per-wave rows of the batched engine: with a hook, the propagation kernel
+// writes each particle of the wave as row s = its position in the wave
+// (p0 at the start of its propagation, pf and rf at its end, pid, mass,
+// weight 1, pkey: the record engine's row of that particle; a dead entry
+// leaves pid 0), and fn runs on the run's stream after the wave's
+// propagation kernel with the wave's n_rows rows.  The host loop runs the
+// waves of such a run.
+struct WaveRowsHook {
+  pt_status (*fn)(void* ctx, const pt_particles* rows, int64_t n_rows, cudaStream_t st);
+  void* ctx;
+};
+pt_status run_batch_rows(pt_handle* h, const double* p0, const double* r0, const int32_t* pid, const double* mass,
+                         int64_t n, const pt_opts* o, pt_tally* tally, int64_t queue_capacity,
+                         const WaveRowsHook* hook, cudaStream_t st);

@@ -244,6 +244,21 @@ class DarkEngine:
         out["n"] = n
         return out
 
+    def run_batch(self, prms, p0, r0, pid, mass, opts, tally, queue_capacity: int = 0, device_inputs=None):
+        """The SM engine's batched transport with dark vectors produced on
+        every wave (pt_run_batch_dark) for each parameter set in ``prms``
+        (one pt_dark_params, or a list: several masses on the same showers):
+        returns (tally, yield [sets, N_DARK+1], yield_E [sets, N_DARK+1],
+        vectors) with the yields as numpy arrays."""
+        import torch
+        prms = [prms] if isinstance(prms, _lib.PtDarkParams) else list(prms)
+        arr = (_lib.PtDarkParams * len(prms))(*prms)
+        yld = torch.zeros((len(prms), _lib.N_DARK + 1), dtype=torch.float64, device=self.device)
+        yldE = torch.zeros_like(yld)
+        tally, nv = self.sm.run_batch(p0, r0, pid, mass, opts, tally, queue_capacity, device_inputs,
+                                      dark=(self.handle, arr, yld, yldE))
+        return tally, yld.cpu().numpy(), yldE.cpu().numpy(), nv
+
     def yield_forward(self, process: int, energy, mV, mass_index, n_samples: int, seed: int, anchor=None):
         import torch
         n = energy.shape[0]
@@ -364,6 +379,17 @@ class DarkShower(Shower):
 
     def get_mV(self):
         return self._mV
+
+    def _run_batch_tallied(self, opts, tally, queue_capacity, device_inputs) -> dict:
+        """run_tallied of a DarkShower: the batched transport with the dark
+        vectors of every particle (GetBSMWeights and produce_bsm_particle on
+        each particle's row, as generate_dark_shower over the SM list) tallied:
+        summed weights and weight * E_V per dark process, and the count."""
+        _, y, yE, nv = self._dark_engine.run_batch(self._prm, None, None, None, None, opts, tally, queue_capacity,
+                                                   device_inputs)
+        return {"dark_yield": {p: float(y[0, k]) for k, p in enumerate(DARK_PROCESSES)},
+                "dark_yield_E": {p: float(yE[0, k]) for k, p in enumerate(DARK_PROCESSES)},
+                "dark_vectors": int(nv)}
 
     # ------------------------------------------------------------- weights
     def GetBSMWeights(self, particle, process):

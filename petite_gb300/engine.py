@@ -315,11 +315,15 @@ class SMEngine:
         return Tally(n_primaries, self.device, z_max)
 
     def run_batch(self, p0, r0, pid, mass, opts: _lib.PtOpts, tally: "Tally", queue_capacity: int = 0,
-                  device_inputs=None):
+                  device_inputs=None, dark=None):
         """Transports primaries without storing particle lists; accumulates into `tally`.
 
         p0 (n,4), r0 (n,3), pid (n,), mass (n,) host arrays, or device tensors in
-        `device_inputs` = (p0 [4,n], r0 [3,n], pid [n], mass [n]) already resident."""
+        `device_inputs` = (p0 [4,n], r0 [3,n], pid [n], mass [n]) already resident.
+        ``dark`` = (dark handle, pt_dark_params array, yield, yield_E) runs
+        pt_run_batch_dark instead: dark vectors on every wave for each
+        parameter set, yields accumulated into the two device tensors
+        ([sets, N_DARK + 1]); returns (tally, vectors)."""
         torch = _torch()
         if device_inputs is None:
             p0 = np.asarray(p0, np.float64).reshape(-1, 4)
@@ -332,17 +336,34 @@ class SMEngine:
         else:
             P0, R0, PID, M = device_inputs
             n = P0.shape[1]
+        # the kernels read n entries of every input: a short one is refused here
+        shapes = [tuple(P0.shape), tuple(R0.shape), tuple(PID.shape), tuple(M.shape)]
+        if shapes != [(4, n), (3, n), (n,), (n,)] or not all(t.is_contiguous() for t in (P0, R0, PID, M)):
+            raise ValueError(f"run_batch: inputs p0 [4,n], r0 [3,n], pid [n], mass [n] (contiguous) expected, "
+                             f"got {shapes}")
+        if PID.dtype != torch.int32 or not all(t.dtype == torch.float64 for t in (P0, R0, M)):
+            raise ValueError("run_batch: pid int32 and float64 p0, r0, mass expected")
         cap = int(queue_capacity) if queue_capacity else (1 << 24)
         while True:
-            s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
-                                      C.byref(tally.abi()), cap, self._stream())
+            if dark is None:
+                s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
+                                          C.byref(tally.abi()), cap, self._stream())
+            else:
+                dh, prm, yld, yldE = dark
+                nv = C.c_int64()
+                s = self.lib.pt_run_batch_dark(self.handle, dh, prm, len(prm), _ptr(P0), _ptr(R0), _ptr(PID),
+                                               _ptr(M), n, C.byref(opts), C.byref(tally.abi()), cap, _ptr(yld),
+                                               _ptr(yldE), C.byref(nv), self._stream())
             if s == _lib.PT_OOM and cap < (1 << 28):
                 # the live population outgrew the ring: start over with twice the room
                 tally.zero_()
+                if dark is not None:
+                    dark[2].zero_()
+                    dark[3].zero_()
                 cap *= 2
                 continue
-            self._raise(s, "pt_run_batch")
-            return tally
+            self._raise(s, "pt_run_batch" if dark is None else "pt_run_batch_dark")
+            return tally if dark is None else (tally, int(nv.value))
 
     def sample_only(self, process: int, energy, pkey, opts: _lib.PtOpts):
         torch = _torch()

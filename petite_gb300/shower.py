@@ -193,6 +193,11 @@ class Shower:
         if mass is None:
             mass = torch.as_tensor([MASS[int(q)] for q in pidt.tolist()], dtype=torch.float64)
         mt = torch.as_tensor(mass, dtype=torch.float64)
+        if mt.dim() == 0:                               # one mass for every primary
+            mt = mt.expand(n).contiguous()
+        if mt.shape != (n,) or pidt.shape != (n,) or tuple(p0t.shape) != (n, 4):
+            raise ValueError(f"run_tallied: p0 (n,4), pid and mass (n,) expected, got {tuple(p0t.shape)}, "
+                             f"{tuple(pidt.shape)}, {tuple(mt.shape)}")
         P0 = p0t.to(dev, non_blocking=True).t().contiguous()
         R0 = (torch.zeros((3, n), dtype=torch.float64, device=dev) if r0 is None
               else torch.as_tensor(r0, dtype=torch.float64).to(dev, non_blocking=True).t().contiguous())
@@ -205,13 +210,18 @@ class Shower:
         opts.primary_offset = int(first_primary)
         zmax = z_max if z_max is not None else 30.0 * radiation_length_m(self._target_material)
         t = self._engine.new_tally(n, zmax)
-        self._engine.run_batch(None, None, None, None, opts, t, queue_capacity, device_inputs=(P0, R0, PID, M))
+        extra = self._run_batch_tallied(opts, t, queue_capacity, (P0, R0, PID, M))
         out = t.summary()
+        out.update(extra)
         out["hist"] = t.hist.cpu().numpy()
         out["primary_count"] = t.primary_count.cpu().numpy()
         out["primary_edep"] = t.primary_edep.cpu().numpy()
         out["z_max"] = zmax
         return out
+
+    def _run_batch_tallied(self, opts, tally, queue_capacity, device_inputs) -> dict:
+        self._engine.run_batch(None, None, None, None, opts, tally, queue_capacity, device_inputs=device_inputs)
+        return {}
 
     def generate_shower(self, p0, VB=False, GlobalMS=True):
         """Generates a particle shower from an initial particle (shower.py:603-708)."""

@@ -378,3 +378,64 @@ def test_generate_dark_shower_reads_petite_shower_files():
     _, vs2 = ds.generate_dark_shower(ExDir=parts)
     assert [v.get_ids()["parent_ID"] for v in vs] == [v.get_ids()["parent_ID"] for v in vs2]
     np.testing.assert_array_equal(np.array([v.get_p0() for v in vs]), np.array([v.get_p0() for v in vs2]))
+
+
+def _record_dark(sh, p0, pid, m):
+    """pt_run_sm rows of the primaries (stream offset 0), then pt_run_dark."""
+    n = len(p0)
+    opts = sh._opts(True, "fp64")
+    opts.primary_offset = 0
+    st, nr = sh._engine.run_sm(p0, np.zeros((n, 3)), np.full(n, pid, np.int32), np.full(n, m), np.ones(n), opts)
+    return sh._dark_engine.run_dark(sh._prm, st, nr, sh._opts(), keep_records=False), nr
+
+
+@pytest.mark.parametrize("case", ["e10_graphite", "mu400_lead"])
+def test_batched_dark_yields_match_record_rows(showers, case):
+    """DarkShower.run_tallied (pt_run_batch_dark: the batched engine with dark
+    vectors produced from every particle's row on each wave) against
+    pt_run_sm + pt_run_dark on the same primaries and streams.  In float64
+    the rows are the record engine's, so the vectors are the same ones: equal
+    counts, yields equal up to the order of the atomic sums.  The mixed form
+    agrees within its statistics."""
+    from petite_gb300 import DarkShower
+    if case == "e10_graphite":
+        sh, pid, E0, m, n = showers[(0.1, "graphite")], 11, 10.0, 0.000511, 60
+    else:
+        sh = DarkShower(os.path.join(BUNDLED_DIR, "400GeV"), "lead", 0.010, 0.1, seed=SEED,
+                        active_processes=["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"])
+        pid, E0, m, n = 13, 400.0, 0.1056583755, 2
+    p0 = np.tile([E0, 0.0, 0.0, math.sqrt(E0 * E0 - m * m)], (n, 1))
+    rec, nr = _record_dark(sh, p0, pid, m)
+    b = sh.run_tallied(p0, pid=pid, mass=m, precision="fp64", first_primary=0)
+    assert b["steps"] == nr
+    assert b["dark_vectors"] == rec["n"] > 100
+    for k, p in enumerate(("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")):
+        np.testing.assert_allclose(b["dark_yield"][p], rec["yield"][k], rtol=1e-9, atol=0)
+        np.testing.assert_allclose(b["dark_yield_E"][p], rec["yield_E"][k], rtol=1e-9, atol=0)
+    if case == "mu400_lead":
+        assert b["dark_yield"]["DarkMuonBrem"] > 0
+    mx = sh.run_tallied(p0, pid=pid, mass=m, precision="mixed", first_primary=0)
+    tot_f, tot_m = sum(b["dark_yield"].values()), sum(mx["dark_yield"].values())
+    print(case, "vectors", b["dark_vectors"], mx["dark_vectors"], "yield", tot_f, tot_m)
+    assert abs(tot_m / tot_f - 1) < 0.05
+    assert abs(mx["dark_vectors"] / b["dark_vectors"] - 1) < 0.05
+
+
+def test_batched_dark_several_masses_on_one_run(showers):
+    """Two dark masses on the same batched showers: each set's yields equal
+    a run with that set alone."""
+    a, c = showers[(0.1, "graphite")], showers[(0.3, "graphite")]
+    n, m = 40, 0.000511
+    p0 = np.tile([10.0, 0.0, 0.0, math.sqrt(100.0 - m * m)], (n, 1))
+    import torch
+    dev = a._engine.device
+    ins = (torch.as_tensor(np.ascontiguousarray(p0.T), device=dev), torch.zeros((3, n), dtype=torch.float64, device=dev),
+           torch.full((n,), 11, dtype=torch.int32, device=dev), torch.full((n,), m, dtype=torch.float64, device=dev))
+    opts = a._opts(True, "fp64")
+    both = a._dark_engine.run_batch([a._prm, c._prm], None, None, None, None, opts, a._engine.new_tally(n), 0, ins)
+    one = a._dark_engine.run_batch(a._prm, None, None, None, None, opts, a._engine.new_tally(n), 0, ins)
+    other = a._dark_engine.run_batch(c._prm, None, None, None, None, opts, a._engine.new_tally(n), 0, ins)
+    np.testing.assert_allclose(both[1][0], one[1][0], rtol=1e-9)
+    np.testing.assert_allclose(both[1][1], other[1][0], rtol=1e-9)
+    assert both[3] == one[3] + other[3]
+    assert not np.allclose(both[1][0], both[1][1])
