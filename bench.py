@@ -64,6 +64,15 @@ WORKLOADS = {
     "dark_mu400_lead_1e3": dict(target="lead", cut=0.010, n=1000, species=(13,), emin=400.0, emax=400.0,
                                 seed=3, masses=(0.1,), chunk=1000, mode="dark", tables="400GeV",
                                 dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")),
+    # the same two dark configurations on the batched engine
+    # (pt_run_batch_dark): the showers are not stored, every wave's particles
+    # go through the dark production, all masses on one run (mixed precision)
+    "batchdark_e10_graphite_2e4": dict(target="graphite", cut=0.010, n=20_000, species=(11,), emin=10.0, emax=10.0,
+                                       seed=0, masses=(0.01, 0.05, 0.1, 0.3), mode="batchdark", precision="mixed",
+                                       dark_processes=("DarkBrem", "DarkAnn", "DarkComp")),
+    "batchdark_mu400_lead_1e3": dict(target="lead", cut=0.010, n=1000, species=(13,), emin=400.0, emax=400.0,
+                                     seed=3, masses=(0.1,), mode="batchdark", precision="mixed", tables="400GeV",
+                                     dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")),
     # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
     # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
@@ -621,6 +630,66 @@ def bench_yield(args, w, name, dist, rank, ws):
         "grad_finite_fraction": float(torch.isfinite(g).float().mean().item()), "clocks": clk.summary()}))
 
 
+def bench_batchdark(args, w, name, dist, rank, ws):
+    """The batched engine with dark vectors on every wave for all masses at
+    once (DarkShower.run_tallied, pt_run_batch_dark); a step is the batch of
+    primaries, host inputs copied in and the yields read back inside it."""
+    import torch
+    from petite_gb300.dark import DarkShower
+    n = args.primaries or w["n"]
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    procs = list(w["dark_processes"])
+    showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
+                          active_processes=procs) for m in w["masses"]]
+    sh = showers[0]
+    prms = [d._prm for d in showers]
+
+    def step(s):
+        p0, pid, mass = make_primaries(w, n, offset=block_index(s, rank, ws))
+        ins = (torch.as_tensor(np.ascontiguousarray(p0.T)).pin_memory(), torch.as_tensor(pid).pin_memory(),
+               torch.as_tensor(mass).pin_memory())
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        dins = (ins[0].to(dev, non_blocking=True), torch.zeros((3, n), dtype=torch.float64, device=dev),
+                ins[1].to(dev, non_blocking=True), ins[2].to(dev, non_blocking=True))
+        opts = sh._opts(True, w["precision"])
+        opts.primary_offset = first_primary(s, rank, ws, n)
+        tally = sh._engine.new_tally(n, 1.0)
+        _, y, yE, nv = sh._dark_engine.run_batch(prms, None, None, None, None, opts, tally, 1 << 24, dins)
+        steps = tally.summary()["steps"]
+        torch.cuda.synchronize(dev)
+        return steps, nv, y, time.perf_counter() - t0
+
+    for s in range(args.warmup):
+        step(1000 + s)
+    steps = vecs = 0
+    ysum = np.zeros((len(showers), 5))
+    t = 0.0
+    with ClockSampler(dev.index or 0) as clk:
+        for s in range(args.steps):
+            a, v, y, dt = step(s)
+            steps += a
+            vecs += v
+            ysum += y
+            t += dt
+    if rank != 0:
+        return
+    per_mass = {f"{d.get_mV()}": {"yield_per_primary": (ysum[k][:4] / (n * args.steps)).tolist()}
+                for k, d in enumerate(showers)}
+    print(json.dumps({
+        "metric": "SM showers with dark-vector production on the batched engine: particle-steps/s",
+        "value": steps / t, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if w["precision"] == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": name, "primaries_per_step": n, "E0_GeV": w["emin"], "target": w["target"],
+                   "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "precision": w["precision"],
+                   "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
+                   "tables": w.get("tables", "bundled"), "timed": "host inputs in, yields out"},
+        "row_masses_per_s": steps * len(showers) / t, "vectors": vecs, "vectors_per_s": vecs / t,
+        "yields": per_mass, "clocks": clk.summary()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -650,6 +719,8 @@ def main():
         bench_batch(args, w, args.workload, dist, rank, ws)
     elif w["mode"] == "dark":
         bench_dark(args, w, args.workload, dist, rank, ws)
+    elif w["mode"] == "batchdark":
+        bench_batchdark(args, w, args.workload, dist, rank, ws)
     elif w["mode"] == "yield":
         bench_yield(args, w, args.workload, dist, rank, ws)
     else:

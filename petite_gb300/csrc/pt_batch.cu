@@ -1459,7 +1459,8 @@ struct BatchScratch {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};   // around each wave's two kernels
   WavePlan* plan = nullptr;       // device-planned waves
   unsigned int* bar = nullptr;    // the persistent kernel's grid barrier
-  void* rows_mem = nullptr;       // per-wave rows for a WaveRowsHook (list_cap rows)
+  void* rows_mem = nullptr;       // rows for a WaveRowsHook (rows_cap rows)
+  int64_t rows_cap = 0;
 };
 
 #define PT_CUDA(call)                                                                 \
@@ -1694,10 +1695,13 @@ static pt_status run_persistent(HandleParts& hp, BatchScratch* S, WaveCtx<PREC> 
   return finish_planned(hp, S, st, 1, ms);
 }
 
-// The per-wave rows in the scratch (allocated on first use): pt_particles
-// layout over list_cap rows, the fields a WaveRowsHook reads.
+// The rows in the scratch (allocated on first use): pt_particles layout over
+// rows_cap rows (at least one wave; 2^25 rows, 4 GB, so that many waves of a
+// deep shower collect before the hook runs), the fields a WaveRowsHook reads.
+constexpr int64_t kMinRows = (int64_t)1 << 25;
 static pt_status wave_rows(BatchScratch* S, pt_particles* r) {
-  const int64_t L = S->list_cap;
+  const int64_t L = S->list_cap > kMinRows ? S->list_cap : kMinRows;
+  S->rows_cap = L;
   const size_t bytes = (size_t)L * (13 * sizeof(double) + sizeof(int32_t) + sizeof(uint64_t)) + 8 * 256;
   if (!S->rows_mem && cudaMalloc(&S->rows_mem, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -1748,8 +1752,10 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.chunk[1] = tu[3] ? tu[3] : kChunkSample;
   c.plan = nullptr;
   c.rows = pt_particles{};
+  pt_particles rows_all{};        // every collected row; c.rows views it from the wave's first row
+  int64_t rows_used = 0;
   if (hook) {
-    const pt_status rs = wave_rows(S, &c.rows);
+    const pt_status rs = wave_rows(S, &rows_all);
     if (rs != PT_OK) return rs;
   }
   c.in_p0 = p0; c.in_r0 = r0; c.in_pid = pid; c.in_mass = mass;
@@ -1808,6 +1814,21 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
       return PT_OOM;
     }
     PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
+    if (hook) {
+      // the hook runs over the collected rows when the next wave would not fit
+      if (rows_used + k > rows_all.capacity) {
+        const pt_status hs = hook->fn(hook->ctx, &rows_all, rows_used, st);
+        if (hs != PT_OK) {
+          hp.launches[0] = nl; hp.launches[1] = nw;
+          return hs;
+        }
+        ++nl;
+        rows_used = 0;
+      }
+      c.rows = rows_all;
+      c.rows.p0 += rows_used; c.rows.pf += rows_used; c.rows.rf += rows_used;
+      c.rows.mass += rows_used; c.rows.weight += rows_used; c.rows.pid += rows_used; c.rows.pkey += rows_used;
+    }
     c.head = head;
     c.tail = tail;
     c.n_in = k;
@@ -1821,14 +1842,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     PT_CUDA(cudaLaunchKernel(ks, dim3(gs), dim3(nt), args, 0, st));
     PT_CUDA(cudaEventRecord(S->ev[2], st));
     PT_CUDA(cudaGetLastError());
-    if (hook) {
-      const pt_status hs = hook->fn(hook->ctx, &c.rows, k, st);
-      if (hs != PT_OK) {
-        hp.launches[0] = nl; hp.launches[1] = nw;
-        return hs;
-      }
-      ++nl;
-    }
+    rows_used += hook ? k : 0;
     nl += 3;
     ++nw;
     PT_CUDA(cudaMemcpyAsync(S->h_ctr, S->ctr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -1847,6 +1861,14 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     hp.kernel_ms[1] += ms_s;
     head += (uint64_t)k;
     tail += S->h_ctr[2];
+  }
+  if (hook && rows_used > 0) {
+    const pt_status hs = hook->fn(hook->ctx, &rows_all, rows_used, st);
+    ++nl;
+    if (hs != PT_OK) {
+      hp.launches[0] = nl; hp.launches[1] = nw;
+      return hs;
+    }
   }
   hp.launches[0] = nl;
   hp.launches[1] = nw;

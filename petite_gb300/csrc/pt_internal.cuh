@@ -23,13 +23,13 @@ struct HandleParts {
 };
 HandleParts handle_parts(pt_handle* h);
 
-// Per-wave rows of the batched engine: with a hook, the propagation kernel
-// writes each particle of the wave as row s = its position in the wave
-// (p0 at the start of its propagation, pf and rf at its end, pid, mass,
-// weight 1, pkey: the record engine's row of that particle; a dead entry
-// leaves pid 0), and fn runs on the run's stream after the wave's
-// propagation kernel with the wave's n_rows rows.  The host loop runs the
-// waves of such a run.
+// Rows of the batched engine: with a hook, the propagation kernel writes
+// each particle of a wave as a row (p0 at the start of its propagation, pf
+// and rf at its end, pid, mass, weight 1, pkey: the record engine's row of
+// that particle; a dead entry leaves pid 0).  The rows of successive waves
+// collect in one buffer; fn runs on the run's stream over the first n_rows
+// rows when the next wave would not fit, and once at the end of the run.
+// The host loop runs the waves of such a run.
 struct WaveRowsHook {
   pt_status (*fn)(void* ctx, const pt_particles* rows, int64_t n_rows, cudaStream_t st);
   void* ctx;
