@@ -26,9 +26,11 @@ struct pt_dark {
   pt_dark_maps M;
   int* status = nullptr;
   double* err_info = nullptr;
-  unsigned long long* counter = nullptr;
+  unsigned long long* counter = nullptr;   // [0] vectors, [1] tasks, [2] tasks taken
   int* h_status = nullptr;
   unsigned long long* h_counter = nullptr;
+  void* tasks = nullptr;                   // (row, process, weight) of a launch
+  int64_t tasks_cap = 0;
 };
 
 namespace {
@@ -49,6 +51,7 @@ __device__ void dark_raise(int* status, double* info, int code, int process, dou
 }
 
 constexpr int kMaxPeTrials = 1 << 22;   // draw_pe_sample accepts ~1 in 3 trials
+constexpr unsigned kFull = 0xffffffffu;
 
 // interp1d(kind='linear', bounds_error=False, fill_value=fill) on 1-D tables
 __device__ __forceinline__ double interp_fill(const double* xs, const double* ys, int n, double v, double fill) {
@@ -86,44 +89,67 @@ __device__ __forceinline__ T dark_dsigma(const pt_dark_maps& M, int p, const dou
   }
 }
 
-// draw_dark_sample (dark_shower.py:649-704); false when no sample was found
-// within max_n_integrators*neval proposals (the reference returns None).
+// draw_dark_sample (dark_shower.py:649-704) as a state and one proposal at a
+// time: up to max_n_integrators * neval proposals from the map row nearest
+// E (its LU key), each accepted when max_F * u < wgt * f(x).
+struct DarkDraw {
+  int r, d, neval, key;
+  double maxF, E;
+  int64_t made, limit;          // proposals made; max_n_integrators * neval
+  float tconv;
+};
+
+__device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block, int p, double E,
+                                                int64_t max_n_integrators, DarkDraw& D) {
+  D.key = dark_lu_key(M, block, E);
+  D.r = M.map_base[block] + D.key;
+  D.maxF = M.map_maxF[D.r];
+  D.neval = (int)M.map_neval[D.r];
+  D.d = dark_dim(p);
+  D.E = E;
+  D.made = 0;
+  D.limit = max_n_integrators * (int64_t)D.neval;
+  const bool brem = (p == PT_DARKBREM || p == PT_DARKMUONBREM);
+  D.tconv = brem ? (float)dark_brem_tconv(E, M.A, p == PT_DARKMUONBREM ? kMmu : kMe) : 0.f;
+}
+
+// One proposal: 1 accepted (x holds it), 0 rejected, -1 the limit was
+// reached before it (the reference returns None).
+__device__ int dark_propose(const pt_dark_maps& M, int p, double mV, DarkDraw& D, Rng& rng, double* x) {
+  if (D.made >= D.limit) return -1;
+  double jac = 1.0;
+  for (int k = 0; k < D.d; ++k) {
+    const double y = rng.u();
+    x[k] = map_dim(M.grid_nodes + M.grid_offset[D.r * 4 + k], M.grid_ninc[D.r * 4 + k], y, jac);
+  }
+  const double wgt = jac / D.neval;
+  ++D.made;
+  const double u = rng.u();
+  // Screen: a sample clearly outside the allowed region is rejected; where
+  // the float32 estimate is trustworthy and the proposal is rejected even
+  // at four times that estimate, the float64 value (within a few per
+  // mille of it) cannot be accepted either.  Otherwise float64 decides.
+  if (p == PT_DARKBREM || p == PT_DARKMUONBREM) {
+    float f32;
+    const int sc = dark_brem_screen32(x, D.E, mV, M.A, p == PT_DARKMUONBREM ? kMmu : kMe, M.Z, M.A, D.tconv, f32);
+    if (sc == kScreenOutside) return 0;                          // integrand 0: rejected
+    if (sc == kScreenValue && D.maxF * u > 4.0 * wgt * (double)f32) return 0;
+  }
+  const double f = dark_dsigma<double>(M, p, x, D.E, mV);
+  return D.maxF * u < wgt * f ? 1 : 0;
+}
+
+// The whole loop; false when no sample was found.
 __device__ bool draw_dark(const pt_dark_maps& M, int block, int p, double E, double mV, int64_t max_n_integrators,
                           Rng& rng, double* x, int& key, int64_t& proposals) {
-  key = dark_lu_key(M, block, E);
-  const int r = M.map_base[block] + key;
-  const double maxF = M.map_maxF[r];
-  const int neval = (int)M.map_neval[r];
-  const int d = dark_dim(p);
-  proposals = 0;
-  const bool brem = (p == PT_DARKBREM || p == PT_DARKMUONBREM);
-  const double mlep = p == PT_DARKMUONBREM ? kMmu : kMe;
-  const float tconv = brem ? (float)dark_brem_tconv(E, M.A, mlep) : 0.f;
-  for (int64_t used = 0; used < max_n_integrators; ++used) {
-    for (int j = 0; j < neval; ++j) {
-      double jac = 1.0;
-      for (int k = 0; k < d; ++k) {
-        const double y = rng.u();
-        x[k] = map_dim(M.grid_nodes + M.grid_offset[r * 4 + k], M.grid_ninc[r * 4 + k], y, jac);
-      }
-      const double wgt = jac / neval;
-      ++proposals;
-      const double u = rng.u();
-      // Screen: a sample clearly outside the allowed region is rejected; where
-      // the float32 estimate is trustworthy and the proposal is rejected even
-      // at four times that estimate, the float64 value (within a few per
-      // mille of it) cannot be accepted either.  Otherwise float64 decides.
-      float f32;
-      if (brem) {
-        const int sc = dark_brem_screen32(x, E, mV, M.A, mlep, M.Z, M.A, tconv, f32);
-        if (sc == kScreenOutside) continue;                          // integrand 0: rejected
-        if (sc == kScreenValue && maxF * u > 4.0 * wgt * (double)f32) continue;
-      }
-      const double f = dark_dsigma<double>(M, p, x, E, mV);
-      if (maxF * u < wgt * f) return true;
-    }
+  DarkDraw D;
+  dark_draw_begin(M, block, p, E, max_n_integrators, D);
+  key = D.key;
+  int res;
+  while ((res = dark_propose(M, p, mV, D, rng, x)) == 0) {
   }
-  return false;
+  proposals = D.made;
+  return res == 1;
 }
 
 // ----------------------------------------------------------- GetBSMWeights
@@ -246,11 +272,17 @@ __device__ void two_body_V(const DarkRow& r, double mV, Rng& rng, double* V) {
   for (int i = 0; i < 4; ++i) V[i] = (M[i][0] * q[0] + M[i][1] * q[1] + M[i][2] * q[2] + M[i][3] * q[3]).v;
 }
 
-// produce_bsm_particle (dark_shower.py:721-804).  Returns false when the
-// reference returns None; on true, V and wg hold the vector and its weight.
-__device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
-                            const DarkRow& r, int p, double& wg, double* V, Rng& rng, int* status, double* info) {
-  double pf[4] = {r.pf[0], r.pf[1], r.pf[2], r.pf[3]};
+// produce_bsm_particle (dark_shower.py:721-804) in three stages, so that a
+// lane can run the map's accept/reject loop one proposal at a time.
+//
+// Stage 1: the interaction energy from dR/dE, multiple scattering and the
+// continuous loss up to it (pf becomes the parent's momentum there), and the
+// thresholds' closed forms.  Returns 0 when the reference returns None, 1
+// when the vector is known (v, in pf's frame), 2 when the map draw follows
+// (D set up for dark_propose).
+__device__ int bsm_begin(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
+                         const DarkRow& r, int p, Rng& rng, double* pf, V4& v, DarkDraw& D) {
+  for (int c = 0; c < 4; ++c) pf[c] = r.pf[c];
   int table = -1;
   if (p == PT_DARKANN && r.pid == -11) table = 2;
   else if (p == PT_DARKBREM) table = (r.pid == 11) ? 0 : 1;
@@ -273,7 +305,7 @@ __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_
     const double* bins = P.dr_bins[table] + (size_t)j * P.dr_nbmax[table] * 2;
     const int nb = P.dr_nbins[table][j];
     const double tot = np_sum_weights(bins, nb);
-    if (tot == 0.0) return false;                 // dark_shower.py:742-743, before any draw
+    if (tot == 0.0) return 0;                     // dark_shower.py:742-743, before any draw
     const int idx = drate_choice(bins, nb, tot, rng.u());
     const double E_int = (S(bins[2 * idx]) + (S(E0) - S(Ei[j]))).v;
     const double dEdx = T.t.dEdx_GeV_per_m;
@@ -284,146 +316,147 @@ __device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_
     lose_energy(pf, r.mass, (S(E0) - S(E_int)).v);
   }
   const double E0 = pf[0];
-  const Rot R = rotation_from(pf);
   const double mV = P.mV, me = kMe;
-  V4 v;
   const bool bound = P.bound_electron != 0;
   if (p == PT_DARKANN && bound && E0 <= P.E_res) {
     const double pz = sqrt((S(E0) * S(E0) - S(me) * S(me)).v);
     v = {sqrt((S(E0) * S(E0) - S(me) * S(me) + S(mV) * S(mV)).v), 0.0, 0.0, pz};
-  } else if (p == PT_DARKCOMP && bound && E0 <= P.E_compth) {
+    return 1;
+  }
+  if (p == PT_DARKCOMP && bound && E0 <= P.E_compth) {
     v = {sqrt((S(E0) * S(E0) + S(mV) * S(mV)).v), 0.0, 0.0, E0};
-  } else if (p == PT_DARKANN && !bound && E0 <= P.ann_E0) {
+    return 1;
+  }
+  if (p == PT_DARKANN && !bound && E0 <= P.ann_E0) {
     // free electrons below the first saved energy (dark_shower.py:767-768)
     v = {P.E_res, 0.0, 0.0, sqrt((S(P.E_res) * S(P.E_res) - S(mV) * S(mV)).v)};
-  } else {
-    double x[4] = {0, 0, 0, 0};
-    int key;
-    int64_t props;
-    const int block = P.mass_index * PT_N_DARK + p;
-    if (!draw_dark(M, block, p, E0, mV, o.max_n_integrators, rng, x, key, props)) return false;
-    if (p == PT_DARKCOMP && bound) {
-      // draw_pe_sample (dark_shower.py:706-719)
-      const S lam = S(kAlpha) * S(P.Zeff) * S(me);
-      const S lam5(pow(lam.v, 5.0));
-      auto wave = [&](S pe) {
-        return S(32.0) / S(kPi) * lam5 * (pe * pe) / S(pow((pe * pe + lam * lam).v, 4.0));
-      };
-      const S c = wave(lam / S(sqrt(3.0)));
-      double pe = -1.0;
-      for (int it = 0; it < kMaxPeTrials; ++it) {
-        const S xx = S(0.0) + (S(1e-3) - S(0.0)) * S(rng.u());
-        const S uu = S(0.0) + (S(1.0) - S(0.0)) * S(rng.u());
-        if (uu.v < (wave(xx) / c).v) { pe = xx.v; break; }
-      }
-      if (pe < 0.0) { dark_raise(status, info, PT_TIMEOUT, p, E0, 0); return false; }
-      const double c0 = (S(-1.0) + (S(1.0) - S(-1.0)) * S(rng.u())).v;
-      const S s = S(me) * S(me) + S(2.0) * S(E0) * (ssqrt(S(me) * S(me) + S(pe) * S(pe)) - S(c0) * S(pe));
-      const S Ee = (s - S(mV) * S(mV) + S(me) * S(me)) / (S(2.0) * ssqrt(s));
-      if (Ee.v < me) {
-        v = {mV, 0.0, 0.0, 0.0};
-        wg = 0.0;
-      } else {
-        // compton_fourvecs_boundelectron (kinematics.py:134-183), the V row
-        const S Eg(E0), ct(x[0]), Pe(pe), cte(c0), mv(mV), m(me);
-        const S rs = ssqrt(s);
-        const S EV = (s + mv * mv - m * m) / (S(2.0) * rs);
-        const S pF = ssqrt(Ee * Ee - m * m);
-        const S bnum = ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
-        const S bden = Eg + ssqrt(m * m + Pe * Pe);
-        const S b0 = bnum / bden;
-        const S g0 = S(1.0) / ssqrt(S(1.0) - b0 * b0);
-        const S ph = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
-        const S st = ssqrt(S(1.0) - ct * ct);
-        const S EVL = g0 * EV - b0 * g0 * pF * ct;
-        const S a0 = pF * st * S(sin(ph.v)), a1 = pF * st * S(cos(ph.v)), a2 = b0 * g0 * EV - g0 * pF * ct;
-        const S ctz = (Eg + cte * Pe) / ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
-        const S stz = ssqrt(S(1.0) - ctz * ctz);
-        const S phe = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
-        const S cf(cos(phe.v)), sf(sin(phe.v));
-        v = {EVL.v, (ctz * cf * a0 + (-sf) * a1 + stz * cf * a2).v, (ctz * sf * a0 + cf * a1 + stz * sf * a2).v,
-             ((-stz) * a0 + S(0.0) * a1 + ctz * a2).v};
-      }
-    } else if (p == PT_DARKBREM || p == PT_DARKMUONBREM) {
-      // l_to_lV_fourvecs (kinematics.py:43-68), the V row
-      const S ep(E0), m(r.mass), mv(mV);
-      const S w = S(x[0]) * ep;
-      const S ct = S(1.0) - S(pow(10.0, x[1]));
-      const S k = ssqrt(w * w - mv * mv);
-      const S al = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
-      const S cal(cos(al.v)), sal(sin(al.v));
-      const S st = ssqrt(S(1.0) - ct * ct);
-      (void)m;
-      v = {w.v, (k * cal * st).v, (k * sal * st).v, (k * ct).v};
-    } else if (p == PT_DARKANN) {
-      // radiative_return_fourvecs (kinematics.py:267-299) with boost
-      // (radiative_return.py:18-24)
-      const S s = S(2.0) * S(me) * (S(me) + S(E0));
-      const double beta = (S(2.0) * S(kAlpha) / S(kPi) * (S(log((s / (S(me) * S(me))).v)) - S(1.0))).v;
-      const S umax = S(pow((S(1.0) - S(mV) * S(mV) / s).v, beta / 2.0));
-      const S x1 = S(1.0) - S(pow((S(x[0]) * umax).v, 2.0 / beta));
-      const S x2 = S(mV) * S(mV) / (x1 * s);
-      const S rs = ssqrt(s);
-      const S E1 = x1 * rs / S(2.0), E2 = x2 * rs / S(2.0);
-      const S q0 = rs / S(2.0), q3 = -ssqrt(s / S(4.0) - S(me) * S(me));
-      const S w0 = E1 + E2, w3 = E1 + (-E2);
-      const S rsq = ssqrt(q0 * q0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * q3);
-      const S v0 = (q0 * w0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * w3) / rsq;
-      const S c1 = (w0 + v0) / (rsq + q0);
-      v = {v0.v, (S(0.0) - c1 * S(0.0)).v, (S(0.0) - c1 * S(0.0)).v, (w3 - c1 * q3).v};
+    return 1;
+  }
+  dark_draw_begin(M, P.mass_index * PT_N_DARK + p, p, E0, o.max_n_integrators, D);
+  return 2;
+}
+
+// Stage 3: the vector from the accepted sample x (kinematics.py:43-68,
+// 104-183, 267-299 and draw_pe_sample, dark_shower.py:706-719), in the
+// frame of the parent's momentum (energy E0).  false: the reference's None
+// (draw_pe_sample's bounded loop ran out; PT_TIMEOUT is recorded).
+__device__ bool bsm_finish(const pt_dark_params& P, const DarkRow& r, int p, double E0, const double* x, Rng& rng,
+                           double& wg, V4& v, int* status, double* info) {
+  const double mV = P.mV, me = kMe;
+  const bool bound = P.bound_electron != 0;
+  if (p == PT_DARKCOMP && bound) {
+    // draw_pe_sample (dark_shower.py:706-719)
+    const S lam = S(kAlpha) * S(P.Zeff) * S(me);
+    const S lam5(pow(lam.v, 5.0));
+    auto wave = [&](S pe) {
+      return S(32.0) / S(kPi) * lam5 * (pe * pe) / S(pow((pe * pe + lam * lam).v, 4.0));
+    };
+    const S c = wave(lam / S(sqrt(3.0)));
+    double pe = -1.0;
+    for (int it = 0; it < kMaxPeTrials; ++it) {
+      const S xx = S(0.0) + (S(1e-3) - S(0.0)) * S(rng.u());
+      const S uu = S(0.0) + (S(1.0) - S(0.0)) * S(rng.u());
+      if (uu.v < (wave(xx) / c).v) { pe = xx.v; break; }
+    }
+    if (pe < 0.0) { dark_raise(status, info, PT_TIMEOUT, p, E0, 0); return false; }
+    const double c0 = (S(-1.0) + (S(1.0) - S(-1.0)) * S(rng.u())).v;
+    const S s = S(me) * S(me) + S(2.0) * S(E0) * (ssqrt(S(me) * S(me) + S(pe) * S(pe)) - S(c0) * S(pe));
+    const S Ee = (s - S(mV) * S(mV) + S(me) * S(me)) / (S(2.0) * ssqrt(s));
+    if (Ee.v < me) {
+      v = {mV, 0.0, 0.0, 0.0};
+      wg = 0.0;
     } else {
-      // compton_fourvecs with mV (kinematics.py:104-132), the V row
-      const S Eg(E0), ct(x[0]), m(me), mv(mV);
-      const S s = m * m + S(2.0) * Eg * m;
+      // compton_fourvecs_boundelectron (kinematics.py:134-183), the V row
+      const S Eg(E0), ct(x[0]), Pe(pe), cte(c0), mv(mV), m(me);
       const S rs = ssqrt(s);
-      const S Ee0 = (s + m * m) / (S(2.0) * rs);
-      const S Ee = (s - mv * mv + m * m) / (S(2.0) * rs);
       const S EV = (s + mv * mv - m * m) / (S(2.0) * rs);
       const S pF = ssqrt(Ee * Ee - m * m);
-      const S g0 = Ee0 / m;
-      const S b0 = S(1.0) / g0 * ssqrt(g0 * g0 - S(1.0));
+      const S bnum = ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
+      const S bden = Eg + ssqrt(m * m + Pe * Pe);
+      const S b0 = bnum / bden;
+      const S g0 = S(1.0) / ssqrt(S(1.0) - b0 * b0);
       const S ph = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
       const S st = ssqrt(S(1.0) - ct * ct);
-      v = {(g0 * EV - b0 * g0 * pF * ct).v, (pF * st * S(sin(ph.v))).v, (pF * st * S(cos(ph.v))).v,
-           (b0 * g0 * EV - g0 * pF * ct).v};
+      const S EVL = g0 * EV - b0 * g0 * pF * ct;
+      const S a0 = pF * st * S(sin(ph.v)), a1 = pF * st * S(cos(ph.v)), a2 = b0 * g0 * EV - g0 * pF * ct;
+      const S ctz = (Eg + cte * Pe) / ssqrt(Eg * Eg + S(2.0) * cte * Eg * Pe + Pe * Pe);
+      const S stz = ssqrt(S(1.0) - ctz * ctz);
+      const S phe = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+      const S cf(cos(phe.v)), sf(sin(phe.v));
+      v = {EVL.v, (ctz * cf * a0 + (-sf) * a1 + stz * cf * a2).v, (ctz * sf * a0 + cf * a1 + stz * sf * a2).v,
+           ((-stz) * a0 + S(0.0) * a1 + ctz * a2).v};
     }
+  } else if (p == PT_DARKBREM || p == PT_DARKMUONBREM) {
+    // l_to_lV_fourvecs (kinematics.py:43-68), the V row
+    const S ep(E0), m(r.mass), mv(mV);
+    const S w = S(x[0]) * ep;
+    const S ct = S(1.0) - S(pow(10.0, x[1]));
+    const S k = ssqrt(w * w - mv * mv);
+    const S al = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+    const S cal(cos(al.v)), sal(sin(al.v));
+    const S st = ssqrt(S(1.0) - ct * ct);
+    (void)m;
+    v = {w.v, (k * cal * st).v, (k * sal * st).v, (k * ct).v};
+  } else if (p == PT_DARKANN) {
+    // radiative_return_fourvecs (kinematics.py:267-299) with boost
+    // (radiative_return.py:18-24)
+    const S s = S(2.0) * S(me) * (S(me) + S(E0));
+    const double beta = (S(2.0) * S(kAlpha) / S(kPi) * (S(log((s / (S(me) * S(me))).v)) - S(1.0))).v;
+    const S umax = S(pow((S(1.0) - S(mV) * S(mV) / s).v, beta / 2.0));
+    const S x1 = S(1.0) - S(pow((S(x[0]) * umax).v, 2.0 / beta));
+    const S x2 = S(mV) * S(mV) / (x1 * s);
+    const S rs = ssqrt(s);
+    const S E1 = x1 * rs / S(2.0), E2 = x2 * rs / S(2.0);
+    const S q0 = rs / S(2.0), q3 = -ssqrt(s / S(4.0) - S(me) * S(me));
+    const S w0 = E1 + E2, w3 = E1 + (-E2);
+    const S rsq = ssqrt(q0 * q0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * q3);
+    const S v0 = (q0 * w0 - S(0.0) * S(0.0) - S(0.0) * S(0.0) - q3 * w3) / rsq;
+    const S c1 = (w0 + v0) / (rsq + q0);
+    v = {v0.v, (S(0.0) - c1 * S(0.0)).v, (S(0.0) - c1 * S(0.0)).v, (w3 - c1 * q3).v};
+  } else {
+    // compton_fourvecs with mV (kinematics.py:104-132), the V row
+    const S Eg(E0), ct(x[0]), m(me), mv(mV);
+    const S s = m * m + S(2.0) * Eg * m;
+    const S rs = ssqrt(s);
+    const S Ee0 = (s + m * m) / (S(2.0) * rs);
+    const S Ee = (s - mv * mv + m * m) / (S(2.0) * rs);
+    const S EV = (s + mv * mv - m * m) / (S(2.0) * rs);
+    const S pF = ssqrt(Ee * Ee - m * m);
+    const S g0 = Ee0 / m;
+    const S b0 = S(1.0) / g0 * ssqrt(g0 * g0 - S(1.0));
+    const S ph = S(0.0) + (S(2.0 * kPi) - S(0.0)) * S(rng.u());
+    const S st = ssqrt(S(1.0) - ct * ct);
+    v = {(g0 * EV - b0 * g0 * pF * ct).v, (pF * st * S(sin(ph.v))).v, (pF * st * S(cos(ph.v))).v,
+         (b0 * g0 * EV - g0 * pF * ct).v};
   }
-  const V4 lab = to_lab(R, v);
+  return true;
+}
+
+// The three stages in one call.  Returns false when the reference returns
+// None; on true, V and wg hold the vector (lab frame) and its weight.
+__device__ bool produce_bsm(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
+                            const DarkRow& r, int p, double& wg, double* V, Rng& rng, int* status, double* info) {
+  double pf[4];
+  V4 v;
+  DarkDraw D;
+  const int s = bsm_begin(T, M, P, o, r, p, rng, pf, v, D);
+  if (s == 0) return false;
+  if (s == 2) {
+    double x[4] = {0, 0, 0, 0};
+    int res;
+    while ((res = dark_propose(M, p, P.mV, D, rng, x)) == 0) {
+    }
+    if (res < 0) return false;
+    if (!bsm_finish(P, r, p, pf[0], x, rng, wg, v, status, info)) return false;
+  }
+  const V4 lab = to_lab(rotation_from(pf), v);
   V[0] = lab.e; V[1] = lab.x; V[2] = lab.y; V[3] = lab.z;
   return true;
 }
 
-__global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, pt_particles sm, int64_t n_rows,
-                           int ncol, pt_dark_out out, unsigned long long* counter, int* status, double* info) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_rows * ncol) return;
-  // process-major: a warp works on one dark process for 32 consecutive rows;
-  // column PT_TWOBODY (launched when active) decays the pi0 rows
-  const int p = (int)(t / n_rows);
-  const int64_t row = t - (int64_t)p * n_rows;
-  DarkRow r;
-  r.pid = sm.pid[row];
-  if (p == PT_TWOBODY && r.pid != 111) return;
-  const int64_t cap = sm.capacity;
-  for (int c = 0; c < 4; ++c) { r.p0[c] = sm.p0[c * cap + row]; r.pf[c] = sm.pf[c * cap + row]; }
-  for (int c = 0; c < 3; ++c) r.rf[c] = sm.rf[c * cap + row];
-  r.mass = sm.mass[row];
-  r.weight = sm.weight[row];
-  r.key = sm.pkey[row];
-  Rng rng;
-  double V[4];
-  double wg;
-  if (p == PT_TWOBODY) {
-    wg = twobody_weight(P, r.pid, r.mass);
-    if (!(wg > 0.0)) return;
-    rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
-    two_body_V(r, P.mV, rng, V);
-  } else {
-    wg = bsm_weight(T, P, r.pid, r.p0[0], p);
-    if (!(wg > 0.0)) return;
-    rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
-    if (!produce_bsm(T, M, P, o, r, p, wg, V, rng, status, info)) return;
-  }
+// A vector and its weight: the yields, and its record when out.p4 is set.
+__device__ void dark_emit(const pt_dark_params& P, const pt_dark_out& out, unsigned long long* counter, int* status,
+                          const DarkRow& r, int64_t row, int p, double wg, const double* V, uint64_t draws) {
   const double w = (S(wg) * S(r.weight)).v;
   if (out.yield) atomicAdd(out.yield + p, w);
   if (out.yield_E) atomicAdd(out.yield_E + p, w * V[0]);
@@ -437,7 +470,130 @@ __global__ void k_run_dark(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o, 
   out.parent[slot] = row;
   out.process[slot] = p == PT_TWOBODY ? PT_TWOBODY_CODE
                                       : p + ((P.bound_electron && (p == PT_DARKANN || p == PT_DARKCOMP)) ? PT_DARK_BOUND : 0);
-  out.draws[slot] = (int32_t)rng.n;
+  out.draws[slot] = (int32_t)draws;
+}
+
+__device__ __forceinline__ void load_row(const pt_particles& sm, int64_t row, DarkRow& r) {
+  const int64_t cap = sm.capacity;
+  r.pid = sm.pid[row];
+  for (int c = 0; c < 4; ++c) { r.p0[c] = sm.p0[c * cap + row]; r.pf[c] = sm.pf[c * cap + row]; }
+  for (int c = 0; c < 3; ++c) r.rf[c] = sm.rf[c * cap + row];
+  r.mass = sm.mass[row];
+  r.weight = sm.weight[row];
+  r.key = sm.pkey[row];
+}
+
+// The (row, process) pairs of a dark run with a positive GetBSMWeights
+// (dark_shower.py:595-647), compacted: most pairs weigh nothing (a photon
+// has no DarkBrem), so the production below runs only on the others.
+struct DarkTasks {
+  int64_t* row;
+  int32_t* proc;
+  double* wg;
+  int64_t cap;
+};
+
+__global__ void k_dark_weigh(Tabs T, pt_dark_params P, pt_particles sm, int64_t n_rows, int ncol, DarkTasks tk,
+                             unsigned long long* counter, int* status) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double wg = 0.0;
+  int p = 0;
+  int64_t row = 0;
+  if (t < n_rows * ncol) {
+    // column PT_TWOBODY (launched when active) decays the pi0 rows
+    p = (int)(t / n_rows);
+    row = t - (int64_t)p * n_rows;
+    const int pid = sm.pid[row];
+    if (p == PT_TWOBODY) wg = twobody_weight(P, pid, sm.mass[row]);
+    else wg = bsm_weight(T, P, pid, sm.p0[row], p);
+  }
+  const bool keep = wg > 0.0;
+  const unsigned m = __ballot_sync(kFull, keep);
+  if (!m) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter + 1, (unsigned long long)__popc(m));
+  base = __shfl_sync(kFull, base, leader);
+  if (!keep) return;
+  const unsigned long long slot = base + __popc(m & ((1u << lane) - 1u));
+  if ((int64_t)slot >= tk.cap) { dark_raise(status, nullptr, PT_OOM, p, 0.0, 0); return; }
+  tk.row[slot] = row;
+  tk.proc[slot] = p;
+  tk.wg[slot] = wg;
+}
+
+// produce_bsm_particle over the tasks with every lane busy: a lane takes a
+// task, runs its first stage, then one map proposal per iteration; a lane
+// whose task ends (vector made, or None) takes the next one while the other
+// lanes keep proposing.  Each task draws from its own stream, in the
+// reference's order, so the vectors are produce_bsm's whatever the schedule.
+constexpr int kDarkThreads = 128;
+__global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o,
+                                                               pt_particles sm, DarkTasks tk, pt_dark_out out,
+                                                               unsigned long long* counter, int* status,
+                                                               double* info) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long nt = __ldcg(counter + 1);
+  const int64_t n = (int64_t)nt < tk.cap ? (int64_t)nt : tk.cap;
+  bool have = false, drained = false;
+  DarkRow r;
+  int p = 0;
+  int64_t row = 0;
+  double wg = 0.0, pf[4], x[4] = {0, 0, 0, 0};
+  Rng rng;
+  DarkDraw D;
+  for (;;) {
+    const bool want = !have && !drained;
+    const unsigned m = __ballot_sync(kFull, want);
+    int64_t t = -1;
+    if (m) {
+      const int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(counter + 2, (unsigned long long)__popc(m));
+      base = __shfl_sync(kFull, base, leader);
+      if (want) {
+        t = (int64_t)(base + __popc(m & ((1u << lane) - 1u)));
+        if (t >= n) {
+          drained = true;
+          t = -1;
+        }
+      }
+    }
+    if (__all_sync(kFull, !have && drained)) break;
+    if (t >= 0) {
+      row = tk.row[t];
+      p = tk.proc[t];
+      wg = tk.wg[t];
+      load_row(sm, row, r);
+      rng.init(o.seed, mix64(r.key + 0x9E3779B97F4A7C15ull * (uint64_t)(3 + p)));
+      double V[4];
+      if (p == PT_TWOBODY) {
+        two_body_V(r, P.mV, rng, V);
+        dark_emit(P, out, counter, status, r, row, p, wg, V, rng.n);
+      } else {
+        V4 v;
+        const int s = bsm_begin(T, M, P, o, r, p, rng, pf, v, D);
+        if (s == 1) {
+          const V4 lab = to_lab(rotation_from(pf), v);
+          V[0] = lab.e; V[1] = lab.x; V[2] = lab.y; V[3] = lab.z;
+          dark_emit(P, out, counter, status, r, row, p, wg, V, rng.n);
+        }
+        have = s == 2;
+      }
+    }
+    if (have) {
+      const int res = dark_propose(M, p, P.mV, D, rng, x);
+      if (res != 0) {
+        have = false;
+        V4 v;
+        if (res == 1 && bsm_finish(P, r, p, pf[0], x, rng, wg, v, status, info)) {
+          const V4 lab = to_lab(rotation_from(pf), v);
+          const double V[4] = {lab.e, lab.x, lab.y, lab.z};
+          dark_emit(P, out, counter, status, r, row, p, wg, V, rng.n);
+        }
+      }
+    }
+  }
 }
 
 __global__ void k_dark_sample_only(pt_dark_maps M, pt_dark_params P, int p, const double* E, const uint64_t* key,
@@ -569,6 +725,53 @@ pt_status read_dark_status(pt_dark* d, cudaStream_t st) {
 
 }  // namespace
 
+// The dark production over rows [0, n_rows) of sm for one parameter set, on
+// the stream without a host wait: k_dark_weigh compacts the (row, process)
+// pairs of positive weight into the handle's task buffer (grown to n_rows *
+// ncol entries), then k_dark_produce runs them on a resident grid.
+static pt_status dark_launch(pt_dark* d, const pt_dark_params& prm, const pt_opts& o, const pt_particles& sm,
+                             int64_t n_rows, int ncol, const pt_dark_out& out, cudaStream_t st) {
+  const int64_t work = n_rows * ncol;
+  if (work <= 0) return PT_OK;
+  if (d->tasks_cap < work) {
+    PT_CUDA(cudaStreamSynchronize(st));             // no launch still reads the old buffer
+    cudaFree(d->tasks);
+    d->tasks = nullptr;
+    d->tasks_cap = 0;
+    if (cudaMalloc(&d->tasks, (size_t)work * (sizeof(int64_t) + sizeof(int32_t) + sizeof(double)) + 512) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      d->tasks = nullptr;
+      return PT_OOM;
+    }
+    d->tasks_cap = work;
+  }
+  DarkTasks tk;
+  tk.cap = d->tasks_cap;
+  char* q = (char*)d->tasks;
+  tk.row = (int64_t*)q;
+  q += ((size_t)tk.cap * sizeof(int64_t) + 255) & ~size_t(255);
+  tk.wg = (double*)q;
+  q += ((size_t)tk.cap * sizeof(double) + 255) & ~size_t(255);
+  tk.proc = (int32_t*)q;
+  PT_CUDA(cudaMemsetAsync(d->counter + 1, 0, 2 * sizeof(unsigned long long), st));
+  const int tb = 128;
+  k_dark_weigh<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(d->T, prm, sm, n_rows, ncol, tk, d->counter,
+                                                               d->status);
+  int dev = 0, sms = 0, per = 0;
+  PT_CUDA(cudaGetDevice(&dev));
+  PT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dark_produce, kDarkThreads, 0));
+  if (per < 1) per = 1;
+  int64_t grid = (int64_t)sms * per;
+  const int64_t need = (work + kDarkThreads - 1) / kDarkThreads;
+  if (grid > need) grid = need;
+  k_dark_produce<<<(unsigned)grid, kDarkThreads, 0, st>>>(d->T, d->M, prm, o, sm, tk, out, d->counter, d->status,
+                                                          d->err_info);
+  PT_CUDA(cudaGetLastError());
+  return PT_OK;
+}
+
 extern "C" pt_status pt_dark_create(pt_handle* sm, const pt_dark_maps* m, pt_dark** out) {
   if (!sm || !m || !out) return PT_BAD_ARG;
   *out = nullptr;
@@ -582,7 +785,7 @@ extern "C" pt_status pt_dark_create(pt_handle* sm, const pt_dark_maps* m, pt_dar
   d->T = *handle_parts(sm).T;
   d->M = *m;
   if (cudaMalloc(&d->status, sizeof(int)) != cudaSuccess || cudaMalloc(&d->err_info, 4 * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&d->counter, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&d->counter, 3 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&d->h_status, sizeof(int)) != cudaSuccess ||
       cudaMallocHost(&d->h_counter, sizeof(unsigned long long)) != cudaSuccess) {
     pt_dark_destroy(d);
@@ -597,6 +800,7 @@ extern "C" void pt_dark_destroy(pt_dark* d) {
   cudaFree(d->status);
   cudaFree(d->err_info);
   cudaFree(d->counter);
+  cudaFree(d->tasks);
   cudaFreeHost(d->h_status);
   cudaFreeHost(d->h_counter);
   delete d;
@@ -653,11 +857,8 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
   PT_CUDA(cudaMemsetAsync(d->status, 0, sizeof(int), st));
   PT_CUDA(cudaMemsetAsync(d->counter, 0, sizeof(unsigned long long), st));
   const int ncol = PT_N_DARK + ((prm->active >> PT_TWOBODY) & 1);
-  const int64_t work = n_rows * ncol;
-  const int tb = 128;
-  k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(d->T, d->M, *prm, *o, *sm, n_rows, ncol, *out,
-                                                             d->counter, d->status, d->err_info);
-  PT_CUDA(cudaGetLastError());
+  const pt_status ls = dark_launch(d, *prm, *o, *sm, n_rows, ncol, *out, st);
+  if (ls != PT_OK) return ls;
   PT_CUDA(cudaMemcpyAsync(d->h_counter, d->counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   const pt_status s = read_dark_status(d, st);
   *n_out = (int64_t)d->h_counter[0];
@@ -676,17 +877,14 @@ struct BatchDark {
   pt_dark_out out[kMaxBatchMasses];
 };
 
-// One k_run_dark per parameter set over the wave's rows.
+// The dark production per parameter set over the collected rows.
 pt_status batch_dark_wave(void* ctx, const pt_particles* rows, int64_t n_rows, cudaStream_t st) {
   BatchDark* b = static_cast<BatchDark*>(ctx);
-  const int64_t work = n_rows * PT_N_DARK;
-  const int tb = 128;
-  if (work > 0)
-    for (int m = 0; m < b->n; ++m)
-      k_run_dark<<<(unsigned)((work + tb - 1) / tb), tb, 0, st>>>(b->d->T, b->d->M, b->prm[m], b->o, *rows, n_rows,
-                                                                 PT_N_DARK, b->out[m], b->d->counter, b->d->status,
-                                                                 b->d->err_info);
-  return cudaGetLastError() == cudaSuccess ? PT_OK : PT_CUDA_ERR;
+  for (int m = 0; m < b->n; ++m) {
+    const pt_status s = dark_launch(b->d, b->prm[m], b->o, *rows, n_rows, PT_N_DARK, b->out[m], st);
+    if (s != PT_OK) return s;
+  }
+  return PT_OK;
 }
 }  // namespace
 
