@@ -865,7 +865,7 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
   return s;
 }
 
-// Dark vectors on the batched engine's waves: k_run_dark over each wave's
+// Dark vectors on the batched engine's waves: the dark production over the
 // rows (the record engine's rows of those particles), yields only.
 namespace {
 constexpr int kMaxBatchMasses = 16;
