@@ -22,7 +22,7 @@ EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_l
            "pt_sample_only", "pt_dsigma", "pt_moliere_inverse_cdf",
            "pt_vegas_accumulate", "pt_vegas_adapt", "pt_find_maxes",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
-           "pt_run_batch_dark",
+           "pt_run_batch_dark", "pt_dark_screen32",
            "pt_dark_yield", "pt_dark_yield_adjoint")
 
 # pt_run_sm_noalloc: largest particle-store capacity (its static scratch)
@@ -174,6 +174,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         getattr(lib, f).restype = C.c_int
     lib.pt_run_batch.argtypes = [vp, vp, vp, vp, vp, i64, C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp]
     lib.pt_run_batch.restype = C.c_int
+    lib.pt_dark_screen32.argtypes = [vp, C.c_int32, vp, vp, i64, C.c_double, vp, vp, vp]
+    lib.pt_dark_screen32.restype = C.c_int
     lib.pt_run_batch_dark.argtypes = [vp, vp, C.POINTER(PtDarkParams), C.c_int32, vp, vp, vp, vp, i64,
                                       C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp, vp, C.POINTER(i64), vp]
     lib.pt_run_batch_dark.restype = C.c_int

@@ -185,6 +185,20 @@ class DarkEngine:
                                            out.data_ptr(), self.sm._stream()), "pt_dark_dsigma")
         return out.cpu().numpy()
 
+    def screen32(self, process: int, x, energy, mV: float):
+        """The float32 dark-brem screen (pt_dark_screen32): (value, code)."""
+        import torch
+        x = np.atleast_2d(np.asarray(x, np.float64))
+        xp = np.zeros((len(x), 4))
+        xp[:, :x.shape[1]] = x
+        X = torch.as_tensor(xp, device=self.device)
+        E = torch.as_tensor(np.asarray(energy, np.float64), device=self.device)
+        val = torch.empty(len(xp), dtype=torch.float32, device=self.device)
+        code = torch.empty(len(xp), dtype=torch.int32, device=self.device)
+        _lib.check(self.lib.pt_dark_screen32(self.handle, process, X.data_ptr(), E.data_ptr(), len(xp), float(mV),
+                                             val.data_ptr(), code.data_ptr(), self.sm._stream()), "pt_dark_screen32")
+        return val.cpu().numpy(), code.cpu().numpy()
+
     def sample_only(self, prm, process: int, energy, keys, opts):
         import torch
         E = torch.as_tensor(np.asarray(energy, np.float64), device=self.device)

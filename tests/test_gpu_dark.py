@@ -439,3 +439,37 @@ def test_batched_dark_several_masses_on_one_run(showers):
     np.testing.assert_allclose(both[1][1], other[1][0], rtol=1e-9)
     assert both[3] == one[3] + other[3]
     assert not np.allclose(both[1][0], both[1][1])
+
+
+@pytest.mark.parametrize("mV,target", [(0.01, "graphite"), (0.1, "lead"), (0.3, "graphite")])
+def test_dark_brem_float32_screen_accuracy(showers, mV, target):
+    """Where the float32 dark-brem screen returns a value, it is within
+    1e-2 of the float64 cross section (the proposal loop rejects with it
+    only when max_F u exceeds four times it), on map samples at every
+    tabulated energy of DarkBrem and DarkMuonBrem; where it reports a point
+    outside the allowed region, the float64 value is 0."""
+    from petite_gb300.dark import DARK_CODE
+    sh = showers[(mV, target)]
+    z = sh._dark.z
+    rng = np.random.default_rng(11)
+    for name in ("DarkBrem", "DarkMuonBrem"):
+        pre = f"m{mV}/{name}"
+        E, grid, nn = z[f"{pre}/energy"], z[f"{pre}/grid"], z[f"{pre}/nnodes"]
+        rows = np.repeat(np.arange(len(E)), 400)
+        x = np.zeros((len(rows), 3))
+        for d in range(3):
+            y = rng.uniform(size=len(rows))
+            ninc = nn[rows, d] - 1
+            t = y * ninc
+            i = np.minimum(t.astype(int), ninc - 1)
+            g0, g1 = grid[rows, d, i], grid[rows, d, i + 1]
+            x[:, d] = g0 + (g1 - g0) * (t - i)
+        f64 = sh._dark_engine.dsigma(DARK_CODE[name], x, E[rows], mV)
+        f32, code = sh._dark_engine.screen32(DARK_CODE[name], x, E[rows], mV)
+        val = code == 1
+        # muon samples sit mostly near cancellations the screen declines
+        assert val.sum() > 100 and (name == "DarkMuonBrem" or val.mean() > 0.3), (name, val.mean())
+        assert (f64[code == 2] == 0).all(), name
+        rel = np.abs(f32[val] / f64[val] - 1)
+        print(name, mV, target, "valued", round(val.mean(), 3), "max rel", rel.max(), "p99.9", np.quantile(rel, 0.999))
+        assert rel.max() < 1e-2, (name, rel.max())
