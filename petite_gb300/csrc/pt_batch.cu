@@ -26,6 +26,7 @@
 
 #include "pt_internal.cuh"
 #include "pt_physics32.cuh"
+#include "pt_tma.cuh"
 
 using namespace pt;
 
@@ -852,24 +853,6 @@ __device__ __forceinline__ int ns_total(const Tabs& T) {
 // PT_TIMEOUT, the block waits once more with the same bound for its copies
 // in flight and returns false.
 constexpr unsigned long long kStageNs = 1000ull * 1000ull * 1000ull;
-__device__ __forceinline__ unsigned long long global_ns() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long bound_ns) {
-  const unsigned long long t0 = global_ns();
-  for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (global_ns() - t0 > bound_ns) return false;
-  }
-}
 
 __device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int pad) {
   __shared__ __align__(8) unsigned long long bar;
@@ -878,16 +861,10 @@ __device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int p
   const int bulk = total & ~3;
   const uint32_t bytes = (uint32_t)bulk * 4u;
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(3u * bytes) : "memory");
+    mbar_init(b);
+    mbar_arrive_expect(b, 3u * bytes);
     if (bytes)
-      for (int a = 0; a < 3; ++a) {
-        const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sh + a * pad);
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(dst), "l"(src[a]), "r"(bytes), "r"(b)
-                     : "memory");
-      }
+      for (int a = 0; a < 3; ++a) bulk_g2s(sh + a * pad, src[a], bytes, b);
   }
   const int rest = total - bulk;
   if (threadIdx.x < 3 * rest) {

@@ -25,6 +25,7 @@
 #include "pt_dark.cuh"
 #include "pt_internal.cuh"
 #include "pt_physics.cuh"
+#include "pt_tma.cuh"
 
 using namespace pt;
 
@@ -33,6 +34,8 @@ namespace {
 constexpr int kTrainThreads = 256;
 constexpr int kMaxInc = 1000;
 constexpr int kMaxDim = 4;
+constexpr unsigned long long kStageNs = 1000ull * 1000ull * 1000ull;
+
 
 // A Tabs carrying only what the SM differential cross sections read.
 __device__ __forceinline__ Tabs train_tabs(const pt_train_target& t) {
@@ -70,6 +73,26 @@ struct MapView {
   int max_nodes;
 };
 
+// A timed-out staging copy (PT_TIMEOUT), read back by the entry points.
+__device__ int g_train_status;
+
+// The block's map row (dims x max_nodes float64 nodes) in shared memory,
+// staged by a TMA bulk copy; nullptr (status recorded) when it did not land.
+__device__ __forceinline__ const double* stage_row(const double* g, const MapView& m) {
+  extern __shared__ __align__(16) double s_row[];
+  __shared__ __align__(8) uint64_t bar;
+  double* out = nullptr;
+  if (!stage_doubles(s_row, g, m.dims * m.max_nodes, &bar, kStageNs, &out)) {
+    if (threadIdx.x == 0) atomicCAS(&g_train_status, 0, (int)PT_TIMEOUT);
+    return nullptr;
+  }
+  return out;
+}
+
+__host__ __device__ inline size_t row_smem_bytes(int dims, int max_nodes) {
+  return ((size_t)dims * max_nodes + 2) * sizeof(double);
+}
+
 // y in [0,1)^dims -> x, jacobian (AdaptiveMap.map: piecewise linear).
 __device__ __forceinline__ double map_point(const MapView& m, const double* g, Rng& rng, double* x, int* inc) {
   double jac = 1.0;
@@ -95,10 +118,10 @@ __global__ void __launch_bounds__(kTrainThreads) k_vegas_accumulate(pt_train_tar
   __shared__ double s_acc[kMaxDim * kMaxInc];
   __shared__ unsigned s_cnt[kMaxDim * kMaxInc];
   for (int k = threadIdx.x; k < m.dims * kMaxInc; k += blockDim.x) { s_acc[k] = 0.0; s_cnt[k] = 0u; }
-  __syncthreads();
   const int row = blockIdx.y;
   const Tabs T = train_tabs(tgt);
-  const double* g = nodes + (size_t)row * m.dims * m.max_nodes;
+  const double* g = stage_row(nodes + (size_t)row * m.dims * m.max_nodes, m);   // synchronises the block
+  if (!g) return;
   const double Er = E[row];
   double s1 = 0.0, s2 = 0.0;
   const uint64_t base = ((uint64_t)row << 40) ^ ((uint64_t)iteration << 34);
@@ -196,7 +219,8 @@ __global__ void __launch_bounds__(kTrainThreads) k_find_maxes(const pt_train_tar
   __shared__ double s_max[kTrainThreads / 32], s_sum[kTrainThreads / 32];
   const int row = blockIdx.x, t = blockIdx.y, nt = gridDim.y;
   const Tabs T = train_tabs(tg[t]);
-  const double* g = nodes + (size_t)row * m.dims * m.max_nodes;
+  const double* g = stage_row(nodes + (size_t)row * m.dims * m.max_nodes, m);
+  if (!g) return;
   const double Er = E[row];
   const int64_t total = (int64_t)neval * n_trials;
   double mx = 0.0, sm = 0.0;
@@ -244,6 +268,20 @@ bool make_view(int dims, const int32_t* ninc, int max_nodes, MapView& m) {
     }                                                                                   \
   } while (0)
 
+int* status_word() {
+  void* p = nullptr;
+  cudaGetSymbolAddress(&p, g_train_status);
+  return (int*)p;
+}
+
+// Waits for the stream and returns a staging timeout, if any.
+pt_status read_status(cudaStream_t st) {
+  int s = 0;
+  PT_T(cudaMemcpyFromSymbolAsync(&s, g_train_status, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  PT_T(cudaStreamSynchronize(st));
+  return (pt_status)s;
+}
+
 }  // namespace
 
 extern "C" pt_status pt_vegas_accumulate(int32_t process, const pt_train_target* target, const double* energy,
@@ -258,10 +296,13 @@ extern "C" pt_status pt_vegas_accumulate(int32_t process, const pt_train_target*
   cudaStream_t st = (cudaStream_t)stream;
   int64_t bx = (points_per_row + kTrainThreads * 16 - 1) / (kTrainThreads * 16);
   if (bx > 1024) bx = 1024;
-  k_vegas_accumulate<<<dim3((unsigned)bx, (unsigned)n_rows), kTrainThreads, 0, st>>>(
+  const size_t smem = row_smem_bytes(dims, max_nodes);
+  PT_T(cudaFuncSetAttribute(k_vegas_accumulate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PT_T(cudaMemsetAsync(status_word(), 0, sizeof(int), st));
+  k_vegas_accumulate<<<dim3((unsigned)bx, (unsigned)n_rows), kTrainThreads, smem, st>>>(
       *target, process, energy, m, nodes, points_per_row, seed, (uint32_t)iteration, acc, cnt, sums);
   PT_T(cudaGetLastError());
-  return PT_OK;
+  return read_status(st);
 }
 
 extern "C" pt_status pt_vegas_adapt(int32_t n_rows, int32_t dims, const int32_t* ninc, double* nodes,
@@ -289,10 +330,12 @@ extern "C" pt_status pt_find_maxes(int32_t process, const pt_train_target* targe
   pt_train_target* d_t = nullptr;
   PT_T(cudaMallocAsync((void**)&d_t, sizeof(pt_train_target) * n_targets, st));
   PT_T(cudaMemcpyAsync(d_t, targets, sizeof(pt_train_target) * n_targets, cudaMemcpyHostToDevice, st));
-  k_find_maxes<<<dim3((unsigned)n_rows, (unsigned)n_targets), kTrainThreads, 0, st>>>(
+  const size_t smem = row_smem_bytes(dims, max_nodes);
+  PT_T(cudaFuncSetAttribute(k_find_maxes, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PT_T(cudaMemsetAsync(status_word(), 0, sizeof(int), st));
+  k_find_maxes<<<dim3((unsigned)n_rows, (unsigned)n_targets), kTrainThreads, smem, st>>>(
       d_t, process, energy, m, nodes, neval, n_trials, seed, max_F, xsec);
   PT_T(cudaGetLastError());
   PT_T(cudaFreeAsync(d_t, st));
-  PT_T(cudaStreamSynchronize(st));
-  return PT_OK;
+  return read_status(st);
 }
