@@ -76,3 +76,17 @@ def test_struct_layout_matches_header(tmp_path):
         assert got[(cname, "sizeof")] == C.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_entry_points_refuse_missing_handles_without_a_device(lib):
+    """Argument checks that return before any CUDA call: null handles and
+    out-of-range counts give PT_BAD_ARG on a machine without a GPU."""
+    from petite_gb300 import _lib
+    i64 = C.c_int64()
+    opts, tally, prm = _lib.PtOpts(), _lib.PtTally(), _lib.PtDarkParams()
+    assert lib.pt_run_batch(None, None, None, None, None, 1, C.byref(opts), C.byref(tally), 0, None) == _lib.PT_BAD_ARG
+    assert lib.pt_run_batch_dark(None, None, C.byref(prm), 1, None, None, None, None, 1, C.byref(opts),
+                                 C.byref(tally), 0, None, None, C.byref(i64), None) == _lib.PT_BAD_ARG
+    assert lib.pt_dark_screen32(None, 0, None, None, 1, 0.1, None, None, None) == _lib.PT_BAD_ARG
+    assert lib.pt_set_batch_tuning(None, None) == _lib.PT_BAD_ARG
+    assert lib.pt_vegas_adapt(0, 1, None, None, 2, None, None, 0.5, None) == _lib.PT_BAD_ARG
