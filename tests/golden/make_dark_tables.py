@@ -12,6 +12,7 @@ max_F come from ``dark_maps.pkl`` rebuilt by ``rebuild_maps.py --dark``.
 
 Usage: python tests/golden/make_dark_tables.py DARK_DICT_DIR SM_DICT_DIR [OUT.npz]
        python tests/golden/make_dark_tables.py --add-free DARK_DICT_DIR SM_DICT_DIR [OUT.npz]
+(every target of PETITE's find_maxes: graphite, lead, iron, aluminum, molybdenum)
 (SM_DICT_DIR: the output of rebuild_maps.py, which DarkShower's Shower base reads)
 """
 import multiprocessing as mp
@@ -30,7 +31,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import refimport  # noqa: E402
 
 MASSES = [0.003, 0.01, 0.03, 0.1, 0.3]
-TARGETS = ["graphite", "lead"]
+TARGETS = ["graphite", "lead", "iron", "aluminum", "molybdenum"]
 PROCS = ["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"]
 DRATE = {"brem_elec": "_d_rate_dict_elec_brem", "brem_positron": "_d_rate_dict_positron_brem",
          "ann": "_d_rate_dict_positron_ann", "muon_brem": "_d_rate_dict_muon_brem"}

@@ -221,14 +221,15 @@ def test_dark_yield_gradient_matches_fp64_reference(showers):
             assert abs(g[i] - ref) <= 1e-6 * abs(ref), (proc, E[i], mVh[i], g[i], ref)
 
 
-def test_dark_on_gpu_showers_matches_oracle(showers):
+@pytest.mark.parametrize("mV,target", [(0.1, "graphite"), (0.03, "iron"), (0.3, "molybdenum")])
+def test_dark_on_gpu_showers_matches_oracle(showers, mV, target):
     """SM showers from the GPU record engine, then pt_run_dark against the
-    oracle's produce_bsm_particle on the same rows and streams (10 GeV e-,
-    graphite, mV = 0.1 GeV)."""
-    import torch
+    oracle's produce_bsm_particle on the same rows and streams (10 GeV e-)."""
     from oracle import dark as D
     from oracle.shower import OracleTables
-    sh = showers[(0.1, "graphite")]
+    from petite_gb300.dark import DarkShower
+    sh = showers.get((mV, target)) or DarkShower(None, target, 0.010, mV, seed=SEED, active_processes=[
+        "DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"])
     n = 4
     p = math.sqrt(100.0 - 0.000511 ** 2)
     opts = sh._opts(True, "fp64")
@@ -246,7 +247,7 @@ def test_dark_on_gpu_showers_matches_oracle(showers):
         r.p0, r.pf, r.rf = tuple(rows["p0"][k]), tuple(rows["pf"][k]), tuple(rows["rf"][k])
         r.pid, r.mass, r.weight, r.pkey = int(rows["pid"][k]), float(rows["mass"][k]), 1.0, int(rows["pkey"][k])
         recs.append(r)
-    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, "graphite", 0.1), OracleTables(BUNDLED_NPZ, "graphite"), SEED)
+    orc = D.DarkOracle(D.DarkTables(DARK_NPZ, target, mV), OracleTables(BUNDLED_NPZ, target), SEED)
     out = orc.dark_shower(recs, processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"))
     want = np.array([[k, D.DARK_CODE[pp], w, *v] for k, pp, w, v, _ in out])
     want = want[np.lexsort((want[:, 1], want[:, 0]))]
