@@ -18,7 +18,7 @@ arrays, dR/dE tables, bound-electron cross sections and thresholds, as PETITE
 computes them), and bundles the maps with those tables in the layout of
 ``dark_tables.npz``.  Runs only in the development container.
 
-Usage: python tests/golden/make_dark_tables_400GeV.py MAPS.npz [--targets lead] [OUT.npz]
+Usage: python tests/golden/make_dark_tables_400GeV.py MAPS.npz [--targets graphite lead ...] [OUT.npz]
 """
 import argparse
 import multiprocessing as mp
@@ -85,7 +85,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("maps_npz")
     ap.add_argument("out", nargs="?", default=os.path.join(ROOT, "petite_gb300", "data", "400GeV", "dark_tables.npz"))
-    ap.add_argument("--targets", nargs="+", default=["lead"])
+    ap.add_argument("--targets", nargs="+", default=["graphite", "lead", "iron", "aluminum", "molybdenum"])
     a = ap.parse_args()
     work = tempfile.mkdtemp(prefix="dark400_")
     masses, z = write_dict_dir(os.path.abspath(a.maps_npz), work)

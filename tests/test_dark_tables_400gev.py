@@ -14,7 +14,7 @@ PATH = os.path.join(BUNDLED_DIR, "400GeV", "dark_tables.npz")
 
 def test_layout_and_coverage():
     d = DarkData(PATH)
-    assert d.masses == [0.1] and d.targets == ["lead"]
+    assert d.masses == [0.1] and d.targets == ["graphite", "lead", "iron", "aluminum", "molybdenum"]
     m = d.maps_for("lead", 1.0)
     rows = m["rows"][0]
     assert list(rows[:4]) == [150, 150, 150, 150]
