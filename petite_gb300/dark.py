@@ -6,7 +6,7 @@ differentiable dark-vector yield.
 the dark-vector production runs in ``pt_run_dark`` over the SM particle
 rows.  Tables come from the dict_dir's ``dark_tables.npz`` (bundled:
 ``data/dark_tables.npz``, and ``data/400GeV/dark_tables.npz`` for the
-400 GeV tables, mV = 0.1 GeV, lead): the dark VEGAS maps (PETITE's shipped
+400 GeV tables, mV = 0.1 GeV, five targets): the dark VEGAS maps (PETITE's shipped
 ``<Process>/mV_*`` maps, or maps trained by ``petite_gb300.train`` where
 PETITE ships none, with max_F from find_maxes) and, per (mass, target), the
 weight, dR/dE and bound-electron tables PETITE's constructor builds
