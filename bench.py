@@ -44,7 +44,8 @@ WORKLOADS = {
     "sm_e1gev_graphite_1k": dict(target="graphite", cut=0.010, n=1000, species=(11,), emin=1.0, emax=1.0,
                                  seed=0, precision="fp64", fp64_sample=1000, cpu_sample=400, mode="records"),
     # dark vectors on SM showers: 10^5 e- at 10 GeV in graphite, cut 0.010 GeV,
-    # the shipped dark masses nearest below {0.01, 0.05, 0.1, 0.3} GeV
+    # dark masses {0.01, 0.05, 0.1, 0.3} GeV (0.05: maps trained by
+    # petite_gb300.train; PETITE ships the others)
     "dark_e10_graphite_1e5": dict(target="graphite", cut=0.010, n=100_000, species=(11,), emin=10.0, emax=10.0,
                                   seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark"),
     # 10^5 mu- at 400 GeV in lead, cut 0.010 GeV, seed 3 (the SM transport of

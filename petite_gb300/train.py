@@ -281,8 +281,27 @@ def build_400GeV_tables(dict_dir: str, out_path: str, points_per_row: int = 1 <<
     return summary
 
 
+def dark_energies(process: str, mV: float, E_min: float = 0.0016, E_max: float = 100.0, n: int = 100):
+    """The incoming energies of a dark map set (utilities/
+    script_generateintegrators.py:53-82): DarkBrem from 1.25 mV, DarkMuonBrem
+    from 1.25 (mV + m_mu), DarkAnn and DarkComp from their thresholds up to
+    max(E_max, 100 x threshold)."""
+    me, mmu = T.M_ELECTRON, T.M_MUON
+    if process == "DarkBrem":
+        return np.geomspace(1.25 * mV, E_max, n)
+    if process == "DarkMuonBrem":
+        return np.geomspace(1.25 * (mV + mmu), E_max, n)
+    if process == "DarkAnn":
+        e0 = (mV ** 2 - 2 * me ** 2) / (2 * me)
+    else:
+        e0 = mV * (1 + mV / (2 * me))
+    top = np.max([E_max, 100 * e0])
+    return e0 * (1 + np.geomspace(1e-4, (top - e0) / e0, n))
+
+
 def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int = 1 << 21, device="cuda",
-                    targets=FIND_MAXES_TARGETS, log=print) -> dict:
+                    targets=FIND_MAXES_TARGETS, log=print, E_max: float = 100.0, n_energies: int = 100,
+                    train_all: bool = False) -> dict:
     """The dark maps of one mass for a PETITE dict_dir whose DarkBrem and
     DarkMuonBrem maps are not shipped (``data_400GeV``): shipped maps where
     they exist (DarkAnn, DarkComp), trained maps elsewhere at the energies of
@@ -291,20 +310,25 @@ def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int
     find_maxes.py:211-305).  Writes ``out_path`` with the map entries of
     ``dark_tables.npz`` (``m<mV>/<Process>/energy, neval, max_F, grid,
     nnodes``, plus ``xsec`` from find_maxes) and returns, per process, the
-    median ratio of that cross section to ``dark_xsec.pkl`` (lead)."""
+    median ratio of that cross section to ``dark_xsec.pkl`` (lead).  A mass
+    that ``dark_xsec.pkl`` lacks trains every process at the energies of
+    ``dark_energies`` (up to E_max, n_energies rows), as PETITE's generation
+    script would, and reports no ratio.  ``train_all`` trains shipped
+    processes too (to check the trainer against PETITE's rows)."""
     with open(os.path.join(dict_dir, "dark_xsec.pkl"), "rb") as f:
         dx = pickle.load(f)
-    key = [k for k in dx if abs(float(k) - mV) < 1e-12][0]
+    keys = [k for k in dx if abs(float(k) - mV) < 1e-12]
     out, summary = {"targets": np.array(targets)}, {}
     for proc in DARK_PROCESSES:
-        ref = np.asarray(dx[key][proc]["lead"], np.float64)
+        ref = np.asarray(dx[keys[0]][proc]["lead"], np.float64) if keys else None
         ship = os.path.join(dict_dir, proc, mass_dir(mV), f"{proc}_AdaptiveMaps.npy")
-        if os.path.exists(ship):
+        if os.path.exists(ship) and not train_all:
             E, grids = load_shipped_maps(dict_dir, proc, mV)
             ms = MapSet.from_grids(proc, E, grids, device, mV=mV)
             how = "shipped"
         else:
-            ms = train(MapSet.uniform(proc, ref[:, 0], device, mV=mV), points_per_row=points_per_row)
+            E = ref[:, 0] if ref is not None else dark_energies(proc, mV, E_max=E_max, n=n_energies)
+            ms = train(MapSet.uniform(proc, E, device, mV=mV), points_per_row=points_per_row)
             how = "trained"
         mf, xs = find_maxes(ms, targets=targets)
         g = ms.nodes.cpu().numpy()
@@ -316,11 +340,14 @@ def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int
         out[f"{pre}/xsec"] = xs
         out[f"{pre}/grid"] = g
         out[f"{pre}/nnodes"] = nn
-        j = list(targets).index("lead")
-        r = np.interp(ms.energies, ref[:, 0], ref[:, 1])
-        ok = r > 0
         summary[proc] = {"maps": how, "rows": len(ms.energies), "E_max": float(ms.energies.max()),
-                         "xsec_ratio_lead_median": float(np.median(xs[ok, j] / r[ok])) if ok.any() else None}
+                         "xsec_ratio_lead_median": None}
+        if ref is not None:
+            j = list(targets).index("lead")
+            r = np.interp(ms.energies, ref[:, 0], ref[:, 1])
+            ok = r > 0
+            if ok.any():
+                summary[proc]["xsec_ratio_lead_median"] = float(np.median(xs[ok, j] / r[ok]))
         log(proc, summary[proc])
     np.savez_compressed(out_path, **out)
     return summary

@@ -52,3 +52,20 @@ def test_trained_cross_sections_match_petite_rows():
         # its scale follows the cross section: max_F * neval above the mean
         mf = z[f"m0.1/{p}/max_F"][idx, targets.index("lead")]
         assert (mf * 300 > ref[:, 1]).all()
+
+
+def test_trained_mass_in_the_10gev_bundle():
+    """mV = 0.05 GeV, which PETITE ships no maps for: maps trained at the
+    energies of PETITE's generation script (petite_gb300.train.dark_energies,
+    which reproduces the shipped masses' energies exactly), tables on every
+    target."""
+    from petite_gb300.train import dark_energies
+    d = DarkData(os.path.join(BUNDLED_DIR, "dark_tables.npz"))
+    assert 0.05 in d.masses and len(d.targets) == 5
+    for p in ("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"):
+        for mV in (0.03, 0.05):
+            np.testing.assert_allclose(d.z[f"m{mV}/{p}/energy"], dark_energies(p, mV), rtol=1e-14)
+        assert (d.z[f"m0.05/{p}/max_F"] > 0).all()
+    for t in d.targets:
+        prm = d.params_for(0.05, t)
+        assert prm["w/brem_elec"][:, 1].max() > 0 and prm["E_res"] > 0

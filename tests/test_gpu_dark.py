@@ -221,7 +221,7 @@ def test_dark_yield_gradient_matches_fp64_reference(showers):
             assert abs(g[i] - ref) <= 1e-6 * abs(ref), (proc, E[i], mVh[i], g[i], ref)
 
 
-@pytest.mark.parametrize("mV,target", [(0.1, "graphite"), (0.03, "iron"), (0.3, "molybdenum")])
+@pytest.mark.parametrize("mV,target", [(0.1, "graphite"), (0.03, "iron"), (0.3, "molybdenum"), (0.05, "lead")])
 def test_dark_on_gpu_showers_matches_oracle(showers, mV, target):
     """SM showers from the GPU record engine, then pt_run_dark against the
     oracle's produce_bsm_particle on the same rows and streams (10 GeV e-)."""
