@@ -366,6 +366,17 @@ typedef struct pt_dark_params {
 } pt_dark_params;
 
 /* Vectors produced by pt_run_dark (device pointers; SoA like pt_particles). */
+/* A histogram of dark-vector energies: counts[p * bins + b] += weight for
+ * process p and b = floor(bins * (log10(E_V/GeV) - log10_lo) / (log10_hi -
+ * log10_lo)), clamped to [0, bins): the bins of a process sum to its yield.
+ * No reference counterpart (PETITE returns the vectors). */
+typedef struct pt_dark_hist {
+  double* counts;      /* [PT_N_DARK + 1][bins] (accumulated); NULL: none */
+  int32_t bins;
+  int32_t reserved0;
+  double log10_lo, log10_hi;
+} pt_dark_hist;
+
 typedef struct pt_dark_out {
   double* p4;          /* [4][capacity] lab four-momentum */
   double* r;           /* [3][capacity] production point (the parent's final position) */
@@ -376,6 +387,7 @@ typedef struct pt_dark_out {
   int64_t capacity;
   double* yield;       /* [PT_N_DARK + 1] summed weights per process, PT_TWOBODY last (accumulated) */
   double* yield_E;     /* [PT_N_DARK + 1] summed weight * E_V per process (accumulated) */
+  pt_dark_hist hist;   /* energy histogram of the vectors (counts NULL: none) */
 } pt_dark_out;
 
 typedef struct pt_dark pt_dark;
@@ -421,15 +433,16 @@ pt_status pt_dark_sample_only(pt_dark* d, const pt_dark_params* prm, int32_t pro
  * GetBSMWeights and produce_bsm_particle for each of n_params parameter
  * sets (dark masses, 1..16) on the same showers, so precision 0 gives
  * pt_run_sm + pt_run_dark's vectors.  Only the yields are kept:
- * yield/yield_E (device, [n_params][PT_N_DARK + 1], accumulated) and
- * *n_vectors (all sets).  d must be bound to h.  The waves run on the host
+ * yield/yield_E (device, [n_params][PT_N_DARK + 1], accumulated), the
+ * energy histogram when hist is not NULL (hist->counts: [n_params][PT_N_DARK
+ * + 1][bins], accumulated) and *n_vectors (all sets).  d must be bound to h.  The waves run on the host
  * loop; TwoBody_BSMDecay is not applied (SM showers hold no mesons).  No
  * reference counterpart as one call: PETITE runs generate_shower and then
  * generate_dark_shower over its list, once per mass. */
 pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_params* prm, int32_t n_params, const double* p0,
                             const double* r0, const int32_t* pid, const double* mass, int64_t n_primaries,
                             const pt_opts* opts, pt_tally* tally, int64_t queue_capacity, double* yield,
-                            double* yield_E, int64_t* n_vectors, void* stream);
+                            double* yield_E, const pt_dark_hist* hist, int64_t* n_vectors, void* stream);
 
 pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt_particles* sm, int64_t n_rows,
                       const pt_opts* opts, pt_dark_out* out, int64_t* n_out, void* stream);

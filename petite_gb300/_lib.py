@@ -97,10 +97,15 @@ class PtDarkParams(C.Structure):
                 ("ii_x", C.c_void_p * 3), ("ii_y", C.c_void_p * 3), ("ii_n", C.c_int32 * 3)]
 
 
+class PtDarkHist(C.Structure):
+    _fields_ = [("counts", C.c_void_p), ("bins", C.c_int32), ("reserved0", C.c_int32), ("log10_lo", C.c_double),
+                ("log10_hi", C.c_double)]
+
+
 class PtDarkOut(C.Structure):
     _fields_ = [("p4", C.c_void_p), ("r", C.c_void_p), ("weight", C.c_void_p), ("parent", C.c_void_p),
                 ("process", C.c_void_p), ("draws", C.c_void_p), ("capacity", C.c_int64),
-                ("yield_", C.c_void_p), ("yield_E", C.c_void_p)]
+                ("yield_", C.c_void_p), ("yield_E", C.c_void_p), ("hist", PtDarkHist)]
 
 
 class PtTrainTarget(C.Structure):
@@ -177,7 +182,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_dark_screen32.argtypes = [vp, C.c_int32, vp, vp, i64, C.c_double, vp, vp, vp]
     lib.pt_dark_screen32.restype = C.c_int
     lib.pt_run_batch_dark.argtypes = [vp, vp, C.POINTER(PtDarkParams), C.c_int32, vp, vp, vp, vp, i64,
-                                      C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp, vp, C.POINTER(i64), vp]
+                                      C.POINTER(PtOpts), C.POINTER(PtTally), i64, vp, vp, C.POINTER(PtDarkHist),
+                                      C.POINTER(i64), vp]
     lib.pt_run_batch_dark.restype = C.c_int
     lib.pt_sample_only.argtypes = [vp, i32, vp, vp, i64, C.POINTER(PtOpts), vp, vp, vp, vp]
     lib.pt_sample_only.restype = C.c_int

@@ -462,6 +462,13 @@ __device__ void dark_emit(const pt_dark_params& P, const pt_dark_out& out, unsig
   const double w = (S(wg) * S(r.weight)).v;
   if (out.yield) atomicAdd(out.yield + p, w);
   if (out.yield_E) atomicAdd(out.yield_E + p, w * V[0]);
+  if (out.hist.counts) {
+    const pt_dark_hist& H = out.hist;
+    const double f = (log10(V[0]) - H.log10_lo) / (H.log10_hi - H.log10_lo);
+    int b = f >= 0.0 ? (int)(f * H.bins) : 0;         // NaN and underflow: the first bin
+    if (b > H.bins - 1) b = H.bins - 1;
+    atomicAdd(H.counts + (size_t)p * H.bins + b, w);
+  }
   const unsigned long long slot = atomicAdd(counter, 1ull);   // vectors produced (returned in *n_out)
   if (!out.p4) return;
   if ((int64_t)slot >= out.capacity) { dark_raise(status, nullptr, PT_OOM, p, r.p0[0], 0); return; }
@@ -917,10 +924,12 @@ pt_status batch_dark_wave(void* ctx, const pt_particles* rows, int64_t n_rows, c
 extern "C" pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_params* prm, int32_t n_params,
                                        const double* p0, const double* r0, const int32_t* pid, const double* mass,
                                        int64_t n, const pt_opts* o, pt_tally* tally, int64_t queue_capacity,
-                                       double* yield, double* yield_E, int64_t* n_vectors, void* stream) {
+                                       double* yield, double* yield_E, const pt_dark_hist* hist, int64_t* n_vectors,
+                                       void* stream) {
   if (!h || !d || !prm || !o || !tally || !yield || !yield_E || !n_vectors || n < 0 || n_params < 1 ||
       n_params > kMaxBatchMasses)
     return PT_BAD_ARG;
+  if (hist && hist->counts && (hist->bins < 1 || !(hist->log10_hi > hist->log10_lo))) return PT_BAD_ARG;
   for (int m = 0; m < n_params; ++m) {
     const pt_dark_params* q = prm + m;
     if (q->mass_index < 0 || q->mass_index >= d->M.n_masses) return PT_BAD_TABLE;
@@ -947,6 +956,10 @@ extern "C" pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_p
     b->out[m] = pt_dark_out{};
     b->out[m].yield = yield + (size_t)m * (PT_N_DARK + 1);
     b->out[m].yield_E = yield_E + (size_t)m * (PT_N_DARK + 1);
+    if (hist && hist->counts) {
+      b->out[m].hist = *hist;
+      b->out[m].hist.counts = hist->counts + (size_t)m * (PT_N_DARK + 1) * hist->bins;
+    }
   }
   const WaveRowsHook hook{batch_dark_wave, b};
   const pt_status s = run_batch_rows(h, p0, r0, pid, mass, n, o, tally, queue_capacity, &hook, st);

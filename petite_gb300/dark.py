@@ -40,6 +40,10 @@ TWOBODY = "TwoBody_BSMDecay"
 MESON_TWOBODY_BR_PI0 = 0.98823                  # meson_twobody_branchingratios[111], particle.py:39-48
 DARK_NPZ = os.path.join(T.BUNDLED_DIR, "dark_tables.npz")
 _TABLES = ("brem_elec", "brem_positron", "ann", "muon_brem")
+# DarkShower.run_tallied's vector-energy histogram: log bins over
+# [1e-3, 1e3] GeV (under- and overflow in the end bins)
+DARK_HIST_BINS = 60
+DARK_HIST_E = (1e-3, 1e3)
 
 
 def closest_lesser_value(input_list, input_value):
@@ -258,20 +262,30 @@ class DarkEngine:
         out["n"] = n
         return out
 
-    def run_batch(self, prms, p0, r0, pid, mass, opts, tally, queue_capacity: int = 0, device_inputs=None):
+    def run_batch(self, prms, p0, r0, pid, mass, opts, tally, queue_capacity: int = 0, device_inputs=None,
+                  hist=None):
         """The SM engine's batched transport with dark vectors produced on
         every wave (pt_run_batch_dark) for each parameter set in ``prms``
         (one pt_dark_params, or a list: several masses on the same showers):
         returns (tally, yield [sets, N_DARK+1], yield_E [sets, N_DARK+1],
-        vectors) with the yields as numpy arrays."""
+        vectors), and with ``hist`` = (bins, log10 E_lo, log10 E_hi) the
+        vectors' energy histogram [sets, N_DARK+1, bins] as a fifth item;
+        the yields and histogram as numpy arrays."""
         import torch
         prms = [prms] if isinstance(prms, _lib.PtDarkParams) else list(prms)
         arr = (_lib.PtDarkParams * len(prms))(*prms)
         yld = torch.zeros((len(prms), _lib.N_DARK + 1), dtype=torch.float64, device=self.device)
         yldE = torch.zeros_like(yld)
+        counts = h = None
+        if hist is not None:
+            bins, lo, hi = hist
+            counts = torch.zeros((len(prms), _lib.N_DARK + 1, int(bins)), dtype=torch.float64, device=self.device)
+            h = _lib.PtDarkHist()
+            h.counts, h.bins, h.log10_lo, h.log10_hi = counts.data_ptr(), int(bins), float(lo), float(hi)
         tally, nv = self.sm.run_batch(p0, r0, pid, mass, opts, tally, queue_capacity, device_inputs,
-                                      dark=(self.handle, arr, yld, yldE))
-        return tally, yld.cpu().numpy(), yldE.cpu().numpy(), nv
+                                      dark=(self.handle, arr, yld, yldE, h, counts))
+        out = (tally, yld.cpu().numpy(), yldE.cpu().numpy(), nv)
+        return out + (counts.cpu().numpy(),) if counts is not None else out
 
     def yield_forward(self, process: int, energy, mV, mass_index, n_samples: int, seed: int, anchor=None):
         import torch
@@ -399,10 +413,13 @@ class DarkShower(Shower):
         vectors of every particle (GetBSMWeights and produce_bsm_particle on
         each particle's row, as generate_dark_shower over the SM list) tallied:
         summed weights and weight * E_V per dark process, and the count."""
-        _, y, yE, nv = self._dark_engine.run_batch(self._prm, None, None, None, None, opts, tally, queue_capacity,
-                                                   device_inputs)
+        lo, hi = math.log10(DARK_HIST_E[0]), math.log10(DARK_HIST_E[1])
+        _, y, yE, nv, h = self._dark_engine.run_batch(self._prm, None, None, None, None, opts, tally, queue_capacity,
+                                                      device_inputs, hist=(DARK_HIST_BINS, lo, hi))
         return {"dark_yield": {p: float(y[0, k]) for k, p in enumerate(DARK_PROCESSES)},
                 "dark_yield_E": {p: float(yE[0, k]) for k, p in enumerate(DARK_PROCESSES)},
+                "dark_energy_hist": {p: h[0, k] for k, p in enumerate(DARK_PROCESSES)},
+                "dark_energy_edges": np.logspace(lo, hi, DARK_HIST_BINS + 1),
                 "dark_vectors": int(nv)}
 
     # ------------------------------------------------------------- weights

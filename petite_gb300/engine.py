@@ -320,10 +320,12 @@ class SMEngine:
 
         p0 (n,4), r0 (n,3), pid (n,), mass (n,) host arrays, or device tensors in
         `device_inputs` = (p0 [4,n], r0 [3,n], pid [n], mass [n]) already resident.
-        ``dark`` = (dark handle, pt_dark_params array, yield, yield_E) runs
-        pt_run_batch_dark instead: dark vectors on every wave for each
+        ``dark`` = (dark handle, pt_dark_params array, yield, yield_E, hist, counts)
+        runs pt_run_batch_dark instead: dark vectors on every wave for each
         parameter set, yields accumulated into the two device tensors
-        ([sets, N_DARK + 1]); returns (tally, vectors)."""
+        ([sets, N_DARK + 1]) and, with ``hist`` a PtDarkHist over the device
+        tensor ``counts`` (or both None), their energy histogram; returns
+        (tally, vectors)."""
         torch = _torch()
         if device_inputs is None:
             p0 = np.asarray(p0, np.float64).reshape(-1, 4)
@@ -349,17 +351,20 @@ class SMEngine:
                 s = self.lib.pt_run_batch(self.handle, _ptr(P0), _ptr(R0), _ptr(PID), _ptr(M), n, C.byref(opts),
                                           C.byref(tally.abi()), cap, self._stream())
             else:
-                dh, prm, yld, yldE = dark
+                dh, prm, yld, yldE, hist = dark[:5]
                 nv = C.c_int64()
                 s = self.lib.pt_run_batch_dark(self.handle, dh, prm, len(prm), _ptr(P0), _ptr(R0), _ptr(PID),
                                                _ptr(M), n, C.byref(opts), C.byref(tally.abi()), cap, _ptr(yld),
-                                               _ptr(yldE), C.byref(nv), self._stream())
+                                               _ptr(yldE), C.byref(hist) if hist is not None else None,
+                                               C.byref(nv), self._stream())
             if s == _lib.PT_OOM and cap < (1 << 28):
                 # the live population outgrew the ring: start over with twice the room
                 tally.zero_()
                 if dark is not None:
                     dark[2].zero_()
                     dark[3].zero_()
+                    if dark[5] is not None:
+                        dark[5].zero_()
                 cap *= 2
                 continue
             self._raise(s, "pt_run_batch" if dark is None else "pt_run_batch_dark")

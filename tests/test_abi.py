@@ -59,7 +59,7 @@ def test_struct_layout_matches_header(tmp_path):
     structs = {"pt_tables": _lib.PtTables, "pt_particles": _lib.PtParticles, "pt_opts": _lib.PtOpts,
                "pt_tally": _lib.PtTally, "pt_dark_maps": _lib.PtDarkMaps, "pt_dark_params": _lib.PtDarkParams,
                "pt_dark_out": _lib.PtDarkOut, "pt_batch_tuning": _lib.PtBatchTuning,
-               "pt_train_target": _lib.PtTrainTarget}
+               "pt_train_target": _lib.PtTrainTarget, "pt_dark_hist": _lib.PtDarkHist}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "petite_gpu.h"', "int main(void) {"]
     for cname, cls in structs.items():
         lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
@@ -86,7 +86,7 @@ def test_entry_points_refuse_missing_handles_without_a_device(lib):
     opts, tally, prm = _lib.PtOpts(), _lib.PtTally(), _lib.PtDarkParams()
     assert lib.pt_run_batch(None, None, None, None, None, 1, C.byref(opts), C.byref(tally), 0, None) == _lib.PT_BAD_ARG
     assert lib.pt_run_batch_dark(None, None, C.byref(prm), 1, None, None, None, None, 1, C.byref(opts),
-                                 C.byref(tally), 0, None, None, C.byref(i64), None) == _lib.PT_BAD_ARG
+                                 C.byref(tally), 0, None, None, None, C.byref(i64), None) == _lib.PT_BAD_ARG
     assert lib.pt_dark_screen32(None, 0, None, None, 1, 0.1, None, None, None) == _lib.PT_BAD_ARG
     assert lib.pt_set_batch_tuning(None, None) == _lib.PT_BAD_ARG
     assert lib.pt_vegas_adapt(0, 1, None, None, 2, None, None, 0.5, None) == _lib.PT_BAD_ARG

@@ -387,7 +387,7 @@ def _record_dark(sh, p0, pid, m):
     opts = sh._opts(True, "fp64")
     opts.primary_offset = 0
     st, nr = sh._engine.run_sm(p0, np.zeros((n, 3)), np.full(n, pid, np.int32), np.full(n, m), np.ones(n), opts)
-    return sh._dark_engine.run_dark(sh._prm, st, nr, sh._opts(), keep_records=False), nr
+    return sh._dark_engine.run_dark(sh._prm, st, nr, sh._opts()), nr
 
 
 @pytest.mark.parametrize("case", ["e10_graphite", "mu400_lead"])
@@ -415,6 +415,17 @@ def test_batched_dark_yields_match_record_rows(showers, case):
         np.testing.assert_allclose(b["dark_yield_E"][p], rec["yield_E"][k], rtol=1e-9, atol=0)
     if case == "mu400_lead":
         assert b["dark_yield"]["DarkMuonBrem"] > 0
+    # the vectors' energy histogram: the record vectors binned the same way
+    edges = b["dark_energy_edges"]
+    lo, hi, nb = math.log10(edges[0]), math.log10(edges[-1]), len(edges) - 1
+    for k, p in enumerate(("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")):
+        h = b["dark_energy_hist"][p]
+        np.testing.assert_allclose(h.sum(), b["dark_yield"][p], rtol=1e-9, atol=0)
+        sel = rec["process"] % 4 == k
+        f = (np.log10(rec["p4"][sel, 0]) - lo) / (hi - lo)
+        idx = np.clip(np.floor(np.where(f >= 0, f, 0.0) * nb).astype(int), 0, nb - 1)
+        want = np.bincount(idx, weights=rec["weight"][sel], minlength=nb)
+        np.testing.assert_allclose(h, want, rtol=1e-9, atol=1e-12 * max(want.sum(), 1e-300))
     mx = sh.run_tallied(p0, pid=pid, mass=m, precision="mixed", first_primary=0)
     tot_f, tot_m = sum(b["dark_yield"].values()), sum(mx["dark_yield"].values())
     print(case, "vectors", b["dark_vectors"], mx["dark_vectors"], "yield", tot_f, tot_m)
