@@ -1681,9 +1681,12 @@ static pt_status wave_rows(BatchScratch* S, pt_particles* r) {
   S->rows_cap = L;
   const size_t bytes = (size_t)L * (13 * sizeof(double) + sizeof(int32_t) + sizeof(uint64_t)) + 8 * 256;
   if (!S->rows_mem && cudaMalloc(&S->rows_mem, bytes) != cudaSuccess) {
+    // a device allocation, not the ring's capacity: PT_OOM would invite a
+    // retry with a larger ring
     cudaGetLastError();
     S->rows_mem = nullptr;
-    return PT_OOM;
+    fprintf(stderr, "petite_gpu: no device memory for %zu bytes of shower rows\n", bytes);
+    return PT_CUDA_ERR;
   }
   char* p = (char*)S->rows_mem;
   auto take = [&](size_t b) { char* q = p; p += (b + 255) & ~size_t(255); return q; };

@@ -759,11 +759,12 @@ static pt_status dark_launch(pt_dark* d, const pt_dark_params& prm, const pt_opt
     cudaFree(d->tasks);
     d->tasks = nullptr;
     d->tasks_cap = 0;
-    if (cudaMalloc(&d->tasks, (size_t)work * (sizeof(int64_t) + sizeof(int32_t) + sizeof(double)) + 512) !=
-        cudaSuccess) {
+    const size_t bytes = (size_t)work * (sizeof(int64_t) + sizeof(int32_t) + sizeof(double)) + 512;
+    if (cudaMalloc(&d->tasks, bytes) != cudaSuccess) {     // a device allocation: not PT_OOM (see pt_run_dark)
       cudaGetLastError();
       d->tasks = nullptr;
-      return PT_OOM;
+      fprintf(stderr, "petite_gpu: no device memory for %zu bytes of dark tasks\n", bytes);
+      return PT_CUDA_ERR;
     }
     d->tasks_cap = work;
   }
