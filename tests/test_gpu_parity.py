@@ -75,7 +75,12 @@ def test_draw_sample_matches_oracle(engines):
     orc = _oracle("graphite")
     for code, proc in enumerate(PROCESSES):
         if proc == "MuonBrem":
-            continue          # its maps sample outside the Brem formula's support
+            # MuonBrem's maps sample where three terms of the Brem form cancel
+            # to 1e-9 (all_processes.py:1120-1127): the GPU's fused
+            # multiply-adds move the value by up to 1e-6, enough to flip an
+            # accept/reject against the oracle; its showers are compared
+            # statistically instead
+            continue
         Es = np.geomspace(0.3 if proc == "MuonE" else 0.02, 90.0, 24)
         keys = np.array([1000 * code + i + 1 for i in range(len(Es))], np.uint64)
         opts = sh._opts()
