@@ -216,6 +216,63 @@ def cpu_baseline(w, n_sample, cores=None):
                       f"oracle (CPU restatement of PETITE's transport loop) over {cores} spawned processes"}
 
 
+def cpu_dark_worker(args):
+    """The CPU oracle on the primaries of one spawned process: each one's SM
+    shower (untimed), then its produce_bsm_particle on every row and mass
+    (timed), until the dark part has taken `budget` seconds: rows, vectors,
+    dark seconds."""
+    sys.path.insert(0, ROOT)
+    from oracle.shower import OracleShower, OracleTables
+    from oracle import dark as D
+    target, cut, seed, p0, pid, mass, first, masses, procs, tdir, budget = args
+    sm_t = OracleTables(os.path.join(tdir, "sm_tables.npz"), target)
+    sh = OracleShower(sm_t, cut, seed=seed)
+    orcs = [D.DarkOracle(D.DarkTables(os.path.join(tdir, "dark_tables.npz"), target, mV), sm_t, seed)
+            for mV in masses]
+    rows = vecs = 0
+    t_dark = 0.0
+    for i in range(len(p0)):
+        recs = sh.generate_shower(tuple(p0[i]), pid=int(pid[i]), mass=float(mass[i]), primary_index=first + i)
+        t0 = time.perf_counter()
+        for orc in orcs:
+            vecs += len(orc.dark_shower(recs, processes=tuple(procs)))
+        t_dark += time.perf_counter() - t0
+        rows += len(recs)
+        if t_dark > budget:
+            break
+    return rows, vecs, t_dark
+
+
+def dark_cpu_sample(w):
+    """A bounded CPU sample: a 400 GeV muon shower takes the oracle about a
+    minute, so those workloads take one primary per process."""
+    return {"budget": 10.0, "per_proc": 1} if w["emin"] > 100.0 else {"budget": 15.0, "per_proc": 64}
+
+
+def cpu_dark_baseline(w, n_proc=None, budget=15.0, per_proc=64):
+    """The dark part on the host cores: row x mass per second of the oracle's
+    dark production, summed over spawned processes that each take primaries
+    drawn like the workload until their dark part has run about `budget`
+    seconds (the SM showers are made first and not timed)."""
+    import multiprocessing as mp
+    n_proc = n_proc or os.cpu_count()
+    p0, pid, m = make_primaries(w, n_proc * per_proc, offset=10_000)
+    procs = list(w.get("dark_processes", ("DarkBrem", "DarkAnn", "DarkComp")))
+    jobs = []
+    for k in range(n_proc):
+        sl = slice(k * per_proc, (k + 1) * per_proc)
+        jobs.append((w["target"], w["cut"], w["seed"], p0[sl], pid[sl], m[sl], k * per_proc, list(w["masses"]),
+                     procs, tables_dir(w), budget))
+    with mp.get_context("spawn").Pool(n_proc) as pool:
+        res = pool.map(cpu_dark_worker, jobs)
+    rate = sum(r[0] * len(w["masses"]) / r[2] for r in res if r[2] > 0)   # the processes run side by side
+    rows, vecs = sum(r[0] for r in res), sum(r[1] for r in res)
+    return {"value": rate, "unit": "row-masses/s", "cores": n_proc, "kind": "port",
+            "sample": f"primaries drawn like the workload over {n_proc} spawned processes: the oracle's "
+                      f"produce_bsm_particle on {rows} SM rows x {len(w['masses'])} masses ({vecs} vectors), "
+                      f"about {budget:.0f} s of dark work per process (the SM showers untimed)"}
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -232,9 +289,27 @@ def run_reference(args, w, name):
     dist, rank, ws = dist_setup()
     if rank != 0:
         return
+    if w["mode"] == "dark":
+        # the same metric on the host cores: the oracle's dark production
+        vals, cb = [], None
+        for _ in range(args.steps):
+            cb = cpu_dark_baseline(w, **dark_cpu_sample(w))
+            vals.append(cb["value"])
+        v = float(np.median(vals))
+        print(json.dumps({"impl": "reference", "metric": "dark-vector production: SM rows x dark masses per second "
+                          "(pt_run_dark)", "value": v, "unit": "row-masses/s", "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": name, "target": w["target"], "cut_GeV": w["cut"],
+                                     "masses_GeV": list(w["masses"])},
+                          "cpu_baseline": {**cb, "value": v},
+                          "e2e": {"value": v, "unit": "row-masses/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
     if w["mode"] not in ("batch", "records"):
-        print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {name} workload; "
-                          "the dark path is compared with the oracle in tests/test_gpu_dark.py"}))
+        print(json.dumps({"impl": "reference", "unavailable": f"no CPU arm for the {name} workload (its metric "
+                          "counts the GPU's SM and dark work together); the dark_* workloads time the oracle's "
+                          "dark production"}))
         return
     vals, cb = [], None
     for _ in range(args.steps):
@@ -569,6 +644,7 @@ def bench_dark(args, w, name, dist, rank, ws):
         return
     per_mass = {f"{d.get_mV()}": {"yield_per_primary": (ysum[k] / (n * args.steps)).tolist()}
                 for k, d in enumerate(showers)}
+    cb = None if args.no_cpu_baseline else cpu_dark_baseline(w, **dark_cpu_sample(w))
     print(json.dumps({
         "metric": "dark-vector production: SM rows x dark masses per second (pt_run_dark)",
         "value": rows * len(showers) / t_dark, "unit": "row-masses/s", "n_gpus": ws, "steps": args.steps,
@@ -579,7 +655,7 @@ def bench_dark(args, w, name, dist, rank, ws):
                    "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
                    "tables": w.get("tables", "bundled")},
         "sm_rows": rows, "sm_rows_per_s": rows / t_sm, "vectors": vecs, "vectors_per_s": vecs / t_dark,
-        "yields": per_mass, "clocks": clk.summary()}))
+        "yields": per_mass, "cpu_baseline": cb, "clocks": clk.summary()}))
 
 
 def bench_yield(args, w, name, dist, rank, ws):
@@ -677,6 +753,9 @@ def bench_batchdark(args, w, name, dist, rank, ws):
         return
     per_mass = {f"{d.get_mV()}": {"yield_per_primary": (ysum[k][:4] / (n * args.steps)).tolist()}
                 for k, d in enumerate(showers)}
+    # the host cores' rate of the dark part alone (row x mass per second), for
+    # the row_masses_per_s figure of this line
+    cb = None if args.no_cpu_baseline else cpu_dark_baseline(w, **dark_cpu_sample(w))
     print(json.dumps({
         "metric": "SM showers with dark-vector production on the batched engine: particle-steps/s",
         "value": steps / t, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -688,7 +767,7 @@ def bench_batchdark(args, w, name, dist, rank, ws):
                    "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
                    "tables": w.get("tables", "bundled"), "timed": "host inputs in, yields out"},
         "row_masses_per_s": steps * len(showers) / t, "vectors": vecs, "vectors_per_s": vecs / t,
-        "yields": per_mass, "clocks": clk.summary()}))
+        "yields": per_mass, "cpu_baseline": cb, "clocks": clk.summary()}))
 
 
 def main():
