@@ -878,6 +878,36 @@ BETHE_CASES = [
     ("mu5_graphite", "graphite", 0.010, 13, 5.0, 2, 0.1056583755),
 ]
 
+def gen_findmax(path, seed=20261206):
+    """PETITE's do_find_max_work (utilities/find_maxes.py:56-115, unmodified)
+    on a few shipped map rows, neval 300, 3 trials, graphite and lead, with
+    the VEGAS shim drawing from numpy's default_rng(seed + row): max_F and
+    the cross section per target, and the rows' grids.  Pins
+    oracle.vegas_train.find_maxes_row."""
+    refimport.setup()
+    import vegas
+    import find_maxes as fm
+    out = {"seed": np.array(seed)}
+    for proc, rows in (("Comp", (5, 40, 90)), ("Brem", (10, 60))):
+        arr = np.load(os.path.join(refimport.REFERENCE, "data", proc, f"{proc}_AdaptiveMaps.npy"), allow_pickle=True)
+        for r in rows:
+            event_info, amap = arr[r]
+            vegas.UNIFORM = np.random.default_rng(seed + r).random
+            params = {"process_targets": ["graphite", "lead"], "neval": 300, "n_trials": 3,
+                      "diff_xsec": fm.process_info[proc]["diff_xsection"]}
+            samp, xsec, E = fm.do_find_max_work(params, [event_info, amap])
+            pre = f"{proc}/{r}"
+            out[f"{pre}/E"] = np.array(float(E))
+            for d, g in enumerate(amap.grid):
+                out[f"{pre}/grid{d}"] = np.asarray(g, float)
+            out[f"{pre}/max_F"] = np.array([samp[1]["max_F"][t] for t in ("graphite", "lead")])
+            out[f"{pre}/xsec"] = np.array([xsec[t] for t in ("graphite", "lead")])
+            out[f"{pre}/Eg_min"] = np.array(event_info["Eg_min"])
+            out[f"{pre}/Ee_min"] = np.array(event_info["Ee_min"])
+    vegas.UNIFORM = np.random.random
+    np.savez_compressed(path, **out)
+
+
 def gen_dark_xsec_400(path, mV=0.1, every=15):
     """Rows of data_400GeV/dark_xsec.pkl (find_maxes' cross sections with
     PETITE's own DarkBrem/DarkMuonBrem maps, which it does not ship): the
@@ -914,6 +944,8 @@ if __name__ == "__main__":
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
     if which in ("all", "darkfree"):
         gen_dark_free(d, os.path.join(HERE, "dark_free.npz"))
+    if which in ("all", "findmax"):
+        gen_findmax(os.path.join(HERE, "findmax.npz"))
     if which in ("all", "darkxsec400"):
         gen_dark_xsec_400(os.path.join(HERE, "dark_xsec_400GeV.npz"))
     if which in ("all", "particles"):

@@ -34,3 +34,28 @@ def test_compressed_weights_are_shared_equally():
     w = np.array([1, 1, 1, 1, 100, 100, 1, 1, 1, 1], float)
     out = adapt(g, w, np.ones(10, int), alpha=0.0)      # alpha = 0: every nonzero increment weighs 1
     np.testing.assert_allclose(out, g, atol=1e-12)
+
+
+def test_find_maxes_restatement_matches_the_reference():
+    """oracle.vegas_train.find_maxes_row against the reference's own
+    do_find_max_work on shipped Comp and Brem map rows, both drawing from
+    the same seeded generator (tests/golden/findmax.npz)."""
+    import os
+    from conftest import GOLDEN
+    from oracle import physics as P
+    from oracle.vegas_train import find_maxes_row
+    z = np.load(os.path.join(GOLDEN, "findmax.npz"))
+    seed = int(z["seed"])
+    Z = {"graphite": 6, "lead": 82}
+    me = 0.0005109989499999999
+    n = 0
+    for key in sorted({k.rsplit("/", 1)[0] for k in z.files if k.count("/") == 2}):
+        proc, row = key.split("/")
+        E, Eg, Ee = float(z[f"{key}/E"]), float(z[f"{key}/Eg_min"]), float(z[f"{key}/Ee_min"])
+        grids = [z[f"{key}/grid{d}"] for d in range(4) if f"{key}/grid{d}" in z]
+        fs = {t: (lambda x, zt=Z[t]: P.dsigma(proc, x, E, zt, Eg, Ee, me)) for t in ("graphite", "lead")}
+        mx, xs = find_maxes_row(grids, fs, 300, 3, np.random.default_rng(seed + int(row)).random)
+        np.testing.assert_allclose([mx["graphite"], mx["lead"]], z[f"{key}/max_F"], rtol=1e-10)
+        np.testing.assert_allclose([xs["graphite"], xs["lead"]], z[f"{key}/xsec"], rtol=1e-10)
+        n += 1
+    assert n == 5
