@@ -878,6 +878,23 @@ BETHE_CASES = [
     ("mu5_graphite", "graphite", 0.010, 13, 5.0, 2, 0.1056583755),
 ]
 
+def gen_ranges(path):
+    """PETITE's integration_range (all_processes.py:1102-1160) for the
+    processes the table builder trains, at several energies and masses."""
+    refimport.setup()
+    import PETITE.all_processes as proc
+    rows = []
+    for p in ("PairProd", "Brem", "MuonBrem", "Comp", "Ann", "Moller", "Bhabha", "MuonE",
+              "DarkBrem", "DarkMuonBrem", "DarkComp", "DarkAnn"):
+        for E in (0.01, 0.3, 7.0, 350.0):
+            for mV in ((0.0,) if not p.startswith("Dark") else (0.003, 0.05, 0.3)):
+                ev = {"E_inc": E, "mV": mV, "Eg_min": 0.001, "Ee_min": 0.005}
+                r = np.asarray(proc.integration_range(ev, p), float).ravel()
+                rows.append((p, E, mV, np.pad(r, (0, 8 - len(r)), constant_values=np.nan)))
+    np.savez_compressed(path, process=np.array([r[0] for r in rows]), E=np.array([r[1] for r in rows]),
+                        mV=np.array([r[2] for r in rows]), ranges=np.array([r[3] for r in rows]))
+
+
 def gen_findmax(path, seed=20261206):
     """PETITE's do_find_max_work (utilities/find_maxes.py:56-115, unmodified)
     on a few shipped map rows, neval 300, 3 trials, graphite and lead, with
@@ -944,6 +961,8 @@ if __name__ == "__main__":
         gen_moliere(d, os.path.join(HERE, "moliere.npz"))
     if which in ("all", "darkfree"):
         gen_dark_free(d, os.path.join(HERE, "dark_free.npz"))
+    if which in ("all", "ranges"):
+        gen_ranges(os.path.join(HERE, "ranges.npz"))
     if which in ("all", "findmax"):
         gen_findmax(os.path.join(HERE, "findmax.npz"))
     if which in ("all", "darkxsec400"):

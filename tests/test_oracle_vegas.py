@@ -59,3 +59,17 @@ def test_find_maxes_restatement_matches_the_reference():
         np.testing.assert_allclose([xs["graphite"], xs["lead"]], z[f"{key}/xsec"], rtol=1e-10)
         n += 1
     assert n == 5
+
+
+def test_integration_ranges_match_the_reference():
+    """petite_gb300.train.integration_range against PETITE's own
+    integration_range for every process the table builder trains
+    (tests/golden/ranges.npz)."""
+    import os
+    from conftest import GOLDEN
+    from petite_gb300.train import integration_range
+    z = np.load(os.path.join(GOLDEN, "ranges.npz"))
+    for p, E, mV, want in zip(z["process"], z["E"], z["mV"], z["ranges"]):
+        got = np.asarray(integration_range(str(p), float(E), mV=float(mV)), float).ravel()
+        w = want[~np.isnan(want)]
+        np.testing.assert_allclose(got, w, rtol=1e-15, atol=0, err_msg=f"{p} {E} {mV}")
