@@ -79,22 +79,26 @@ WORKLOADS = {
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
 }
 
-# Algorithmic HBM bytes of the batched engine's two kernels, per unit of work,
-# for the ring's structure of arrays (E and key are 8 B; momentum, position
-# and mass 8 B in the float64 form and 4 B in the mixed form; pid, primary,
-# generation, map row and draw counter 4 B each).  Tables (maps, n*sigma) are
-# L2-resident and not counted.
-#   propagation, per particle-step: read E, p, r, mass, key, pid, primary;
-#     per sampled particle: park E, p, r, draw, row and write its task index.
-#   sampler, per sampled particle: read the task index and E, p, r, key, pid,
-#     primary, generation, row, draw; per pushed daughter: write E, p, r,
-#     mass, key, pid, primary, generation.
+# Algorithmic HBM bytes of the batched engine's two kernels, per unit of work.
+# The ring is a structure of arrays (E and key 8 B; momentum, position and
+# mass 8 B in the float64 form and 4 B in the mixed form, where E also has a
+# 4 B float copy; pid, primary and generation 4 B each).  A particle that
+# interacts is parked as one task record (64 B mixed, 96 B float64) in a
+# chunk of 32 records of its process, plus a 4-byte chunk-list entry per
+# chunk.  Tables (maps, n*sigma) are L2-resident and not counted.
+#   propagation, per particle-step: read E, p, r, mass, key, pid, primary
+#     (and the float copy of E); per sampled particle: write its task record
+#     (reading the generation it carries).
+#   sampler, per sampled particle: read its task record; per pushed
+#     daughter: write E, p, r, mass, key, pid, primary, generation.
 def ring_bytes(precision):
     f = 8 if precision == "fp64" else 4
-    return {"prop_per_step": 8 + 7 * f + 8 + 8,
-            "prop_per_sampled": 8 + 6 * f + 8 + 4,
-            "sample_per_sampled": 4 + 8 + 6 * f + 8 + 20,
-            "sample_per_pushed": 8 + 7 * f + 8 + 12}
+    rec = 96 if precision == "fp64" else 64
+    e32 = 0 if precision == "fp64" else 4
+    return {"prop_per_step": 8 + e32 + 7 * f + 8 + 8,
+            "prop_per_sampled": rec + 4 + 4 / 32,
+            "sample_per_sampled": rec + 4 / 32,
+            "sample_per_pushed": 8 + e32 + 7 * f + 8 + 12}
 # Record engine: read the live row (100 B), write its final state (60 B) and
 # the one row it creates on average (176 B).
 BYTES_PER_STEP_RECORDS = 336

@@ -29,7 +29,11 @@ typedef enum pt_status {
   PT_OK = 0,
   PT_NO_SAMPLE = 1,   /* rejection sampler exhausted max_n_integrators*neval proposals
                          ("No Sample Found", shower.py:460-461) */
-  PT_TIMEOUT = 2,     /* a bounded device loop hit its iteration limit */
+  PT_TIMEOUT = 2,     /* a bounded device loop or wait hit its limit; pt_last_error_info's process is
+                         -1 for a loop bound (substep loop, waves of a run, the persistent kernel's
+                         grid barrier) and -2 for a table-staging copy into shared memory that did
+                         not land in time: that copy may still be in flight, so later results on
+                         the device are suspect and the handle should be discarded */
   PT_BAD_TABLE = 3,   /* inconsistent table description */
   PT_OOM = 4,         /* output/queue capacity too small: retry with more rows */
   PT_CUDA_ERR = 5,    /* a CUDA runtime call failed */
@@ -133,7 +137,10 @@ typedef struct pt_opts {
   int64_t primary_offset;        /* primary i draws from the stream of index primary_offset + i */
   int32_t mcs_mode;              /* 0 = Shower(fast_MCS_mode=True): Lynch-Dahl Gaussian (moliere.py:350-400);
                                     1 = fast_MCS_mode=False: Bethe-Moliere (moliere.py:403-453) */
-  int32_t reserved0;             /* 0 */
+  int32_t loop_limit;            /* 0 = the library's bounds (2^22 substeps per particle in pt_run_sm,
+                                    2^20 waves per pt_run_batch).  > 0: pt_run_sm ends a particle's
+                                    substep loop after this many iterations and pt_run_batch ends after
+                                    this many waves, with PT_TIMEOUT; for tests of the bounded paths */
 } pt_opts;
 
 /* Shower.generate_shower (shower.py:603-708) for n_primaries independent
@@ -157,7 +164,8 @@ pt_status pt_run_sm(pt_handle* h, pt_particles* out, int64_t n_primaries,
  *    rejected with PT_BAD_ARG and a message on stderr.
  *  - The first call on each device looks up the array's address
  *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    before any stream capture.  A failed lookup returns PT_CUDA_ERR and is
+ *    tried again by the next call; only a successful one is kept.
  *  - The status word, error record and counters are zeroed (cudaMemsetAsync)
  *    at the start of every call.
  *  - All calls on a device share the one array: calls that overlap in time
@@ -230,7 +238,8 @@ typedef struct pt_batch_tuning {
   int32_t loop;
   int32_t staging;
   int32_t threads;
-  int32_t reserved0;
+  int32_t barrier_ns;             /* the persistent kernel's bound on one grid-barrier wait, ns (0 = 20 s);
+                                     a wait that runs out returns PT_TIMEOUT.  For tests of that path. */
 } pt_batch_tuning;
 /* Stores the settings on the handle (NULL restores the defaults);
  * PT_BAD_ARG for a value out of range. */
@@ -242,6 +251,12 @@ pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t);
  * PT_LOOP_PERSISTENT: the whole run, and 0).  Diagnostic; no reference
  * counterpart. */
 pt_status pt_last_kernel_times(pt_handle* h, double* propagate_ms, double* sample_ms);
+
+/* Measured arithmetic peaks of the current GPU, for the rooflines of the
+ * issue-bound kernels: float32 and float64 fused multiply-add throughput in
+ * flop/s (chains of independent FMAs on every SM, timed with CUDA events on
+ * `stream`; about 10 ms).  Diagnostic; no reference counterpart. */
+pt_status pt_alu_peaks(double* fp32_flops, double* fp64_flops, void* stream);
 
 /* Shower.draw_sample (shower.py:401-465) for a batch: for each i, draws the
  * final-state variables of `process` at energy energy[i] from stream key

@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "PT_OK", 1: "PT_NO_SAMPLE", 2: "PT_TIMEOUT", 3: "PT_BAD_TABLE
 PT_OK, PT_NO_SAMPLE, PT_TIMEOUT, PT_BAD_TABLE, PT_OOM, PT_CUDA_ERR, PT_BAD_ARG = range(7)
 
 EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_last_run_stats",
-           "pt_last_kernel_times", "pt_set_batch_tuning", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch",
+           "pt_last_kernel_times", "pt_alu_peaks", "pt_set_batch_tuning", "pt_run_sm", "pt_run_sm_noalloc", "pt_run_batch",
            "pt_sample_only", "pt_dsigma", "pt_moliere_inverse_cdf",
            "pt_vegas_accumulate", "pt_vegas_adapt", "pt_find_maxes",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
@@ -66,7 +66,7 @@ class PtTally(C.Structure):
 class PtOpts(C.Structure):
     _fields_ = [("min_energy", C.c_double), ("max_n_integrators", C.c_int64), ("rescale_MCS", C.c_double),
                 ("multiple_scattering", C.c_int32), ("precision", C.c_int32), ("seed", C.c_uint64),
-                ("primary_offset", C.c_int64), ("mcs_mode", C.c_int32), ("reserved0", C.c_int32)]
+                ("primary_offset", C.c_int64), ("mcs_mode", C.c_int32), ("loop_limit", C.c_int32)]
 
 
 N_DARK = 4
@@ -118,7 +118,7 @@ TRAIN_DARK = 16
 
 class PtBatchTuning(C.Structure):
     _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("staging", C.c_int32),
-                ("threads", C.c_int32), ("reserved0", C.c_int32)]
+                ("threads", C.c_int32), ("barrier_ns", C.c_int32)]
 
 
 class PetiteGPUError(RuntimeError):
@@ -158,6 +158,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_last_run_stats.restype = C.c_int
     lib.pt_last_kernel_times.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pt_last_kernel_times.restype = C.c_int
+    lib.pt_alu_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), vp]
+    lib.pt_alu_peaks.restype = C.c_int
     lib.pt_set_batch_tuning.argtypes = [vp, C.POINTER(PtBatchTuning)]
     lib.pt_set_batch_tuning.restype = C.c_int
     lib.pt_run_sm.argtypes = [vp, C.POINTER(PtParticles), i64, C.POINTER(PtOpts), C.POINTER(i64), vp]

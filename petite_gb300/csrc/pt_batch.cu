@@ -44,18 +44,48 @@ constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kHB = PT_HIST_BINS;
 constexpr int kHist = 3 * 4 * kHB;
-constexpr int kBuf = 64;        // per-warp, per-process task buffer (published at >= 32)
 
 // Ring entry fields.  Energies are float64 in both engines; the mixed engine
 // keeps momenta, positions and masses in float32.
 template <int PREC> struct RingT {
   using R = typename std::conditional<PREC == 0, double, float>::type;
   double* E;
+  float* E32;                           // (float)E, written with E in the mixed form: the propagation
+                                        // kernel's refill then needs no float64 conversion
   R *px, *py, *pz, *x, *y, *z, *mass;
   uint64_t* key;
-  int32_t *pid, *prim, *gen, *row;
-  uint32_t* draw;
+  int32_t *pid, *prim, *gen;
 };
+
+// A sampling task: the state of a particle that interacts, after its
+// propagation (energy, momentum, position), its stream position, its map
+// row and what its daughters inherit.  One record per task, so the sampler
+// reads two 32-byte sectors per task in the mixed form instead of gathering
+// a sector for each ring field.  The first 32 bytes hold what the sampler
+// reads when it takes the task; the rest is read by the kinematics.
+template <int PREC> struct Park;
+template <> struct alignas(64) Park<1> {
+  double E;
+  uint64_t key;
+  int32_t row;
+  uint32_t draw;
+  int32_t pid, gen;
+  float px, py, pz, x, y, z, mass;
+  int32_t prim;
+};
+template <> struct alignas(32) Park<0> {
+  double E;
+  uint64_t key;
+  int32_t row;
+  uint32_t draw;
+  int32_t pid, gen;
+  double px, py, pz, x, y, z, mass;
+  int32_t prim, pad;
+};
+static_assert(sizeof(Park<1>) == 64 && sizeof(Park<0>) == 96, "task record layout");
+// Tasks are parked in chunks of 32 records of one process.  A chunk-list
+// entry is (chunk id << 5) | (tasks in the chunk - 1).
+constexpr int kChunkTasks = 32;
 
 struct Tally {
   unsigned long long* counts;
@@ -89,16 +119,21 @@ template <int PREC> struct WaveCtx {
   uint64_t mask;                      // ring capacity - 1
   uint64_t head, tail;                // ring positions of this wave's first entry and of the append point
   int64_t n_in;                       // entries in this wave
-  int64_t list_cap;                   // entries per process list
+  int64_t list_cap;                   // largest wave
   int out_chunk;                      // output slots reserved per warp at a time (0 = exact)
-  int32_t* idx;                       // [8][list_cap] ring indices of sampling tasks by process
-  unsigned long long* ctr;            // [0] head1, [1] head2, [2] appended, [8..15] per-process counts
+  Park<PREC>* park;                   // [chunk_cap * 32] task records, in chunks of one process
+  int32_t* chunks;                    // [8][chunk_cap] published chunks of each process
+  int64_t chunk_cap;                  // chunks a wave may claim
+  unsigned long long* ctr;            // [0] head1, [1] head2, [2] appended, [3] chunks claimed,
+                                      // [8..15] chunks published per process
   int* status;
   double* err_info;
   Tally tally;
   int refill_min[2];                  // idle lanes a warp gathers before refilling: [0] propagation, [1] sampler
   int chunk[2];                       // pool entries a warp claims per atomic: [0] propagation, [1] sampler
   PhiloxRK rk;                        // round keys of `seed` (float32 kernels)
+  int64_t max_waves;                  // waves a run may take (PT_TIMEOUT beyond)
+  unsigned long long barrier_ns;      // the persistent kernel's bound on one grid-barrier wait
   // device-planned waves (null: the host plans each wave and passes it here)
   WavePlan* plan;
   pt_particles rows;                  // per-wave rows for a WaveRowsHook (capacity 0: none)
@@ -258,61 +293,82 @@ __device__ __forceinline__ void out_take(OutPool& P, unsigned long long* ctr, in
 // ---------------------------------------------- float32 table lookups
 // The float32 n*sigma tables (nodes, values, slopes) read either through the
 // read-only data path (SH = false) or from a block's shared-memory copy
-// (SH = true; staged by TMA bulk copies, stage_ns_tables).
-template <bool SH> struct Ns32 { const float* x; const float* y; const float* s; };
+// (SH = true; staged by TMA bulk copies, stage_ns_tables).  Each slot's
+// first entry, length and index-guess constants sit in a small header in the
+// block's shared memory, so lanes of different species look up different
+// slots with the same instructions (one copy of the lookup code instead of
+// one per species, which also keeps the kernel's code small).
+struct NsHdr { int base, len; float lnx0, idl; };
+template <bool SH> struct Ns32 { const float* x; const float* y; const float* s; const NsHdr* h; };
 template <bool SH> __device__ __forceinline__ float ld32(const float* p) {
   if constexpr (SH) return *p;
   else return __ldg(p);
 }
-__device__ __forceinline__ Ns32<false> ns_global(const Tabs& T) { return {T.t.ns_x32, T.t.ns_y32, T.t.ns_s32}; }
+__device__ __forceinline__ Ns32<false> ns_global(const Tabs& T) {
+  return {T.t.ns_x32, T.t.ns_y32, T.t.ns_s32, nullptr};
+}
+
+// One thread fills the block's slot headers (call before a block barrier).
+__device__ __forceinline__ void fill_ns_hdr(const Tabs& T, NsHdr* h) {
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < PT_N_NSIGMA; ++s) h[s] = {T.t.ns_base[s], T.t.ns_len[s], T.t.ns_lnx0[s], T.t.ns_invdlog[s]};
+  }
+}
 
 template <bool SH>
-__device__ __forceinline__ int geo_index(const float* x, int n, float lnx0, float idl, float E) {
-  int j = (int)((__logf(E) - lnx0) * idl);
+__device__ __forceinline__ int geo_index(const float* x, int n, float lnx0, float idl, float lnE, float E) {
+  int j = (int)((lnE - lnx0) * idl);
   j = j < 0 ? 0 : (j > n - 2 ? n - 2 : j);
   while (j > 0 && ld32<SH>(x + j) > E) --j;
   while (j < n - 2 && ld32<SH>(x + j + 1) <= E) ++j;
   return j;
 }
 
-// interp1d(kind='linear', fill_value=0) in float32 (shower.py:280-295)
+// interp1d(kind='linear', fill_value=0) in float32 (shower.py:280-295);
+// lnE = __logf(E), for the index guess on the geometric grid.
 template <bool SH>
-__device__ __forceinline__ float nsig32(const Tabs& T, const Ns32<SH>& v, int slot, float E) {
-  const int b = T.t.ns_base[slot], n = T.t.ns_len[slot];
-  const float* x = v.x + b;
+__device__ __forceinline__ float nsig32(const Ns32<SH>& v, int slot, float E, float lnE) {
+  const NsHdr h = v.h[slot];
+  const float* x = v.x + h.base;
+  const int n = h.len;
   if (!(E >= ld32<SH>(x)) || E > ld32<SH>(x + n - 1)) return 0.f;
-  const int j = geo_index<SH>(x, n, T.t.ns_lnx0[slot], T.t.ns_invdlog[slot], E);
-  return fmaf(E - ld32<SH>(x + j), ld32<SH>(v.s + b + j), ld32<SH>(v.y + b + j));
+  const int j = geo_index<SH>(x, n, h.lnx0, h.idl, lnE, E);
+  return fmaf(E - ld32<SH>(x + j), ld32<SH>(v.s + h.base + j), ld32<SH>(v.y + h.base + j));
 }
 
+// Mean free path (shower.py:357-389): the slots summed in the reference's
+// order -- photon PairProd + Comp, electron Brem + Moller, positron Brem +
+// Bhabha + Ann, muon MuonBrem + MuonE -- chosen by selects on the PID.
 template <bool SH>
-__device__ __forceinline__ float mfp32(const Tabs& T, const Ns32<SH>& v, int pid, float E) {
-  float ns;
-  if (pid == 22) ns = nsig32(T, v, 1, E) + nsig32(T, v, 3, E);
-  else if (pid == 11) ns = nsig32(T, v, 0, E) + nsig32(T, v, 4, E);
-  else if (pid == -11) ns = nsig32(T, v, 0, E) + nsig32(T, v, 5, E) + nsig32(T, v, 2, E);
-  else ns = nsig32(T, v, 7, E) + nsig32(T, v, 6, E);
+__device__ __forceinline__ float mfp32(const Ns32<SH>& v, int pid, float E) {
+  const int a = pid == 22 ? 1 : (pid == 11 || pid == -11 ? 0 : 7);
+  const int b = pid == 22 ? 3 : (pid == 11 ? 4 : (pid == -11 ? 5 : 6));
+  const float lnE = __logf(E);
+  float ns = nsig32(v, a, E, lnE) + nsig32(v, b, E, lnE);
+  if (pid == -11) ns += nsig32(v, 2, E, lnE);
   return ns > 0.f ? (float)kCmToM / ns : 1.0e12f;
 }
 
-// Process choice in float32 (shower.py:665-698)
+// Process choice in float32 (shower.py:665-698): electron {Brem, Moller},
+// positron {Brem, Ann, Bhabha}, photon {PairProd, Comp}, muon {MuonE,
+// MuonBrem}, with slots and process codes chosen by selects on the PID.
 template <bool SH>
-__device__ __forceinline__ int choose32(const Tabs& T, const Ns32<SH>& v, int pid, float E, float u) {
-  float c0, c1, c2 = 0.f;
-  int n0, n1, n2 = -1;
-  if (pid == 11) { n0 = PT_BREM; n1 = PT_MOLLER; c0 = nsig32(T, v, 0, E); c1 = nsig32(T, v, 4, E); }
-  else if (pid == -11) {
-    n0 = PT_BREM; n1 = PT_ANN; n2 = PT_BHABHA;
-    c0 = nsig32(T, v, 0, E); c1 = nsig32(T, v, 2, E); c2 = nsig32(T, v, 5, E);
-  }
-  else if (pid == 22) { n0 = PT_PAIRPROD; n1 = PT_COMP; c0 = nsig32(T, v, 1, E); c1 = nsig32(T, v, 3, E); }
-  else { n0 = PT_MUONE; n1 = PT_MUONBREM; c0 = nsig32(T, v, 6, E); c1 = nsig32(T, v, 7, E); }
+__device__ __forceinline__ int choose32(const Ns32<SH>& v, int pid, float E, float u) {
+  const bool g = pid == 22, em = pid == 11, ep = pid == -11;
+  const int s0 = g ? 1 : (em || ep ? 0 : 6);
+  const int s1 = g ? 3 : (em ? 4 : (ep ? 2 : 7));
+  const int n0 = g ? PT_PAIRPROD : (em || ep ? PT_BREM : PT_MUONE);
+  const int n1 = g ? PT_COMP : (em ? PT_MOLLER : (ep ? PT_ANN : PT_MUONBREM));
+  const float lnE = __logf(E);
+  const float c0 = nsig32(v, s0, E, lnE), c1 = nsig32(v, s1, E, lnE);
+  const float c2 = ep ? nsig32(v, 5, E, lnE) : 0.f;
   const float sum = c0 + c1 + c2;
   if (!(sum > 0.f)) return -1;
   const float t = u * sum;
   if (c0 > t) return n0;
-  if (c0 + c1 > t || n2 < 0) return n1;
-  return n2;
+  if (c0 + c1 > t || !ep) return n1;
+  return PT_BHABHA;
 }
 
 // LU_Key (shower.py:416-426) in float32: argmin |E_i - E| + 1, clipped.
@@ -323,7 +379,7 @@ __device__ __forceinline__ int lu_key32(const Tabs& T, int process, float E) {
   if (!(E > __ldg(Ei))) best = 0;
   else if (E >= __ldg(Ei + n - 1)) best = n - 1;
   else {
-    const int j = geo_index<false>(Ei, n, T.t.map_lnE0[process], T.t.map_invdlog[process], E);  // Ei[j] <= E < Ei[j+1]
+    const int j = geo_index<false>(Ei, n, T.t.map_lnE0[process], T.t.map_invdlog[process], __logf(E), E);  // Ei[j] <= E < Ei[j+1]
     best = (E - __ldg(Ei + j) <= __ldg(Ei + j + 1) - E) ? j : j + 1;
   }
   const int key = best + 1;
@@ -359,55 +415,84 @@ __device__ int choose_process_b(const Tabs& T, int pid, double E, Rng& rng) {
   return names[idx];
 }
 
-// Publishes this iteration's sampling tasks: lanes with `emit` append ring
-// index `i` to the warp's buffer for `process`; full buffers go to the global
-// per-process lists 32 at a time.  `cnt` (shared, per warp) is written by
-// lane 0 only.  All 32 lanes call it.
+// Places this iteration's sampling tasks: returns, for each lane with
+// `emit`, the record slot of its task of `process` in the warp's open chunk
+// of that process (-1 for the other lanes); the caller writes the record.
+// A warp holds one open chunk per process (`open[p]`: chunk id, or -1, and
+// its fill; shared, written by lane 0 only), claims a new chunk from the
+// wave's counter when the open one cannot take the group, and publishes a
+// chunk to its process's list once it is full.  A claim beyond chunk_cap
+// (the wave's bound, which the host's sizing keeps) records PT_OOM and those
+// tasks get no slot.  All 32 lanes call it.
 template <class Ctx>
-__device__ __forceinline__ void publish_tasks(const Ctx& c, int32_t (*buf)[kBuf], volatile int* cnt, bool emit,
-                                              int process, int32_t i) {
+__device__ __forceinline__ long long park_slot(const Ctx& c, volatile int (*open)[2], bool emit, int process) {
   unsigned left = __ballot_sync(kFull, emit);
   const int lane = threadIdx.x & 31;
+  long long slot = -1;
   while (left) {
     const int leader = __ffs(left) - 1;
     const int p = __shfl_sync(kFull, process, leader);
     const unsigned m = __ballot_sync(kFull, emit && process == p);
-    const int cp = cnt[p];
-    if (emit && process == p) buf[p][cp + __popc(m & lanemask_lt())] = i;
-    int now = cp + __popc(m);
+    const int cnt = __popc(m);
+    const int id = open[p][0], f = open[p][1];
+    const int avail = id < 0 ? 0 : kChunkTasks - f;
+    long long id2 = -1;
+    if (cnt > avail) {
+      unsigned long long b = 0;
+      if (lane == 0) b = atomicAdd(c.ctr + 3, 1ull);
+      id2 = (long long)__shfl_sync(kFull, b, 0);
+      if (id2 >= c.chunk_cap) {
+        if (lane == 0) atomicCAS(c.status, 0, PT_OOM);
+        id2 = -1;
+      }
+    }
+    if (emit && process == p) {
+      const int r = __popc(m & lanemask_lt());
+      if (r < avail) slot = (long long)id * kChunkTasks + f + r;
+      else if (id2 >= 0) slot = id2 * kChunkTasks + (r - avail);
+    }
+    // the chunks this group filled go to the process's list
+    int nid = id, nf = f + cnt;
+    if (cnt >= avail) {
+      if (lane == 0 && avail > 0) {
+        const unsigned long long q = atomicAdd(c.ctr + 8 + p, 1ull);
+        c.chunks[(int64_t)p * c.chunk_cap + (int64_t)q] = (int32_t)(((unsigned)id << 5) | (kChunkTasks - 1));
+      }
+      nid = (int)id2;
+      nf = cnt - avail;
+      if (nid >= 0 && nf == kChunkTasks) {
+        if (lane == 0) {
+          const unsigned long long q = atomicAdd(c.ctr + 8 + p, 1ull);
+          c.chunks[(int64_t)p * c.chunk_cap + (int64_t)q] = (int32_t)(((unsigned)nid << 5) | (kChunkTasks - 1));
+        }
+        nid = -1;
+      }
+      if (nid < 0) nf = 0;
+    }
     left &= ~m;
     __syncwarp();
-    if (now >= 32) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(c.ctr + 8 + p, 32ull);
-      base = __shfl_sync(kFull, base, 0);
-      c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
-      __syncwarp();
-      const int rest = now - 32;
-      const int32_t carry = lane < rest ? buf[p][32 + lane] : 0;
-      __syncwarp();
-      if (lane < rest) buf[p][lane] = carry;
-      now = rest;
-    }
-    if (lane == 0) cnt[p] = now;
+    if (lane == 0) { open[p][0] = nid; open[p][1] = nf; }
     __syncwarp();
   }
+  return slot;
 }
 
+// Publishes the warp's partly filled chunks and closes them.  All lanes call.
 template <class Ctx>
-__device__ __forceinline__ void publish_rest(const Ctx& c, int32_t (*buf)[kBuf], volatile int* cnt) {
-  const int lane = threadIdx.x & 31;
-  for (int p = 0; p < 8; ++p) {
-    const int cp = cnt[p];
-    if (!cp) continue;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(c.ctr + 8 + p, (unsigned long long)cp);
-    base = __shfl_sync(kFull, base, 0);
-    if (lane < cp) c.idx[(int64_t)p * c.list_cap + (int64_t)base + lane] = buf[p][lane];
-    __syncwarp();
-    if (lane == 0) cnt[p] = 0;
-    __syncwarp();
+__device__ __forceinline__ void park_rest(const Ctx& c, volatile int (*open)[2]) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    for (int p = 0; p < 8; ++p) {
+      const int id = open[p][0], f = open[p][1];
+      if (id >= 0 && f > 0) {
+        const unsigned long long q = atomicAdd(c.ctr + 8 + p, 1ull);
+        c.chunks[(int64_t)p * c.chunk_cap + (int64_t)q] = (int32_t)(((unsigned)id << 5) | (unsigned)(f - 1));
+      }
+      open[p][0] = -1;
+      open[p][1] = 0;
+    }
   }
+  __syncwarp();
 }
 
 // ------------------------------------------------------ per-wave rows
@@ -434,22 +519,21 @@ __device__ __forceinline__ void row_end(const pt_particles& r, int64_t s, double
 // Same device functions and operation order as the record engine (pt_run_sm).
 struct PropShared64 {
   unsigned int hist[kHist];
-  int32_t buf[kWarps][8][kBuf];
-  int bcnt[kWarps][8];
+  int open[kWarps][8][2];         // each warp's open task chunk per process: id, fill
 };
 
 template <int BETHE>
 __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropShared64& sm) {
   unsigned int* sh_hist = sm.hist;
-  int32_t (*sh_buf)[8][kBuf] = sm.buf;
-  int (*sh_bcnt)[8] = sm.bcnt;
   const int64_t wave_n = w_n(c);
   const uint64_t wave_head = w_head(c);
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
-  if (threadIdx.x < kWarps * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
+  if (threadIdx.x < kWarps * 8) {
+    sm.open[threadIdx.x / 8][threadIdx.x % 8][0] = -1;
+    sm.open[threadIdx.x / 8][threadIdx.x % 8][1] = 0;
+  }
   __syncthreads();
-  int32_t (*buf)[kBuf] = sh_buf[threadIdx.x / 32];
-  volatile int* bcnt = sh_bcnt[threadIdx.x / 32];
+  volatile int (*open)[2] = sm.open[threadIdx.x / 32];
   const Tabs& T = c.T;
   LocalTally L;
   WarpPool pool;
@@ -547,6 +631,7 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
     int process = -1;
     bool emit = false;
     double edep = 0.0;
+    int row = 0;
     if (finish) {
       const int sp = species_of(pid);
       if (c.rows.capacity) row_end(c.rows, (int64_t)((i - wave_head) & c.mask), E, px, py, pz, x, y, z);
@@ -556,11 +641,7 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
       process = choose_process_b(T, pid, E, rng);
       emit = process >= 0 && E > pme;
       if (emit) {
-        // park the post-propagation state in place for the sampler
-        c.q.E[i] = E; c.q.px[i] = px; c.q.py[i] = py; c.q.pz[i] = pz;
-        c.q.x[i] = x; c.q.y[i] = y; c.q.z[i] = z;
-        c.q.draw[i] = (uint32_t)rng.n;
-        c.q.row[i] = T.t.map_base[process] + lu_key(T, process, E);
+        row = T.t.map_base[process] + lu_key(T, process, E);
         edep = eloss;
       } else {
         ++L.ended;
@@ -570,10 +651,15 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
     }
     if (__any_sync(kFull, finish)) {
       primary_tally(c.tally, finish, prim, edep);
-      publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
+      const long long slot = park_slot(c, open, emit, process);
+      if (slot >= 0) {                 // the post-propagation state, parked for the sampler
+        Park<0>& r = c.park[slot];
+        r.E = E; r.key = c.q.key[i]; r.row = row; r.draw = (uint32_t)rng.n; r.pid = pid; r.gen = c.q.gen[i];
+        r.px = px; r.py = py; r.pz = pz; r.x = x; r.y = y; r.z = z; r.mass = mass; r.prim = prim; r.pad = 0;
+      }
     }
   }
-  publish_rest(c, buf, bcnt);
+  park_rest(c, open);
   flush_tally(c.tally, L, sh_hist);
 }
 
@@ -587,51 +673,67 @@ __global__ void __launch_bounds__(kThreads) k_propagate_fp64(WaveCtx<0> c) {
 // A particle whose propagation ended, waiting for the process choice and its
 // sampling task.  Finished particles are queued per warp and handled 32 at a
 // time so this per-particle work runs with every lane busy.
+// The float64 energy after propagation, E0 - loss clamped at the mass, is
+// formed in run_finish, where every lane of the warp takes part: a float64
+// instruction costs the narrow float64 pipe the same cycles whether one lane
+// or thirty-two execute it.
 struct FinEntry {
   uint32_t i, draw;
   int32_t pid, prim;
-  double E, E0;
+  double E0;
+  uint64_t key;
+  float loss;                               // continuous loss along the track (float32 sum)
   float px, py, pz, x, y, z, u, pme, th0;   // th0: polar angle of p0 (creation histogram)
+  float mass;
+  int32_t gen;
 };
 
 template <bool SH>
-__device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq, int count, int32_t (*buf)[kBuf],
-                           volatile int* bcnt, LocalTally& L, unsigned int* sh_hist) {
+__device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq, int count, volatile int (*open)[2],
+                           LocalTally& L, unsigned int* sh_hist) {
   const int lane = threadIdx.x & 31;
   const bool on = lane < count;
   int process = -1, prim = 0;
   bool emit = false;
-  double edep = 0.0;
+  double edep = 0.0, Eout = 0.0;
   uint32_t i = 0;
+  int row = 0;
   if (on) {
     const FinEntry& e = fq[lane];
     i = e.i;
     prim = e.prim;
+    const bool moved = e.loss != 0.f;
+    double E = moved ? e.E0 - (double)e.loss : e.E0;    // float64 energy bookkeeping
+    if (moved && E <= (double)e.mass) E = (double)e.mass;
     const int sp = species_of(e.pid);
     atomicAdd(&sh_hist[(0 * 4 + sp) * kHB + bin_of(log10f((float)e.E0), -2.f, 2.f)], 1u);
     atomicAdd(&sh_hist[(1 * 4 + sp) * kHB + bin_of(e.th0 > 0.f ? log10f(e.th0) : -6.f, -6.f, 0.5f)], 1u);
     atomicAdd(&sh_hist[(2 * 4 + sp) * kHB + bin_of(e.z, 0.f, c.tally.z_max)], 1u);
-    const double eloss = e.E0 - e.E;
+    const double eloss = e.E0 - E;
     L.e_cont += eloss;
     if (c.rows.capacity)
-      row_end(c.rows, (int64_t)((i - w_head(c)) & c.mask), e.E, e.px, e.py, e.pz, e.x, e.y, e.z);
-    const float Ef = (float)e.E;
-    process = choose32(c.T, ns, e.pid, Ef, e.u);         // shower.py:665-698
+      row_end(c.rows, (int64_t)((i - w_head(c)) & c.mask), E, e.px, e.py, e.pz, e.x, e.y, e.z);
+    const float Ef = (float)E;
+    process = choose32(ns, e.pid, Ef, e.u);             // shower.py:665-698
     emit = process >= 0 && Ef > e.pme;
-    if (emit) {                                          // park the state for the sampler
-      c.q.E[i] = e.E; c.q.px[i] = e.px; c.q.py[i] = e.py; c.q.pz[i] = e.pz;
-      c.q.x[i] = e.x; c.q.y[i] = e.y; c.q.z[i] = e.z;
-      c.q.draw[i] = e.draw;
-      c.q.row[i] = c.T.t.map_base[process] + lu_key32(c.T, process, Ef);
+    if (emit) {
+      row = c.T.t.map_base[process] + lu_key32(c.T, process, Ef);
       edep = eloss;
     } else {
       ++L.ended;
-      L.e_ended += e.E;
-      edep = eloss + e.E;
+      L.e_ended += E;
+      edep = eloss + E;
     }
+    Eout = E;
   }
   primary_tally(c.tally, on, prim, edep);
-  publish_tasks(c, buf, bcnt, emit, process, (int32_t)i);
+  const long long slot = park_slot(c, open, emit, process);
+  if (slot >= 0) {                                       // the state parked for the sampler
+    const FinEntry& e = fq[lane];
+    Park<1>& r = c.park[slot];
+    r.E = Eout; r.key = e.key; r.row = row; r.draw = e.draw; r.pid = e.pid; r.gen = e.gen;
+    r.px = e.px; r.py = e.py; r.pz = e.pz; r.x = e.x; r.y = e.y; r.z = e.z; r.mass = e.mass; r.prim = e.prim;
+  }
 }
 
 // BETHE: Shower(fast_MCS_mode=False); a separate instantiation keeps the
@@ -639,29 +741,31 @@ __device__ void run_finish(const WaveCtx<1>& c, const Ns32<SH>& ns, FinEntry* fq
 // NW: warps per block (the block size is a tuning choice of the float32 kernels).
 template <int NW> struct PropSharedMixedT {
   unsigned int hist[kHist];
-  int32_t buf[NW][8][kBuf];
-  int bcnt[NW][8];
+  int open[NW][8][2];             // each warp's open task chunk per process: id, fill
   FinEntry fin[NW][64];
+  NsHdr hdr[PT_N_NSIGMA];
 };
 using PropSharedMixed = PropSharedMixedT<kWarps>;
 
 template <int BETHE, bool SH, int NW>
-__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixedT<NW>& sm, const Ns32<SH> ns) {
+__device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSharedMixedT<NW>& sm, Ns32<SH> ns) {
   unsigned int* sh_hist = sm.hist;
-  int32_t (*sh_buf)[8][kBuf] = sm.buf;
-  int (*sh_bcnt)[8] = sm.bcnt;
   FinEntry (*sh_fin)[64] = sm.fin;
   const int64_t wave_n = w_n(c);
   const uint64_t wave_head = w_head(c);
-  for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
-  if (threadIdx.x < NW * 8) (&sh_bcnt[0][0])[threadIdx.x] = 0;
-  __syncthreads();
-  const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
-  int32_t (*buf)[kBuf] = sh_buf[w];
-  FinEntry* fq = sh_fin[w];
-  volatile int* bcnt = sh_bcnt[w];
-  int fcount = 0;                                        // warp-uniform
   const Tabs& T = c.T;
+  for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
+  if (threadIdx.x < NW * 8) {
+    sm.open[threadIdx.x / 8][threadIdx.x % 8][0] = -1;
+    sm.open[threadIdx.x / 8][threadIdx.x % 8][1] = 0;
+  }
+  fill_ns_hdr(T, sm.hdr);
+  __syncthreads();
+  ns.h = sm.hdr;
+  const int w = threadIdx.x / 32, lane = threadIdx.x & 31;
+  FinEntry* fq = sh_fin[w];
+  volatile int (*open)[2] = sm.open[w];
+  int fcount = 0;                                        // warp-uniform
   const float mc0 = (float)T.t.min_calc_photon, mc1 = (float)T.t.min_calc_electron,
               mc2 = (float)T.t.min_calc_positron, mc3 = (float)T.t.min_calc_muon;
   const float minE = (float)c.min_energy;
@@ -707,7 +811,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       mf = c.q.mass[i];
       prim = c.q.prim[i];
       rng.init(c.seed, c.q.key[i]);
-      E0f = (float)E0;
+      E0f = c.q.E32[i];
       Ef = E0f;
       const int sp = species_of(pid);
       const float mcs = sp == 0 ? mc0 : (sp == 1 ? mc1 : (sp == 2 ? mc2 : mc3));
@@ -742,13 +846,13 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       rng.peek(dr, c.rk);
       int base = 1;                                       // first multiple-scattering draw
       if (!charged) {
-        step = -mfp32(T, ns, pid, Ef) * log1pf(-dr.u[0]); // mfp log(1/(1-u))
+        step = -mfp32(ns, pid, Ef) * log1pf(-dr.u[0]); // mfp log(1/(1-u))
       } else if (!(Ef >= pmef)) {
         step = dr.u[0] * dzf;                             // shower.py:584-585
         mlep = me;                                        // shower.py:596-598: electron mass
       } else {
         ++L.substeps;
-        const float mfp = mfp32(T, ns, pid, Ef);
+        const float mfp = mfp32(ns, pid, Ef);
         const float u_hard = dr.u[0];
         const float q = fmaf(14.f, dr.u[1], 6.f);         // delta_z = mfp / U(6, 20)
         dzf = mfp / q;
@@ -802,10 +906,10 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
         e.i = i;
         e.pid = pid;
         e.prim = prim;
-        const bool moved = lossf != 0.f;
-        double E = moved ? E0 - (double)lossf : E0;      // float64 energy bookkeeping
-        if (moved && E <= (double)mf) E = (double)mf;
-        e.E = E;
+        e.gen = c.q.gen[i];
+        e.key = (uint64_t)rng.k0 | ((uint64_t)rng.k1 << 32);
+        e.mass = mf;
+        e.loss = lossf;
         e.E0 = E0;
         e.px = pmag * dir.x; e.py = pmag * dir.y; e.pz = pmag * dir.z;
         e.x = pos.x + disp.x; e.y = pos.y + disp.y; e.z = pos.z + disp.z;
@@ -819,7 +923,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       fcount += __popc(fm);
       __syncwarp();
       if (fcount >= 32) {
-        run_finish(c, ns, fq, 32, buf, bcnt, L, sh_hist);
+        run_finish(c, ns, fq, 32, open, L, sh_hist);
         __syncwarp();
         const int rest = fcount - 32;
         FinEntry carry;
@@ -831,8 +935,8 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       }
     }
   }
-  if (fcount > 0) run_finish(c, ns, fq, fcount, buf, bcnt, L, sh_hist);
-  publish_rest(c, buf, bcnt);
+  if (fcount > 0) run_finish(c, ns, fq, fcount, open, L, sh_hist);
+  park_rest(c, open);
   flush_tally(c.tally, L, sh_hist);
 }
 
@@ -874,8 +978,10 @@ __device__ bool stage_ns_tables(const WaveCtx<1>& c, float* sh, int total, int p
   __syncthreads();                                       // the barrier is initialised before any wait
   const bool landed = __syncthreads_and(mbar_wait(b, 0, kStageNs));
   if (!landed) {
+    // process -2: a copy may still be in flight into this block's shared
+    // memory, so the host treats the handle's later results as suspect
     if (threadIdx.x == 0) {
-      atomicCAS(c.status, 0, PT_TIMEOUT);
+      raise_status(c.status, c.err_info, PT_TIMEOUT, -2, 0.0, 0);
       mbar_wait(b, 0, kStageNs);
     }
     __syncthreads();
@@ -893,7 +999,7 @@ __global__ void __launch_bounds__(NW * 32, min_blocks32<NW>()) k_propagate_mixed
     extern __shared__ __align__(16) float ns_sh[];
     const int total = ns_total(c.T), pad = (total + 3) & ~3;
     if (!stage_ns_tables(c, ns_sh, total, pad)) return;
-    propagate_mixed_body<BETHE, true>(c, sm, Ns32<true>{ns_sh, ns_sh + pad, ns_sh + 2 * pad});
+    propagate_mixed_body<BETHE, true>(c, sm, Ns32<true>{ns_sh, ns_sh + pad, ns_sh + 2 * pad, nullptr});
   } else {
     propagate_mixed_body<BETHE, false>(c, sm, ns_global(c.T));
   }
@@ -1029,11 +1135,12 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
     const KinEntry<PREC>& e = kq[lane];
     i = e.i;
     const int process = e.process;
-    const double E = c.q.E[i];
-    const int pid = c.q.pid[i];
+    const Park<PREC>& P = c.park[i];                     // the parent's task record
+    const double E = P.E;
+    const int pid = P.pid;
     if constexpr (PREC == 0) {
-      const double mass = c.q.mass[i];
-      const double pf[4] = {E, c.q.px[i], c.q.py[i], c.q.pz[i]};
+      const double mass = P.mass;
+      const double pf[4] = {E, P.px, P.py, P.pz};
       const double* xd = reinterpret_cast<const KinEntry<0>&>(e).x;
       const double ph = reinterpret_cast<const KinEntry<0>&>(e).ph;
       const Rot R = rotation_from(pf);
@@ -1053,8 +1160,8 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
     } else {
       const KinEntry<1>& f = reinterpret_cast<const KinEntry<1>&>(e);
       KinOut k;
-      kin_mixed(process, pid, E, c.q.mass[i], f.x, f.ph, k);
-      const float fx = c.q.px[i], fy = c.q.py[i], fz = c.q.pz[i];
+      kin_mixed(process, pid, E, P.mass, f.x, f.ph, k);
+      const float fx = P.px, fy = P.py, fz = P.pz;
       const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
       const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
       const Rot32 Rm = rot32_from(pd);
@@ -1066,10 +1173,10 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
     want = (dg[0].E > c.min_energy) + (dg[1].E > c.min_energy);
     for (int j = 0; j < 2; ++j)
       if (!(dg[j].E > c.min_energy)) { ++L.below; L.e_below += dg[j].E; below += dg[j].E; }
-    prim = c.q.prim[i];
-    key = c.q.key[i];
-    gen = c.q.gen[i];
-    x0 = c.q.x[i]; y0 = c.q.y[i]; z0 = c.q.z[i];
+    prim = P.prim;
+    key = P.key;
+    gen = P.gen;
+    x0 = P.x; y0 = P.y; z0 = P.z;
     if (below != 0.0) atomicAdd(c.tally.prim_edep + prim, below);
   }
   uint64_t slots[2] = {0, 0};
@@ -1080,6 +1187,7 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
     const uint64_t q = (w_tail(c) + slots[slot++]) & c.mask;
     ++L.pushed;
     c.q.E[q] = dg[j].E; c.q.px[q] = dg[j].px; c.q.py[q] = dg[j].py; c.q.pz[q] = dg[j].pz;
+    if (PREC == 1) c.q.E32[q] = (float)dg[j].E;
     c.q.x[q] = x0; c.q.y[q] = y0; c.q.z[q] = z0;
     c.q.mass[q] = (R)table_mass(dg[j].pid);
     c.q.key[q] = daughter_key(key, j);
@@ -1099,8 +1207,8 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
   unsigned long long* sh_off = sm.off;
   KinEntry<PREC> (*sh_kq)[kKinQ] = sm.kq;
   if (threadIdx.x == 0) {
-    unsigned long long acc = 0;
-    for (int p = 0; p < 8; ++p) { sh_off[p] = acc; acc += __ldcg(c.ctr + 8 + p); }
+    unsigned long long acc = 0;            // task index space: 32 per published chunk, process by process
+    for (int p = 0; p < 8; ++p) { sh_off[p] = acc; acc += (unsigned long long)kChunkTasks * __ldcg(c.ctr + 8 + p); }
     sh_off[8] = acc;
   }
   __syncthreads();
@@ -1130,14 +1238,19 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
     const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
     const bool fresh = need && t >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
+    int32_t chunk_ent = 0;
     if (fresh) {
       process = 0;
       while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
-      i = (uint64_t)c.idx[(int64_t)process * c.list_cap + (t - (int64_t)sh_off[process])];
-      E = c.q.E[i];
-      row = c.q.row[i];
-      rng.init(c.seed, c.q.key[i]);
-      rng.n = c.q.draw[i];
+      chunk_ent = c.chunks[(int64_t)process * c.chunk_cap + ((t - (int64_t)sh_off[process]) >> 5)];
+    }
+    // a slot past a partly filled chunk's tasks holds no task: the lane asks again
+    if (fresh && (int)(t & 31) <= (chunk_ent & 31)) {
+      i = ((uint64_t)((uint32_t)chunk_ent >> 5) << 5) + (uint64_t)(t & 31);
+      E = c.park[i].E;
+      row = c.park[i].row;
+      rng.init(c.seed, c.park[i].key);
+      rng.n = c.park[i].draw;
       if (rng.n & 1ull) {   // resume inside a Philox block: regenerate its second half
         const uint64_t blk = rng.n >> 1;
         const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), rng.k0, rng.k1), rng.s0, rng.s1);
@@ -1269,6 +1382,7 @@ __global__ void k_feed(RingT<PREC> q, uint64_t mask, uint64_t tail, const double
   const int64_t g = first + j;
   const uint64_t i = (tail + (uint64_t)j) & mask;
   q.E[i] = p0[0 * n_total + g]; q.px[i] = p0[1 * n_total + g]; q.py[i] = p0[2 * n_total + g];
+  if (PREC == 1) q.E32[i] = (float)p0[0 * n_total + g];
   q.pz[i] = p0[3 * n_total + g];
   q.x[i] = r0[0 * n_total + g]; q.y[i] = r0[1 * n_total + g]; q.z[i] = r0[2 * n_total + g];
   q.mass[i] = mass[g]; q.pid[i] = pid[g]; q.prim[i] = (int32_t)g; q.gen[i] = 0;
@@ -1290,8 +1404,8 @@ __device__ void plan_step(const WaveCtx<PREC>& c) {
   P.feed_m = 0;
   for (int k = 0; k < 16; ++k) c.ctr[k] = 0;
   if (*(volatile int*)c.status != 0) { P.done = 1; return; }
-  if (P.waves >= kMaxPlannedWaves) {              // a bound on the loop, far above any run's need
-    raise_status(c.status, nullptr, PT_TIMEOUT, 0, 0.0, 0);
+  if (P.waves >= c.max_waves) {                   // a bound on the loop, far above any run's need
+    raise_status(c.status, c.err_info, PT_TIMEOUT, -1, 0.0, 0);
     P.done = 1;
     return;
   }
@@ -1339,6 +1453,7 @@ __device__ __forceinline__ void feed_planned(const WaveCtx<PREC>& c, int64_t j, 
     const int64_t g = first + j;
     const uint64_t i = (at + (uint64_t)j) & c.mask;
     c.q.E[i] = c.in_p0[0 * n + g]; c.q.px[i] = c.in_p0[1 * n + g]; c.q.py[i] = c.in_p0[2 * n + g];
+    if (PREC == 1) c.q.E32[i] = (float)c.in_p0[0 * n + g];
     c.q.pz[i] = c.in_p0[3 * n + g];
     c.q.x[i] = c.in_r0[0 * n + g]; c.q.y[i] = c.in_r0[1 * n + g]; c.q.z[i] = c.in_r0[2 * n + g];
     c.q.mass[i] = c.in_mass[g]; c.q.pid[i] = c.in_pid[g]; c.q.prim[i] = (int32_t)g; c.q.gen[i] = 0;
@@ -1364,10 +1479,11 @@ __global__ void k_feed_planned(WaveCtx<PREC> c) {
 
 // Grid-wide barrier of the persistent kernel, whose blocks the cooperative
 // launch makes co-resident: arrivals in bar[0], the generation in bar[1].
-// Bounded: a block that waits longer than kBarrierNs records PT_TIMEOUT and
-// returns false, and every block then leaves the kernel within the same bound.
+// Bounded: a block that waits longer than bound_ns (kBarrierNs unless
+// pt_batch_tuning.barrier_ns sets it) records PT_TIMEOUT and returns false,
+// and every block then leaves the kernel within the same bound.
 constexpr unsigned long long kBarrierNs = 20ull * 1000ull * 1000ull * 1000ull;
-__device__ bool grid_barrier(unsigned int* bar, int* status) {
+__device__ bool grid_barrier(unsigned int* bar, int* status, double* err_info, unsigned long long bound_ns) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1382,12 +1498,12 @@ __device__ bool grid_barrier(unsigned int* bar, int* status) {
     } else {
       const unsigned long long t0 = global_ns();
       while (*gen == g) {
-        if (global_ns() - t0 > kBarrierNs) { good = 0; break; }
+        if (global_ns() - t0 > bound_ns) { good = 0; break; }
         __nanosleep(200);
       }
     }
     __threadfence();
-    if (!good) atomicCAS(status, 0, PT_TIMEOUT);
+    if (!good) raise_status(status, err_info, PT_TIMEOUT, -1, 0.0, 0);
     ok = good;
   }
   __syncthreads();
@@ -1410,15 +1526,15 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_persistent(Wave
   __shared__ Shared sm;
   for (;;) {
     if (blockIdx.x == 0 && threadIdx.x == 0) plan_step(c);
-    if (!grid_barrier(bar, c.status)) break;
+    if (!grid_barrier(bar, c.status, c.err_info, c.barrier_ns)) break;
     if (__ldcg(&c.plan->done)) break;
     feed_planned(c, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
-    if (!grid_barrier(bar, c.status)) break;
+    if (!grid_barrier(bar, c.status, c.err_info, c.barrier_ns)) break;
     if constexpr (PREC == 1) propagate_mixed_body<BETHE, false>(c, sm.p, ns_global(c.T));
     else propagate_fp64_body<BETHE>(c, sm.p);
-    if (!grid_barrier(bar, c.status)) break;
+    if (!grid_barrier(bar, c.status, c.err_info, c.barrier_ns)) break;
     sample_body<PREC, kWarps>(c, sm.s);
-    if (!grid_barrier(bar, c.status)) break;
+    if (!grid_barrier(bar, c.status, c.err_info, c.barrier_ns)) break;
   }
 }
 
@@ -1427,9 +1543,11 @@ __global__ void __launch_bounds__(kThreads, PREC == 1 ? 5 : 1) k_persistent(Wave
 // ------------------------------------------------------------- host side
 struct BatchScratch {
   int64_t cap = 0;          // ring capacity (power of two)
-  int64_t list_cap = 0;     // entries per process list (= max wave size)
+  int64_t list_cap = 0;     // largest wave (entries)
+  int64_t chunk_cap = 0;    // task chunks per wave
   void* mem = nullptr;
-  int32_t* idx = nullptr;
+  void* park = nullptr;     // chunk_cap * 32 task records (sized for the float64 record)
+  int32_t* chunks = nullptr;
   unsigned long long* ctr = nullptr;
   unsigned long long* h_ctr = nullptr;
   int* h_status = nullptr;
@@ -1449,7 +1567,20 @@ struct BatchScratch {
     }                                                                                 \
   } while (0)
 
-static size_t ring_bytes(int64_t cap) { return (size_t)cap * (9 * 8 + 5 * 4) + 16 * 256; }
+static size_t ring_bytes(int64_t cap) { return (size_t)cap * (9 * 8 + 4 * 4) + 16 * 256; }
+
+// Task chunks a wave can claim: one per 32 tasks of full chunks (a wave of
+// k entries has at most k tasks), plus the partly filled chunk of each
+// process that every propagation warp may end with.
+static int64_t chunk_capacity(int64_t list_cap) {
+  int dev = 0, sms = 0, threads = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  if (sms < 1) sms = 1;
+  const int warps = threads > 0 ? threads / 32 : 64;
+  return (list_cap + kChunkTasks - 1) / kChunkTasks + 8 * (int64_t)sms * warps + 8;
+}
 
 pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
   int64_t c2 = 1 << 10;
@@ -1461,8 +1592,10 @@ pt_status batch_scratch_alloc(BatchScratch** out, int64_t cap) {
   s = new BatchScratch();
   s->cap = c2;
   s->list_cap = c2 / 2;
+  s->chunk_cap = chunk_capacity(s->list_cap);
   if (cudaMalloc(&s->mem, ring_bytes(c2)) != cudaSuccess ||
-      cudaMalloc(&s->idx, (size_t)8 * s->list_cap * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&s->park, (size_t)s->chunk_cap * kChunkTasks * sizeof(Park<0>)) != cudaSuccess ||
+      cudaMalloc(&s->chunks, (size_t)8 * s->chunk_cap * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&s->ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&s->plan, sizeof(WavePlan)) != cudaSuccess || cudaMalloc(&s->bar, 2 * sizeof(unsigned int)) != cudaSuccess ||
       cudaMallocHost(&s->h_ctr, 16 * sizeof(unsigned long long)) != cudaSuccess ||
@@ -1525,19 +1658,20 @@ static RingT<PREC> carve_ring(BatchScratch* s) {
   auto take = [&](size_t b) { char* r = p; p += (b + 255) & ~size_t(255); return r; };
   RingT<PREC> q;
   q.E = (double*)take(c2 * 8);
+  q.E32 = (float*)take(c2 * 4);
   q.px = (R*)take(c2 * sizeof(R)); q.py = (R*)take(c2 * sizeof(R)); q.pz = (R*)take(c2 * sizeof(R));
   q.x = (R*)take(c2 * sizeof(R)); q.y = (R*)take(c2 * sizeof(R)); q.z = (R*)take(c2 * sizeof(R));
   q.mass = (R*)take(c2 * sizeof(R));
   q.key = (uint64_t*)take(c2 * 8);
   q.pid = (int32_t*)take(c2 * 4); q.prim = (int32_t*)take(c2 * 4); q.gen = (int32_t*)take(c2 * 4);
-  q.row = (int32_t*)take(c2 * 4); q.draw = (uint32_t*)take(c2 * 4);
   return q;
 }
 
 void batch_scratch_free(BatchScratch* s) {
   if (!s) return;
   cudaFree(s->mem);
-  cudaFree(s->idx);
+  cudaFree(s->park);
+  cudaFree(s->chunks);
   cudaFree(s->ctr);
   cudaFree(s->plan);
   cudaFree(s->bar);
@@ -1718,7 +1852,9 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.q = carve_ring<PREC>(S);
   c.mask = (uint64_t)S->cap - 1;
   c.list_cap = S->list_cap;
-  c.idx = S->idx;
+  c.park = reinterpret_cast<Park<PREC>*>(S->park);
+  c.chunks = S->chunks;
+  c.chunk_cap = S->chunk_cap;
   c.ctr = S->ctr;
   c.status = hp.status;
   c.err_info = hp.err_info;
@@ -1726,6 +1862,8 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
              (float)(tally->z_max > 0 ? tally->z_max : 1.0)};
   c.rk = philox_round_keys(o->seed);
   const int32_t* tu = hp.tuning;      // 0 = default
+  c.max_waves = o->loop_limit > 0 ? o->loop_limit : kMaxPlannedWaves;
+  c.barrier_ns = tu[7] > 0 ? (unsigned long long)tu[7] : kBarrierNs;
   c.refill_min[0] = tu[0] ? tu[0] : kRefillMinPropagate;
   c.refill_min[1] = tu[1] ? tu[1] : kRefillMinSample;
   c.chunk[0] = tu[2] ? tu[2] : kChunkPropagate;
@@ -1792,6 +1930,11 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
     if (k <= 0) {                   // the live population filled the ring
       hp.launches[0] = nl; hp.launches[1] = nw;
       return PT_OOM;
+    }
+    if (nw >= c.max_waves) {        // a bound on the loop, far above any run's need
+      hp.launches[0] = nl; hp.launches[1] = nw;
+      hp.last_info[0] = -1; hp.last_info[1] = 0.0; hp.last_info[2] = 0;
+      return PT_TIMEOUT;
     }
     PT_CUDA(cudaMemsetAsync(S->ctr, 0, 16 * sizeof(unsigned long long), st));
     if (hook) {

@@ -5,6 +5,7 @@
 // process choice, draw_sample's accept/reject loop, final-state kinematics,
 // lab rotation and the push of daughters above min_energy.  Daughters of a
 // wave form the next wave.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,7 @@ struct RunCtx {
   unsigned long long* n_rows;
   int* status;
   double* err_info;   // [process, energy, lu_key]
+  int loop_limit;     // substep iterations per particle
 };
 
 __device__ void raise_status(int* status, double* info, int code, int process, double E, int key) {
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(128) k_transport_fp64(RunCtx c) {
       double dz = 0.0;
       int guard = 0;
       while (!hard && pf[0] >= pme) {
-        if (++guard > (1 << 22)) { raise_status(c.status, c.err_info, PT_TIMEOUT, -1, pf[0], 0); break; }
+        if (++guard > c.loop_limit) { raise_status(c.status, c.err_info, PT_TIMEOUT, -1, pf[0], 0); break; }
         const double mfp = mfp_of(T, pid, pf[0]);
         const double u_hard = rng.u();
         dz = (S(mfp) / (S(6.0) + S(14.0) * S(rng.u()))).v;
@@ -284,7 +286,7 @@ struct pt_handle {
   double last_info[3] = {0, 0, 0};
   int64_t launches[2] = {0, 0};   // kernel launches, waves of the last run
   double kernel_ms[2] = {0, 0};   // batched run: propagation and sampler device time
-  int32_t tuning[7] = {0, 0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
+  int32_t tuning[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
   BatchScratch* batch = nullptr;
 };
 
@@ -415,6 +417,7 @@ extern "C" pt_status pt_run_sm(pt_handle* h, pt_particles* P, int64_t n_primarie
   c.n_rows = h->counters + 1;
   c.status = h->status;
   c.err_info = h->err_info;
+  c.loop_limit = o->loop_limit > 0 ? o->loop_limit : (1 << 22);
   int cur = 0;
   int64_t n_in = n_primaries;
   const int tbt = 128;
@@ -466,21 +469,26 @@ constexpr int kNoAllocMaxDevices = 64;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices];
-cudaError_t g_noalloc_err[kNoAllocMaxDevices];
-std::once_flag g_noalloc_once[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
 
-// Device address of the static scratch on the current device (set up on the
-// first call per device).
+// Device address of the static scratch on the current device, looked up on
+// the first call per device.  Only a successful lookup is kept: a lookup that
+// failed (no context yet, or a call made during a stream capture) is tried
+// again on the next call.
 pt_status noalloc_scratch(unsigned char** out) {
   int dev = 0;
   PT_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices) return PT_BAD_ARG;
-  std::call_once(g_noalloc_once[dev], [dev] {
-    g_noalloc_err[dev] = cudaGetSymbolAddress((void**)&g_noalloc_ptr[dev], g_noalloc_scratch);
-  });
-  if (g_noalloc_err[dev] != cudaSuccess || !g_noalloc_ptr[dev]) {
-    fprintf(stderr, "petite_gpu: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(g_noalloc_err[dev]));
-    return PT_CUDA_ERR;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      fprintf(stderr, "petite_gpu: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+      return PT_CUDA_ERR;
+    }
+    g_noalloc_ptr[dev] = (unsigned char*)p;
   }
   *out = g_noalloc_ptr[dev];
   return PT_OK;
@@ -529,6 +537,7 @@ extern "C" pt_status pt_run_sm_noalloc(pt_handle* h, pt_particles* P, int64_t n_
   c.n_rows = counters + 1;
   c.status = status;
   c.err_info = err_info;
+  c.loop_limit = o->loop_limit > 0 ? o->loop_limit : (1 << 22);
   int cur = 0;
   int64_t n_in = n_primaries;
   const int tbt = 128;
@@ -570,7 +579,7 @@ extern "C" pt_status pt_last_run_stats(pt_handle* h, int64_t* launches, int64_t*
 extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t) {
   if (!h) return PT_BAD_ARG;
   if (!t) {
-    for (int k = 0; k < 7; ++k) h->tuning[k] = 0;
+    for (int k = 0; k < 8; ++k) h->tuning[k] = 0;
     return PT_OK;
   }
   for (int k = 0; k < 2; ++k) {
@@ -580,6 +589,7 @@ extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t)
   if (t->loop < PT_LOOP_HOST || t->loop > PT_LOOP_PERSISTENT) return PT_BAD_ARG;
   if (t->staging < PT_STAGE_DEFAULT || t->staging > PT_STAGE_SHARED) return PT_BAD_ARG;
   if (t->threads != 0 && t->threads != 64 && t->threads != 128 && t->threads != 256) return PT_BAD_ARG;
+  if (t->barrier_ns < 0) return PT_BAD_ARG;
   h->tuning[0] = t->refill_min[0];
   h->tuning[1] = t->refill_min[1];
   h->tuning[2] = t->chunk[0];
@@ -587,6 +597,7 @@ extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t)
   h->tuning[4] = t->loop;
   h->tuning[5] = t->staging;
   h->tuning[6] = t->threads;
+  h->tuning[7] = t->barrier_ns;
   return PT_OK;
 }
 
@@ -595,6 +606,70 @@ extern "C" pt_status pt_last_kernel_times(pt_handle* h, double* propagate_ms, do
   if (propagate_ms) *propagate_ms = h->kernel_ms[0];
   if (sample_ms) *sample_ms = h->kernel_ms[1];
   return PT_OK;
+}
+
+// ------------------------------------------------- arithmetic peak of the GPU
+// Eight independent fused multiply-add chains per thread (a = a*b + c, which
+// converges to c/(1-b): no overflow, no subnormals) on a grid that fills
+// every SM's threads.  2 flops per FMA.
+namespace {
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_chains(T* sink, int iters, T b, T c) {
+  T a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = (T)(threadIdx.x + 8 * k) * (T)1e-3;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == (T)-1) sink[blockIdx.x] = s;     // never true: keeps the chains live
+}
+
+template <class T>
+pt_status fma_rate(T* sink, cudaStream_t st, double* flops_per_s) {
+  int dev = 0, sms = 0, per = 0;
+  PT_CUDA(cudaGetDevice(&dev));
+  PT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fma_chains<T>, 256, 0));
+  const int grid = sms * (per > 0 ? per : 1);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  PT_CUDA(cudaEventCreate(&e0));
+  PT_CUDA(cudaEventCreate(&e1));
+  pt_status rs = PT_OK;
+  int iters = 256;
+  float ms = 0.f;
+  for (int pass = 0; pass < 8; ++pass) {         // grow the run to about 5 ms, then time it
+    k_fma_chains<T><<<grid, 256, 0, st>>>(sink, iters, (T)0.999, (T)1e-3);
+    cudaEventRecord(e0, st);
+    k_fma_chains<T><<<grid, 256, 0, st>>>(sink, iters, (T)0.999, (T)1e-3);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rs = PT_CUDA_ERR;
+      break;
+    }
+    if (ms >= 4.f || iters >= (1 << 26)) break;
+    iters = ms > 0.05f ? (int)std::min<double>(iters * 5.0 / ms, double(1 << 26)) : iters * 16;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rs != PT_OK || ms <= 0.f) return PT_CUDA_ERR;
+  *flops_per_s = 2.0 * 8.0 * (double)iters * grid * 256.0 / (ms * 1e-3);
+  return PT_OK;
+}
+}  // namespace
+
+extern "C" pt_status pt_alu_peaks(double* fp32_flops, double* fp64_flops, void* stream) {
+  if (!fp32_flops || !fp64_flops) return PT_BAD_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  double* sink = nullptr;
+  PT_CUDA(cudaMalloc(&sink, 65536 * sizeof(double)));
+  pt_status s = fma_rate<float>(reinterpret_cast<float*>(sink), st, fp32_flops);
+  if (s == PT_OK) s = fma_rate<double>(sink, st, fp64_flops);
+  cudaFree(sink);
+  return s;
 }
 
 extern "C" pt_status pt_sample_only(pt_handle* h, int32_t process, const double* energy, const uint64_t* pkey,

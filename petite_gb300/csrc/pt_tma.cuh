@@ -54,7 +54,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigne
 // share their alignment.  The aligned interior goes by one bulk copy on
 // `bar`; the head and tail (at most one double each) by plain loads.  Call
 // with every thread of the block; false (after a second bounded wait for
-// the copy in flight) when the copy did not land within bound_ns.
+// the copy in flight) when the copy did not land within bound_ns.  The copy
+// may then still be in flight into this block's shared memory, where a later
+// block on the same SM could find its bytes: the caller records PT_TIMEOUT,
+// and the device's results after it are suspect (the host discards the
+// handle whose run reported it).
 __device__ __forceinline__ bool stage_doubles(double* raw, const double* src, int n, uint64_t* bar_word,
                                               unsigned long long bound_ns, double** out) {
   const int off = ((uintptr_t)src & 15u) ? 1 : 0;

@@ -120,6 +120,9 @@ class Tally:
 class SMEngine:
     """Uploads one target's tables and exposes the C-ABI entry points."""
 
+    MAX_ROWS = 2 ** 31 - 1          # largest particle store run_sm grows to
+    MAX_RING = 1 << 28              # largest live-particle ring run_batch grows to
+
     def __init__(self, tables: SMTables, device="cuda"):
         torch = _torch()
         if not torch.cuda.is_available():
@@ -127,6 +130,8 @@ class SMEngine:
         self.lib = _lib.load()
         self.device = torch.device(device)
         self.tables = tables
+        self.unusable = None            # set when a device copy may still be in flight
+        self.last_store_capacity = 0    # particle store of the last run_sm (after PT_OOM retries)
         dev = self.device
         f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float64), device=dev)
         self._keep = {
@@ -236,7 +241,19 @@ class SMEngine:
             self.lib.pt_last_error_info(self.handle, C.byref(proc), C.byref(E), C.byref(key))
             from .tables import PROCESSES
             raise Exception("No Sample Found", PROCESSES[proc.value], E.value, key.value)
+        if status == _lib.PT_TIMEOUT:
+            proc, E, key = C.c_int32(), C.c_double(), C.c_int32()
+            self.lib.pt_last_error_info(self.handle, C.byref(proc), C.byref(E), C.byref(key))
+            if proc.value == -2:
+                # a table-staging copy into shared memory did not land in time
+                # and may still be in flight: nothing this handle computes on
+                # the device afterwards can be trusted
+                self.unusable = f"{what}: a table-staging copy timed out; make a new Shower"
         _lib.check(status, what)
+
+    def _usable(self):
+        if self.unusable:
+            raise _lib.PetiteGPUError(_lib.PT_TIMEOUT, self.unusable)
 
     @staticmethod
     def opts(min_energy, max_n_integrators=10000, rescale_MCS=1.0, ms=True, precision="fp64", seed=0,
@@ -254,13 +271,14 @@ class SMEngine:
 
     def run_sm(self, p0, r0, pid, mass, weight, opts: _lib.PtOpts, capacity: int | None = None):
         """Transports primaries (host arrays); returns (store, n_rows)."""
+        self._usable()
         torch = _torch()
         p0 = np.asarray(p0, np.float64).reshape(-1, 4)
         n = len(p0)
         r0 = np.asarray(r0, np.float64).reshape(n, 3)
         if capacity is None:
             est = np.sum(2.0 * p0[:, 0] / max(opts.min_energy, 1e-3)) + 16 * n
-            capacity = int(min(max(est, 1024), 2 ** 31 - 1))
+            capacity = int(min(max(est, 1024), self.MAX_ROWS))
         while True:
             st = ParticleStore(capacity, self.device)
             st.t["p0"][:, :n] = torch.as_tensor(p0.T, device=self.device)
@@ -271,8 +289,10 @@ class SMEngine:
             abi = st.abi()
             nrows = C.c_int64()
             s = self.lib.pt_run_sm(self.handle, C.byref(abi), n, C.byref(opts), C.byref(nrows), self._stream())
-            if s == _lib.PT_OOM:
-                capacity *= 2
+            self.last_store_capacity = capacity
+            if s == _lib.PT_OOM and capacity < self.MAX_ROWS:
+                # the showers outgrew the store: start over with twice the rows
+                capacity = min(2 * capacity, self.MAX_ROWS)
                 del st
                 continue
             self._raise(s, "pt_run_sm")
@@ -286,7 +306,7 @@ class SMEngine:
     LOOPS = {"host": 0, "graph": 1, "persistent": 2}
     STAGING = {"default": 0, "cached": 1, "shared": 2}
 
-    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default", threads=0):
+    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default", threads=0, barrier_ns=0):
         """Work distribution of the batched engine (0 = library default), who
         runs its waves -- "host" (two launches per wave, counters read back),
         "graph" (a CUDA graph's conditional loop, planned on the GPU) or
@@ -294,13 +314,15 @@ class SMEngine:
         propagation kernel reads the n*sigma tables: "shared" (each block's
         shared memory, filled by TMA bulk copies; "default"), or "cached"
         (the read-only data cache) -- and the mixed kernels' threads per block
-        (64, 128 or 256; 0 = 128)."""
+        (64, 128 or 256; 0 = 128) -- and the persistent kernel's bound on a
+        grid-barrier wait in ns (0 = the library's 20 s)."""
         t = _lib.PtBatchTuning()
         t.refill_min[0], t.refill_min[1] = int(refill_min[0]), int(refill_min[1])
         t.chunk[0], t.chunk[1] = int(chunk[0]), int(chunk[1])
         t.loop = self.LOOPS[loop]
         t.staging = self.STAGING[staging]
         t.threads = int(threads)
+        t.barrier_ns = int(barrier_ns)
         _lib.check(self.lib.pt_set_batch_tuning(self.handle, C.byref(t)), "pt_set_batch_tuning")
         self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk), "loop": loop, "staging": staging,
                        "threads": int(threads)}
@@ -326,6 +348,7 @@ class SMEngine:
         ([sets, N_DARK + 1]) and, with ``hist`` a PtDarkHist over the device
         tensor ``counts`` (or both None), their energy histogram; returns
         (tally, vectors)."""
+        self._usable()
         torch = _torch()
         if device_inputs is None:
             p0 = np.asarray(p0, np.float64).reshape(-1, 4)
@@ -357,7 +380,7 @@ class SMEngine:
                                                _ptr(M), n, C.byref(opts), C.byref(tally.abi()), cap, _ptr(yld),
                                                _ptr(yldE), C.byref(hist) if hist is not None else None,
                                                C.byref(nv), self._stream())
-            if s == _lib.PT_OOM and cap < (1 << 28):
+            if s == _lib.PT_OOM and cap < self.MAX_RING:
                 # the live population outgrew the ring: start over with twice the room
                 tally.zero_()
                 if dark is not None:

@@ -9,10 +9,13 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = os.environ.get("PETITE_REFERENCE", "/root/reference")
+# the PETITE checkout (the directory holding src/PETITE), given by the caller
+REFERENCE = os.environ.get("PETITE_REFERENCE", "")
 
 
 def setup():
+    if not REFERENCE:
+        raise RuntimeError("set PETITE_REFERENCE to a PETITE checkout (the directory holding src/PETITE)")
     for p in (os.path.join(HERE, "refshim"), os.path.join(REFERENCE, "src"),
               os.path.join(REFERENCE, "utilities")):
         if p not in sys.path:

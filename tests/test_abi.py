@@ -90,3 +90,31 @@ def test_entry_points_refuse_missing_handles_without_a_device(lib):
     assert lib.pt_dark_screen32(None, 0, None, None, 1, 0.1, None, None, None) == _lib.PT_BAD_ARG
     assert lib.pt_set_batch_tuning(None, None) == _lib.PT_BAD_ARG
     assert lib.pt_vegas_adapt(0, 1, None, None, 2, None, None, 0.5, None) == _lib.PT_BAD_ARG
+
+
+def test_staging_timeout_marks_the_handle_unusable():
+    """PT_TIMEOUT whose error record names a table-staging copy (process -2)
+    makes the engine refuse further device work: that copy may still be in
+    flight.  A loop bound (process -1) does not."""
+    from petite_gb300 import _lib
+    from petite_gb300.engine import SMEngine
+
+    class FakeLib:
+        def __init__(self, proc):
+            self.proc = proc
+
+        def pt_last_error_info(self, h, proc, E, key):
+            C.cast(proc, C.POINTER(C.c_int32))[0] = self.proc
+            return 0
+
+    for proc, unusable in ((-1, False), (-2, True)):
+        eng = object.__new__(SMEngine)
+        eng.unusable = None
+        eng.handle = None
+        eng.lib = FakeLib(proc)
+        with pytest.raises(_lib.PetiteGPUError):
+            eng._raise(_lib.PT_TIMEOUT, "pt_run_batch")
+        assert (eng.unusable is not None) == unusable
+        if unusable:
+            with pytest.raises(_lib.PetiteGPUError):
+                eng._usable()

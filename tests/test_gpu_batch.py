@@ -58,26 +58,46 @@ def test_ring_capacity_does_not_change_results(lead, precision):
     np.testing.assert_allclose(big.primary_edep.cpu().numpy(), small.primary_edep.cpu().numpy(), rtol=1e-9)
 
 
+def mixed_vs_fp64_errors(f, x, z_max):
+    """Per-observable error of the mixed form against the float64 form on the
+    same random streams (the float64 form equals the record engine, which
+    equals the oracle draw for draw)."""
+    sf, sx = f.summary(), x.summary()
+    cf, cx = f.primary_count.cpu().numpy(), x.primary_count.cpu().numpy()
+    ef, ex = f.primary_edep.cpu().numpy(), x.primary_edep.cpu().numpy()
+    hf, hx = f.hist.cpu().numpy().astype(np.int64), x.hist.cpu().numpy().astype(np.int64)
+    out = {"identical showers": float(np.mean(cf == cx)),
+           "multiplicity (total)": abs(sx["steps"] - sf["steps"]) / sf["steps"],
+           "E_dep (total)": abs(sx["E_deposited"] - sf["E_deposited"]) / sf["E_deposited"],
+           "E_dep (largest per shower)": float(np.max(np.abs(ex - ef) / ef))}
+    lo_hi = ((-2.0, 2.0), (-6.0, 0.5), (0.0, z_max))
+    for k, name in enumerate(("creation energy", "polar angle", "depth")):
+        a, b = hf[k].sum(axis=0), hx[k].sum(axis=0)
+        centres = lo_hi[k][0] + (np.arange(a.size) + 0.5) * (lo_hi[k][1] - lo_hi[k][0]) / a.size
+        out[f"{name} (entries in another bin)"] = float(np.abs(hf[k] - hx[k]).sum() / (2 * hf[k].sum()))
+        out[f"{name} (binned mean)"] = float(abs((centres * b).sum() / b.sum() - (centres * a).sum() / a.sum())
+                                             / abs((centres * a).sum() / a.sum()))
+    return out
+
+
 def test_mixed_matches_fp64(lead):
     """Same random streams: the float32 sampler changes a decision only when a
-    uniform falls within float32 rounding of the acceptance boundary."""
+    uniform falls within float32 rounding of the acceptance boundary, and the
+    shower below that decision is then drawn again.  The benchmark spec's bound is
+    total deposited energy within 1e-5 of float64."""
     p0, pid, m = primaries(3000, seed=11, emax=100.0)
     f = run_batch(lead, p0, pid, m, "fp64")
     x = run_batch(lead, p0, pid, m, "mixed")
-    sf, sx = f.summary(), x.summary()
-    cf, cx = f.primary_count.cpu().numpy(), x.primary_count.cpu().numpy()
-    same = float(np.mean(cf == cx))
-    print("identical showers:", same, "steps", sf["steps"], sx["steps"])
-    assert same > 0.9
-    assert abs(sx["steps"] - sf["steps"]) / sf["steps"] < 2e-3
-    assert abs(sx["E_deposited"] - sf["E_deposited"]) / sf["E_deposited"] < 1e-3
-    # binned spectra: chi2 per bin of creation energies and depths
-    hf, hx = f.hist.cpu().numpy().astype(float), x.hist.cpu().numpy().astype(float)
-    for kind in (0, 2):
-        a, b = hf[kind].ravel(), hx[kind].ravel()
-        mask = (a + b) > 20
-        chi2 = np.sum((a[mask] - b[mask]) ** 2 / (a[mask] + b[mask]))
-        assert chi2 / mask.sum() < 2.0, (kind, chi2 / mask.sum())
+    err = mixed_vs_fp64_errors(f, x, 0.3)
+    print()
+    for k, v in err.items():
+        print(f"  {k:40s} {v:.3e}")
+    assert err["identical showers"] > 0.98
+    assert err["E_dep (total)"] < 1e-5
+    assert err["multiplicity (total)"] < 1e-4
+    for name in ("creation energy", "polar angle", "depth"):
+        assert err[f"{name} (entries in another bin)"] < 2e-2, name
+        assert err[f"{name} (binned mean)"] < 1e-3, name
 
 
 def test_batch_no_sample_reports():

@@ -1,0 +1,84 @@
+"""Independent-stream agreement of the batched engine with CPU showers.
+
+The CPU showers (``tests/golden/spectra.npz``, made by
+``tests/golden/make_spectra.py`` from the oracle's ``generate_shower``, which
+is pinned draw for draw to PETITE's ``Shower.generate_shower``,
+shower.py:603-708) and the GPU showers are drawn from independent random
+streams: another Philox seed, and ten GPU showers of each CPU primary on
+stream indices of their own.  For each workload and both engine forms
+(float64, and float32 sampling with float64 kinematics) the test compares:
+
+* per-shower particle count and deposited energy: two-sample KS;
+* creation energy, polar angle and interaction depth per species: the
+  per-shower mean histograms, by Hotelling's T^2 of the paired difference
+  (``tests/spectra.py:hotelling_paired``), since the particles of one shower
+  are not independent.
+
+Every p-value must exceed 0.01.  The seeds are fixed, so the outcome is
+deterministic for a given engine build.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import spectra
+
+pytestmark = pytest.mark.gpu
+
+P_MIN = 0.01
+KINDS = ("creation energy", "polar angle", "depth")
+
+
+@pytest.fixture(scope="module")
+def cpu():
+    return np.load(os.path.join(GOLDEN, "spectra.npz"))
+
+
+_showers = {}
+
+
+def gpu_run(name, precision):
+    from petite_gb300 import Shower
+    cfg = spectra.CONFIGS[name]
+    key = (cfg["target"], cfg["gpu_seed"])
+    if key not in _showers:
+        _showers[key] = Shower(None, cfg["target"], spectra.MIN_ENERGY, seed=cfg["gpu_seed"])
+    p0, pid, m = spectra.primaries(cfg)
+    k = cfg["replicas"]
+    p0, pid, m = np.tile(p0, (k, 1)), np.tile(pid, k), np.tile(m, k)
+    out = _showers[key].run_tallied(p0, pid, m, precision=precision, first_primary=0, z_max=cfg["z_max"])
+    return cfg, p0, out
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("name", list(spectra.CONFIGS))
+def test_spectra_match_cpu_showers(cpu, name, precision):
+    cfg, p0, out = gpu_run(name, precision)
+    n_gpu, n_cpu = len(p0), cfg["n"]
+    mult_c, edep_c = cpu[f"{name}/mult"], cpu[f"{name}/edep"]
+    mult_g, edep_g = out["primary_count"].astype(np.int64), out["primary_edep"]
+    assert int(mult_g.sum()) == out["steps"]
+    rows = []
+    pvals = {}
+    for label, a, b in (("multiplicity", mult_g, mult_c), ("E_dep", edep_g, edep_c),
+                        ("E_dep - E0", edep_g - p0[:, 0], edep_c - cpu[f"{name}/E0"])):
+        _, p = spectra.ks(a, b)
+        pvals[label] = p
+        ma, ea = spectra.mean_and_error(a)
+        mb, eb = spectra.mean_and_error(b)
+        rows.append((label, ma, mb, (ma - mb) / np.hypot(ea, eb), "KS", p))
+    coarse = spectra.coarse_tally_hist(out["hist"]) / n_gpu
+    hist_c = cpu[f"{name}/hist"].astype(np.int64)
+    for k, kind in enumerate(KINDS):
+        t2, dof, p = spectra.hotelling_paired(coarse[k].ravel(), cfg["replicas"], hist_c[:, k].reshape(n_cpu, -1),
+                                              cpu[f"{name}/pid"], cpu[f"{name}/E0"])
+        pvals[kind] = p
+        rows.append((kind, float(coarse[k].sum()), float(hist_c[:, k].sum() / n_cpu), float("nan"),
+                     f"T2={t2:.1f}/{dof}", p))
+    print(f"\n{name} {precision}: {n_gpu} GPU showers vs {n_cpu} CPU showers")
+    for r in rows:
+        print(f"  {r[0]:16s} gpu {r[1]:12.6g} cpu {r[2]:12.6g} z {r[3]:6.2f} {r[4]:>12s} p {r[5]:.3f}")
+    bad = {k: v for k, v in pvals.items() if not v > P_MIN}
+    assert not bad, bad
