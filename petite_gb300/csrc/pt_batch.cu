@@ -1887,6 +1887,10 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   const int nt = wpb * 32;
   const void* kp = propagate_kernel<PREC>(c.mcs_mode, smem_p > 0, wpb);
   const void* ks = sample_kernel<PREC>(wpb);
+  // the staged tables are dynamic shared memory on top of the kernel's
+  // static share; beyond 48 KB in all, a kernel must be allowed the dynamic
+  // part explicitly
+  if (smem_p) PT_CUDA(cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
   const int rb_p = resident_blocks(kp, nt, smem_p);
   const int rb_s = resident_blocks(ks, nt);
   PT_CUDA(cudaMemsetAsync(hp.status, 0, sizeof(int), st));
