@@ -9,7 +9,7 @@ end without an interaction, as the batched engine's tally counts it), the
 primary's energy and PID, and the coarse per-shower histograms of creation
 energy, polar angle and interaction depth.
 
-Usage: python tests/golden/make_spectra.py [--procs N]   (writes tests/golden/spectra.npz)
+Usage: python tests/golden/make_spectra.py [--procs N] [--workloads a,b]   (writes tests/golden/spectra.npz)
 """
 import argparse
 import multiprocessing as mp
@@ -77,11 +77,18 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--procs", type=int, default=os.cpu_count())
     ap.add_argument("--out", default=os.path.join(HERE, "spectra.npz"))
+    ap.add_argument("--workloads", default=",".join(spectra.CONFIGS),
+                    help="workloads to make; the others are kept from an existing output file")
     a = ap.parse_args()
     out = {}
+    if os.path.exists(a.out):
+        old = np.load(a.out)
+        out = {k: old[k] for k in old.files}
     ctx = mp.get_context("spawn")
     with ctx.Pool(a.procs) as pool:
         for name, cfg in spectra.CONFIGS.items():
+            if name not in a.workloads.split(","):
+                continue
             t0 = time.time()
             p0, pid, m = spectra.primaries(cfg)
             # largest showers first, so the pool's tail is short

@@ -150,7 +150,7 @@ def mean_and_error(x):
 # showers of each CPU primary, all on streams independent of the CPU's
 # (another Philox seed, and other stream indices).
 CONFIGS = {
-    "e1_graphite": dict(target="graphite", species=(11,), E=(1.0, 1.0), z_max=3.0, n=1000, replicas=10,
+    "e1_graphite": dict(target="graphite", species=(11,), E=(1.0, 1.0), z_max=3.0, n=4000, replicas=10,
                         prim_seed=101, cpu_seed=1000, gpu_seed=0),
     "mix_lead": dict(target="lead", species=(11, -11, 22), E=(0.1, 100.0), z_max=0.3, n=2000, replicas=10,
                      prim_seed=102, cpu_seed=1001, gpu_seed=1),
