@@ -343,6 +343,9 @@ typedef struct pt_dark_maps {
   int64_t n_nodes;
   double Z, A;                    /* target Z_T and A_T (A_T is also the target mass
                                      draw_dark_sample passes, dark_shower.py:673) */
+  const float* grid_f32x2;        /* [n_nodes][2] float32 (node, increment to the next node), each rounded
+                                     once from float64: the proposals of pt_dark_params.precision = 1
+                                     (NULL: float64 proposals only) */
 } pt_dark_maps;
 
 /* One DarkShower's per-mass tables (dark_shower.py:69-130, 219-593), all
@@ -378,6 +381,11 @@ typedef struct pt_dark_params {
   const double* ii_x[3];          /* interaction integrals of Brem, Ann, Bhabha (shower.py:296-314): */
   const double* ii_y[3];          /*   interp1d(fill 0) tables behind _positron_exponential_factor */
   int32_t ii_n[3];
+  int32_t precision;              /* draw_dark_sample's proposals: 0 = float64 throughout; 1 = float32
+                                     uniforms, map transform and dark-brem screen, with the float64
+                                     cross section deciding wherever the float32 estimate cannot (near
+                                     the acceptance boundary or a kinematic edge); the vector's
+                                     kinematics stay float64 (needs pt_dark_maps.grid_f32x2) */
 } pt_dark_params;
 
 /* Vectors produced by pt_run_dark (device pointers; SoA like pt_particles). */

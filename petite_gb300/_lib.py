@@ -81,7 +81,7 @@ class PtDarkMaps(C.Structure):
                 ("map_base", C.c_int32 * (DARK_MAX_MASSES * N_DARK)), ("map_rows", C.c_int32 * (DARK_MAX_MASSES * N_DARK)),
                 ("n_rows", C.c_int32), ("map_energy", C.c_void_p), ("map_maxF", C.c_void_p), ("map_neval", C.c_void_p),
                 ("grid_offset", C.c_void_p), ("grid_ninc", C.c_void_p), ("grid_nodes", C.c_void_p),
-                ("n_nodes", C.c_int64), ("Z", C.c_double), ("A", C.c_double)]
+                ("n_nodes", C.c_int64), ("Z", C.c_double), ("A", C.c_double), ("grid_f32x2", C.c_void_p)]
 
 
 class PtDarkParams(C.Structure):
@@ -94,7 +94,7 @@ class PtDarkParams(C.Structure):
                 ("dr_n", C.c_int32 * 4), ("dr_nbmax", C.c_int32 * 4),
                 ("nsc_lx", C.c_void_p), ("nsc_ly", C.c_void_p), ("nsc_n", C.c_int32),
                 ("kinetic_mixing", C.c_double), ("ann_E0", C.c_double), ("ann_K", C.c_double),
-                ("ii_x", C.c_void_p * 3), ("ii_y", C.c_void_p * 3), ("ii_n", C.c_int32 * 3)]
+                ("ii_x", C.c_void_p * 3), ("ii_y", C.c_void_p * 3), ("ii_n", C.c_int32 * 3), ("precision", C.c_int32)]
 
 
 class PtDarkHist(C.Structure):

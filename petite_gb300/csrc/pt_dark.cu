@@ -96,10 +96,11 @@ struct DarkDraw {
   int r, d, neval, key;
   double maxF, E;
   int64_t made, limit;          // proposals made; max_n_integrators * neval
-  float tconv;
+  float maxF32, inv_neval32;    // the float32 proposals' acceptance ratio
+  Screen32K sk;                 // the float32 dark-brem screen's constants
 };
 
-__device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block, int p, double E,
+__device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block, int p, double E, double mV,
                                                 int64_t max_n_integrators, DarkDraw& D) {
   D.key = dark_lu_key(M, block, E);
   D.r = M.map_base[block] + D.key;
@@ -109,8 +110,13 @@ __device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block
   D.E = E;
   D.made = 0;
   D.limit = max_n_integrators * (int64_t)D.neval;
+  D.maxF32 = (float)D.maxF;
+  D.inv_neval32 = 1.f / (float)D.neval;
   const bool brem = (p == PT_DARKBREM || p == PT_DARKMUONBREM);
-  D.tconv = brem ? (float)dark_brem_tconv(E, M.A, p == PT_DARKMUONBREM ? kMmu : kMe) : 0.f;
+  if (brem) {
+    const double m = p == PT_DARKMUONBREM ? kMmu : kMe;
+    D.sk = screen32_constants(E, mV, M.A, m, M.Z, M.A, (float)dark_brem_tconv(E, M.A, m));
+  }
 }
 
 // One proposal: 1 accepted (x holds it), 0 rejected, -1 the limit was
@@ -133,7 +139,7 @@ __device__ int dark_propose(const pt_dark_maps& M, int p, double mV, DarkDraw& D
   // changed nothing measurable: the accepted proposals are few.)
   if (p == PT_DARKBREM || p == PT_DARKMUONBREM) {
     float f32;
-    const int sc = dark_brem_screen32(x, D.E, mV, M.A, p == PT_DARKMUONBREM ? kMmu : kMe, M.Z, M.A, D.tconv, f32);
+    const int sc = dark_brem_screen32k((float)x[0], (float)x[1], (float)x[2], D.sk, f32);
     if (sc == kScreenOutside) return 0;                          // integrand 0: rejected
     if (sc == kScreenValue && D.maxF * u > 4.0 * wgt * (double)f32) return 0;
   }
@@ -141,11 +147,68 @@ __device__ int dark_propose(const pt_dark_maps& M, int p, double mV, DarkDraw& D
   return D.maxF * u < wgt * f ? 1 : 0;
 }
 
+// The same proposal in float32 (pt_dark_params.precision = 1): the draws'
+// float forms (the same draws, their top 24 bits), the map transform on the
+// float32 grid, and the dark-brem screen decide whenever its estimate is
+// trusted and the accept draw lies more than 2 % from the acceptance ratio
+// (the screen is within 1 % of the float64 cross section wherever it
+// returns a value), so such a decision is the float64 one at this sample.
+// Otherwise the float64 cross section decides at the float32 sample.  x
+// receives the sample (as float64) when it is accepted.
+__device__ int dark_propose32(const pt_dark_maps& M, int p, double mV, DarkDraw& D, Rng& rng, const PhiloxRK& rk,
+                              double* x) {
+  if (D.made >= D.limit) return -1;
+  float u[4];
+  if (D.d == 3) {
+    rng.take(u, rk);                                 // three y draws and the accept draw
+  } else {
+    float u2[2];
+    rng.take(u2, rk);
+    u[0] = u2[0];
+    u[1] = u[2] = 0.f;
+    u[3] = u2[1];
+  }
+  const float2* g2 = reinterpret_cast<const float2*>(M.grid_f32x2);
+  float xf[3] = {0.f, 0.f, 0.f};
+  float jac = 1.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (k < D.d) {
+      const int ninc = M.grid_ninc[D.r * 4 + k];
+      const float t = u[k] * (float)ninc;
+      int i = (int)t;
+      if (i > ninc - 1) i = ninc - 1;
+      const float2 g = __ldg(g2 + M.grid_offset[D.r * 4 + k] + i);   // (node, increment)
+      xf[k] = fmaf(g.y, t - (float)i, g.x);
+      jac *= (float)ninc * g.y;
+    }
+  }
+  ++D.made;
+  const float wgt = jac * D.inv_neval32;
+  const float ua = u[3];
+  if ((p == PT_DARKBREM || p == PT_DARKMUONBREM)) {
+    float f32;
+    const int sc = dark_brem_screen32k(xf[0], xf[1], xf[2], D.sk, f32);
+    if (sc == kScreenOutside) return 0;                          // integrand 0: rejected
+    if (sc == kScreenValue && D.maxF32 > 0.f) {
+      const float r = wgt * f32 / D.maxF32;
+      if (ua > 1.02f * r) return 0;
+      if (ua < 0.98f * r) {
+        x[0] = xf[0]; x[1] = xf[1]; x[2] = xf[2];
+        return 1;
+      }
+    }
+  }
+  x[0] = xf[0]; x[1] = xf[1]; x[2] = xf[2];
+  const double f = dark_dsigma<double>(M, p, x, D.E, mV);
+  return D.maxF * (double)ua < (double)wgt * f ? 1 : 0;
+}
+
 // The whole loop; false when no sample was found.
 __device__ bool draw_dark(const pt_dark_maps& M, int block, int p, double E, double mV, int64_t max_n_integrators,
                           Rng& rng, double* x, int& key, int64_t& proposals) {
   DarkDraw D;
-  dark_draw_begin(M, block, p, E, max_n_integrators, D);
+  dark_draw_begin(M, block, p, E, mV, max_n_integrators, D);
   key = D.key;
   int res;
   while ((res = dark_propose(M, p, mV, D, rng, x)) == 0) {
@@ -334,7 +397,7 @@ __device__ int bsm_begin(const Tabs& T, const pt_dark_maps& M, const pt_dark_par
     v = {P.E_res, 0.0, 0.0, sqrt((S(P.E_res) * S(P.E_res) - S(mV) * S(mV)).v)};
     return 1;
   }
-  dark_draw_begin(M, P.mass_index * PT_N_DARK + p, p, E0, o.max_n_integrators, D);
+  dark_draw_begin(M, P.mass_index * PT_N_DARK + p, p, E0, mV, o.max_n_integrators, D);
   return 2;
 }
 
@@ -537,10 +600,11 @@ __global__ void k_dark_weigh(Tabs T, pt_dark_params P, pt_particles sm, int64_t 
 // lanes keep proposing.  Each task draws from its own stream, in the
 // reference's order, so the vectors are produce_bsm's whatever the schedule.
 constexpr int kDarkThreads = 128;
+template <int PREC>
 __global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_maps M, pt_dark_params P, pt_opts o,
                                                                pt_particles sm, DarkTasks tk, pt_dark_out out,
                                                                unsigned long long* counter, int* status,
-                                                               double* info) {
+                                                               double* info, PhiloxRK rk) {
   const int lane = threadIdx.x & 31;
   const unsigned long long nt = __ldcg(counter + 1);
   const int64_t n = (int64_t)nt < tk.cap ? (int64_t)nt : tk.cap;
@@ -591,7 +655,7 @@ __global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_m
       }
     }
     if (have) {
-      const int res = dark_propose(M, p, P.mV, D, rng, x);
+      const int res = PREC == 1 ? dark_propose32(M, p, P.mV, D, rng, rk, x) : dark_propose(M, p, P.mV, D, rng, x);
       if (res != 0) {
         have = false;
         V4 v;
@@ -783,13 +847,20 @@ static pt_status dark_launch(pt_dark* d, const pt_dark_params& prm, const pt_opt
   int dev = 0, sms = 0, per = 0;
   PT_CUDA(cudaGetDevice(&dev));
   PT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  PT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dark_produce, kDarkThreads, 0));
+  const bool f32 = prm.precision == 1;
+  const void* kern = f32 ? (const void*)k_dark_produce<1> : (const void*)k_dark_produce<0>;
+  PT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kDarkThreads, 0));
   if (per < 1) per = 1;
   int64_t grid = (int64_t)sms * per;
   const int64_t need = (work + kDarkThreads - 1) / kDarkThreads;
   if (grid > need) grid = need;
-  k_dark_produce<<<(unsigned)grid, kDarkThreads, 0, st>>>(d->T, d->M, prm, o, sm, tk, out, d->counter, d->status,
-                                                          d->err_info);
+  const PhiloxRK rk = philox_round_keys(o.seed);
+  if (f32)
+    k_dark_produce<1><<<(unsigned)grid, kDarkThreads, 0, st>>>(d->T, d->M, prm, o, sm, tk, out, d->counter,
+                                                               d->status, d->err_info, rk);
+  else
+    k_dark_produce<0><<<(unsigned)grid, kDarkThreads, 0, st>>>(d->T, d->M, prm, o, sm, tk, out, d->counter,
+                                                               d->status, d->err_info, rk);
   PT_CUDA(cudaGetLastError());
   return PT_OK;
 }
@@ -876,6 +947,7 @@ extern "C" pt_status pt_run_dark(pt_dark* d, const pt_dark_params* prm, const pt
                                  const pt_opts* o, pt_dark_out* out, int64_t* n_out, void* stream) {
   if (!d || !prm || !sm || !o || !out || !n_out || n_rows < 0 || n_rows > sm->capacity) return PT_BAD_ARG;
   if (prm->mass_index < 0 || prm->mass_index >= d->M.n_masses) return PT_BAD_TABLE;
+  if (prm->precision != 0 && (prm->precision != 1 || !d->M.grid_f32x2)) return PT_BAD_ARG;
   for (int p = 0; p < PT_N_DARK; ++p)
     if (((prm->active >> p) & 1) && !mass_block_ok(d, prm, p)) return PT_BAD_TABLE;
   for (int k = 0; k < 4; ++k)
@@ -934,6 +1006,7 @@ extern "C" pt_status pt_run_batch_dark(pt_handle* h, pt_dark* d, const pt_dark_p
   for (int m = 0; m < n_params; ++m) {
     const pt_dark_params* q = prm + m;
     if (q->mass_index < 0 || q->mass_index >= d->M.n_masses) return PT_BAD_TABLE;
+    if (q->precision != 0 && (q->precision != 1 || !d->M.grid_f32x2)) return PT_BAD_ARG;
     for (int p = 0; p < PT_N_DARK; ++p)
       if (((q->active >> p) & 1) && !mass_block_ok(d, q, p)) return PT_BAD_TABLE;
     for (int k = 0; k < 4; ++k)

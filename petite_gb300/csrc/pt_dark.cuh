@@ -222,11 +222,30 @@ __device__ T dsig_dark_brem_anchored(const double* xv, double E, T mV, double a,
 // V^2 - ((1-x)E)^2 = (p - k - (1-x)E)(p - k + (1-x)E) + 2 k p (1 - cos theta),
 // and the limits of dark_brem_limits_stable.
 enum { kScreenUnsure = 0, kScreenValue = 1, kScreenOutside = 2 };
-__device__ __forceinline__ int dark_brem_screen32(const double* xv, double E_, double mV_, double MT_, double m_,
-                                                  double Z_, double A_, float tconv, float& out) {
-  const float x = (float)xv[0], E = (float)E_, mV = (float)mV_, MT = (float)MT_, m = (float)m_;
-  const float omc = exp10f((float)xv[1]);
-  const float tt = exp10f((float)xv[2]);
+
+// The screen's per-draw constants (incident energy, masses, target and the
+// form-factor scales), formed once per draw_dark_sample call.
+struct Screen32K { float E, mV, MT, m, Z, cs1, cc2, ap2, tconv; };
+__device__ __forceinline__ Screen32K screen32_constants(double E_, double mV_, double MT_, double m_, double Z_,
+                                                        double A_, float tconv) {
+  Screen32K K;
+  K.E = (float)E_; K.mV = (float)mV_; K.MT = (float)MT_; K.m = (float)m_;
+  const float Z = (float)Z_, A = (float)A_;
+  K.Z = Z;
+  const float cc1 = 111.f * powf(Z, -1.f / 3.f) / (float)kMe;
+  K.cs1 = cc1 * cc1;
+  K.cc2 = 0.164f * powf(A, -2.f / 3.f);
+  const float ap = 773.f * powf(Z, -2.f / 3.f) / (float)kMe;
+  K.ap2 = ap * ap;
+  K.tconv = tconv;
+  return K;
+}
+
+// The screen at a float32 sample (x, log10(1 - cos theta), log10 t~).
+__device__ __forceinline__ int dark_brem_screen32k(float x, float lomc, float ltt, const Screen32K& K, float& out) {
+  const float E = K.E, mV = K.mV, MT = K.MT, m = K.m;
+  const float omc = exp10f(lomc);
+  const float tt = exp10f(ltt);
   const float xE = x * E;
   if (xE < mV * 0.999f) return kScreenOutside;                      // x E >= mV fails
   if (!(xE > mV * 1.001f) || !(x < 1.f)) return kScreenUnsure;
@@ -251,7 +270,7 @@ __device__ __forceinline__ int dark_brem_screen32(const double* xv, double E_, d
   const float Qm = fabsf(ut * (ut + 4.f * MT * Er) / (2.f * (Aq + Bq)));
   const float tp = 2.f * MT * Qp * Qp / (sqrtf(MT * MT + Qp * Qp) + MT);
   const float tm = 2.f * MT * Qm * Qm / (sqrtf(MT * MT + Qm * Qm) + MT);
-  const float t = tt * tconv;
+  const float t = tt * K.tconv;
   if (tp > tm * 1.01f && (t < tm * 0.998f || t > tp * 1.002f)) return kScreenOutside;   // outside (t-, t+)
   if (!(t > tm * 1.002f && t < tp * 0.998f)) return kScreenUnsure;
   const float q0 = -t / (2.f * MT);
@@ -295,19 +314,22 @@ __device__ __forceinline__ int dark_brem_screen32(const double* xv, double E_, d
   if (!(fabsf(ps) > 1e-2f * (fabsf(P0) + fabsf(P1) + fabsf(P2) + fabsf(P3)))) return kScreenUnsure;
   const float phi = ps / (8.f * MT * MT);
   // Gelastic_inelastic_over_tsquared in float32 (all_processes.py:112-133)
-  const float Z = (float)Z_, A = (float)A_;
-  const float cc1 = 111.f * powf(Z, -1.f / 3.f) / (float)kMe, cs1 = cc1 * cc1;
-  const float cc2 = 0.164f * powf(A, -2.f / 3.f);
+  const float Z = K.Z, cs1 = K.cs1, cc2 = K.cc2, ap2 = K.ap2;
   const float g1 = 1.f / (1.f + cs1 * t), g2 = 1.f / (1.f + t / cc2);
-  const float ap = 773.f * powf(Z, -2.f / 3.f) / (float)kMe, ap2 = ap * ap;
   const float g3 = ap2 / (1.f + ap2 * t), g4 = 1.f + t / 0.71f;
   const float Ginel = Z / (cs1 * cs1 * Z * Z) * (g3 * g3) *
                       ((1.f + (2.79f * 2.79f - 1.f) * t / (4.f * (float)(kMproton * kMproton))) / (g4 * g4 * g4 * g4));
   const float ff = Z * Z * cs1 * cs1 * (g1 * g1 * g2 * g2 + Ginel);
   const float al = (float)kAlpha;
   const float ans = ff * (al * al * al) * k * E * phi / (p * V);
-  out = ans * tconv * (omc * tt * (float)(kLn10 * kLn10));
+  out = ans * K.tconv * (omc * tt * (float)(kLn10 * kLn10));
   return (out > 0.f && out < 3.0e38f) ? kScreenValue : kScreenUnsure;
+}
+
+__device__ __forceinline__ int dark_brem_screen32(const double* xv, double E_, double mV_, double MT_, double m_,
+                                                  double Z_, double A_, float tconv, float& out) {
+  return dark_brem_screen32k((float)xv[0], (float)xv[1], (float)xv[2],
+                             screen32_constants(E_, mV_, MT_, m_, Z_, A_, tconv), out);
 }
 
 // ----------------------------------------------------------- dark Compton

@@ -155,6 +155,15 @@ class DarkEngine:
         M.map_energy, M.map_maxF, M.map_neval = (self._keep[k].data_ptr() for k in ("energy", "maxF", "neval"))
         M.grid_offset, M.grid_ninc, M.grid_nodes = (self._keep[k].data_ptr() for k in ("offset", "ninc", "nodes"))
         M.n_nodes = len(mp["nodes"])
+        # float32 (node, increment to the next node) for the float32 proposals
+        nodes = np.asarray(mp["nodes"], np.float64)
+        inc = np.zeros_like(nodes)
+        for o, c in zip(mp["offset"].reshape(-1), mp["ninc"].reshape(-1)):
+            if c > 0:
+                inc[o:o + c] = nodes[o + 1:o + c + 1] - nodes[o:o + c]
+        self._keep["f32x2"] = torch.as_tensor(np.ascontiguousarray(np.stack([nodes, inc], axis=1).astype(np.float32)),
+                                              device=dev)
+        M.grid_f32x2 = self._keep["f32x2"].data_ptr()
         ti = T.TARGET_INFORMATION[target]
         M.Z, M.A = float(ti["Z_T"]), float(ti["A_T"])
         self._M = M
@@ -322,13 +331,15 @@ def _active_bits(processes) -> int:
     return bits | ((1 << _lib.TWOBODY) if TWOBODY in processes else 0)
 
 
-def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, active, coupling, Zeff):
+def _dark_params(engine: DarkEngine, sh, mV_est: float, mV: float, bound: bool, active, coupling, Zeff,
+                 precision: str = "fp64"):
     """pt_dark_params for one DarkShower (tables kept alive on the engine)."""
     import torch
     d = engine.data.params_for(mV_est, sh.get_target_material(), bound)
     dev = engine.device
     keep = {}
     prm = _lib.PtDarkParams()
+    prm.precision = {"fp64": 0, "mixed": 1}[precision]
     prm.mass_index = engine.mass_index(mV_est)
     prm.bound_electron = 1 if bound else 0
     prm.active = _active_bits(active)
@@ -375,7 +386,7 @@ class DarkShower(Shower):
     def __init__(self, dict_dir, target_material, min_energy, mV_in_GeV, mode="exact", maxF_fudge_global=1,
                  max_n_integrators=int(1e4), kinetic_mixing=1.0, Zeff=29.508, bound_electron=True, g_e=None,
                  active_processes=None, fast_MCS_mode=True, rescale_MCS=1, seed=None, device="cuda",
-                 dark_tables=None):
+                 dark_tables=None, dark_precision="fp64"):
         super().__init__(dict_dir, target_material, min_energy, maxF_fudge_global=maxF_fudge_global,
                          max_n_integrators=max_n_integrators, fast_MCS_mode=fast_MCS_mode, seed=seed,
                          rescale_MCS=rescale_MCS, device=device)
@@ -399,8 +410,12 @@ class DarkShower(Shower):
             raise Exception("Mode not valid. Chose exact or approx.")
         self._coupling = self.g_e ** 2 / (4 * np.pi * T.ALPHA_EM)
         self._dark_engine = DarkEngine(self._engine, self._dark, target_material, maxF_fudge_global)
+        if dark_precision not in ("fp64", "mixed"):
+            raise ValueError("dark_precision is 'fp64' or 'mixed'")
+        self.dark_precision = dark_precision
         self._prm, self._prm_keep = _dark_params(self._dark_engine, self, self._mV_estimator, self._mV,
-                                                 bound_electron, self.active_processes, self._coupling, Zeff)
+                                                 bound_electron, self.active_processes, self._coupling, Zeff,
+                                                 dark_precision)
         pd = self._dark.params_for(self._mV_estimator, target_material)
         self._resonant_annihilation_energy = pd["E_res"]
         self._compton_threshold_energy = pd["E_compth"]
