@@ -115,6 +115,37 @@ NCU_TRAFFIC = {
 }
 
 
+# Arithmetic and issue rates of the two mixed-form kernels while they run,
+# from one ncu capture of a mid-run launch of each (the profile named):
+# float32 flop/s = (fadd + fmul + 2 ffma thread instructions) / duration,
+# float64 likewise, the issue-active fraction of the schedulers and the lanes
+# active per executed instruction.  The bench divides the flop rates by the
+# FMA peaks it measures in the same run (pt_alu_peaks).
+NCU_ALU = {
+    "propagate": {"fp32_tflops": 3.815, "fp64_tflops": 0.0064, "issue_active": 0.520, "fp64_pipe": 0.181,
+                  "threads_per_inst": 19.6, "profile": "profiles/alu_batched_lead_20k.md"},
+    "sample": {"fp32_tflops": 2.015, "fp64_tflops": 0.0054, "issue_active": 0.536, "fp64_pipe": 0.071,
+               "threads_per_inst": 17.1, "profile": "profiles/alu_batched_lead_20k.md"},
+}
+
+
+def alu_roofline():
+    """The issue-bound kernels' arithmetic roofline: measured FMA peaks of
+    this GPU and each kernel's fraction of them (rates from NCU_ALU)."""
+    from petite_gb300 import _lib
+    a, b = C.c_double(), C.c_double()
+    if _lib.load().pt_alu_peaks(C.byref(a), C.byref(b), None) != 0:
+        return None
+    p32, p64 = a.value / 1e12, b.value / 1e12
+    ks = {k: {"fp32_tflops": v["fp32_tflops"], "fp32_frac": v["fp32_tflops"] / p32,
+              "fp64_tflops": v["fp64_tflops"], "fp64_frac": v["fp64_tflops"] / p64,
+              "fp64_pipe_busy": v["fp64_pipe"], "issue_active": v["issue_active"],
+              "threads_per_inst": v["threads_per_inst"], "profile": v["profile"]} for k, v in NCU_ALU.items()}
+    return {"bound": "issue", "fp32_peak_tflops": p32, "fp64_peak_tflops": p64,
+            "peak_source": "pt_alu_peaks: FMA chains on every SM, CUDA events, this run (of measured)",
+            "kernels": ks}
+
+
 def measured_traffic(kernel, kd, kt):
     t = NCU_TRAFFIC.get(kernel)
     if not t or kd["launches"] == 0:
@@ -398,6 +429,7 @@ def bench_batch(args, w, name, dist, rank, ws):
         tuning = autotune_batch(sh, precision=w["precision"], n=100_000, ring_capacity=1 << 24, use_cache=False,
                                 choose_loop=False)
     tally = eng.new_tally(n, zmax)
+    alu = alu_roofline() if rank == 0 and not args.quick else None
     for s in range(args.warmup):
         device_step(1000 + s, w["precision"], tally, stage(1000 + s))
     if args.quick:
@@ -504,7 +536,8 @@ def bench_batch(args, w, name, dist, rank, ws):
                      "kernels": kernels,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
                      "note": "issue-bound kernels (Philox, transcendental and table work per byte); "
-                             "HBM fraction of the algorithmic ring traffic"},
+                             "HBM fraction of the algorithmic ring traffic",
+                     "alu": alu},
         "cpu_baseline": cb,
         "clocks": clk.summary(),
         "particle_steps": steps_all,

@@ -62,8 +62,14 @@ def test_spectra_match_cpu_showers(cpu, name, precision):
     assert int(mult_g.sum()) == out["steps"]
     rows = []
     pvals = {}
-    for label, a, b in (("multiplicity", mult_g, mult_c), ("E_dep", edep_g, edep_c),
-                        ("E_dep - E0", edep_g - p0[:, 0], edep_c - cpu[f"{name}/E0"])):
+    # A shower's deposit is E0 plus the rest energy of the target electrons it
+    # sets in motion, so it sits on a comb of values 0.511 MeV apart; the
+    # float32 loss sums of the mixed form move it by ~1e-7 GeV, which a KS
+    # test would read as a shift of every atom.  Deposits are compared on a
+    # 10 keV grid, far below the comb's spacing.
+    q = lambda e: np.round(np.asarray(e) / 1e-5)
+    for label, a, b in (("multiplicity", mult_g, mult_c), ("E_dep", q(edep_g), q(edep_c)),
+                        ("E_dep - E0", q(edep_g - p0[:, 0]), q(edep_c - cpu[f"{name}/E0"]))):
         _, p = spectra.ks(a, b)
         pvals[label] = p
         ma, ea = spectra.mean_and_error(a)
