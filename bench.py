@@ -47,7 +47,8 @@ WORKLOADS = {
     # dark masses {0.01, 0.05, 0.1, 0.3} GeV (0.05: maps trained by
     # petite_gb300.train; PETITE ships the others)
     "dark_e10_graphite_1e5": dict(target="graphite", cut=0.010, n=100_000, species=(11,), emin=10.0, emax=10.0,
-                                  seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark"),
+                                  seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark",
+                                  dark_precision="mixed"),
     # 10^5 mu- at 400 GeV in lead, cut 0.010 GeV, seed 3 (the SM transport of
     # the 400 GeV muon configuration): tables with PETITE's data_400GeV cross
     # sections, its shipped maps and Brem/PairProd/MuonBrem maps trained by
@@ -70,10 +71,11 @@ WORKLOADS = {
     # go through the dark production, all masses on one run (mixed precision)
     "batchdark_e10_graphite_2e4": dict(target="graphite", cut=0.010, n=20_000, species=(11,), emin=10.0, emax=10.0,
                                        seed=0, masses=(0.01, 0.05, 0.1, 0.3), mode="batchdark", precision="mixed",
-                                       dark_processes=("DarkBrem", "DarkAnn", "DarkComp")),
+                                       dark_processes=("DarkBrem", "DarkAnn", "DarkComp"), dark_precision="mixed"),
     "batchdark_mu400_lead_1e3": dict(target="lead", cut=0.010, n=1000, species=(13,), emin=400.0, emax=400.0,
                                      seed=3, masses=(0.1,), mode="batchdark", precision="mixed", tables="400GeV",
-                                     dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem")),
+                                     dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"),
+                                     dark_precision="mixed"),
     # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
     # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
@@ -637,8 +639,9 @@ def bench_dark(args, w, name, dist, rank, ws):
     n = args.primaries or w["n"]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     procs = list(w.get("dark_processes", ("DarkBrem", "DarkAnn", "DarkComp")))
+    dprec = w.get("dark_precision", "fp64")
     showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
-                          active_processes=procs) for m in w["masses"]]
+                          active_processes=procs, dark_precision=dprec) for m in w["masses"]]
     sm = showers[0]
     chunk = min(w["chunk"], n)
 
@@ -681,18 +684,48 @@ def bench_dark(args, w, name, dist, rank, ws):
         return
     per_mass = {f"{d.get_mV()}": {"yield_per_primary": (ysum[k] / (n * args.steps)).tolist()}
                 for k, d in enumerate(showers)}
+    # the float64 form of the dark production on the same rows and streams
+    # (one chunk), against the form timed above
+    cmp64 = None
+    if dprec != "fp64":
+        p0, pid, mass = make_primaries(w, chunk, offset=block_index(0, rank, ws))
+        opts = sm._opts(True, "fp64")
+        opts.primary_offset = first_primary(0, rank, ws, n)
+        st, nr = sm._engine.run_sm(p0, np.zeros((chunk, 3)), pid, mass, np.ones(chunk), opts)
+        t64 = tx = 0.0
+        rel = []
+        for m_ in w["masses"]:
+            d64 = DarkShower(tables_dir(w), w["target"], w["cut"], m_, seed=w["seed"], device=dev,
+                             active_processes=procs, dark_precision="fp64")
+            dx = [d for d in showers if d.get_mV() == d64.get_mV()][0]
+            res = {}
+            for tag, d in (("fp64", d64), ("x", dx)):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                res[tag] = d._dark_engine.run_dark(d._prm, st, nr, d._opts(), keep_records=False)
+                torch.cuda.synchronize(dev)
+                if tag == "fp64":
+                    t64 += time.perf_counter() - t0
+                else:
+                    tx += time.perf_counter() - t0
+            y64, yx = res["fp64"]["yield"][:4], res["x"]["yield"][:4]
+            rel += [abs(a - b) / a for a, b in zip(y64, yx) if a > 0]
+        cmp64 = {"value": nr * len(w["masses"]) / t64, "unit": "row-masses/s", "sample_primaries": chunk,
+                 "dark_over_fp64": t64 / tx, "yield_max_rel_diff": max(rel) if rel else 0.0}
     cb = None if args.no_cpu_baseline else cpu_dark_baseline(w, **dark_cpu_sample(w))
     print(json.dumps({
         "metric": "dark-vector production: SM rows x dark masses per second (pt_run_dark)",
         "value": rows * len(showers) / t_dark, "unit": "row-masses/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * (t_sm + t_dark) / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if dprec == "mixed" else "f64",
+        "data": "synthetic",
         "config": {"workload": name, "primaries_per_step": n, "E0_GeV": w["emin"], "target": w["target"],
                    "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "chunk": chunk,
+                   "dark_precision": dprec,
                    "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
                    "tables": w.get("tables", "bundled")},
         "sm_rows": rows, "sm_rows_per_s": rows / t_sm, "vectors": vecs, "vectors_per_s": vecs / t_dark,
-        "yields": per_mass, "cpu_baseline": cb, "clocks": clk.summary()}))
+        "yields": per_mass, "fp64_dark": cmp64, "cpu_baseline": cb, "clocks": clk.summary()}))
 
 
 def bench_yield(args, w, name, dist, rank, ws):
@@ -753,8 +786,9 @@ def bench_batchdark(args, w, name, dist, rank, ws):
     n = args.primaries or w["n"]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     procs = list(w["dark_processes"])
+    dprec = w.get("dark_precision", "fp64")
     showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
-                          active_processes=procs) for m in w["masses"]]
+                          active_processes=procs, dark_precision=dprec) for m in w["masses"]]
     sh = showers[0]
     prms = [d._prm for d in showers]
 
@@ -801,6 +835,7 @@ def bench_batchdark(args, w, name, dist, rank, ws):
         "data": "synthetic",
         "config": {"workload": name, "primaries_per_step": n, "E0_GeV": w["emin"], "target": w["target"],
                    "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "precision": w["precision"],
+                   "dark_precision": dprec,
                    "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
                    "tables": w.get("tables", "bundled"), "timed": "host inputs in, yields out"},
         "row_masses_per_s": steps * len(showers) / t, "vectors": vecs, "vectors_per_s": vecs / t,
