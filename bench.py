@@ -107,13 +107,13 @@ BYTES_PER_STEP_RECORDS = 336
 
 
 # DRAM traffic per particle-step of each batched kernel, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum over every launch of the
-# kernel, divided by the run's particle-steps); the capture and its command
-# are summarised in the named profile.  The bench scales it to its own
-# launches by the particle-steps they process.
+# of one launch of each (dram__bytes_read.sum + dram__bytes_write.sum, caches
+# as the run leaves them, divided by that wave's particle-steps); the capture
+# and its command are summarised in the named profile.  The bench scales it
+# to its own launches by the particle-steps they process.
 NCU_TRAFFIC = {
-    "propagate": {"bytes_per_step": 64.36, "profile": "profiles/dram_traffic_lead_20k.md"},
-    "sample": {"bytes_per_step": 231.10, "profile": "profiles/dram_traffic_lead_20k.md"},
+    "propagate": {"bytes_per_step": 121.3, "profile": "profiles/batched_kernels_lead_20k.md"},
+    "sample": {"bytes_per_step": 122.7, "profile": "profiles/batched_kernels_lead_20k.md"},
 }
 
 
