@@ -18,6 +18,7 @@
 #include "pt_dark.cuh"
 #include "pt_internal.cuh"
 #include "pt_physics.cuh"
+#include "pt_physics32.cuh"
 
 using namespace pt;
 
@@ -346,7 +347,8 @@ __device__ void two_body_V(const DarkRow& r, double mV, Rng& rng, double* V) {
 // when the vector is known (v, in pf's frame), 2 when the map draw follows
 // (D set up for dark_propose).
 __device__ int bsm_begin(const Tabs& T, const pt_dark_maps& M, const pt_dark_params& P, const pt_opts& o,
-                         const DarkRow& r, int p, Rng& rng, double* pf, V4& v, DarkDraw& D) {
+                         const DarkRow& r, int p, Rng& rng, double* pf, V4& v, DarkDraw& D,
+                         const PhiloxRK* rk = nullptr) {
   for (int c = 0; c < 4; ++c) pf[c] = r.pf[c];
   int table = -1;
   if (p == PT_DARKANN && r.pid == -11) table = 2;
@@ -376,7 +378,25 @@ __device__ int bsm_begin(const Tabs& T, const pt_dark_maps& M, const pt_dark_par
     const double dEdx = T.t.dEdx_GeV_per_m;
     const double dist = ((S(E0) - S(E_int)) / S(dEdx)).v;
     double ps[4] = {r.p0[0], r.p0[1], r.p0[2], r.p0[3]};
-    mcs_apply(o.mcs_mode, ps, (S(T.t.rho) * (S(dist) / S(kCmToM))).v, T.t, o.rescale_MCS, kMe, rng);
+    const double tms = (S(T.t.rho) * (S(dist) / S(kCmToM))).v;
+    if (rk && o.mcs_mode == 0) {
+      // the float32 form (rk given): Lynch-Dahl scattering on the same four
+      // draws in float32 (as the mixed SM engine scatters), the momentum's
+      // magnitude kept in float64
+      const float fx = (float)ps[1], fy = (float)ps[2], fz = (float)ps[3], fE = (float)ps[0];
+      const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
+      if (pn > 0.f) {
+        float u4[4];
+        rng.take(u4, *rk);
+        float3 dir = make_float3(fx / pn, fy / pn, fz / pn);
+        mcs32_u(dir, pn * ((float)kMe / (float)r.mass), fE, (float)tms, (float)T.t.A, (float)T.t.Z,
+                (float)T.t.Z23, (float)o.rescale_MCS, u4[0], u4[2], u4[3], pn / fE);
+        const double pnd = norm3_np(ps[1], ps[2], ps[3]);
+        ps[1] = pnd * (double)dir.x; ps[2] = pnd * (double)dir.y; ps[3] = pnd * (double)dir.z;
+      }
+    } else {
+      mcs_apply(o.mcs_mode, ps, tms, T.t, o.rescale_MCS, kMe, rng);
+    }
     pf[0] = ps[0]; pf[1] = ps[1]; pf[2] = ps[2]; pf[3] = ps[3];
     lose_energy(pf, r.mass, (S(E0) - S(E_int)).v);
   }
@@ -645,7 +665,7 @@ __global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_m
         dark_emit(P, out, counter, status, r, row, p, wg, V, rng.n);
       } else {
         V4 v;
-        const int s = bsm_begin(T, M, P, o, r, p, rng, pf, v, D);
+        const int s = bsm_begin(T, M, P, o, r, p, rng, pf, v, D, PREC == 1 ? &rk : nullptr);
         if (s == 1) {
           const V4 lab = to_lab(rotation_from(pf), v);
           V[0] = lab.e; V[1] = lab.x; V[2] = lab.y; V[3] = lab.z;
@@ -655,7 +675,11 @@ __global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_m
       }
     }
     if (have) {
-      const int res = PREC == 1 ? dark_propose32(M, p, P.mV, D, rng, rk, x) : dark_propose(M, p, P.mV, D, rng, x);
+      // the float32 proposals serve the 3-D dark bremsstrahlung maps; the 1-D
+      // maps keep float64 (the radiative-return map crowds its nodes against
+      // u = 1, closer than float32 resolves)
+      const bool f32 = PREC == 1 && (p == PT_DARKBREM || p == PT_DARKMUONBREM);
+      const int res = f32 ? dark_propose32(M, p, P.mV, D, rng, rk, x) : dark_propose(M, p, P.mV, D, rng, x);
       if (res != 0) {
         have = false;
         V4 v;
