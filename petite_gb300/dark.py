@@ -23,6 +23,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import os
+import warnings
 
 import numpy as np
 
@@ -398,6 +399,17 @@ class DarkShower(Shower):
         # the dict_dir's own dark tables (PETITE reads its dark files from
         # dict_dir, dark_shower.py:69-130), else the bundled ones
         own = os.path.join(self.get_dict_dir(), "dark_tables.npz")
+        if not dark_tables and not os.path.exists(own):
+            pickles = [f for f in ("dark_maps.pkl", "dark_xsec.pkl", "dark_weights.pkl", "dark_drate.pkl")
+                       if os.path.exists(os.path.join(self.get_dict_dir(), f))]
+            if pickles and os.path.realpath(self.get_dict_dir()) != os.path.realpath(T.BUNDLED_DIR):
+                # PETITE's own dark pickles are not converted here: the
+                # weight, dR/dE and bound-electron tables they lead to are
+                # built by PETITE's DarkShower constructor
+                warnings.warn(f"DarkShower: {', '.join(pickles)} in {self.get_dict_dir()} are not read; the bundled "
+                              f"dark tables (PETITE's shipped maps and cross sections, maxima rebuilt with its "
+                              f"find_maxes) are used instead. Pass dark_tables=<path to a dark_tables.npz> to use "
+                              f"other tables.", stacklevel=2)
         self._dark = DarkData(dark_tables or (own if os.path.exists(own) else DARK_NPZ))
         self._mV_list = list(self._dark.masses)
         if mode == "exact":
