@@ -4,13 +4,16 @@ differentiable dark-vector yield.
 ``DarkShower`` keeps PETITE's constructor and methods (``GetBSMWeights``,
 ``draw_dark_sample``, ``produce_bsm_particle``, ``generate_dark_shower``);
 the dark-vector production runs in ``pt_run_dark`` over the SM particle
-rows.  Tables come from the dict_dir's ``dark_tables.npz`` (bundled:
-``data/dark_tables.npz``, and ``data/400GeV/dark_tables.npz`` for the
-400 GeV tables, mV = 0.1 GeV, five targets): the dark VEGAS maps (PETITE's shipped
-``<Process>/mV_*`` maps, or maps trained by ``petite_gb300.train`` where
-PETITE ships none, with max_F from find_maxes) and, per (mass, target), the
-weight, dR/dE and bound-electron tables PETITE's constructor builds
-(dark_shower.py:219-593).
+rows.  Tables come from the dict_dir, as PETITE reads them: its
+``dark_maps.pkl`` and ``dark_xsec.pkl`` (with the ``dark_weights.pkl`` and
+``dark_drate.pkl`` caches), from which ``petite_gb300.darktables`` builds
+the weight, dR/dE and bound-electron tables PETITE's constructor builds
+(dark_shower.py:219-593); or a ``dark_tables.npz`` bundle of the same
+content.  Bundled: ``data/dark_tables.npz`` (six masses, five targets), and
+``data/400GeV/dark_tables.npz`` for the 400 GeV tables (mV = 0.1 GeV, five
+targets): the dark VEGAS maps (PETITE's shipped ``<Process>/mV_*`` maps, or
+maps trained by ``petite_gb300.train`` where PETITE ships none, with max_F
+from find_maxes) and the constructor's tables.
 
 ``dark_yield`` is a ``torch.autograd.Function``: forward = the map estimate
 of a dark cross section and its V-energy moment at fixed Philox uniforms
@@ -59,14 +62,32 @@ def closest_lesser_value(input_list, input_value):
 
 
 class DarkData:
-    """Content of ``dark_tables.npz`` (all masses and targets)."""
+    """Content of ``dark_tables.npz`` (all masses and targets), or the same
+    content built from a PETITE dict_dir's dark pickles (``from_pickles``)."""
 
-    def __init__(self, path: str = DARK_NPZ):
-        if not os.path.exists(path):
-            raise FileNotFoundError(path)
-        self.z = np.load(path, allow_pickle=False)
+    def __init__(self, path: str = DARK_NPZ, content=None):
+        if content is None:
+            if not os.path.exists(path):
+                raise FileNotFoundError(path)
+            content = np.load(path, allow_pickle=False)
+        self.z = content
         self.masses = [float(m) for m in self.z["masses"]]
         self.targets = [str(t) for t in self.z["targets"]]
+
+    @classmethod
+    def from_pickles(cls, dict_dir: str, sm_for_target, Zeff: float = 29.508):
+        """``dark_maps.pkl`` + ``dark_xsec.pkl`` (+ the ``dark_weights.pkl`` and
+        ``dark_drate.pkl`` caches) of a PETITE dict_dir: maps up front, each
+        (mass, target)'s tables built on first use (``petite_gb300.darktables``)."""
+        from .darktables import PickleTables
+        return cls(content=PickleTables(dict_dir, sm_for_target, Zeff))
+
+    def use_mass(self, mV: float) -> None:
+        """The vector mass of the thresholds and bound-electron cross sections
+        of tables built from pickles (PETITE's ``_mV``, which differs from the
+        map mass in mode='approx'); the bundled tables are at the map mass."""
+        if hasattr(self.z, "mV_actual"):
+            self.z.mV_actual = float(mV)
 
     def maps_for(self, target: str, fudge: float):
         """Dense map arrays of every mass for one target (pt_dark_maps layout)."""
@@ -396,21 +417,27 @@ class DarkShower(Shower):
         self.bound_electron = bound_electron
         self.Zeff = Zeff
         self.g_e = kinetic_mixing * np.sqrt(4 * np.pi * T.ALPHA_EM) if g_e is None else g_e
-        # the dict_dir's own dark tables (PETITE reads its dark files from
-        # dict_dir, dark_shower.py:69-130), else the bundled ones
-        own = os.path.join(self.get_dict_dir(), "dark_tables.npz")
-        if not dark_tables and not os.path.exists(own):
-            pickles = [f for f in ("dark_maps.pkl", "dark_xsec.pkl", "dark_weights.pkl", "dark_drate.pkl")
-                       if os.path.exists(os.path.join(self.get_dict_dir(), f))]
-            if pickles and os.path.realpath(self.get_dict_dir()) != os.path.realpath(T.BUNDLED_DIR):
-                # PETITE's own dark pickles are not converted here: the
-                # weight, dR/dE and bound-electron tables they lead to are
-                # built by PETITE's DarkShower constructor
-                warnings.warn(f"DarkShower: {', '.join(pickles)} in {self.get_dict_dir()} are not read; the bundled "
-                              f"dark tables (PETITE's shipped maps and cross sections, maxima rebuilt with its "
-                              f"find_maxes) are used instead. Pass dark_tables=<path to a dark_tables.npz> to use "
-                              f"other tables.", stacklevel=2)
-        self._dark = DarkData(dark_tables or (own if os.path.exists(own) else DARK_NPZ))
+        # the dict_dir's dark files, as PETITE reads them (dark_shower.py:
+        # 69-130): a dark_tables.npz bundle, else PETITE's dark_maps.pkl and
+        # dark_xsec.pkl (tables built natively), else the bundled tables
+        ddir = self.get_dict_dir()
+        own = os.path.join(ddir, "dark_tables.npz")
+        pkl = [os.path.exists(os.path.join(ddir, f)) for f in ("dark_maps.pkl", "dark_xsec.pkl")]
+        if dark_tables:
+            self._dark = DarkData(dark_tables)
+        elif os.path.exists(own):
+            self._dark = DarkData(own)
+        elif all(pkl):
+            raw = self._raw
+            self._dark = DarkData.from_pickles(
+                ddir, lambda t: self.tables if t == target_material else T.SMTables(raw, t), Zeff)
+        else:
+            if any(pkl) and os.path.realpath(ddir) != os.path.realpath(T.BUNDLED_DIR):
+                have, miss = (", ".join(f for f, h in zip(("dark_maps.pkl", "dark_xsec.pkl"), pkl) if h is v)
+                              for v in (True, False))
+                warnings.warn(f"DarkShower: {ddir} has {have} but not {miss}; the bundled dark tables are used",
+                              stacklevel=2)
+            self._dark = DarkData(DARK_NPZ)
         self._mV_list = list(self._dark.masses)
         if mode == "exact":
             self._mV = closest_lesser_value(self._mV_list, mV_in_GeV)
@@ -420,6 +447,7 @@ class DarkShower(Shower):
             self._mV_estimator = closest_lesser_value(self._mV_list, mV_in_GeV)
         else:
             raise Exception("Mode not valid. Chose exact or approx.")
+        self._dark.use_mass(self._mV)
         self._coupling = self.g_e ** 2 / (4 * np.pi * T.ALPHA_EM)
         self._dark_engine = DarkEngine(self._engine, self._dark, target_material, maxF_fudge_global)
         if dark_precision not in ("fp64", "mixed"):
