@@ -44,10 +44,11 @@ WORKLOADS = {
     "sm_e1gev_graphite_1k": dict(target="graphite", cut=0.010, n=1000, species=(11,), emin=1.0, emax=1.0,
                                  seed=0, precision="fp64", fp64_sample=1000, cpu_sample=400, mode="records"),
     # dark vectors on SM showers: 10^5 e- at 10 GeV in graphite, cut 0.010 GeV,
-    # dark masses {0.01, 0.05, 0.1, 0.3} GeV (0.05: maps trained by
-    # petite_gb300.train; PETITE ships the others)
+    # dark masses {0.001, 0.01, 0.05, 0.1, 0.3} GeV (0.001 and 0.05: maps
+    # trained by petite_gb300.train; PETITE ships the others; no DarkAnn at
+    # 0.001, below 2 m_e)
     "dark_e10_graphite_1e5": dict(target="graphite", cut=0.010, n=100_000, species=(11,), emin=10.0, emax=10.0,
-                                  seed=0, masses=(0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark",
+                                  seed=0, masses=(0.001, 0.01, 0.05, 0.1, 0.3), chunk=10_000, mode="dark",
                                   dark_precision="mixed"),
     # 10^5 mu- at 400 GeV in lead, cut 0.010 GeV, seed 3 (the SM transport of
     # the 400 GeV muon configuration): tables with PETITE's data_400GeV cross
@@ -70,7 +71,8 @@ WORKLOADS = {
     # (pt_run_batch_dark): the showers are not stored, every wave's particles
     # go through the dark production, all masses on one run (mixed precision)
     "batchdark_e10_graphite_2e4": dict(target="graphite", cut=0.010, n=20_000, species=(11,), emin=10.0, emax=10.0,
-                                       seed=0, masses=(0.01, 0.05, 0.1, 0.3), mode="batchdark", precision="mixed",
+                                       seed=0, masses=(0.001, 0.01, 0.05, 0.1, 0.3), mode="batchdark",
+                                       precision="mixed",
                                        dark_processes=("DarkBrem", "DarkAnn", "DarkComp"), dark_precision="mixed"),
     "batchdark_mu400_lead_1e3": dict(target="lead", cut=0.010, n=1000, species=(13,), emin=400.0, emax=400.0,
                                      seed=3, masses=(0.1,), mode="batchdark", precision="mixed", tables="400GeV",
@@ -271,8 +273,10 @@ def cpu_dark_worker(args):
     for i in range(len(p0)):
         recs = sh.generate_shower(tuple(p0[i]), pid=int(pid[i]), mass=float(mass[i]), primary_index=first + i)
         t0 = time.perf_counter()
-        for orc in orcs:
-            vecs += len(orc.dark_shower(recs, processes=tuple(procs)))
+        for orc, mV in zip(orcs, masses):
+            # no DarkAnn below mV = 2 m_e (no resonance, no map set)
+            ps = tuple(p for p in procs if p != "DarkAnn" or mV >= 2 * D.P.m_electron)
+            vecs += len(orc.dark_shower(recs, processes=ps))
         t_dark += time.perf_counter() - t0
         rows += len(recs)
         if t_dark > budget:
@@ -635,13 +639,14 @@ def bench_dark(args, w, name, dist, rank, ws):
     """SM showers (float64 record engine) then dark-vector production for every
     mass on the same rows; a step is the whole batch of primaries."""
     import torch
-    from petite_gb300.dark import DarkShower
+    from petite_gb300.dark import DarkShower, processes_at_mass
     n = args.primaries or w["n"]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     procs = list(w.get("dark_processes", ("DarkBrem", "DarkAnn", "DarkComp")))
     dprec = w.get("dark_precision", "fp64")
     showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
-                          active_processes=procs, dark_precision=dprec) for m in w["masses"]]
+                          active_processes=processes_at_mass(procs, m), dark_precision=dprec)
+               for m in w["masses"]]
     sm = showers[0]
     chunk = min(w["chunk"], n)
 
@@ -740,15 +745,15 @@ def bench_yield(args, w, name, dist, rank, ws):
     n = args.primaries or w["n"]
     E = 10 ** rng.uniform(math.log10(0.05), 1.0, n)
     mVh = 10 ** rng.uniform(-3, math.log10(0.3), n)
-    mi = map_mass_index(eng.data.masses, mVh)
     Et = torch.as_tensor(E, device=dev)
     procs = ("DarkBrem", "DarkComp", "DarkAnn")
+    mi = {p: map_mass_index(eng.data.masses, mVh, eng.has_maps(p), p) for p in procs}
 
     def step():
         mV = torch.tensor(mVh, dtype=torch.float64, device=dev, requires_grad=True)
         loss = 0
         for p in procs:
-            Y, M = dark_yield(eng, p, Et, mV, n_samples=w["samples"], seed=w["seed"], mass_index=mi)
+            Y, M = dark_yield(eng, p, Et, mV, n_samples=w["samples"], seed=w["seed"], mass_index=mi[p])
             loss = loss + Y.sum() + 1e-3 * M.sum()
         loss.backward()
         return mV.grad
@@ -782,13 +787,14 @@ def bench_batchdark(args, w, name, dist, rank, ws):
     once (DarkShower.run_tallied, pt_run_batch_dark); a step is the batch of
     primaries, host inputs copied in and the yields read back inside it."""
     import torch
-    from petite_gb300.dark import DarkShower
+    from petite_gb300.dark import DarkShower, processes_at_mass
     n = args.primaries or w["n"]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     procs = list(w["dark_processes"])
     dprec = w.get("dark_precision", "fp64")
     showers = [DarkShower(tables_dir(w), w["target"], w["cut"], m, seed=w["seed"], device=dev,
-                          active_processes=procs, dark_precision=dprec) for m in w["masses"]]
+                          active_processes=processes_at_mass(procs, m), dark_precision=dprec)
+               for m in w["masses"]]
     sh = showers[0]
     prms = [d._prm for d in showers]
 

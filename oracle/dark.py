@@ -450,6 +450,8 @@ class DarkTables:
         self.coupling = g_e ** 2 / (4 * math.pi * P.alpha_em)
         self.maps = {}
         for p in DARK_PROCESSES:
+            if f"{key}/{p}/energy" not in z:         # no maps (DarkAnn below mV = 2 m_e)
+                continue
             E = z[f"{key}/{p}/energy"]
             grid, nn = z[f"{key}/{p}/grid"], z[f"{key}/{p}/nnodes"]
             self.maps[p] = [dict(E=float(E[i]), neval=int(z[f"{key}/{p}/neval"][i]),

@@ -764,7 +764,17 @@ __global__ void __launch_bounds__(kYieldThreads) k_dark_yield(pt_dark_maps M, in
   T mV;
   if constexpr (ADJ) mV = T{mVin[i], 1.0};
   else mV = mVin[i];
-  const int block = mass_index[i] * PT_N_DARK + p;
+  const int mi = mass_index[i];
+  const int block = mi * PT_N_DARK + p;
+  if (mi < 0 || mi >= M.n_masses || M.map_rows[block] < 2) {
+    // no maps for this process at this mass (DarkAnn below mV = 2 m_e): it
+    // makes no vectors, so its yield and moment are 0 (uniform per block)
+    if (threadIdx.x == 0) {
+      if constexpr (ADJ) g_mV[i] = 0.0;
+      else { yield[i] = 0.0; moment[i] = 0.0; }
+    }
+    return;
+  }
   const int key = dark_lu_key(M, block, E);
   const int r = M.map_base[block] + key;
   const int d = dark_dim(p);

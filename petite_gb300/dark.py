@@ -50,6 +50,13 @@ DARK_HIST_BINS = 60
 DARK_HIST_E = (1e-3, 1e3)
 
 
+def processes_at_mass(processes, mV: float):
+    """``processes`` without DarkAnn below mV = 2 m_e, where e+ e- -> V has
+    no resonance (its energy lies below the positron's rest mass) and no
+    map set exists."""
+    return [p for p in processes if p != "DarkAnn" or mV >= 2 * T.M_ELECTRON]
+
+
 def closest_lesser_value(input_list, input_value):
     """dark_shower.py:158-165 for values at or above the smallest mass."""
     arr = np.asarray(input_list, dtype=float)
@@ -101,6 +108,9 @@ class DarkData:
         for m, mv in enumerate(self.masses):
             for p, name in enumerate(DARK_PROCESSES):
                 pre = f"m{mv}/{name}"
+                if f"{pre}/energy" not in self.z:      # no maps (DarkAnn below mV = 2 m_e)
+                    base[m, p], rows[m, p] = n_rows, 0
+                    continue
                 E = self.z[f"{pre}/energy"]
                 grid, nn = self.z[f"{pre}/grid"], self.z[f"{pre}/nnodes"]
                 base[m, p], rows[m, p] = n_rows, len(E)
@@ -138,6 +148,8 @@ class DarkData:
             out[f"dr/{k}/nbins"] = z[f"{pre}/drate/{k}/nbins"].astype(np.int32)
         if not bound_electron:
             f = f"{pre}/free"
+            if f"{f}/xsec/DarkAnn" not in z:
+                raise Exception("Process String does not match library")     # dark_shower.py:210
             out["min_dark"] = z[f"{f}/min_dark"].astype(np.float64)
             out["xsec_DarkComp"] = z[f"{f}/xsec/DarkComp"]
             out["ann_E0"] = float(z[f"{f}/xsec/DarkAnn"][0, 0])
@@ -203,6 +215,11 @@ class DarkEngine:
             self.close()
         except Exception:
             pass
+
+    def has_maps(self, process: str):
+        """Per mass, whether ``process`` has a map set there."""
+        p = DARK_CODE[process]
+        return [self._M.map_rows[m * _lib.N_DARK + p] >= 2 for m in range(len(self.data.masses))]
 
     def mass_index(self, mV_est: float) -> int:
         return [abs(m - mV_est) < 1e-12 for m in self.data.masses].index(True)
@@ -448,6 +465,11 @@ class DarkShower(Shower):
         else:
             raise Exception("Mode not valid. Chose exact or approx.")
         self._dark.use_mass(self._mV)
+        for p in self.active_processes:
+            # set_dark_samples (dark_shower.py:181-202) loads a map set for
+            # every active dark process
+            if p in DARK_CODE and f"m{self._mV_estimator}/{p}/energy" not in self._dark.z:
+                raise Exception("Process String does not match library")
         self._coupling = self.g_e ** 2 / (4 * np.pi * T.ALPHA_EM)
         self._dark_engine = DarkEngine(self._engine, self._dark, target_material, maxF_fudge_global)
         if dark_precision not in ("fp64", "mixed"):
@@ -692,12 +714,28 @@ class _DarkYieldFn:
         return cls.fn
 
 
-def map_mass_index(masses, mV):
-    """Map block per pair: the shipped mass at or below mV (the smallest one
-    below the grid)."""
+def map_mass_index(masses, mV, has_maps=None, process=None):
+    """Map block per pair: the bundled mass at or below mV (the smallest one
+    below the grid).  With ``has_maps`` (per mass, whether ``process`` has
+    maps there) a mass without maps gives way to the nearest lower one with
+    maps, else the smallest with maps; DarkAnn below mV = 2 m_e, where it
+    makes no vectors, keeps a mass without DarkAnn maps if there is one, so
+    that its yield is 0."""
     m = np.asarray(masses)
-    idx = np.searchsorted(m, np.asarray(mV, np.float64), side="right") - 1
-    return np.clip(idx, 0, len(m) - 1).astype(np.int32)
+    mv = np.atleast_1d(np.asarray(mV, np.float64))
+    idx = np.clip(np.searchsorted(m, mv, side="right") - 1, 0, len(m) - 1).astype(np.int32)
+    if has_maps is None:
+        return idx
+    ok = np.asarray(has_maps, bool)
+    if not ok.any():
+        raise Exception("Process String does not match library")
+    lower = np.array([max([j for j in range(i + 1) if ok[j]], default=int(np.argmax(ok))) for i in range(len(m))],
+                     np.int32)
+    out = lower[idx]
+    if process == "DarkAnn" and not ok.all():
+        below = mv < 2 * T.M_ELECTRON
+        out[below] = int(np.argmin(ok))
+    return out
 
 
 def dark_yield(engine: DarkEngine, process: str, energy, mV, n_samples: int = 10_000, seed: int = 0,
@@ -713,7 +751,7 @@ def dark_yield(engine: DarkEngine, process: str, energy, mV, n_samples: int = 10
     energy = torch.as_tensor(energy, dtype=torch.float64, device=dev).contiguous()
     mV = torch.as_tensor(mV, dtype=torch.float64, device=dev)
     if mass_index is None:
-        mass_index = map_mass_index(engine.data.masses, mV.detach().cpu().numpy())
+        mass_index = map_mass_index(engine.data.masses, mV.detach().cpu().numpy(), engine.has_maps(process), process)
     mi = torch.as_tensor(np.asarray(mass_index, np.int32), device=dev).contiguous()
     if anchor is not None:
         a = torch.as_tensor(anchor, dtype=torch.float64, device=dev).contiguous()

@@ -298,12 +298,14 @@ class DarkTableBuilder:
         self.sm, self.target, self.mV, self.Zeff = sm, target, float(mV), float(Zeff)
         for p in DARK_PROCESSES:
             if p not in xsec:
+                if p == "DarkAnn":
+                    continue                 # no DarkAnn below mV = 2 m_e: the free-electron tables are left out
                 raise Exception("Process String does not match library")     # dark_shower.py:210
             if target not in xsec[p]:
                 raise Exception("Target Material is not in library")         # dark_shower.py:216
         self.DBS = _strip_zero_rows(xsec["DarkBrem"][target])
         self.DMBS = _strip_zero_rows(xsec["DarkMuonBrem"][target])
-        self.DAnnS_free = np.asarray(xsec["DarkAnn"][target], np.float64)
+        self.DAnnS_free = np.asarray(xsec["DarkAnn"][target], np.float64) if "DarkAnn" in xsec else None
         self.DCS_free = np.asarray(xsec["DarkComp"][target], np.float64)
         me = T.M_ELECTRON
         self.E_res = (self.mV ** 2 - 2 * me ** 2) / (2 * me)                 # dark_shower.py:232-233
@@ -320,7 +322,8 @@ class DarkTableBuilder:
         self.ns_brem = LogLog(self.DBS[:, 0], self.nZ * g * self.DBS[:, 1])
         self.ns_mubrem = LogLog(self.DMBS[:, 0], self.nZ * g * self.DMBS[:, 1])
         self.ns_ann_bound = LogLog(self.DAnnS_bound[:, 0], self.ne * g * self.DAnnS_bound[:, 1])
-        self.ns_ann_free = LogLog(self.DAnnS_free[:, 0], self.ne * g * self.DAnnS_free[:, 1], shift=self.E_res)
+        self.ns_ann_free = None if self.DAnnS_free is None else \
+            LogLog(self.DAnnS_free[:, 0], self.ne * g * self.DAnnS_free[:, 1], shift=self.E_res)
 
     def _bound_xsec(self, sigma, E_min, E_max):
         E = np.logspace(np.log10(E_min), np.log10(E_max), 200)
@@ -429,14 +432,16 @@ class DarkTableBuilder:
             Ei, bins, cnt = _pad_bins(self.drate(name, True))
             out[f"{pre}/drate/{name}/Ei"], out[f"{pre}/drate/{name}/bins"], out[f"{pre}/drate/{name}/nbins"] = \
                 Ei, bins, cnt
+        for k, v in self.interaction_integrals().items():
+            out[f"{self.target}/ii/{k}"] = v
+        if self.DAnnS_free is None:
+            return out
         f = f"{pre}/free"
         out[f"{f}/xsec/DarkAnn"], out[f"{f}/xsec/DarkComp"] = self.DAnnS_free, self.DCS_free
         out[f"{f}/weights/ann"] = self.weights("ann", False)
         Ei, bins, cnt = _pad_bins(self.drate("ann", False))
         out[f"{f}/drate/ann/Ei"], out[f"{f}/drate/ann/bins"], out[f"{f}/drate/ann/nbins"] = Ei, bins, cnt
         out[f"{f}/min_dark"] = self.min_dark(False)
-        for k, v in self.interaction_integrals().items():
-            out[f"{self.target}/ii/{k}"] = v
         return out
 
 
@@ -474,7 +479,7 @@ def maps_entries(maps: dict, targets) -> dict:
         mV = float(key)
         for p in DARK_PROCESSES:
             if p not in maps[key]:
-                raise Exception("Process String does not match library")
+                continue                     # a process without maps at this mass cannot be made active
             rows = maps[key][p]
             d = len(rows[0][1]["adaptive_map"].grid)
             nmax = max(len(g) for r in rows for g in r[1]["adaptive_map"].grid)
@@ -538,3 +543,37 @@ class PickleTables:
                     self._build(float(m), parts[0])
                     break
         return self._z[key]
+
+
+def bundle_mass(maps_npz: str, bundle: str, sm_npz: str, out: str | None = None) -> float:
+    """Adds one dark mass to a ``dark_tables.npz`` bundle, as PETITE's own
+    pipeline adds one once find_maxes has written its maps and cross
+    sections: the maps, max_F and find_maxes cross sections of
+    ``petite_gb300.train.build_dark_maps`` (``maps_npz``), and for every
+    target of the bundle the tables PETITE's constructor derives from them
+    (``DarkTableBuilder`` on the SM tables ``sm_npz``).  Returns the mass."""
+    z = dict(np.load(bundle, allow_pickle=False))
+    m = np.load(maps_npz, allow_pickle=False)
+    mt = [str(t) for t in m["targets"]]
+    bt = [str(t) for t in z["targets"]]
+    masses = sorted({float(k.split("/")[0][1:]) for k in m.files if k.startswith("m")})
+    if len(masses) != 1:
+        raise ValueError(f"{maps_npz} holds masses {masses}; one is expected")
+    mV = masses[0]
+    cols = [mt.index(t) for t in bt]
+    xsec = {}
+    for p in DARK_PROCESSES:
+        pre = f"m{mV}/{p}"
+        if f"{pre}/energy" not in m.files:
+            continue
+        E = m[f"{pre}/energy"]
+        xsec[p] = {t: np.column_stack((E, m[f"{pre}/xsec"][:, c])) for t, c in zip(bt, cols)}
+        z[f"{pre}/energy"], z[f"{pre}/neval"] = E, m[f"{pre}/neval"]
+        z[f"{pre}/max_F"] = m[f"{pre}/max_F"][:, cols]
+        z[f"{pre}/grid"], z[f"{pre}/nnodes"] = m[f"{pre}/grid"], m[f"{pre}/nnodes"]
+    raw = T.load_npz(sm_npz)
+    for t in bt:
+        z.update(DarkTableBuilder(T.SMTables(raw, t), xsec, t, mV).npz_entries(mV))
+    z["masses"] = np.array(sorted({float(v) for v in z["masses"]} | {mV}))
+    np.savez_compressed(out or bundle, **z)
+    return mV

@@ -301,7 +301,7 @@ def dark_energies(process: str, mV: float, E_min: float = 0.0016, E_max: float =
 
 def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int = 1 << 21, device="cuda",
                     targets=FIND_MAXES_TARGETS, log=print, E_max: float = 100.0, n_energies: int = 100,
-                    train_all: bool = False) -> dict:
+                    train_all: bool = False, processes=None) -> dict:
     """The dark maps of one mass for a PETITE dict_dir whose DarkBrem and
     DarkMuonBrem maps are not shipped (``data_400GeV``): shipped maps where
     they exist (DarkAnn, DarkComp), trained maps elsewhere at the energies of
@@ -314,12 +314,18 @@ def build_dark_maps(dict_dir: str, out_path: str, mV: float, points_per_row: int
     that ``dark_xsec.pkl`` lacks trains every process at the energies of
     ``dark_energies`` (up to E_max, n_energies rows), as PETITE's generation
     script would, and reports no ratio.  ``train_all`` trains shipped
-    processes too (to check the trainer against PETITE's rows)."""
+    processes too (to check the trainer against PETITE's rows).
+    ``processes`` defaults to all four, less DarkAnn below mV = 2 m_e: there
+    e+ e- -> V has no resonance (its energy (mV^2 - 2 m_e^2) / (2 m_e) lies
+    below the positron's rest mass) and PETITE's generation script has no
+    map energies for it."""
     with open(os.path.join(dict_dir, "dark_xsec.pkl"), "rb") as f:
         dx = pickle.load(f)
     keys = [k for k in dx if abs(float(k) - mV) < 1e-12]
     out, summary = {"targets": np.array(targets)}, {}
-    for proc in DARK_PROCESSES:
+    if processes is None:
+        processes = [p for p in DARK_PROCESSES if p != "DarkAnn" or mV >= 2 * T.M_ELECTRON]
+    for proc in processes:
         ref = np.asarray(dx[keys[0]][proc]["lead"], np.float64) if keys else None
         ship = os.path.join(dict_dir, proc, mass_dir(mV), f"{proc}_AdaptiveMaps.npy")
         if os.path.exists(ship) and not train_all:

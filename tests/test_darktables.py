@@ -4,6 +4,7 @@ tables PETITE's own DarkShower constructor made (the bundled
 from the constructed reference objects), and DarkShower's reading of a
 PETITE dict_dir's dark pickles (CPU only: no engine is made)."""
 import os
+import platform
 
 import numpy as np
 import pytest
@@ -20,6 +21,8 @@ SM400 = os.path.join(BUNDLED_DIR, "400GeV", "sm_tables.npz")
 # instead of integrating; the others were integrated by the constructor.
 CASES = [(B10, SM10, 0.003, "lead"), (B10, SM10, 0.01, "aluminum"), (B10, SM10, 0.1, "graphite"),
          (B10, SM10, 0.3, "molybdenum"), (B10, SM10, 0.05, "iron"), (B400, SM400, 0.1, "iron")]
+
+CANCELLING = ("xsec/DarkAnn_bound", "xsec/DarkComp_bound", "weights/ann", "drate/ann/bins")
 
 
 def _xsec_from_bundle(z, mV, t):
@@ -55,8 +58,17 @@ def test_builder_reproduces_petite_constructor_tables(bundle, smz, mV, target):
         assert v.shape == ref.shape, k
         if ref.dtype.kind in "iu":
             assert np.array_equal(v, ref), k
-        else:
+        elif platform.machine() == "x86_64":
+            # the machine family the bundled tables were made on
             np.testing.assert_allclose(v, ref, rtol=1e-12, atol=0, err_msg=k)
+        elif k.endswith(CANCELLING):
+            # PETITE's closed forms of the bound-electron cross sections
+            # cancel strongly where they are small, so a last-digit change of
+            # a libm function moves those entries; the others stay put
+            big = np.abs(ref) > 1e-9 * np.abs(ref).max()
+            np.testing.assert_allclose(v[big], ref[big], rtol=1e-6, atol=0, err_msg=k)
+        else:
+            np.testing.assert_allclose(v, ref, rtol=1e-9, atol=0, err_msg=k)
 
 
 def test_interaction_integrals_carry_quads_error():
@@ -174,3 +186,27 @@ def test_approx_mode_thresholds_use_the_actual_mass(pickle_dir):
     assert d["E_res"] == (0.02 ** 2 - 2 * me ** 2) / (2 * me)
     assert d["E_compth"] == 0.02 ** 2 / (2 * me) + 0.02
     np.testing.assert_allclose(d["min_dark"][2:4], [d["E_res"] / 1000.0, d["E_compth"] / 1000.0], rtol=0)
+
+
+def test_bundled_mass_below_two_electron_masses():
+    """mV = 0.001 GeV (trained maps, natively built tables): DarkBrem,
+    DarkComp and DarkMuonBrem maps on all five targets, no DarkAnn maps and
+    no free-electron tables (no resonance below 2 m_e); the device map
+    arrays give DarkAnn no rows there."""
+    from petite_gb300.dark import DarkData
+    d = DarkData(B10)
+    assert d.masses[0] == 0.001
+    z = d.z
+    for p in ("DarkBrem", "DarkComp", "DarkMuonBrem"):
+        assert len(z[f"m0.001/{p}/energy"]) == 100
+        assert np.isfinite(z[f"m0.001/{p}/max_F"]).all()
+    assert "m0.001/DarkAnn/energy" not in z
+    for t in d.targets:
+        assert f"m0.001/{t}/free/xsec/DarkAnn" not in z
+        w = z[f"m0.001/{t}/weights/brem_elec"]
+        assert (w[:, 1] >= 0).all() and w[-1, 1] > 0
+    mp = d.maps_for("graphite", 1.0)
+    assert mp["rows"][0, 1] == 0 and (mp["rows"][0, [0, 2, 3]] == 100).all()
+    with pytest.raises(Exception, match="Process String"):
+        d.params_for(0.001, "graphite", False)
+    assert d.params_for(0.001, "graphite", True)["E_res"] < 0.000511

@@ -159,10 +159,10 @@ def test_dark_yield_gradient_matches_finite_differences(showers):
     n = 4096
     E = 10 ** rng.uniform(math.log10(0.05), 1.0, n)
     mVh = 10 ** rng.uniform(-3, math.log10(0.3), n)
-    mi = map_mass_index(eng.data.masses, mVh)
     h = 1e-4 * mVh
     results = {}
     for proc in ("DarkBrem", "DarkComp", "DarkAnn"):
+        mi = map_mass_index(eng.data.masses, mVh, eng.has_maps(proc), proc)
         mV = torch.tensor(mVh, dtype=torch.float64, device=eng.device, requires_grad=True)
         Y, M = dark_yield(eng, proc, E, mV, n_samples=10_000, seed=SEED, mass_index=mi)
         (Y.sum()).backward()
@@ -221,15 +221,17 @@ def test_dark_yield_gradient_matches_fp64_reference(showers):
             assert abs(g[i] - ref) <= 1e-6 * abs(ref), (proc, E[i], mVh[i], g[i], ref)
 
 
-@pytest.mark.parametrize("mV,target", [(0.1, "graphite"), (0.03, "iron"), (0.3, "molybdenum"), (0.05, "lead")])
+@pytest.mark.parametrize("mV,target", [(0.1, "graphite"), (0.03, "iron"), (0.3, "molybdenum"), (0.05, "lead"),
+                                       (0.001, "graphite")])
 def test_dark_on_gpu_showers_matches_oracle(showers, mV, target):
     """SM showers from the GPU record engine, then pt_run_dark against the
-    oracle's produce_bsm_particle on the same rows and streams (10 GeV e-)."""
+    oracle's produce_bsm_particle on the same rows and streams (10 GeV e-).
+    mV = 0.001 GeV: maps trained here, tables built natively, no DarkAnn."""
     from oracle import dark as D
     from oracle.shower import OracleTables
-    from petite_gb300.dark import DarkShower
-    sh = showers.get((mV, target)) or DarkShower(None, target, 0.010, mV, seed=SEED, active_processes=[
-        "DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"])
+    from petite_gb300.dark import DarkShower, processes_at_mass
+    procs = processes_at_mass(["DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"], mV)
+    sh = showers.get((mV, target)) or DarkShower(None, target, 0.010, mV, seed=SEED, active_processes=procs)
     n = 4
     p = math.sqrt(100.0 - 0.000511 ** 2)
     opts = sh._opts(True, "fp64")
@@ -248,7 +250,7 @@ def test_dark_on_gpu_showers_matches_oracle(showers, mV, target):
         r.pid, r.mass, r.weight, r.pkey = int(rows["pid"][k]), float(rows["mass"][k]), 1.0, int(rows["pkey"][k])
         recs.append(r)
     orc = D.DarkOracle(D.DarkTables(DARK_NPZ, target, mV), OracleTables(BUNDLED_NPZ, target), SEED)
-    out = orc.dark_shower(recs, processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"))
+    out = orc.dark_shower(recs, processes=tuple(procs))
     want = np.array([[k, D.DARK_CODE[pp], w, *v] for k, pp, w, v, _ in out])
     want = want[np.lexsort((want[:, 1], want[:, 0]))]
     proc = res["process"] % 4
@@ -485,3 +487,25 @@ def test_dark_brem_float32_screen_accuracy(showers, mV, target):
         rel = np.abs(f32[val] / f64[val] - 1)
         print(name, mV, target, "valued", round(val.mean(), 3), "max rel", rel.max(), "p99.9", np.quantile(rel, 0.999))
         assert rel.max() < 1e-2, (name, rel.max())
+
+
+def test_no_dark_annihilation_below_two_electron_masses():
+    """mV = 0.001 GeV < 2 m_e: no DarkAnn map set, so an active DarkAnn is
+    refused as PETITE refuses a process without maps (dark_shower.py:
+    181-202), and the differentiable DarkAnn yield there is 0 with a 0
+    gradient; DarkBrem and DarkComp run on the trained maps."""
+    import torch
+    from petite_gb300.dark import DarkShower, dark_yield
+    with pytest.raises(Exception, match="Process String"):
+        DarkShower(None, "graphite", 0.010, 0.001, seed=SEED, active_processes=["DarkBrem", "DarkAnn"])
+    sh = DarkShower(None, "graphite", 0.010, 0.001, seed=SEED, active_processes=["DarkBrem", "DarkComp"])
+    eng = sh._dark_engine
+    E = np.array([0.5, 2.0, 8.0])
+    mV = torch.tensor([0.001, 0.0012, 0.002], dtype=torch.float64, device=eng.device, requires_grad=True)
+    Y, M = dark_yield(eng, "DarkAnn", E, mV, n_samples=500, seed=SEED)
+    (Y.sum() + M.sum()).backward()
+    assert Y.detach().cpu().numpy()[0] == 0.0 and M.detach().cpu().numpy()[0] == 0.0
+    assert mV.grad.cpu().numpy()[0] == 0.0
+    for proc in ("DarkBrem", "DarkComp"):
+        Y, M = dark_yield(eng, proc, E, mV.detach(), n_samples=500, seed=SEED)
+        assert (Y.cpu().numpy() > 0).all(), proc
