@@ -240,6 +240,13 @@ typedef struct pt_batch_tuning {
   int32_t threads;
   int32_t barrier_ns;             /* the persistent kernel's bound on one grid-barrier wait, ns (0 = 20 s);
                                      a wait that runs out returns PT_TIMEOUT.  For tests of that path. */
+  int32_t lanes;                  /* 0 or 1: one wave at a time.  2..8 (host loop only): the primaries
+                                     split into that many contiguous groups, each with its own ring,
+                                     task pools and CUDA stream, whose waves the host interleaves, so
+                                     that one group's kernels use the SMs another group's wave tail
+                                     leaves idle.  Every primary keeps its stream, so the showers and
+                                     integer tallies are those of one lane; each extra lane holds a ring
+                                     of queue_capacity entries. */
 } pt_batch_tuning;
 /* Stores the settings on the handle (NULL restores the defaults);
  * PT_BAD_ARG for a value out of range. */

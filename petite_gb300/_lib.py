@@ -118,7 +118,7 @@ TRAIN_DARK = 16
 
 class PtBatchTuning(C.Structure):
     _fields_ = [("refill_min", C.c_int32 * 2), ("chunk", C.c_int32 * 2), ("loop", C.c_int32), ("staging", C.c_int32),
-                ("threads", C.c_int32), ("barrier_ns", C.c_int32)]
+                ("threads", C.c_int32), ("barrier_ns", C.c_int32), ("lanes", C.c_int32)]
 
 
 class PetiteGPUError(RuntimeError):

@@ -21,6 +21,8 @@
 // as pt_run_sm, hence the same showers); PREC = 1 samples, scatters and
 // builds directions in float32 and keeps energies in float64.
 #include <algorithm>
+#include <chrono>
+#include <thread>
 #include <cstdio>
 #include <type_traits>
 
@@ -1197,9 +1199,20 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
   }
 }
 
+// A task of the cooperative finish: its index, process, proposals made and
+// next draw.
+struct CoopTask {
+  uint64_t i;
+  int64_t props;
+  uint64_t n;
+  int32_t process;
+};
+
 template <int PREC, int NW = kWarps> struct SampShared {
   unsigned long long off[9];
   KinEntry<PREC> kq[NW][kKinQ];
+  CoopTask cq[NW][32];
+  int cqh[NW][2];
 };
 
 template <int PREC, int NW>
@@ -1231,35 +1244,52 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
   const double* g64[4] = {nullptr, nullptr, nullptr, nullptr};
   int ninc[4] = {1, 1, 1, 1};
 
+  // Once the task pool is empty, a warp's remaining tasks are finished
+  // cooperatively, one at a time: the 32 lanes make proposals p..p+31 of one
+  // task at once (proposal j of a task reads draws n0 + j(d+1) .. of its
+  // stream, d + 1 per proposal), and the first accepted one in proposal
+  // order is the task's sample: the sequential loop's sample, found up to
+  // 32 times sooner.  A wave's tail is a few tasks with thousands of
+  // proposals (a muon's mu-e scattering at some energies), which the
+  // sequential loop runs on one lane each.
+  CoopTask* cq = sm.cq[threadIdx.x / 32];
+  int* cqh = sm.cqh[threadIdx.x / 32];  // the queue's length and head (shared: fewer live registers)
+  bool coop = false, drained = false;  // warp-uniform
   for (;;) {
     __syncwarp();
-    const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
-    const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
-    const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
-    const bool fresh = need && t >= 0;
-    if (__all_sync(kFull, !active && !fresh)) break;
-    int32_t chunk_ent = 0;
-    if (fresh) {
-      process = 0;
-      while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
-      chunk_ent = c.chunks[(int64_t)process * c.chunk_cap + ((t - (int64_t)sh_off[process]) >> 5)];
+    bool fresh = false;
+    if (!coop) {
+      const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
+      const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
+      const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
+      fresh = need && t >= 0;
+      drained = drained || __any_sync(kFull, need && t < 0);   // the pool is empty for the rest of the wave
+      if (__all_sync(kFull, !active && !fresh)) break;
+      int32_t chunk_ent = 0;
+      if (fresh) {
+        process = 0;
+        while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
+        chunk_ent = c.chunks[(int64_t)process * c.chunk_cap + ((t - (int64_t)sh_off[process]) >> 5)];
+      }
+      // a slot past a partly filled chunk's tasks holds no task: the lane asks again
+      fresh = fresh && (int)(t & 31) <= (chunk_ent & 31);
+      if (fresh) i = ((uint64_t)((uint32_t)chunk_ent >> 5) << 5) + (uint64_t)(t & 31);
+    } else {
+      const int h = cqh[1];
+      if (h >= cqh[0]) break;
+      i = cq[h].i;                     // every lane loads the queue head's task
+      process = cq[h].process;
+      fresh = true;
     }
-    // a slot past a partly filled chunk's tasks holds no task: the lane asks again
-    if (fresh && (int)(t & 31) <= (chunk_ent & 31)) {
-      i = ((uint64_t)((uint32_t)chunk_ent >> 5) << 5) + (uint64_t)(t & 31);
+    if (fresh) {
       E = c.park[i].E;
       row = c.park[i].row;
       rng.init(c.seed, c.park[i].key);
-      rng.n = c.park[i].draw;
-      if (rng.n & 1ull) {   // resume inside a Philox block: regenerate its second half
-        const uint64_t blk = rng.n >> 1;
-        const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), rng.k0, rng.k1), rng.s0, rng.s1);
-        rng.spare = (uint64_t)o.z | ((uint64_t)o.w << 32);
-      }
-      neval = T.t.map_neval[row];
       d = process_dim(process);
+      neval = T.t.map_neval[row];
       cap = c.max_n_integrators * (int64_t)neval;
-      props = 0;
+      props = coop ? cq[cqh[1]].props + lane : 0;
+      rng.seek(coop ? cq[cqh[1]].n + (uint64_t)lane * (uint64_t)(d + 1) : c.park[i].draw);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (k < d) {
@@ -1284,7 +1314,7 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
           default: muone32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
         }
       }
-      active = true;
+      active = !coop || props < cap;
     }
     bool accept = false;
     KinEntry<PREC> ent;
@@ -1328,18 +1358,43 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
         accept = ua < r;
         if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf(c.rk);
       }
-      ++props;
-      ++L.props;
-      if (accept) {
-        active = false;
-        ++L.sampled;
-      } else if (props >= cap) {
-        raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
-        active = false;
+      if (!coop) {
+        ++props;
+        ++L.props;
+        if (accept) {
+          active = false;
+          ++L.sampled;
+        } else if (props >= cap) {
+          raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
+          active = false;
+        }
       }
     }
+    unsigned am = __ballot_sync(kFull, accept);
+    if (coop) {
+      // the task's sample is its first accepted proposal
+      const int w = am ? __ffs(am) - 1 : 32;
+      accept = accept && lane == w;
+      active = false;
+      if (lane == 0) {
+        CoopTask& q = cq[cqh[1]];
+        const int64_t p0 = q.props;
+        L.props += (unsigned long long)(w < 32 ? (int64_t)w + 1 : (cap - p0 < 32 ? cap - p0 : 32));
+        if (w < 32) {
+          ++L.sampled;
+          ++cqh[1];
+        } else if (p0 + 32 >= cap) {
+          raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
+          ++cqh[1];
+        } else {
+          q.props = p0 + 32;
+          q.n += (uint64_t)32 * (uint64_t)(d + 1);
+        }
+      }
+      am = am ? (1u << w) : 0u;
+      __syncwarp();
+    }
     // ---- queue accepted proposals; run kinematics 32 at a time with all lanes
-    const unsigned am = __ballot_sync(kFull, accept);
     if (am) {
       if (accept) {
         ent.i = (uint32_t)i;
@@ -1359,6 +1414,22 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
         kcount = rest;
         __syncwarp();
       }
+    }
+    if (drained && !coop) {
+      // hand the warp's open tasks to its cooperative queue (measured: as
+      // soon as the pool is empty beats waiting for fewer open lanes)
+      const unsigned open = __ballot_sync(kFull, active);
+      if (active) {
+        CoopTask& q = cq[__popc(open & lanemask_lt())];
+        q.i = i;
+        q.process = process;
+        q.props = props;
+        q.n = rng.n;
+      }
+      active = false;
+      if (lane == 0) { cqh[0] = __popc(open); cqh[1] = 0; }
+      coop = true;
+      __syncwarp();
     }
   }
   if (kcount > 0) run_kinematics<PREC>(c, kq, kcount, opool, L);
@@ -1836,6 +1907,234 @@ static pt_status wave_rows(BatchScratch* S, pt_particles* r) {
   return PT_OK;
 }
 
+// PT_LOOP_HOST with pt_batch_tuning.lanes > 1: the primaries split into
+// `lanes` contiguous groups, each with its own ring, task pools and counters
+// (its own scratch) and its own CUDA stream.  Each lane runs the host loop's
+// waves; the host launches a lane's next wave as soon as its last one has
+// ended, so one lane's kernels take the SMs that another lane's wave tail
+// leaves idle (a deep shower's waves are small and end on a few long tasks).
+// Every primary keeps its index and stream, and the tallies are shared
+// (atomic adds), so the showers and integer tallies are those of one lane.
+// A row hook runs per lane over that lane's rows, the calls ordered on the
+// GPU through one event, since the hook's own scratch is shared.
+template <int PREC>
+static pt_status run_lanes(pt_handle* h, HandleParts& hp, int lanes, const WaveCtx<PREC>& c0, const void* kp,
+                           size_t smem_p, const void* ks, int rb_p, int rb_s, int wpb, const double* p0,
+                           const double* r0, const int32_t* pid, const double* mass, int64_t n, const pt_opts* o,
+                           cudaStream_t st, const WaveRowsHook* hook, int64_t ring_cap) {
+  struct Lane {
+    BatchScratch* S = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;        // after the wave's counter and status copies
+    WaveCtx<PREC> c;
+    int64_t first = 0, n = 0, fed = 0, k = 0, waves = 0, rows_used = 0, seq = 0;
+    uint64_t head = 0, tail = 0;
+    bool busy = false, over = false;
+    pt_particles rows_all{};
+  };
+  const int nt = wpb * 32;
+  if (lanes > n) lanes = (int)n;
+  Lane L[kMaxLanes];
+  cudaEvent_t start = nullptr, hook_ev = nullptr;
+  bool hook_used = false;
+  int64_t nl = 0, nw = 0, seq = 0;
+  pt_status rs = PT_OK;
+  hp.kernel_ms[0] = hp.kernel_ms[1] = 0.0;
+#define PT_L(call)                                                                          \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      fprintf(stderr, "petite_gpu: %s failed: %s\n", #call, cudaGetErrorString(e_));         \
+      rs = PT_CUDA_ERR;                                                                     \
+      goto drain;                                                                           \
+    }                                                                                       \
+  } while (0)
+#define PT_LS(expr)                                                                         \
+  do {                                                                                      \
+    const pt_status s_ = (expr);                                                            \
+    if (s_ != PT_OK) { rs = s_; goto drain; }                                               \
+  } while (0)
+  PT_L(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  PT_L(cudaEventCreateWithFlags(&hook_ev, cudaEventDisableTiming));
+  PT_L(cudaEventRecord(start, st));      // the inputs, tallies and status word are ready on st
+  for (int l = 0; l < lanes; ++l) {
+    Lane& a = L[l];
+    PT_LS(batch_lane_scratch_get(h, l, &a.S, ring_cap));
+    PT_L(cudaStreamCreateWithFlags(&a.s, cudaStreamNonBlocking));
+    PT_L(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+    PT_L(cudaStreamWaitEvent(a.s, start, 0));
+    a.first = n * l / lanes;
+    a.n = n * (l + 1) / lanes - a.first;
+    a.c = c0;
+    a.c.q = carve_ring<PREC>(a.S);
+    a.c.mask = (uint64_t)a.S->cap - 1;
+    a.c.list_cap = a.S->list_cap;
+    a.c.park = reinterpret_cast<Park<PREC>*>(a.S->park);
+    a.c.chunks = a.S->chunks;
+    a.c.chunk_cap = a.S->chunk_cap;
+    a.c.ctr = a.S->ctr;
+    a.c.cap = a.S->cap;
+    if (hook) PT_LS(wave_rows(a.S, &a.rows_all));
+  }
+  for (;;) {
+    bool launched = false, any_busy = false;
+    for (int l = 0; l < lanes; ++l) {
+      Lane& a = L[l];
+      if (a.over) continue;
+      if (a.busy) {
+        const cudaError_t q = cudaEventQuery(a.done);
+        if (q == cudaErrorNotReady) { any_busy = true; continue; }
+        PT_L(q);
+        a.busy = false;
+        if (*a.S->h_status != PT_OK) {
+          rs = (pt_status)*a.S->h_status;
+          if (rs == PT_NO_SAMPLE || rs == PT_TIMEOUT)
+            PT_L(cudaMemcpy(hp.last_info, hp.err_info, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+          goto drain;
+        }
+        float ms_p = 0.f, ms_s = 0.f;
+        PT_L(cudaEventElapsedTime(&ms_p, a.S->ev[0], a.S->ev[1]));
+        PT_L(cudaEventElapsedTime(&ms_s, a.S->ev[1], a.S->ev[2]));
+        hp.kernel_ms[0] += ms_p;
+        hp.kernel_ms[1] += ms_s;
+        a.head += (uint64_t)a.k;
+        a.tail += a.S->h_ctr[2];
+      }
+      if (a.fed >= a.n && a.tail == a.head) {           // this lane's showers are done
+        if (hook && a.rows_used > 0) {
+          if (hook_used) PT_L(cudaStreamWaitEvent(a.s, hook_ev, 0));
+          PT_LS(hook->fn(hook->ctx, &a.rows_all, a.rows_used, a.s));
+          PT_L(cudaEventRecord(hook_ev, a.s));
+          hook_used = true;
+          ++nl;
+          a.rows_used = 0;
+        }
+        a.over = true;
+        continue;
+      }
+      // the next wave of this lane: the host loop's feed and sizing
+      const int64_t cap = a.S->cap;
+      const int64_t feed_max = cap / 1024 > 256 ? cap / 1024 : 256;
+      int64_t live = (int64_t)(a.tail - a.head);
+      if (a.fed < a.n && live < cap / 8) {
+        int64_t m = a.n - a.fed;
+        if (m > cap / 8 - live) m = cap / 8 - live;
+        if (m > feed_max) m = feed_max;
+        k_feed<PREC><<<(unsigned)((m + 255) / 256), 256, 0, a.s>>>(a.c.q, a.c.mask, a.tail, p0, r0, pid, mass, n,
+                                                                  a.first + a.fed, m, o->primary_offset);
+        ++nl;
+        a.tail += (uint64_t)m;
+        a.fed += m;
+        live += m;
+      }
+      a.c.out_chunk = kOutChunk;
+      int64_t k = (cap - live - (int64_t)rb_s * wpb * kOutChunk) / 2;
+      if (k > live) k = live;
+      if (k > a.S->list_cap) k = a.S->list_cap;
+      if (k < 16 * 1024) {
+        a.c.out_chunk = 0;
+        k = (cap - live) / 2;
+        if (k > live) k = live;
+        if (k > a.S->list_cap) k = a.S->list_cap;
+      }
+      if (k <= 0) { rs = PT_OOM; goto drain; }
+      if (a.waves >= a.c.max_waves) {
+        hp.last_info[0] = -1; hp.last_info[1] = 0.0; hp.last_info[2] = 0;
+        rs = PT_TIMEOUT;
+        goto drain;
+      }
+      PT_L(cudaMemsetAsync(a.S->ctr, 0, 16 * sizeof(unsigned long long), a.s));
+      if (hook) {
+        if (a.rows_used + k > a.rows_all.capacity) {
+          if (hook_used) PT_L(cudaStreamWaitEvent(a.s, hook_ev, 0));
+          PT_LS(hook->fn(hook->ctx, &a.rows_all, a.rows_used, a.s));
+          PT_L(cudaEventRecord(hook_ev, a.s));
+          hook_used = true;
+          ++nl;
+          a.rows_used = 0;
+        }
+        a.c.rows = a.rows_all;
+        a.c.rows.p0 += a.rows_used; a.c.rows.pf += a.rows_used; a.c.rows.rf += a.rows_used;
+        a.c.rows.mass += a.rows_used; a.c.rows.weight += a.rows_used; a.c.rows.pid += a.rows_used;
+        a.c.rows.pkey += a.rows_used;
+      }
+      a.c.head = a.head;
+      a.c.tail = a.tail;
+      a.c.n_in = k;
+      a.k = k;
+      {
+        const int64_t want_blocks = (k + nt - 1) / nt;
+        const unsigned gp = (unsigned)(want_blocks < rb_p ? want_blocks : rb_p);
+        const unsigned gs = (unsigned)(want_blocks < rb_s ? want_blocks : rb_s);
+        void* args[] = {&a.c};
+        PT_L(cudaEventRecord(a.S->ev[0], a.s));
+        PT_L(cudaLaunchKernel(kp, dim3(gp), dim3(nt), args, smem_p, a.s));
+        PT_L(cudaEventRecord(a.S->ev[1], a.s));
+        PT_L(cudaLaunchKernel(ks, dim3(gs), dim3(nt), args, 0, a.s));
+        PT_L(cudaEventRecord(a.S->ev[2], a.s));
+      }
+      PT_L(cudaGetLastError());
+      a.rows_used += hook ? k : 0;
+      PT_L(cudaMemcpyAsync(a.S->h_ctr, a.S->ctr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, a.s));
+      PT_L(cudaMemcpyAsync(a.S->h_status, hp.status, sizeof(int), cudaMemcpyDeviceToHost, a.s));
+      PT_L(cudaEventRecord(a.done, a.s));
+      nl += 3;
+      ++nw;
+      ++a.waves;
+      a.busy = true;
+      a.seq = ++seq;
+      launched = any_busy = true;
+    }
+    if (!any_busy) break;                              // every lane is over
+    if (!launched) {
+      // poll until any lane's wave ends (blocking on one lane's event would
+      // hold back a lane whose wave ends first); a wave that runs far past
+      // any wave's length ends the wait on the oldest lane instead
+      const auto t0 = std::chrono::steady_clock::now();
+      for (bool ready = false; !ready;) {
+        for (int l = 0; l < lanes && !ready; ++l) {
+          if (!L[l].busy) continue;
+          const cudaError_t q = cudaEventQuery(L[l].done);
+          if (q != cudaErrorNotReady) { PT_L(q); ready = true; }
+        }
+        if (!ready && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(200)) {
+          int w = -1;
+          for (int l = 0; l < lanes; ++l)
+            if (L[l].busy && (w < 0 || L[l].seq < L[w].seq)) w = l;
+          PT_L(cudaEventSynchronize(L[w].done));
+          ready = true;
+        }
+        if (!ready) std::this_thread::yield();
+      }
+    }
+  }
+drain:
+  // every lane's work has ended before its stream goes; the caller's stream
+  // then follows the lanes
+  for (int l = 0; l < lanes; ++l) {
+    if (!L[l].s) continue;
+    if (cudaStreamSynchronize(L[l].s) != cudaSuccess && rs == PT_OK) rs = PT_CUDA_ERR;
+    if (L[l].done && cudaEventRecord(L[l].done, L[l].s) == cudaSuccess) cudaStreamWaitEvent(st, L[l].done, 0);
+  }
+  if (rs == PT_OK) {
+    int hs = PT_OK;
+    if (cudaMemcpy(&hs, hp.status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rs = PT_CUDA_ERR;
+    else rs = (pt_status)hs;
+  }
+  for (int l = 0; l < lanes; ++l) {
+    if (L[l].done) cudaEventDestroy(L[l].done);
+    if (L[l].s) cudaStreamDestroy(L[l].s);
+  }
+  if (start) cudaEventDestroy(start);
+  if (hook_ev) cudaEventDestroy(hook_ev);
+#undef PT_L
+#undef PT_LS
+  if (rs == PT_CUDA_ERR) cudaGetLastError();
+  hp.launches[0] = nl;
+  hp.launches[1] = nw;
+  return rs;
+}
+
 template <int PREC>
 static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0, const double* r0, const int32_t* pid,
                                 const double* mass, int64_t n, const pt_opts* o, pt_tally* tally, cudaStream_t st,
@@ -1897,6 +2196,9 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   if (!hook && tu[4] == PT_LOOP_GRAPH) return run_graph_loop<PREC>(hp, S, c, kp, smem_p, ks, wpb, rb_p, rb_s, st);
   if (!hook && tu[4] == PT_LOOP_PERSISTENT)
     return c.mcs_mode ? run_persistent<PREC, 1>(hp, S, c, st) : run_persistent<PREC, 0>(hp, S, c, st);
+  if (tu[8] > 1 && n > 1)
+    return run_lanes<PREC>(h, hp, tu[8], c, kp, smem_p, ks, rb_p, rb_s, wpb, p0, r0, pid, mass, n, o, st, hook,
+                           S->cap);
   const int64_t cap = S->cap;
   // A fed primary can grow to a few hundred live particles before its shower
   // thins out, so primaries enter in small increments while the ring is

@@ -92,6 +92,15 @@ struct Rng {
     ++n;
     return (uint64_t)o.x | ((uint64_t)o.y << 32);
   }
+  // Positions the stream at draw m (the odd half of a block is regenerated).
+  __device__ __forceinline__ void seek(uint64_t m) {
+    n = m;
+    if (m & 1ull) {
+      const uint64_t blk = m >> 1;
+      const uint4 o = philox4x32_10(make_uint4((uint32_t)blk, (uint32_t)(blk >> 32), k0, k1), s0, s1);
+      spare = (uint64_t)o.z | ((uint64_t)o.w << 32);
+    }
+  }
   __device__ __forceinline__ double u() { return (double)(next_u64() >> 11) * 0x1p-53; }
   // float form of the same draw (its top 24 bits); used by the float32 sampler.
   // Converted from a 32-bit integer: 64-bit conversions run on the FP64 pipe.

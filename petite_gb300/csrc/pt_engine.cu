@@ -286,13 +286,22 @@ struct pt_handle {
   double last_info[3] = {0, 0, 0};
   int64_t launches[2] = {0, 0};   // kernel launches, waves of the last run
   double kernel_ms[2] = {0, 0};   // batched run: propagation and sampler device time
-  int32_t tuning[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
+  int32_t tuning[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};   // pt_set_batch_tuning (0 = library default)
   BatchScratch* batch = nullptr;
+  BatchScratch* lane_batch[kMaxLanes] = {};   // lanes 1.. of a run with pt_batch_tuning.lanes > 1
 };
 
 pt_status batch_scratch_get(pt_handle* h, BatchScratch** out, int64_t ring_capacity) {
   pt_status s = batch_scratch_alloc(&h->batch, ring_capacity);
   *out = h->batch;
+  return s;
+}
+
+pt_status batch_lane_scratch_get(pt_handle* h, int lane, BatchScratch** out, int64_t ring_capacity) {
+  if (lane == 0) return batch_scratch_get(h, out, ring_capacity);
+  if (lane < 0 || lane >= kMaxLanes) return PT_BAD_ARG;
+  pt_status s = batch_scratch_alloc(&h->lane_batch[lane], ring_capacity);
+  *out = h->lane_batch[lane];
   return s;
 }
 
@@ -348,6 +357,7 @@ extern "C" pt_status pt_create(const pt_tables* t, pt_handle** out) {
 extern "C" void pt_destroy(pt_handle* h) {
   if (!h) return;
   batch_scratch_free(h->batch);
+  for (BatchScratch* b : h->lane_batch) batch_scratch_free(b);
   cudaFree(h->live[0]);
   cudaFree(h->live[1]);
   cudaFree(h->counters);
@@ -579,7 +589,7 @@ extern "C" pt_status pt_last_run_stats(pt_handle* h, int64_t* launches, int64_t*
 extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t) {
   if (!h) return PT_BAD_ARG;
   if (!t) {
-    for (int k = 0; k < 8; ++k) h->tuning[k] = 0;
+    for (int k = 0; k < 9; ++k) h->tuning[k] = 0;
     return PT_OK;
   }
   for (int k = 0; k < 2; ++k) {
@@ -590,6 +600,7 @@ extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t)
   if (t->staging < PT_STAGE_DEFAULT || t->staging > PT_STAGE_SHARED) return PT_BAD_ARG;
   if (t->threads != 0 && t->threads != 64 && t->threads != 128 && t->threads != 256) return PT_BAD_ARG;
   if (t->barrier_ns < 0) return PT_BAD_ARG;
+  if (t->lanes < 0 || t->lanes > kMaxLanes || (t->lanes > 1 && t->loop != PT_LOOP_HOST)) return PT_BAD_ARG;
   h->tuning[0] = t->refill_min[0];
   h->tuning[1] = t->refill_min[1];
   h->tuning[2] = t->chunk[0];
@@ -598,6 +609,7 @@ extern "C" pt_status pt_set_batch_tuning(pt_handle* h, const pt_batch_tuning* t)
   h->tuning[5] = t->staging;
   h->tuning[6] = t->threads;
   h->tuning[7] = t->barrier_ns;
+  h->tuning[8] = t->lanes;
   return PT_OK;
 }
 

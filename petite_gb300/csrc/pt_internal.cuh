@@ -7,7 +7,11 @@ struct pt_handle;
 struct BatchScratch;
 
 // Batched-engine scratch owned by a handle (allocated on first use).
+// Lanes of a batched run (pt_batch_tuning.lanes): lane 0 is the handle's
+// scratch, lanes 1.. their own, kept for the next run.
+constexpr int kMaxLanes = 8;
 pt_status batch_scratch_get(pt_handle* h, BatchScratch** out, int64_t ring_capacity);
+pt_status batch_lane_scratch_get(pt_handle* h, int lane, BatchScratch** out, int64_t ring_capacity);
 pt_status batch_scratch_alloc(BatchScratch** s, int64_t ring_capacity);
 void batch_scratch_free(BatchScratch* s);
 

@@ -306,7 +306,8 @@ class SMEngine:
     LOOPS = {"host": 0, "graph": 1, "persistent": 2}
     STAGING = {"default": 0, "cached": 1, "shared": 2}
 
-    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default", threads=0, barrier_ns=0):
+    def set_tuning(self, refill_min=(0, 0), chunk=(0, 0), loop="host", staging="default", threads=0, barrier_ns=0,
+                   lanes=0):
         """Work distribution of the batched engine (0 = library default), who
         runs its waves -- "host" (two launches per wave, counters read back),
         "graph" (a CUDA graph's conditional loop, planned on the GPU) or
@@ -315,7 +316,9 @@ class SMEngine:
         shared memory, filled by TMA bulk copies; "default"), or "cached"
         (the read-only data cache) -- and the mixed kernels' threads per block
         (64, 128 or 256; 0 = 128) -- and the persistent kernel's bound on a
-        grid-barrier wait in ns (0 = the library's 20 s)."""
+        grid-barrier wait in ns (0 = the library's 20 s) -- and, with the host
+        loop, the lanes: groups of primaries with their own rings and streams
+        whose waves interleave (0 or 1 = one; up to 8)."""
         t = _lib.PtBatchTuning()
         t.refill_min[0], t.refill_min[1] = int(refill_min[0]), int(refill_min[1])
         t.chunk[0], t.chunk[1] = int(chunk[0]), int(chunk[1])
@@ -323,9 +326,10 @@ class SMEngine:
         t.staging = self.STAGING[staging]
         t.threads = int(threads)
         t.barrier_ns = int(barrier_ns)
+        t.lanes = int(lanes)
         _lib.check(self.lib.pt_set_batch_tuning(self.handle, C.byref(t)), "pt_set_batch_tuning")
         self.tuning = {"refill_min": list(refill_min), "chunk": list(chunk), "loop": loop, "staging": staging,
-                       "threads": int(threads)}
+                       "threads": int(threads), "lanes": int(lanes)}
 
     def last_kernel_times(self):
         """Device seconds of the last batched run: (propagation, sampler)."""

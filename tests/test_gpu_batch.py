@@ -228,3 +228,39 @@ def test_device_planned_loop_in_bethe_mode():
     assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
     ha, hb = a.hist.cpu().numpy().astype(np.int64), b.hist.cpu().numpy().astype(np.int64)
     assert (np.abs(ha - hb).sum(axis=(1, 2)) <= 1e-5 * ha.sum(axis=(1, 2))).all()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("lanes", [2, 3, 8])
+def test_lanes_give_identical_results(lead, precision, lanes):
+    """pt_batch_tuning.lanes: the primaries split over lanes with their own
+    rings and streams whose waves interleave.  Every primary keeps its
+    stream, so the particles, spectra and deposits are one lane's; only the
+    summation order of the float64 deposits differs (and, through the
+    float32 loss sums' order, nothing else: the histograms are equal)."""
+    p0, pid, m = primaries(1500, seed=41, emax=50.0)
+    eng = lead._engine
+    a = run_batch(lead, p0, pid, m, precision, cap=1 << 16, offset=9)
+    eng.set_tuning((0, 0), (0, 0), "host", lanes=lanes)
+    try:
+        b = run_batch(lead, p0, pid, m, precision, cap=1 << 16, offset=9)
+        launches, waves = eng.last_run_stats()
+    finally:
+        eng.set_tuning((0, 0), (0, 0))
+    assert waves > 0
+    assert np.array_equal(a.primary_count.cpu().numpy(), b.primary_count.cpu().numpy())
+    assert np.array_equal(a.counts.cpu().numpy(), b.counts.cpu().numpy())
+    assert np.array_equal(a.hist.cpu().numpy(), b.hist.cpu().numpy())
+    np.testing.assert_allclose(a.primary_edep.cpu().numpy(), b.primary_edep.cpu().numpy(), rtol=1e-12)
+    np.testing.assert_allclose(a.energy.cpu().numpy(), b.energy.cpu().numpy(), rtol=1e-12)
+
+
+def test_lanes_need_the_host_loop(lead):
+    from petite_gb300 import _lib
+    eng = lead._engine
+    for loop in ("graph", "persistent"):
+        with pytest.raises(_lib.PetiteGPUError):
+            eng.set_tuning((0, 0), (0, 0), loop, lanes=2)
+    with pytest.raises(_lib.PetiteGPUError):
+        eng.set_tuning((0, 0), (0, 0), "host", lanes=9)
+    eng.set_tuning((0, 0), (0, 0))

@@ -126,3 +126,18 @@ def test_batch_ring_size_does_not_change_the_tallies(lead):
     ring: a ring of 2^10 entries gives the tallies of a ring of 2^22."""
     p0, pid, m = primaries(64, seed=24, emin=20.0, emax=100.0)
     same(batch(lead, p0, pid, m, cap=1 << 22), batch(lead, p0, pid, m, cap=1 << 10))
+
+
+def test_wave_bound_with_lanes(lead):
+    """The wave bound holds per lane, and the handle recovers."""
+    p0, pid, m = primaries(300, seed=23, emax=20.0)
+    ref = batch(lead, p0, pid, m)
+    lead._engine.set_tuning((0, 0), (0, 0), "host", lanes=3)
+    try:
+        with pytest.raises(_lib.PetiteGPUError) as e:
+            batch(lead, p0, pid, m, loop_limit=2)
+        assert e.value.status == _lib.PT_TIMEOUT
+        again = batch(lead, p0, pid, m)
+    finally:
+        lead._engine.set_tuning((0, 0), (0, 0))
+    same(ref, again)

@@ -509,3 +509,21 @@ def test_no_dark_annihilation_below_two_electron_masses():
     for proc in ("DarkBrem", "DarkComp"):
         Y, M = dark_yield(eng, proc, E, mV.detach(), n_samples=500, seed=SEED)
         assert (Y.cpu().numpy() > 0).all(), proc
+
+
+def test_batched_dark_with_lanes(showers):
+    """The batched dark run over three lanes (their own rings, streams and
+    rows; the dark production per lane, ordered on the GPU): the vectors
+    and yields of one lane."""
+    sh = showers[(0.1, "graphite")]
+    p0 = np.tile([10.0, 0.0, 0.0, math.sqrt(100.0 - 0.000511 ** 2)], (40, 1))
+    a = sh.run_tallied(p0, pid=11, mass=0.000511, precision="fp64", first_primary=0)
+    sh._engine.set_tuning((0, 0), (0, 0), "host", lanes=3)
+    try:
+        b = sh.run_tallied(p0, pid=11, mass=0.000511, precision="fp64", first_primary=0)
+    finally:
+        sh._engine.set_tuning((0, 0), (0, 0))
+    assert a["steps"] == b["steps"] and a["dark_vectors"] == b["dark_vectors"] > 100
+    for p in ("DarkBrem", "DarkAnn", "DarkComp"):
+        np.testing.assert_allclose(b["dark_yield"][p], a["dark_yield"][p], rtol=1e-9, atol=0)
+        np.testing.assert_allclose(b["dark_energy_hist"][p], a["dark_energy_hist"][p], rtol=1e-9, atol=1e-300)
