@@ -432,8 +432,12 @@ def bench_batch(args, w, name, dist, rank, ws):
         # (the loops are timed too: host waves, graph loop, persistent kernel;
         # the timed steps keep the host loop, whose per-kernel times the
         # roofline uses)
-        tuning = autotune_batch(sh, precision=w["precision"], n=100_000, ring_capacity=1 << 24, use_cache=False,
-                                choose_loop=False)
+        # calibration primaries drawn like the workload's (a deep muon line
+        # picks lanes, the broad mix one lane)
+        ncal = 500 if w["emin"] > 100.0 else 100_000
+        cal = make_primaries(w, ncal, offset=20_000_000)
+        tuning = autotune_batch(sh, precision=w["precision"], n=ncal, ring_capacity=1 << 24, use_cache=False,
+                                choose_loop=False, primaries=cal)
     tally = eng.new_tally(n, zmax)
     alu = alu_roofline() if rank == 0 and not args.quick else None
     for s in range(args.warmup):
@@ -797,6 +801,14 @@ def bench_batchdark(args, w, name, dist, rank, ws):
                for m in w["masses"]]
     sh = showers[0]
     prms = [d._prm for d in showers]
+    tuning = None
+    if not args.no_autotune:
+        # the SM engine's work distribution and lanes, calibrated on primaries
+        # drawn like the workload's (outside the timed region)
+        from petite_gb300.autotune import autotune_batch
+        ncal = min(n, 500 if w["emin"] > 100.0 else 20_000)
+        tuning = autotune_batch(sh, precision=w["precision"], n=ncal, ring_capacity=1 << 24, use_cache=False,
+                                choose_loop=False, primaries=make_primaries(w, ncal, offset=20_000_000))
 
     def step(s):
         p0, pid, mass = make_primaries(w, n, offset=block_index(s, rank, ws))
@@ -843,7 +855,8 @@ def bench_batchdark(args, w, name, dist, rank, ws):
                    "cut_GeV": w["cut"], "masses_GeV": [d.get_mV() for d in showers], "precision": w["precision"],
                    "dark_precision": dprec,
                    "processes": [p + "_bound" if p in ("DarkAnn", "DarkComp") else p for p in procs],
-                   "tables": w.get("tables", "bundled"), "timed": "host inputs in, yields out"},
+                   "tables": w.get("tables", "bundled"), "timed": "host inputs in, yields out",
+                   "tuning": tuning},
         "row_masses_per_s": steps * len(showers) / t, "vectors": vecs, "vectors_per_s": vecs / t,
         "yields": per_mass, "cpu_baseline": cb, "clocks": clk.summary()}))
 

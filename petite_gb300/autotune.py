@@ -7,9 +7,13 @@ the threads per block of the mixed kernels, where the mixed propagation
 kernel reads its cross-section tables (the
 read-only data cache, or shared memory staged by TMA bulk copies), and who
 runs the waves (the host, a CUDA graph's conditional loop, or one
-persistent kernel) -- by timing short calibration transports (CUDA events
-around the whole run on its stream) over a small grid, one coordinate at a
-time.
+persistent kernel), and with the host loop the lanes (groups of primaries
+with their own rings and streams whose waves interleave) -- by timing short
+calibration transports (CUDA events around the whole run on its stream)
+over a small grid, one coordinate at a time.  The calibration primaries
+are a mix of e-, e+ and photons at 0.1-100 GeV unless the caller passes
+primaries drawn like its workload (a deep muon line wants lanes, a broad
+mix does not).
 Results are cached in ``$XDG_CACHE_HOME/petite_gb300/tuning.json`` (or
 ``~/.cache/...``) keyed by device name, target and precision.
 """
@@ -22,9 +26,10 @@ import os
 import numpy as np
 
 GRID = {"refill_min": (4, 8, 12, 16), "chunk_propagate": (64, 128, 256), "chunk_sample": (32, 64, 128),
-        "threads": (64, 128, 256), "staging": ("cached", "shared"), "loop": ("host", "graph", "persistent")}
-DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host", "staging": "shared", "threads": 128}
-CACHE_VERSION = 4
+        "threads": (64, 128, 256), "staging": ("cached", "shared"), "loop": ("host", "graph", "persistent"),
+        "lanes": (1, 2, 4, 8)}
+DEFAULT = {"refill_min": (8, 8), "chunk": (128, 64), "loop": "host", "staging": "shared", "threads": 128, "lanes": 1}
+CACHE_VERSION = 5
 
 
 def _cache_path():
@@ -41,16 +46,19 @@ def _calibration_primaries(n, seed):
 
 
 def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
-                   verbose=False, choose_loop=True):
+                   verbose=False, choose_loop=True, primaries=None):
     """Tunes ``shower``'s engine and returns the chosen settings
-    ``{"refill_min": [p, s], "chunk": [p, s], "threads": b, "staging": g, "loop": l, "seconds": t,
-    "threads_seconds": {...}, "staging_seconds": {...}, "loop_seconds": {...}}`` (``*_seconds``: the
-    calibration run under each option, the earlier coordinates already
-    chosen).  ``choose_loop=False`` times the loops but keeps the host
-    loop, whose per-kernel event times a roofline needs."""
+    ``{"refill_min": [p, s], "chunk": [p, s], "threads": b, "staging": g, "loop": l, "lanes": k,
+    "seconds": t, "threads_seconds": {...}, "staging_seconds": {...}, "loop_seconds": {...},
+    "lanes_seconds": {...}}`` (``*_seconds``: the calibration run under each option, the earlier
+    coordinates already chosen).  ``choose_loop=False`` times the loops but keeps the host
+    loop, whose per-kernel event times a roofline needs.  ``primaries`` =
+    (p0 (n,4), pid, mass): calibrate on these instead of the mix (not cached)."""
     import torch
     eng = shower._engine
     key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}|v{CACHE_VERSION}"
+    if primaries is not None:
+        use_cache = False
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -62,10 +70,11 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     if use_cache and key in cache:
         best = cache[key]
         eng.set_tuning(best["refill_min"], best["chunk"], best.get("loop", "host"), best.get("staging", "default"),
-                       best.get("threads", 0))
+                       best.get("threads", 0), lanes=best.get("lanes", 1))
         return best
 
-    p0, pid, m = _calibration_primaries(n, seed)
+    p0, pid, m = _calibration_primaries(n, seed) if primaries is None else primaries
+    n = len(p0)
     dev = eng.device
     P0 = torch.as_tensor(np.ascontiguousarray(p0.T), device=dev)
     R0 = torch.zeros((3, n), dtype=torch.float64, device=dev)
@@ -77,7 +86,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
 
     def run(cfg):
         eng.set_tuning(cfg["refill_min"], cfg["chunk"], cfg["loop"], cfg["staging"],
-                       cfg["threads"] if precision == "mixed" else 0)
+                       cfg["threads"] if precision == "mixed" else 0, lanes=cfg["lanes"])
         opts = shower._opts(True, precision)
         tally.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -89,16 +98,18 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
         return a.elapsed_time(b) / 1e3
 
     cfg = {"refill_min": list(DEFAULT["refill_min"]), "chunk": list(DEFAULT["chunk"]), "loop": DEFAULT["loop"],
-           "staging": DEFAULT["staging"], "threads": DEFAULT["threads"]}
+           "staging": DEFAULT["staging"], "threads": DEFAULT["threads"], "lanes": DEFAULT["lanes"]}
     run(cfg)                                            # warm-up (scratch, caches)
     best_t = run(cfg)
-    seconds = {"threads": {}, "staging": {}, "loop": {}}
+    seconds = {"threads": {}, "staging": {}, "loop": {}, "lanes": {}}
     for name, values in GRID.items():
         if name in ("threads", "staging") and precision != "mixed":
             continue                                    # float32 kernels only
+        if name == "lanes" and cfg["loop"] != "host":
+            continue                                    # lanes are a form of the host loop
         for v in values:
             trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"],
-                     "staging": cfg["staging"], "threads": cfg["threads"]}
+                     "staging": cfg["staging"], "threads": cfg["threads"], "lanes": cfg["lanes"]}
             if name == "refill_min":
                 trial["refill_min"] = [v, v]
             elif name == "chunk_propagate":
@@ -111,6 +122,8 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
                 if name in seconds:
                     seconds[name][v] = best_t
                 continue
+            if name == "lanes":
+                run(trial)                              # a new lane's scratch is allocated on its first run
             t = run(trial)
             if name in seconds:
                 seconds[name][v] = t
@@ -118,14 +131,14 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
                     continue
             if verbose:
                 print("autotune", trial, round(t, 4))
-            if t < best_t * 0.99:                       # a change must beat noise
+            if t < best_t * 0.97:                       # a change must beat run-to-run noise (~1-2 %)
                 best_t, cfg = t, trial
     best = {"refill_min": cfg["refill_min"], "chunk": cfg["chunk"], "threads": cfg["threads"],
-            "staging": cfg["staging"], "loop": cfg["loop"], "seconds": best_t,
+            "staging": cfg["staging"], "loop": cfg["loop"], "lanes": cfg["lanes"], "seconds": best_t,
             "threads_seconds": seconds["threads"], "staging_seconds": seconds["staging"],
-            "loop_seconds": seconds["loop"]}
+            "loop_seconds": seconds["loop"], "lanes_seconds": seconds["lanes"]}
     eng.set_tuning(best["refill_min"], best["chunk"], best["loop"], best["staging"],
-                   best["threads"] if precision == "mixed" else 0)
+                   best["threads"] if precision == "mixed" else 0, lanes=best["lanes"])
     if use_cache:
         cache[key] = best
         try:

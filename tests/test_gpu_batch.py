@@ -132,7 +132,21 @@ def test_autotune_picks_valid_settings(lead):
     assert best["staging"] in GRID["staging"]
     assert best["threads"] in GRID["threads"]
     assert set(best["staging_seconds"]) == set(GRID["staging"])
+    assert best["lanes"] in GRID["lanes"]
+    assert best["lanes"] == 1 or best["loop"] == "host"
     assert best["seconds"] > 0
+    lead._engine.set_tuning((0, 0), (0, 0))
+
+
+def test_autotune_on_the_workloads_primaries(lead):
+    """Calibration on muons of the workload: lanes are timed with the host loop."""
+    from petite_gb300.autotune import GRID, autotune_batch
+    n = 40
+    p0 = np.tile([50.0, 0.0, 0.0, math.sqrt(2500.0 - 0.1056583755 ** 2)], (n, 1))
+    best = autotune_batch(lead, n=0, ring_capacity=1 << 18, choose_loop=False,
+                          primaries=(p0, np.full(n, 13, np.int32), np.full(n, 0.1056583755)))
+    assert best["loop"] == "host" and best["lanes"] in GRID["lanes"]
+    assert set(best["lanes_seconds"]) == set(GRID["lanes"])
     lead._engine.set_tuning((0, 0), (0, 0))
 
 
