@@ -1212,8 +1212,177 @@ template <int PREC, int NW = kWarps> struct SampShared {
   unsigned long long off[9];
   KinEntry<PREC> kq[NW][kKinQ];
   CoopTask cq[NW][32];
-  int cqh[NW][2];
 };
+
+// One task's sampling state, as a lane holds it.
+template <int PREC> struct SampTask {
+  int process = 0, d = 1, row = 0;
+  uint64_t i = 0;
+  int64_t props = 0, cap = 0;
+  double E = 0, maxF = 0, neval = 1;
+  Rng rng;
+  Samp32 S32;
+  const float4* g32[4] = {nullptr, nullptr, nullptr, nullptr};
+  const double* g64[4] = {nullptr, nullptr, nullptr, nullptr};
+  int ninc[4] = {1, 1, 1, 1};
+};
+
+// Loads task i of `process` (its parked record) and positions its stream at
+// draw n.
+template <int PREC>
+__device__ __forceinline__ void samp_load(const WaveCtx<PREC>& c, SampTask<PREC>& k, uint64_t i, int process,
+                                          uint64_t n) {
+  const Tabs& T = c.T;
+  k.i = i;
+  k.process = process;
+  k.E = c.park[i].E;
+  k.row = c.park[i].row;
+  k.rng.init(c.seed, c.park[i].key);
+  k.rng.seek(n);
+  k.neval = T.t.map_neval[k.row];
+  k.d = process_dim(process);
+  k.cap = c.max_n_integrators * (int64_t)k.neval;
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    if (m < k.d) {
+      const int64_t off = T.t.grid_offset[(int64_t)k.row * 4 + m];
+      k.ninc[m] = T.t.grid_ninc[(int64_t)k.row * 4 + m];
+      if (PREC == 0) k.g64[m] = T.t.grid_nodes + off;
+      else k.g32[m] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
+    }
+  }
+  if (PREC == 0) {
+    k.maxF = T.t.map_maxF[k.row];
+  } else {
+    const float Ef = (float)k.E, Cr = __ldg(T.t.map_cnorm32 + k.row), a0sq = (float)T.a0sq;
+    switch (process) {
+      case PT_BREM: brem32_setup(k.S32, Ef, (float)kMe, (float)T.t.Eg_min, a0sq, Cr); break;
+      case PT_MUONBREM: brem32_setup(k.S32, Ef, (float)kMmu, (float)T.t.Eg_min, a0sq, Cr); break;
+      case PT_PAIRPROD: pair32_setup(k.S32, Ef, a0sq, Cr); break;
+      case PT_COMP: comp32_setup(k.S32, Ef, Cr); break;
+      case PT_ANN: ann32_setup(k.S32, Ef, (float)T.t.Eg_min, Cr); break;
+      case PT_MOLLER: moller32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
+      case PT_BHABHA: bhabha32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
+      default: muone32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
+    }
+  }
+}
+
+// One proposal (d uniforms for y, then the accept uniform; on acceptance
+// the azimuth draw): true when accepted, with the sample in ent.
+template <int PREC>
+__device__ __forceinline__ bool samp_propose(const WaveCtx<PREC>& c, SampTask<PREC>& k, KinEntry<PREC>& ent) {
+  bool accept;
+  if constexpr (PREC == 0) {
+    double* xd = reinterpret_cast<KinEntry<0>&>(ent).x;
+    double jac = 1.0;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+      if (m < k.d) xd[m] = map_dim(k.g64[m], k.ninc[m], k.rng.u(), jac);
+    const double f = dsigma_any(c.T, k.process, xd, k.E);
+    accept = k.maxF * k.rng.u() < (jac / k.neval) * f;
+    if (accept) reinterpret_cast<KinEntry<0>&>(ent).ph = 2.0 * kPi * k.rng.u();
+  } else {
+    MapPt32* xm = reinterpret_cast<KinEntry<1>&>(ent).x;
+    float jac = 1.f;
+    float ua;                      // the accept draw
+    if (k.d == 4) {                // four y draws and the accept draw in three Philox blocks
+      float u5[5];
+      k.rng.take(u5, c.rk);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) xm[m] = map_dim32(k.g32[m], k.ninc[m], u5[m], jac);
+      ua = u5[4];
+    } else {
+      float u2[2];
+      k.rng.take(u2, c.rk);
+      xm[0] = map_dim32(k.g32[0], k.ninc[0], u2[0], jac);
+      ua = u2[1];
+    }
+    float r;
+    switch (k.process) {
+      case PT_BREM: case PT_MUONBREM: r = brem32_ratio(k.S32, xm, jac); break;
+      case PT_PAIRPROD: r = pair32_ratio(k.S32, xm, jac); break;
+      case PT_COMP: r = comp32_ratio(k.S32, xm[0], jac); break;
+      case PT_ANN: r = ann32_ratio(k.S32, xm[0], jac); break;
+      case PT_MOLLER: r = moller32_ratio(k.S32, xm[0], jac); break;
+      case PT_BHABHA: r = bhabha32_ratio(k.S32, xm[0], jac); break;
+      default: r = muone32_ratio(k.S32, xm[0], jac); break;
+    }
+    accept = ua < r;
+    if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * k.rng.uf(c.rk);
+  }
+  return accept;
+}
+
+// Queues one ballot's accepted proposals and runs their kinematics 32 at a
+// time with all lanes.
+template <int PREC>
+__device__ __forceinline__ void samp_queue(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int& kcount, unsigned am,
+                                           bool accept, const KinEntry<PREC>& ent, OutPool& opool, LocalTally& L) {
+  const int lane = threadIdx.x & 31;
+  if (!am) return;
+  if (accept) kq[kcount + __popc(am & lanemask_lt())] = ent;
+  kcount += __popc(am);
+  __syncwarp();
+  if (kcount >= 32) {
+    run_kinematics<PREC>(c, kq, 32, opool, L);
+    __syncwarp();
+    KinEntry<PREC> carry;
+    const int rest = kcount - 32;
+    if (lane < rest) carry = kq[32 + lane];
+    __syncwarp();
+    if (lane < rest) kq[lane] = carry;
+    kcount = rest;
+    __syncwarp();
+  }
+}
+
+// The cooperative finish of a warp's open tasks, once the pool is empty for
+// the rest of the wave: one task at a time, lane l makes proposal p + l of
+// it from draw n0 + l (d + 1) of its stream (every proposal takes d map
+// draws and one accept draw), and the first accepted proposal in proposal
+// order is the task's sample -- the sequential loop's sample, with its
+// proposal count, later draws and PT_NO_SAMPLE cap, found up to 32 times
+// sooner.  A wave ends on a few tasks with thousands of proposals (a
+// muon's mu-e scattering at some energies), which the lanes' own loops run
+// one lane each.  Not inlined: its registers are its own, so the main
+// loop's allocation stays as it was.
+template <int PREC>
+__device__ __noinline__ void samp_coop_finish(const WaveCtx<PREC>& c, CoopTask* cq, int n_open, KinEntry<PREC>* kq,
+                                              int& kcount, OutPool& opool, LocalTally& L) {
+  const int lane = threadIdx.x & 31;
+  SampTask<PREC> k;
+  for (int h = 0; h < n_open;) {
+    const CoopTask q = cq[h];
+    samp_load(c, k, q.i, q.process, q.n + (uint64_t)lane * (uint64_t)(process_dim(q.process) + 1));
+    KinEntry<PREC> ent;
+    const bool mine = q.props + lane < k.cap;
+    bool accept = mine && samp_propose(c, k, ent);
+    const unsigned am = __ballot_sync(kFull, accept);
+    const int w = am ? __ffs(am) - 1 : 32;
+    accept = accept && lane == w;
+    bool done = w < 32;
+    if (lane == 0) {
+      L.props += (unsigned long long)(w < 32 ? (int64_t)w + 1 : (k.cap - q.props < 32 ? k.cap - q.props : 32));
+      if (w < 32) {
+        ++L.sampled;
+      } else if (q.props + 32 >= k.cap) {
+        raise_status(c.status, c.err_info, PT_NO_SAMPLE, q.process, k.E, k.row - c.T.t.map_base[q.process]);
+      } else {
+        cq[h].props = q.props + 32;
+        cq[h].n = q.n + (uint64_t)32 * (uint64_t)(k.d + 1);
+      }
+    }
+    done = done || q.props + 32 >= k.cap;
+    __syncwarp();
+    if (accept) {
+      ent.i = (uint32_t)q.i;
+      ent.process = q.process;
+    }
+    samp_queue(c, kq, kcount, am ? (1u << w) : 0u, accept, ent, opool, L);
+    if (done) ++h;
+  }
+}
 
 template <int PREC, int NW>
 __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<PREC, NW>& sm) {
@@ -1228,210 +1397,65 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
   KinEntry<PREC>* kq = sh_kq[threadIdx.x / 32];
   int kcount = 0;                      // warp-uniform
   const int64_t total = (int64_t)sh_off[8];
-  const Tabs& T = c.T;
   const int lane = threadIdx.x & 31;
   LocalTally L;
   WarpPool pool;
   OutPool opool;
   bool active = false;
-  int process = 0, d = 1, row = 0;
-  uint64_t i = 0;
-  int64_t props = 0, cap = 0;
-  double E = 0, maxF = 0, neval = 1;
-  Rng rng;
-  Samp32 S32;
-  const float4* g32[4] = {nullptr, nullptr, nullptr, nullptr};
-  const double* g64[4] = {nullptr, nullptr, nullptr, nullptr};
-  int ninc[4] = {1, 1, 1, 1};
+  int n_open = 0;                      // tasks handed to the cooperative finish
+  SampTask<PREC> k;
 
-  // Once the task pool is empty, a warp's remaining tasks are finished
-  // cooperatively, one at a time: the 32 lanes make proposals p..p+31 of one
-  // task at once (proposal j of a task reads draws n0 + j(d+1) .. of its
-  // stream, d + 1 per proposal), and the first accepted one in proposal
-  // order is the task's sample: the sequential loop's sample, found up to
-  // 32 times sooner.  A wave's tail is a few tasks with thousands of
-  // proposals (a muon's mu-e scattering at some energies), which the
-  // sequential loop runs on one lane each.
-  CoopTask* cq = sm.cq[threadIdx.x / 32];
-  int* cqh = sm.cqh[threadIdx.x / 32];  // the queue's length and head (shared: fewer live registers)
-  bool coop = false, drained = false;  // warp-uniform
   for (;;) {
     __syncwarp();
-    bool fresh = false;
-    if (!coop) {
-      const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
-      const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
-      const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
-      fresh = need && t >= 0;
-      drained = drained || __any_sync(kFull, need && t < 0);   // the pool is empty for the rest of the wave
-      if (__all_sync(kFull, !active && !fresh)) break;
-      int32_t chunk_ent = 0;
-      if (fresh) {
-        process = 0;
-        while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
-        chunk_ent = c.chunks[(int64_t)process * c.chunk_cap + ((t - (int64_t)sh_off[process]) >> 5)];
-      }
-      // a slot past a partly filled chunk's tasks holds no task: the lane asks again
-      fresh = fresh && (int)(t & 31) <= (chunk_ent & 31);
-      if (fresh) i = ((uint64_t)((uint32_t)chunk_ent >> 5) << 5) + (uint64_t)(t & 31);
-    } else {
-      const int h = cqh[1];
-      if (h >= cqh[0]) break;
-      i = cq[h].i;                     // every lane loads the queue head's task
-      process = cq[h].process;
-      fresh = true;
-    }
+    const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
+    const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
+    const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
+    const bool fresh = need && t >= 0;
+    const bool drained = __any_sync(kFull, need && t < 0);   // the pool is empty for the rest of the wave
+    if (__all_sync(kFull, !active && !fresh)) break;
+    int32_t chunk_ent = 0;
+    int process = 0;
     if (fresh) {
-      E = c.park[i].E;
-      row = c.park[i].row;
-      rng.init(c.seed, c.park[i].key);
-      d = process_dim(process);
-      neval = T.t.map_neval[row];
-      cap = c.max_n_integrators * (int64_t)neval;
-      props = coop ? cq[cqh[1]].props + lane : 0;
-      rng.seek(coop ? cq[cqh[1]].n + (uint64_t)lane * (uint64_t)(d + 1) : c.park[i].draw);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k < d) {
-          const int64_t off = T.t.grid_offset[(int64_t)row * 4 + k];
-          ninc[k] = T.t.grid_ninc[(int64_t)row * 4 + k];
-          if (PREC == 0) g64[k] = T.t.grid_nodes + off;
-          else g32[k] = reinterpret_cast<const float4*>(T.t.grid_f32x4) + off;
-        }
-      }
-      if (PREC == 0) {
-        maxF = T.t.map_maxF[row];
-      } else {
-        const float Ef = (float)E, Cr = __ldg(T.t.map_cnorm32 + row), a0sq = (float)T.a0sq;
-        switch (process) {
-          case PT_BREM: brem32_setup(S32, Ef, (float)kMe, (float)T.t.Eg_min, a0sq, Cr); break;
-          case PT_MUONBREM: brem32_setup(S32, Ef, (float)kMmu, (float)T.t.Eg_min, a0sq, Cr); break;
-          case PT_PAIRPROD: pair32_setup(S32, Ef, a0sq, Cr); break;
-          case PT_COMP: comp32_setup(S32, Ef, Cr); break;
-          case PT_ANN: ann32_setup(S32, Ef, (float)T.t.Eg_min, Cr); break;
-          case PT_MOLLER: moller32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
-          case PT_BHABHA: bhabha32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
-          default: muone32_setup(S32, Ef, (float)T.t.Ee_min, Cr); break;
-        }
-      }
-      active = !coop || props < cap;
+      while (process < 7 && (unsigned long long)t >= sh_off[process + 1]) ++process;
+      chunk_ent = c.chunks[(int64_t)process * c.chunk_cap + ((t - (int64_t)sh_off[process]) >> 5)];
+    }
+    // a slot past a partly filled chunk's tasks holds no task: the lane asks again
+    if (fresh && (int)(t & 31) <= (chunk_ent & 31)) {
+      const uint64_t i = ((uint64_t)((uint32_t)chunk_ent >> 5) << 5) + (uint64_t)(t & 31);
+      samp_load(c, k, i, process, c.park[i].draw);
+      k.props = 0;
+      active = true;
     }
     bool accept = false;
     KinEntry<PREC> ent;
     if (active) {
-      // ---- one proposal (d uniforms for y, then the accept uniform)
-      if constexpr (PREC == 0) {
-        double* xd = reinterpret_cast<KinEntry<0>&>(ent).x;
-        double jac = 1.0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (k < d) xd[k] = map_dim(g64[k], ninc[k], rng.u(), jac);
-        const double f = dsigma_any(T, process, xd, E);
-        accept = maxF * rng.u() < (jac / neval) * f;
-        if (accept) reinterpret_cast<KinEntry<0>&>(ent).ph = 2.0 * kPi * rng.u();
-      } else {
-        MapPt32* xm = reinterpret_cast<KinEntry<1>&>(ent).x;
-        float jac = 1.f;
-        float ua;                      // the accept draw
-        if (d == 4) {                  // four y draws and the accept draw in three Philox blocks
-          float u5[5];
-          rng.take(u5, c.rk);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) xm[k] = map_dim32(g32[k], ninc[k], u5[k], jac);
-          ua = u5[4];
-        } else {
-          float u2[2];
-          rng.take(u2, c.rk);
-          xm[0] = map_dim32(g32[0], ninc[0], u2[0], jac);
-          ua = u2[1];
-        }
-        float r;
-        switch (process) {
-          case PT_BREM: case PT_MUONBREM: r = brem32_ratio(S32, xm, jac); break;
-          case PT_PAIRPROD: r = pair32_ratio(S32, xm, jac); break;
-          case PT_COMP: r = comp32_ratio(S32, xm[0], jac); break;
-          case PT_ANN: r = ann32_ratio(S32, xm[0], jac); break;
-          case PT_MOLLER: r = moller32_ratio(S32, xm[0], jac); break;
-          case PT_BHABHA: r = bhabha32_ratio(S32, xm[0], jac); break;
-          default: r = muone32_ratio(S32, xm[0], jac); break;
-        }
-        accept = ua < r;
-        if (accept) reinterpret_cast<KinEntry<1>&>(ent).ph = 2.f * (float)kPi * rng.uf(c.rk);
-      }
-      if (!coop) {
-        ++props;
-        ++L.props;
-        if (accept) {
-          active = false;
-          ++L.sampled;
-        } else if (props >= cap) {
-          raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
-          active = false;
-        }
-      }
-    }
-    unsigned am = __ballot_sync(kFull, accept);
-    if (coop) {
-      // the task's sample is its first accepted proposal
-      const int w = am ? __ffs(am) - 1 : 32;
-      accept = accept && lane == w;
-      active = false;
-      if (lane == 0) {
-        CoopTask& q = cq[cqh[1]];
-        const int64_t p0 = q.props;
-        L.props += (unsigned long long)(w < 32 ? (int64_t)w + 1 : (cap - p0 < 32 ? cap - p0 : 32));
-        if (w < 32) {
-          ++L.sampled;
-          ++cqh[1];
-        } else if (p0 + 32 >= cap) {
-          raise_status(c.status, c.err_info, PT_NO_SAMPLE, process, E, row - T.t.map_base[process]);
-          ++cqh[1];
-        } else {
-          q.props = p0 + 32;
-          q.n += (uint64_t)32 * (uint64_t)(d + 1);
-        }
-      }
-      am = am ? (1u << w) : 0u;
-      __syncwarp();
-    }
-    // ---- queue accepted proposals; run kinematics 32 at a time with all lanes
-    if (am) {
+      accept = samp_propose(c, k, ent);
+      ++k.props;
+      ++L.props;
       if (accept) {
-        ent.i = (uint32_t)i;
-        ent.process = process;
-        kq[kcount + __popc(am & lanemask_lt())] = ent;
-      }
-      kcount += __popc(am);
-      __syncwarp();
-      if (kcount >= 32) {
-        run_kinematics<PREC>(c, kq, 32, opool, L);
-        __syncwarp();
-        KinEntry<PREC> carry;
-        const int rest = kcount - 32;
-        if (lane < rest) carry = kq[32 + lane];
-        __syncwarp();
-        if (lane < rest) kq[lane] = carry;
-        kcount = rest;
-        __syncwarp();
+        active = false;
+        ++L.sampled;
+      } else if (k.props >= k.cap) {
+        raise_status(c.status, c.err_info, PT_NO_SAMPLE, k.process, k.E, k.row - c.T.t.map_base[k.process]);
+        active = false;
       }
     }
-    if (drained && !coop) {
-      // hand the warp's open tasks to its cooperative queue (measured: as
-      // soon as the pool is empty beats waiting for fewer open lanes)
+    if (accept) {
+      ent.i = (uint32_t)k.i;
+      ent.process = k.process;
+    }
+    samp_queue(c, kq, kcount, __ballot_sync(kFull, accept), accept, ent, opool, L);
+    if (drained) {
+      // hand the warp's open tasks to the cooperative finish
+      CoopTask* cq = sm.cq[threadIdx.x / 32];
       const unsigned open = __ballot_sync(kFull, active);
-      if (active) {
-        CoopTask& q = cq[__popc(open & lanemask_lt())];
-        q.i = i;
-        q.process = process;
-        q.props = props;
-        q.n = rng.n;
-      }
-      active = false;
-      if (lane == 0) { cqh[0] = __popc(open); cqh[1] = 0; }
-      coop = true;
+      if (active) cq[__popc(open & lanemask_lt())] = CoopTask{k.i, k.props, k.rng.n, k.process};
+      n_open = __popc(open);
       __syncwarp();
+      break;
     }
   }
+  if (n_open > 0) samp_coop_finish<PREC>(c, sm.cq[threadIdx.x / 32], n_open, kq, kcount, opool, L);
   if (kcount > 0) run_kinematics<PREC>(c, kq, kcount, opool, L);
   // unused slots of the warp's last output chunk become dead entries
   const uint64_t wave_tail = w_tail(c);
