@@ -705,7 +705,7 @@ def bench_dark(args, w, name, dist, rank, ws):
         rel = []
         for m_ in w["masses"]:
             d64 = DarkShower(tables_dir(w), w["target"], w["cut"], m_, seed=w["seed"], device=dev,
-                             active_processes=procs, dark_precision="fp64")
+                             active_processes=processes_at_mass(procs, m_), dark_precision="fp64")
             dx = [d for d in showers if d.get_mV() == d64.get_mV()][0]
             res = {}
             for tag, d in (("fp64", d64), ("x", dx)):
