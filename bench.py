@@ -114,8 +114,8 @@ BYTES_PER_STEP_RECORDS = 336
 # and its command are summarised in the named profile.  The bench scales it
 # to its own launches by the particle-steps they process.
 NCU_TRAFFIC = {
-    "propagate": {"bytes_per_step": 121.3, "profile": "profiles/batched_kernels_lead_20k.md"},
-    "sample": {"bytes_per_step": 122.7, "profile": "profiles/batched_kernels_lead_20k.md"},
+    "propagate": {"bytes_per_step": 96.0, "profile": "profiles/batched_kernels_lead_20k.md"},
+    "sample": {"bytes_per_step": 138.0, "profile": "profiles/batched_kernels_lead_20k.md"},
 }
 
 
@@ -126,10 +126,10 @@ NCU_TRAFFIC = {
 # active per executed instruction.  The bench divides the flop rates by the
 # FMA peaks it measures in the same run (pt_alu_peaks).
 NCU_ALU = {
-    "propagate": {"fp32_tflops": 3.815, "fp64_tflops": 0.0064, "issue_active": 0.520, "fp64_pipe": 0.181,
+    "propagate": {"fp32_tflops": 3.88, "fp64_tflops": 0.0065, "issue_active": 0.523, "fp64_pipe": 0.181,
                   "threads_per_inst": 19.6, "profile": "profiles/alu_batched_lead_20k.md"},
-    "sample": {"fp32_tflops": 2.015, "fp64_tflops": 0.0054, "issue_active": 0.536, "fp64_pipe": 0.071,
-               "threads_per_inst": 17.1, "profile": "profiles/alu_batched_lead_20k.md"},
+    "sample": {"fp32_tflops": 3.54, "fp64_tflops": 0.0098, "issue_active": 0.455, "fp64_pipe": 0.101,
+               "threads_per_inst": 21.7, "profile": "profiles/alu_batched_lead_20k.md"},
 }
 
 
