@@ -436,10 +436,11 @@ void pt_dark_destroy(pt_dark* d);
 pt_status pt_dark_dsigma(pt_dark* d, int32_t process, const double* x, const double* energy, int64_t n, double mV,
                          double* value, void* stream);
 
-/* The float32 estimate of the DarkBrem / DarkMuonBrem integrand that screens
- * the map's accept/reject decisions (no reference counterpart; diagnostic):
- * code[i] = 0 estimate not trusted (near a kinematic edge or a cancellation),
- * 1 value[i] holds it, 2 the point lies outside the allowed region. */
+/* The float32 estimate of the DarkBrem / DarkMuonBrem integrand, or of the
+ * DarkAnn (radiative-return) one, that screens the map's accept/reject
+ * decisions (no reference counterpart; diagnostic): code[i] = 0 estimate not
+ * trusted (near a kinematic edge or a cancellation), 1 value[i] holds it,
+ * 2 the point lies outside the allowed region (dark bremsstrahlung only). */
 pt_status pt_dark_screen32(pt_dark* d, int32_t process, const double* x, const double* energy, int64_t n, double mV,
                            float* value, int32_t* code, void* stream);
 

@@ -99,6 +99,7 @@ struct DarkDraw {
   int64_t made, limit;          // proposals made; max_n_integrators * neval
   float maxF32, inv_neval32;    // the float32 proposals' acceptance ratio
   Screen32K sk;                 // the float32 dark-brem screen's constants
+  Ann32K ak;                    // the float32 radiative-return screen's constants
 };
 
 __device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block, int p, double E, double mV,
@@ -118,6 +119,7 @@ __device__ __forceinline__ void dark_draw_begin(const pt_dark_maps& M, int block
     const double m = p == PT_DARKMUONBREM ? kMmu : kMe;
     D.sk = screen32_constants(E, mV, M.A, m, M.Z, M.A, (float)dark_brem_tconv(E, M.A, m));
   }
+  if (p == PT_DARKANN) D.ak = ann32_constants(E, mV);
 }
 
 // One proposal: 1 accepted (x holds it), 0 rejected, -1 the limit was
@@ -203,6 +205,29 @@ __device__ int dark_propose32(const pt_dark_maps& M, int p, double mV, DarkDraw&
   x[0] = xf[0]; x[1] = xf[1]; x[2] = xf[2];
   const double f = dark_dsigma<double>(M, p, x, D.E, mV);
   return D.maxF * (double)ua < (double)wgt * f ? 1 : 0;
+}
+
+// A DarkAnn proposal of the float32 dark form: the float64 draws and map
+// transform (the sample x is the float64 form's; the radiative-return map
+// crowds its nodes against u = 1 closer than float32 resolves), the
+// acceptance decided by the float32 screen when the accept draw lies more
+// than 0.2 % from its ratio, else by the float64 cross section: the float64
+// form's decisions and samples.
+__device__ int dark_propose_ann32(const pt_dark_maps& M, double mV, DarkDraw& D, Rng& rng, double* x) {
+  if (D.made >= D.limit) return -1;
+  double jac = 1.0;
+  x[0] = map_dim(M.grid_nodes + M.grid_offset[D.r * 4], M.grid_ninc[D.r * 4], rng.u(), jac);
+  const double wgt = jac / D.neval;
+  ++D.made;
+  const double u = rng.u();
+  float f32;
+  if (ann_screen32(x[0], D.ak, f32) == kScreenValue && D.maxF32 > 0.f) {
+    const float r = (float)wgt * f32 / D.maxF32, uf = (float)u;
+    if (uf > 1.002f * r) return 0;
+    if (uf < 0.998f * r) return 1;
+  }
+  const double f = dark_dsigma<double>(M, PT_DARKANN, x, D.E, mV);
+  return D.maxF * u < wgt * f ? 1 : 0;
 }
 
 // The whole loop; false when no sample was found.
@@ -425,8 +450,23 @@ __device__ int bsm_begin(const Tabs& T, const pt_dark_maps& M, const pt_dark_par
 // 104-183, 267-299 and draw_pe_sample, dark_shower.py:706-719), in the
 // frame of the parent's momentum (energy E0).  false: the reference's None
 // (draw_pe_sample's bounded loop ran out; PT_TIMEOUT is recorded).
+// draw_pe_sample's acceptance test, uu < wave(pe) / wave(lam / sqrt 3), in
+// float32: with t = pe / lam the ratio is (256/27) t^2 / (t^2 + 1)^4.  The
+// float32 form decides when the accept draw lies more than 1e-3 (relative)
+// from it -- far above its error, so the decision is the float64 one -- and
+// returns -1 otherwise.
+__device__ __forceinline__ int pe_accept32(uint64_t dx, uint64_t du, float inv_lam) {
+  const float xx = __uint2float_rn((uint32_t)(dx >> 40)) * 0x1p-24f * 1e-3f;
+  const float uu = __uint2float_rn((uint32_t)(du >> 40)) * 0x1p-24f;
+  const float t = xx * inv_lam, t2 = t * t, q = t2 + 1.f, q2 = q * q;
+  const float ratio = (256.f / 27.f) * t2 / (q2 * q2);
+  if (uu < 0.999f * ratio) return 1;
+  if (uu > 1.001f * ratio) return 0;
+  return -1;
+}
+
 __device__ bool bsm_finish(const pt_dark_params& P, const DarkRow& r, int p, double E0, const double* x, Rng& rng,
-                           double& wg, V4& v, int* status, double* info) {
+                           double& wg, V4& v, int* status, double* info, bool f32 = false) {
   const double mV = P.mV, me = kMe;
   const bool bound = P.bound_electron != 0;
   if (p == PT_DARKCOMP && bound) {
@@ -438,9 +478,16 @@ __device__ bool bsm_finish(const pt_dark_params& P, const DarkRow& r, int p, dou
     };
     const S c = wave(lam / S(sqrt(3.0)));
     double pe = -1.0;
+    const float inv_lam = 1.f / (float)lam.v;
     for (int it = 0; it < kMaxPeTrials; ++it) {
-      const S xx = S(0.0) + (S(1e-3) - S(0.0)) * S(rng.u());
-      const S uu = S(0.0) + (S(1.0) - S(0.0)) * S(rng.u());
+      // the draws as rng.u() takes them; the float32 form tests them in
+      // float32 first (pe_accept32) and in float64 only near the boundary
+      const uint64_t dx = rng.next_u64(), du = rng.next_u64();
+      const int a = f32 ? pe_accept32(dx, du, inv_lam) : -1;
+      const S xx = S(0.0) + (S(1e-3) - S(0.0)) * S((double)(dx >> 11) * 0x1p-53);
+      if (a == 1) { pe = xx.v; break; }
+      if (a == 0) continue;
+      const S uu = S(0.0) + (S(1.0) - S(0.0)) * S((double)(du >> 11) * 0x1p-53);
       if (uu.v < (wave(xx) / c).v) { pe = xx.v; break; }
     }
     if (pe < 0.0) { dark_raise(status, info, PT_TIMEOUT, p, E0, 0); return false; }
@@ -679,11 +726,13 @@ __global__ void __launch_bounds__(kDarkThreads) k_dark_produce(Tabs T, pt_dark_m
       // maps keep float64 (the radiative-return map crowds its nodes against
       // u = 1, closer than float32 resolves)
       const bool f32 = PREC == 1 && (p == PT_DARKBREM || p == PT_DARKMUONBREM);
-      const int res = f32 ? dark_propose32(M, p, P.mV, D, rng, rk, x) : dark_propose(M, p, P.mV, D, rng, x);
+      const int res = f32 ? dark_propose32(M, p, P.mV, D, rng, rk, x)
+                          : (PREC == 1 && p == PT_DARKANN) ? dark_propose_ann32(M, P.mV, D, rng, x)
+                                                           : dark_propose(M, p, P.mV, D, rng, x);
       if (res != 0) {
         have = false;
         V4 v;
-        if (res == 1 && bsm_finish(P, r, p, pf[0], x, rng, wg, v, status, info)) {
+        if (res == 1 && bsm_finish(P, r, p, pf[0], x, rng, wg, v, status, info, PREC == 1)) {
           const V4 lab = to_lab(rotation_from(pf), v);
           const double V[4] = {lab.e, lab.x, lab.y, lab.z};
           dark_emit(P, out, counter, status, r, row, p, wg, V, rng.n);
@@ -715,9 +764,13 @@ __global__ void k_dark_screen(pt_dark_maps M, int p, const double* x, const doub
   if (i >= n) return;
   double xx[4];
   for (int k = 0; k < 4; ++k) xx[k] = x[i * 4 + k];
-  const double mlep = p == PT_DARKMUONBREM ? kMmu : kMe;
   float f = 0.f;
-  code[i] = dark_brem_screen32(xx, E[i], mV, M.A, mlep, M.Z, M.A, (float)dark_brem_tconv(E[i], M.A, mlep), f);
+  if (p == PT_DARKANN) {
+    code[i] = ann_screen32(xx[0], ann32_constants(E[i], mV), f);
+  } else {
+    const double mlep = p == PT_DARKMUONBREM ? kMmu : kMe;
+    code[i] = dark_brem_screen32(xx, E[i], mV, M.A, mlep, M.Z, M.A, (float)dark_brem_tconv(E[i], M.A, mlep), f);
+  }
   value[i] = f;
 }
 
@@ -947,7 +1000,8 @@ extern "C" pt_status pt_dark_dsigma(pt_dark* d, int32_t process, const double* x
 
 extern "C" pt_status pt_dark_screen32(pt_dark* d, int32_t process, const double* x, const double* energy, int64_t n,
                                       double mV, float* value, int32_t* code, void* stream) {
-  if (!d || (process != PT_DARKBREM && process != PT_DARKMUONBREM) || n < 0) return PT_BAD_ARG;
+  if (!d || (process != PT_DARKBREM && process != PT_DARKMUONBREM && process != PT_DARKANN) || n < 0)
+    return PT_BAD_ARG;
   if (n == 0) return PT_OK;
   if (!x || !energy || !value || !code) return PT_BAD_ARG;
   cudaStream_t st = (cudaStream_t)stream;

@@ -409,6 +409,66 @@ __device__ T dsig_radiative_return(double u0, double Ee, T mV) {
   return 2.0 * prefac * lumi;
 }
 
+// The float32 screen of the radiative-return cross section (the float32
+// dark form's DarkAnn proposals).  Per task, in float64 once: y = mV^2/s,
+// beta, and the constant factor 2 prefac (beta/16)^2 (2/beta) of
+// dsig_radiative_return.  Per proposal, in float32, with q = u0^(2/beta):
+// x1 = y + (1 - y)(1 - q) (= 1 - (u0 umax)^(2/beta), without the
+// cancellation), x2 = y/x1, 1 - x2 = (1 - y)(1 - q)/x1 (the factored form),
+// and the two luminosity factors.  Both factors are positive and free of
+// cancellation (fl_kf >= 4, fl_kf_scaled >= 4), and the powers' relative
+// error is ~|log| x 1e-7, so the estimate is within ~1e-5 of the float64
+// value: measured within 4e-4 of the float64 form (whose own rounding makes
+// up that difference) on map samples at every tabulated energy.
+struct Ann32K {
+  float y, omy, beta, tob, c8, bh, bk, K;
+  int valid;           // s >= mV^2 and a finite constant
+};
+
+__device__ __forceinline__ Ann32K ann32_constants(double Ee, double mV) {
+  Ann32K k{};
+  const double me = kMe, s = 2.0 * me * (Ee + me), mV2 = mV * mV;
+  k.valid = 0;
+  if (!(s >= mV2) || !(mV2 > 4.0 * me * me)) return k;
+  const double beta = kf_beta(s);
+  const double umax = pow(1.0 - mV2 / s, beta / 2.0);
+  const double betaf = sqrt(1.0 - 4.0 * (me * me) / mV2);
+  const double prefac = (4.0 * (kPi * kPi)) * kAlpha * betaf * (3.0 / 2.0 - betaf * betaf / 2.0) / s * umax;
+  const double K = 2.0 * prefac * (beta / 16.) * (beta / 16.) * (2. / beta);
+  k.y = (float)(mV2 / s);
+  k.omy = (float)(1.0 - mV2 / s);
+  k.beta = (float)beta;
+  k.tob = (float)(2.0 / beta);
+  k.c8 = (float)(8. + 3. * beta);
+  k.bh = (float)(beta / 2. - 1.);
+  k.bk = (float)(1. - beta / 2.);
+  k.K = (float)K;
+  k.valid = (beta > 0.0 && K > 0.0 && K < 1e30) ? 1 : 0;
+  return k;
+}
+
+__device__ __forceinline__ int ann_screen32(double u0d, const Ann32K& k, float& out) {
+  out = 0.f;
+  const float u0 = (float)u0d, om = (float)(1.0 - u0d);     // 1 - u0 from float64: u0 sits near 1
+  if (!k.valid || !(u0 > 0.f) || !(om > 0.f)) return kScreenUnsure;
+  const float lq = k.tob * (u0 < 0.5f ? logf(u0) : log1pf(-om));
+  const float q = expf(lq), omq = -expm1f(lq);
+  const float d = k.omy * omq;                               // x1 - y
+  // the float64 form's x1 = 1 - omx1 carries ~1e-16 of rounding, which
+  // 1 - x2 = (x1 - y)/x1 magnifies by 1/(x1 - y): below 1e-11 float64 decides
+  if (!(d > 1e-11f)) return kScreenUnsure;
+  // omx1 may underflow to 0 (u0^(2/beta) below 1e-38): the float64 form's
+  // 1 - x1 is then 0 as well, and the term it scales drops out of both
+  const float omx1 = k.omy * q;
+  const float x1 = d + k.y;
+  const float x2 = k.y / x1;
+  const float omx2 = d / x1;
+  const float fy = k.c8 * powf(omx2, k.bh) - 4.f * (1.f + x2);
+  const float fks = k.c8 - 4.f * (1.f + x1) * powf(omx1, k.bk);
+  out = k.K * fy * fks / x1;
+  return (out > 0.f && out < 3.0e38f) ? kScreenValue : kScreenUnsure;
+}
+
 // ------------------------------------------------ energies of the dark vector
 // Lab energy of V for the yield moments: x*E (kinematics.py:57), the Compton
 // form (kinematics.py:119-130) and the boosted radiative-return form
