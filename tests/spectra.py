@@ -139,6 +139,20 @@ def ks(a, b):
     return float(r.statistic), float(r.pvalue)
 
 
+def chi2_binned(a, b, nbins=20):
+    """Two-sample binned chi^2 (homogeneity of the two histograms), bins at
+    quantiles of the pooled sample: (statistic, dof, p)."""
+    from scipy import stats
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    edges = np.unique(np.quantile(np.concatenate([a, b]), np.linspace(0, 1, nbins + 1)))
+    edges[-1] = np.nextafter(edges[-1], np.inf)
+    ha, _ = np.histogram(a, edges)
+    hb, _ = np.histogram(b, edges)
+    keep = (ha + hb) > 0
+    stat, p, dof, _ = stats.chi2_contingency(np.vstack([ha[keep], hb[keep]]))
+    return float(stat), int(dof), float(p)
+
+
 def mean_and_error(x):
     x = np.asarray(x, np.float64)
     return float(x.mean()), float(x.std(ddof=1) / math.sqrt(len(x)))

@@ -8,7 +8,8 @@ streams: another Philox seed, and ten GPU showers of each CPU primary on
 stream indices of their own.  For each workload and both engine forms
 (float64, and float32 sampling with float64 kinematics) the test compares:
 
-* per-shower particle count and deposited energy: two-sample KS;
+* per-shower particle count and deposited energy: two-sample KS and a
+  binned chi^2 (20 bins at quantiles of the pooled sample);
 * creation energy, polar angle and interaction depth per species: the
   per-shower mean histograms, by Hotelling's T^2 of the paired difference
   (``tests/spectra.py:hotelling_paired``), since the particles of one shower
@@ -75,6 +76,9 @@ def test_spectra_match_cpu_showers(cpu, name, precision):
         ma, ea = spectra.mean_and_error(a)
         mb, eb = spectra.mean_and_error(b)
         rows.append((label, ma, mb, (ma - mb) / np.hypot(ea, eb), "KS", p))
+        c2, dof, pc = spectra.chi2_binned(a, b)
+        pvals[label + " chi2"] = pc
+        rows.append((label, ma, mb, float("nan"), f"chi2={c2:.1f}/{dof}", pc))
     coarse = spectra.coarse_tally_hist(out["hist"]) / n_gpu
     hist_c = cpu[f"{name}/hist"].astype(np.int64)
     for k, kind in enumerate(KINDS):
