@@ -202,6 +202,23 @@ __device__ __forceinline__ int64_t pool_take(WarpPool& P, unsigned long long* he
   return got < n ? got : -1;
 }
 
+// Pool entries claimed per atomic.  The sampler's: the tuned chunk, cut so
+// that every warp of the grid can claim two (a deep shower's waves hold a
+// few thousand tasks; 64-task claims left most warps idle), a multiple of
+// 32, at least 32.  The propagation kernel's: 32 when the wave is no larger
+// than the grid (one entry per thread), else the tuned chunk (cutting it for
+// mid-sized waves on a full grid cost 1.5 % at 10^6 primaries).  The
+// assignment of entries to warps changes no result: every particle and
+// task draws from its own stream.
+__device__ __forceinline__ int wave_chunk(int tuned, int64_t n) {
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t fair = (n / (2 * warps)) & ~(int64_t)31;
+  return (int)(fair >= tuned ? tuned : (fair > 32 ? fair : 32));
+}
+__device__ __forceinline__ int wave_chunk_propagate(int tuned, int64_t n) {
+  return n <= (int64_t)gridDim.x * blockDim.x ? 32 : tuned;
+}
+
 __device__ __forceinline__ int species_of(int pid) {
   return pid == 22 ? 0 : (pid == 11 ? 1 : (pid == -11 ? 2 : 3));
 }
@@ -528,6 +545,7 @@ template <int BETHE>
 __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropShared64& sm) {
   unsigned int* sh_hist = sm.hist;
   const int64_t wave_n = w_n(c);
+  const int chunk_p = wave_chunk_propagate(c.chunk[0], wave_n);
   const uint64_t wave_head = w_head(c);
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
   if (threadIdx.x < kWarps * 8) {
@@ -550,7 +568,7 @@ __device__ __forceinline__ void propagate_fp64_body(const WaveCtx<0>& c, PropSha
   for (;;) {
     __syncwarp();
     const bool need = !active;
-    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, c.chunk[0]);
+    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, chunk_p);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool finish = false;
@@ -754,6 +772,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
   unsigned int* sh_hist = sm.hist;
   FinEntry (*sh_fin)[64] = sm.fin;
   const int64_t wave_n = w_n(c);
+  const int chunk_p = wave_chunk_propagate(c.chunk[0], wave_n);
   const uint64_t wave_head = w_head(c);
   const Tabs& T = c.T;
   for (int k = threadIdx.x; k < kHist; k += blockDim.x) sh_hist[k] = 0;
@@ -795,7 +814,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
     // loads and set-up run for several lanes at once
     const unsigned idle = __ballot_sync(kFull, !active);
     const bool need = !active && (__popc(idle) >= c.refill_min[0] || idle == kFull);
-    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, c.chunk[0]);
+    const int64_t got = pool_take(pool, c.ctr + 0, wave_n, need, chunk_p);
     const bool fresh = need && got >= 0;
     if (__all_sync(kFull, !active && !fresh)) break;
     bool fin = false;
@@ -1397,6 +1416,7 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
   KinEntry<PREC>* kq = sh_kq[threadIdx.x / 32];
   int kcount = 0;                      // warp-uniform
   const int64_t total = (int64_t)sh_off[8];
+  const int chunk_s = wave_chunk(c.chunk[1], total);
   const int lane = threadIdx.x & 31;
   LocalTally L;
   WarpPool pool;
@@ -1409,7 +1429,7 @@ __device__ __forceinline__ void sample_body(const WaveCtx<PREC>& c, SampShared<P
     __syncwarp();
     const unsigned idle = __ballot_sync(kFull, !active);   // refills in groups, as in propagation
     const bool need = !active && (__popc(idle) >= c.refill_min[1] || idle == kFull);
-    const int64_t t = pool_take(pool, c.ctr + 1, total, need, c.chunk[1]);
+    const int64_t t = pool_take(pool, c.ctr + 1, total, need, chunk_s);
     const bool fresh = need && t >= 0;
     const bool drained = __any_sync(kFull, need && t < 0);   // the pool is empty for the rest of the wave
     if (__all_sync(kFull, !active && !fresh)) break;
