@@ -436,8 +436,10 @@ def bench_batch(args, w, name, dist, rank, ws):
         # picks lanes, the broad mix one lane)
         ncal = 500 if w["emin"] > 100.0 else 100_000
         cal = make_primaries(w, ncal, offset=20_000_000)
+        # lanes only where the calibration is the whole batch: 500 muons
+        # run as small waves that lanes overlap, 10^5 fill the GPU
         tuning = autotune_batch(sh, precision=w["precision"], n=ncal, ring_capacity=1 << 24, use_cache=False,
-                                choose_loop=False, primaries=cal)
+                                choose_loop=False, primaries=cal, tune_lanes=ncal >= n)
     tally = eng.new_tally(n, zmax)
     alu = alu_roofline() if rank == 0 and not args.quick else None
     for s in range(args.warmup):
@@ -808,7 +810,8 @@ def bench_batchdark(args, w, name, dist, rank, ws):
         from petite_gb300.autotune import autotune_batch
         ncal = min(n, 500 if w["emin"] > 100.0 else 20_000)
         tuning = autotune_batch(sh, precision=w["precision"], n=ncal, ring_capacity=1 << 24, use_cache=False,
-                                choose_loop=False, primaries=make_primaries(w, ncal, offset=20_000_000))
+                                choose_loop=False, primaries=make_primaries(w, ncal, offset=20_000_000),
+                                tune_lanes=ncal >= n)
 
     def step(s):
         p0, pid, mass = make_primaries(w, n, offset=block_index(s, rank, ws))

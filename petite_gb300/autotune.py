@@ -46,14 +46,17 @@ def _calibration_primaries(n, seed):
 
 
 def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, seed=0, use_cache=True,
-                   verbose=False, choose_loop=True, primaries=None):
+                   verbose=False, choose_loop=True, primaries=None, tune_lanes=True):
     """Tunes ``shower``'s engine and returns the chosen settings
     ``{"refill_min": [p, s], "chunk": [p, s], "threads": b, "staging": g, "loop": l, "lanes": k,
     "seconds": t, "threads_seconds": {...}, "staging_seconds": {...}, "loop_seconds": {...},
     "lanes_seconds": {...}}`` (``*_seconds``: the calibration run under each option, the earlier
     coordinates already chosen).  ``choose_loop=False`` times the loops but keeps the host
     loop, whose per-kernel event times a roofline needs.  ``primaries`` =
-    (p0 (n,4), pid, mass): calibrate on these instead of the mix (not cached)."""
+    (p0 (n,4), pid, mass): calibrate on these instead of the mix (not cached).
+    ``tune_lanes=False`` keeps one lane: lanes pay off for a batch that the
+    GPU runs as a few small waves, so a calibration smaller than the real
+    batch would pick them where the real batch fills the GPU."""
     import torch
     eng = shower._engine
     key = f"{torch.cuda.get_device_name(eng.device)}|{shower.get_target_material()}|{precision}|v{CACHE_VERSION}"
@@ -105,7 +108,7 @@ def autotune_batch(shower, precision="mixed", n=20_000, ring_capacity=1 << 22, s
     for name, values in GRID.items():
         if name in ("threads", "staging") and precision != "mixed":
             continue                                    # float32 kernels only
-        if name == "lanes" and cfg["loop"] != "host":
+        if name == "lanes" and (cfg["loop"] != "host" or not tune_lanes):
             continue                                    # lanes are a form of the host loop
         for v in values:
             trial = {"refill_min": list(cfg["refill_min"]), "chunk": list(cfg["chunk"]), "loop": cfg["loop"],
