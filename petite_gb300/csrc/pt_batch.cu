@@ -366,7 +366,7 @@ __device__ __forceinline__ float mfp32(const Ns32<SH>& v, int pid, float E) {
   const float lnE = __logf(E);
   float ns = nsig32(v, a, E, lnE) + nsig32(v, b, E, lnE);
   if (pid == -11) ns += nsig32(v, 2, E, lnE);
-  return ns > 0.f ? (float)kCmToM / ns : 1.0e12f;
+  return ns > 0.f ? __fdividef((float)kCmToM, ns) : 1.0e12f;   // ns far inside float32's range
 }
 
 // Process choice in float32 (shower.py:665-698): electron {Brem, Moller},
@@ -793,6 +793,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
   const float lossesf = (float)T.t.dEdx_GeV_per_m;
   const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
   const float Z13 = (float)T.t.Z13;
+  const Ld32 ld = ld32_constants(T.t.A, T.t.Z, T.t.Z23);
   const float rescale = (float)c.rescale;
   const float me = (float)kMe;
   LocalTally L;
@@ -845,7 +846,8 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       const float pt = sqrtf(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)));
       pmag = sqrtf(__fadd_rn(__fmul_rn(pt, pt), __fmul_rn(pz, pz)));
       th0 = atan2f(pt, pz);
-      dir = pmag > 0.f ? make_float3(px / pmag, py / pmag, pz / pmag) : make_float3(0.f, 0.f, 1.f);
+      const float ip = __fdividef(1.f, pmag);           // |p| below 2^126; unused at rest
+      dir = pmag > 0.f ? make_float3(px * ip, py * ip, pz * ip) : make_float3(0.f, 0.f, 1.f);
       disp = make_float3(0.f, 0.f, 0.f);
       lossf = 0.f;
       dzf = 0.f;
@@ -876,9 +878,10 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
         const float mfp = mfp32(ns, pid, Ef);
         const float u_hard = dr.u[0];
         const float q = fmaf(14.f, dr.u[1], 6.f);         // delta_z = mfp / U(6, 20)
-        dzf = mfp / q;
-        if (u_hard > __expf(-1.f / q)) {                 // hard scatter: final increment
-          step = -mfp * log1pf(expm1f(-1.f / q) * dr.u[2]);
+        const float iq = __fdividef(-1.f, q);            // q in [6, 20]
+        dzf = -mfp * iq;
+        if (u_hard > __expf(iq)) {                       // hard scatter: final increment
+          step = -mfp * log1pf(expm1f(iq) * dr.u[2]);
           mlep = me;
           base = 3;
         } else {
@@ -906,8 +909,8 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
           used = mcs32_bethe(dir, pmag * (me / mf), pmag / Ef, rho_cm * step, A, Z, Z13, Z23, rescale,
                              pick(dr.u, base), pick(dr.u, base + 1), pick(dr.u, base + 2), pick(dr.u, base + 3));
         } else {
-          mcs32_u(dir, pmag * (mlep / mf), Ef, rho_cm * step, A, Z, Z23, rescale, pick(dr.u, base),
-                  pick(dr.u, base + 2), pick(dr.u, base + 3), pmag / Ef);
+          mcs32_ld(dir, pmag, Ef, mf, mlep, rho_cm * step, ld, rescale, pick(dr.u, base), pick(dr.u, base + 2),
+                   pick(dr.u, base + 3));
           used = 4;
         }
       }
@@ -1034,10 +1037,18 @@ template <class R> struct DaughterT { double E; R px, py, pz; int pid; };
 // (E_a + E_b = E_in + target mass for the two-body processes).
 struct KinOut { double E[2]; float P[2]; float3 d[2]; int pid[2]; };
 
+// One reciprocal square root for |p| and the unit direction; a momentum
+// below 2^-50 GeV keeps the z axis.
 __device__ __forceinline__ void set_dir32(KinOut& k, int j, float pxx, float pyy, float pzz) {
-  const float p = sqrtf(pxx * pxx + pyy * pyy + pzz * pzz);
-  k.P[j] = p;
-  k.d[j] = p > 0.f ? make_float3(pxx / p, pyy / p, pzz / p) : make_float3(0.f, 0.f, 1.f);
+  const float p2 = pxx * pxx + pyy * pyy + pzz * pzz;
+  if (p2 > 0x1p-100f) {
+    const float r = rsqrtf(p2);
+    k.P[j] = p2 * r;
+    k.d[j] = make_float3(pxx * r, pyy * r, pzz * r);
+  } else {
+    k.P[j] = sqrtf(p2);
+    k.d[j] = make_float3(0.f, 0.f, 1.f);
+  }
 }
 
 __device__ void kin_mixed(int process, int pid, double E, double mass, const MapPt32* x, float ph, KinOut& k) {
@@ -1182,10 +1193,7 @@ __device__ void run_kinematics(const WaveCtx<PREC>& c, KinEntry<PREC>* kq, int c
       const KinEntry<1>& f = reinterpret_cast<const KinEntry<1>&>(e);
       KinOut k;
       kin_mixed(process, pid, E, P.mass, f.x, f.ph, k);
-      const float fx = P.px, fy = P.py, fz = P.pz;
-      const float pn = sqrtf(fx * fx + fy * fy + fz * fz);
-      const float3 pd = pn > 0.f ? make_float3(fx / pn, fy / pn, fz / pn) : make_float3(0.f, 0.f, 1.f);
-      const Rot32 Rm = rot32_from(pd);
+      const Rot32 Rm = rot32_from_momentum(P.px, P.py, P.pz);
       for (int j = 0; j < 2; ++j) {
         const float3 v = rot32_apply(Rm, k.d[j]);
         dg[j] = {k.E[j], k.P[j] * v.x, k.P[j] * v.y, k.P[j] * v.z, k.pid[j]};

@@ -12,7 +12,11 @@
 //             a=delta+, b=delta-, c2=cos^2(phi/2), K=(E+ - E-)^2/(2 E+ E-)
 //  * the form factor and prefactors are grouped so no intermediate leaves
 //    the float32 range, and the result is the acceptance ratio
-//    wgt*f/max_F directly.
+//    wgt*f/max_F directly;
+//  * divisions whose divisors stay far inside float32's normal range (below
+//    2^126: the angular denominators D are at most ~1e27 for electrons
+//    below 1 TeV) use the approximate __fdividef (2 ulp) instead of the
+//    correctly rounded division.
 // Energies, positions and the final daughter four-momenta stay float64.
 #pragma once
 #include "pt_physics.cuh"
@@ -65,15 +69,15 @@ __device__ __forceinline__ float brem32_ratio(const Samp32& S, const MapPt32* x,
   const float ab = d * dp;
   const float d2 = d * d;
   const float Anum = 4.f * S.k * S.k * x[1].x * x[2].x * S.E - (1.f + d2) * w;
-  const float mA = S.m * Anum / (2.f * S.E * epp);
+  const float mA = __fdividef(S.m * Anum, 2.f * S.E * epp);
   const float qh = amb * amb + 4.f * ab * s2 + mA * mA;     // qsq / m^2
   const float D = (1.f + d2) * (1.f + dp * dp);
-  const float iD = 1.f / D;
+  const float iD = __fdividef(1.f, D);
   const float t1 = amb * (1.f - ab) * iD;
-  const float W = (w / S.E) * (w / epp);
+  const float W = __fdividef(w, S.E) * __fdividef(w, epp);
   const float T = t1 * t1 + 4.f * ab * s2 * iD + W * (0.5f * amb * amb + 2.f * ab * s2) * iD;
-  const float u = 1.f / fmaf(S.b, qh, 1.f);
-  const float Q = S.aux0 * (epp / w);          // E' E (E - m - Eg) / w
+  const float u = __fdividef(1.f, fmaf(S.b, qh, 1.f));
+  const float Q = S.aux0 * __fdividef(epp, w);  // E' E (E - m - Eg) / w
   return ((S.C * jac) * Q) * ((ab * T) * (u * u));
 }
 
@@ -95,15 +99,15 @@ __device__ __forceinline__ float pair32_ratio(const Samp32& S, const MapPt32* x,
   const float c2 = cp * cp;
   const float dd = 2.f * S.k * x[2].x;         // dp - dm
   const float ab = dp * dm;
-  const float B = (1.f + dp * dp) / (2.f * epp) + (1.f + dm * dm) / (2.f * epm);
+  const float B = __fdividef(1.f + dp * dp, 2.f * epp) + __fdividef(1.f + dm * dm, 2.f * epm);
   const float q = dd * dd + 4.f * ab * c2 + (S.m * B) * (S.m * B);
   const float D = (1.f + dp * dp) * (1.f + dm * dm);
-  const float iD = 1.f / D;
+  const float iD = __fdividef(1.f, D);
   const float dE = S.span * (x[0].x - x[0].omx);          // E+ - E-
-  const float K = 0.5f * (dE / epp) * (dE / epm);
+  const float K = 0.5f * __fdividef(dE, epp) * __fdividef(dE, epm);
   const float spm = dp + dm;
   const float T = (dd * dd * (1.f + spm * spm * iD + K) + 4.f * ab * c2 * (1.f + K)) * iD;
-  const float u = 1.f / fmaf(S.b, q, 1.f);
+  const float u = __fdividef(1.f, fmaf(S.b, q, 1.f));
   const float Q = (epp * epm) * S.aux0;        // E+ E- (w - 2 me) / w
   return ((S.C * jac) * Q) * ((ab * T) * (u * u));
 }
@@ -249,6 +253,73 @@ __device__ __forceinline__ void mcs32_u(float3& dir, float pmag, float E, float 
   mcs32_rotate(dir, lynch_dahl_theta32(pmag, beta, t, A, Z, Z23, u_sign, u_rad) * rescale, u_phi);
 }
 
+// Material constants of the Lynch-Dahl width folded for mcs32_ld.  With p
+// the lepton momentum in GeV (the reference's formula takes MeV), beta and
+// t in g/cm^2:
+//   chi_c^2 = kc t / (p beta)^2,         kc = 0.157e-6 Z (Z+1) / A
+//   chi_c^2 / chi_a^2 = kc t / (ka (beta^2 + k3)),
+//                                        ka = 2.007e-11 Z^(2/3), k3 = 3.34 (Z alpha)^2
+// (p cancels in the ratio), so v = 0.5 (chi_c^2/chi_a^2) / (1 - F) = kv t /
+// (beta^2 + k3) with kv = 25 kc / ka, and theta0^2 = kth t g(v) / (p beta)^2
+// with kth = kc / (1 + F^2), F = 0.98.
+struct Ld32 { float kth, kv, k3; };
+__host__ __device__ inline Ld32 ld32_constants(double A, double Z, double Z23) {
+  const double kc = 0.157e-6 * Z * (Z + 1.0) / A, ka = 2.007e-11 * Z23;
+  const double za = Z * kAlpha;
+  return {(float)(kc / (1.0 + 0.98 * 0.98)), (float)(25.0 * kc / ka), (float)(3.34 * za * za)};
+}
+
+// mcs32_rotate for a unit direction: with rho = |(vx, vy)| the rotation
+// there reduces to
+//   lab = n2 v + n0 (vx vz / rho, vy vz / rho, -rho) + n1 (-vy / rho, vx / rho, 0),
+// one reciprocal square root instead of two square roots and four
+// divisions.  A direction along z (rho = 0) keeps n, as the reference's
+// get_rotation_matrix does there; within 2^-50 of the axis the frame's
+// azimuth is dropped (phi is uniform) and n is flipped for a backward
+// direction.
+__device__ __forceinline__ void mcs32_rotate_unit(float3& dir, float theta, float u_phi) {
+  float sth, cth, sph, cph;
+  sincosf(theta, &sth, &cth);
+  sincospif(2.f * u_phi, &sph, &cph);
+  const float n0 = sph * sth, n1 = -cph * sth, n2 = cth;
+  const float vx = dir.x, vy = dir.y, vz = dir.z;
+  const float r2 = fmaf(vx, vx, vy * vy);
+  float3 o;
+  if (r2 > 0x1p-100f) {
+    const float inv = rsqrtf(r2);
+    const float a = fmaf(n0 * vz, inv, n2), b = n1 * inv;
+    o = make_float3(fmaf(a, vx, -b * vy), fmaf(a, vy, b * vx), fmaf(n2, vz, -n0 * (r2 * inv)));
+  } else {
+    o = make_float3(n0, n1, (vz < 0.f && (vx != 0.f || vy != 0.f)) ? -n2 : n2);
+  }
+  const float s = rsqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
+  dir = make_float3(o.x * s, o.y * s, o.z * s);
+}
+
+// get_scattered_momentum_fast (moliere.py:350-400) for a particle of mass m
+// and momentum pmag (GeV) at energy E, scattered with lepton mass mlep
+// (p = pmag mlep / m, beta = pmag / E): the Lynch-Dahl space angle on its
+// sign, radius and phi draws, from the folded constants K, then the
+// rotation of the unit direction.  Three approximate reciprocals
+// (__fdividef, 2 ulp) on operands far inside float32's range replace the
+// eleven divisions and two square roots of the term-by-term form.
+__device__ __forceinline__ void mcs32_ld(float3& dir, float pmag, float E, float m, float mlep, float t,
+                                         const Ld32& K, float rescale, float u_sign, float u_rad, float u_phi) {
+  const float p2 = pmag * pmag, E2 = E * E;
+  const float v = __fdividef(K.kv * t * E2, fmaf(K.k3, E2, p2));    // beta^2 = p2 / E2
+  float g;                                                            // (1+v) ln(1+v)/v - 1
+  if (v < 1e-2f) {
+    g = v * (0.5f + v * (-1.f / 6.f + v * (1.f / 12.f - v * 0.05f)));
+  } else {
+    const float lg = log1pf(v);
+    g = fmaf(lg, __fdividef(1.f, v), lg - 1.f);
+  }
+  // 1 / (p beta) = E m / (pmag^2 mlep)
+  float theta = sqrtf(K.kth * t * g * (-2.f * __logf(1.f - u_rad))) * __fdividef(E * m, p2 * mlep) * rescale;
+  if (u_sign < 0.5f) theta = -theta;
+  mcs32_rotate_unit(dir, theta, u_phi);
+}
+
 // get_scattered_momentum_Bethe (moliere.py:403-453) on the next four draws
 // u[0..3]; returns how many it used.  b < 2: the Lynch-Dahl angle with the
 // electron mass, draws sign, (pair angle), radius, phi.  Otherwise the
@@ -273,14 +344,26 @@ __device__ __forceinline__ int mcs32_bethe(float3& dir, float pe, float beta, fl
   return 3;
 }
 
-// Lab frame from the parent's unit direction: Particle.rotation_matrix
-// (particle.py:176-185) with cos/sin of ThZ, PhiZ taken from the direction.
+// Lab frame from the parent's momentum: Particle.rotation_matrix
+// (particle.py:176-185) with cos/sin of ThZ, PhiZ taken from the direction,
+// by reciprocal square roots for |p| and for the transverse length.  A
+// momentum below 2^-50 GeV keeps the z axis, and a direction within 2^-50
+// of it the azimuth 0 (as at rho = 0).
 struct Rot32 { float cT, sT, cP, sP; };
-__device__ __forceinline__ Rot32 rot32_from(float3 d) {
-  Rot32 R;
-  const float rho = sqrtf(d.x * d.x + d.y * d.y);
-  R.cT = d.z; R.sT = rho;
-  if (rho > 0.f) { R.cP = d.x / rho; R.sP = d.y / rho; } else { R.cP = 1.f; R.sP = 0.f; }
+__device__ __forceinline__ Rot32 rot32_from_momentum(float px, float py, float pz) {
+  Rot32 R = {1.f, 0.f, 1.f, 0.f};
+  const float p2 = px * px + py * py + pz * pz;
+  if (!(p2 > 0x1p-100f)) return R;
+  const float r = rsqrtf(p2);
+  const float dx = px * r, dy = py * r;
+  const float t2 = dx * dx + dy * dy;
+  R.cT = pz * r;
+  if (t2 > 0x1p-100f) {
+    const float ir = rsqrtf(t2);
+    R.sT = t2 * ir; R.cP = dx * ir; R.sP = dy * ir;
+  } else {
+    R.sT = sqrtf(t2);
+  }
   return R;
 }
 __device__ __forceinline__ float3 rot32_apply(const Rot32& R, float3 v) {
