@@ -111,8 +111,19 @@ struct WavePlan {
   int done;                           // 1: the run has ended (all primaries finished, or an error)
 };
 
+// Float32 forms of the table and option constants, rounded once on the
+// host: the float32 kernels read them as parameters, with no float64
+// conversion (a float64-pipe instruction) left for the compiler to repeat
+// inside their loops.
+struct Consts32 {
+  float mc[4];                        // min_calc energy: photon, electron, positron, muon
+  float min_energy, dedx, rho_cm, A, Z, Z23, Z13, rescale, Eg_min, Ee_min, a0sq;
+  Ld32 ld;
+};
+
 template <int PREC> struct WaveCtx {
   Tabs T;
+  Consts32 k32;
   double min_energy, rescale;
   int64_t max_n_integrators;
   int ms, mcs_mode;
@@ -787,14 +798,13 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
   FinEntry* fq = sh_fin[w];
   volatile int (*open)[2] = sm.open[w];
   int fcount = 0;                                        // warp-uniform
-  const float mc0 = (float)T.t.min_calc_photon, mc1 = (float)T.t.min_calc_electron,
-              mc2 = (float)T.t.min_calc_positron, mc3 = (float)T.t.min_calc_muon;
-  const float minE = (float)c.min_energy;
-  const float lossesf = (float)T.t.dEdx_GeV_per_m;
-  const float rho_cm = (float)(T.t.rho / kCmToM), A = (float)T.t.A, Z = (float)T.t.Z, Z23 = (float)T.t.Z23;
-  const float Z13 = (float)T.t.Z13;
-  const Ld32 ld = ld32_constants(T.t.A, T.t.Z, T.t.Z23);
-  const float rescale = (float)c.rescale;
+  const float mc0 = c.k32.mc[0], mc1 = c.k32.mc[1], mc2 = c.k32.mc[2], mc3 = c.k32.mc[3];
+  const float minE = c.k32.min_energy;
+  const float lossesf = c.k32.dedx;
+  const float rho_cm = c.k32.rho_cm, A = c.k32.A, Z = c.k32.Z, Z23 = c.k32.Z23;
+  const float Z13 = c.k32.Z13;
+  const Ld32 ld = c.k32.ld;
+  const float rescale = c.k32.rescale;
   const float me = (float)kMe;
   LocalTally L;
   WarpPool pool;
@@ -1281,16 +1291,16 @@ __device__ __forceinline__ void samp_load(const WaveCtx<PREC>& c, SampTask<PREC>
   if (PREC == 0) {
     k.maxF = T.t.map_maxF[k.row];
   } else {
-    const float Ef = (float)k.E, Cr = __ldg(T.t.map_cnorm32 + k.row), a0sq = (float)T.a0sq;
+    const float Ef = (float)k.E, Cr = __ldg(T.t.map_cnorm32 + k.row), a0sq = c.k32.a0sq;
     switch (process) {
-      case PT_BREM: brem32_setup(k.S32, Ef, (float)kMe, (float)T.t.Eg_min, a0sq, Cr); break;
-      case PT_MUONBREM: brem32_setup(k.S32, Ef, (float)kMmu, (float)T.t.Eg_min, a0sq, Cr); break;
+      case PT_BREM: brem32_setup(k.S32, Ef, (float)kMe, c.k32.Eg_min, a0sq, Cr); break;
+      case PT_MUONBREM: brem32_setup(k.S32, Ef, (float)kMmu, c.k32.Eg_min, a0sq, Cr); break;
       case PT_PAIRPROD: pair32_setup(k.S32, Ef, a0sq, Cr); break;
       case PT_COMP: comp32_setup(k.S32, Ef, Cr); break;
-      case PT_ANN: ann32_setup(k.S32, Ef, (float)T.t.Eg_min, Cr); break;
-      case PT_MOLLER: moller32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
-      case PT_BHABHA: bhabha32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
-      default: muone32_setup(k.S32, Ef, (float)T.t.Ee_min, Cr); break;
+      case PT_ANN: ann32_setup(k.S32, Ef, c.k32.Eg_min, Cr); break;
+      case PT_MOLLER: moller32_setup(k.S32, Ef, c.k32.Ee_min, Cr); break;
+      case PT_BHABHA: bhabha32_setup(k.S32, Ef, c.k32.Ee_min, Cr); break;
+      default: muone32_setup(k.S32, Ef, c.k32.Ee_min, Cr); break;
     }
   }
 }
@@ -2187,6 +2197,20 @@ drain:
   return rs;
 }
 
+static Consts32 consts32(const Tabs& T, const pt_opts* o) {
+  Consts32 k;
+  k.mc[0] = (float)T.t.min_calc_photon; k.mc[1] = (float)T.t.min_calc_electron;
+  k.mc[2] = (float)T.t.min_calc_positron; k.mc[3] = (float)T.t.min_calc_muon;
+  k.min_energy = (float)o->min_energy;
+  k.dedx = (float)T.t.dEdx_GeV_per_m;
+  k.rho_cm = (float)(T.t.rho / kCmToM);
+  k.A = (float)T.t.A; k.Z = (float)T.t.Z; k.Z23 = (float)T.t.Z23; k.Z13 = (float)T.t.Z13;
+  k.rescale = (float)o->rescale_MCS;
+  k.Eg_min = (float)T.t.Eg_min; k.Ee_min = (float)T.t.Ee_min; k.a0sq = (float)T.a0sq;
+  k.ld = ld32_constants(T.t.A, T.t.Z, T.t.Z23);
+  return k;
+}
+
 template <int PREC>
 static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0, const double* r0, const int32_t* pid,
                                 const double* mass, int64_t n, const pt_opts* o, pt_tally* tally, cudaStream_t st,
@@ -2196,6 +2220,7 @@ static pt_status run_batch_impl(pt_handle* h, BatchScratch* S, const double* p0,
   c.T = *hp.T;
   c.min_energy = o->min_energy;
   c.rescale = o->rescale_MCS;
+  c.k32 = consts32(c.T, o);
   c.max_n_integrators = o->max_n_integrators;
   c.ms = o->multiple_scattering;
   c.mcs_mode = o->mcs_mode;
