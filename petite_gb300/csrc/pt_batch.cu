@@ -878,20 +878,24 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
       Rng::Drawn<8> dr;
       rng.peek(dr, c.rk);
       int base = 1;                                       // first multiple-scattering draw
-      if (!charged) {
-        step = -mfp32(ns, pid, Ef) * log1pf(-dr.u[0]); // mfp log(1/(1-u))
-      } else if (!(Ef >= pmef)) {
+      // One mean free path and one logarithm per lane, however the warp's
+      // lanes branch: a photon's flight is mfp log(1/(1-u)) and a hard
+      // scatter's final increment -mfp log(1 + (e^(-1/q) - 1) u).
+      const float mfp = mfp32(ns, pid, Ef);
+      float lx = -dr.u[0];
+      bool flight = !charged;
+      if (charged && !(Ef >= pmef)) {
         step = dr.u[0] * dzf;                             // shower.py:584-585
         mlep = me;                                        // shower.py:596-598: electron mass
-      } else {
+      } else if (charged) {
         ++L.substeps;
-        const float mfp = mfp32(ns, pid, Ef);
         const float u_hard = dr.u[0];
         const float q = fmaf(14.f, dr.u[1], 6.f);         // delta_z = mfp / U(6, 20)
         const float iq = __fdividef(-1.f, q);            // q in [6, 20]
         dzf = -mfp * iq;
         if (u_hard > __expf(iq)) {                       // hard scatter: final increment
-          step = -mfp * log1pf(expm1f(iq) * dr.u[2]);
+          lx = expm1f(iq) * dr.u[2];
+          flight = true;
           mlep = me;
           base = 3;
         } else {
@@ -900,6 +904,7 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
           base = 2;
         }
       }
+      if (flight) step = -mfp * log1pf(lx);
       if (charged) {                                      // lose_energy (particle.py:143-153)
         lossf = fmaf(lossesf, step, lossf);
         Ef = E0f - lossf;
@@ -917,15 +922,16 @@ __device__ __forceinline__ void propagate_mixed_body(const WaveCtx<1>& c, PropSh
         if constexpr (BETHE) {
           // the electron's momentum throughout (moliere.py:237,244)
           used = mcs32_bethe(dir, pmag * (me / mf), pmag / Ef, rho_cm * step, A, Z, Z13, Z23, rescale,
-                             pick(dr.u, base), pick(dr.u, base + 1), pick(dr.u, base + 2), pick(dr.u, base + 3));
+                             pick_in<1, 3>(dr.u, base), pick_in<2, 4>(dr.u, base + 1), pick_in<3, 5>(dr.u, base + 2),
+                             pick_in<4, 6>(dr.u, base + 3));
         } else {
-          mcs32_ld(dir, pmag, Ef, mf, mlep, rho_cm * step, ld, rescale, pick(dr.u, base), pick(dr.u, base + 2),
-                   pick(dr.u, base + 3));
+          mcs32_ld(dir, pmag, Ef, mf, mlep, rho_cm * step, ld, rescale, pick_in<1, 3>(dr.u, base),
+                   pick_in<3, 5>(dr.u, base + 2), pick_in<4, 6>(dr.u, base + 3));
           used = 4;
         }
       }
       const int after = base + used;
-      if (last) uc = pick(dr.u, after);                  // the process-choice draw
+      if (last) uc = pick_in<1, 7>(dr.u, after);         // the process-choice draw
       rng.advance(dr, after + (last ? 1 : 0));
       have_uc = last;
       if (last) {

@@ -199,12 +199,14 @@ struct Rng {
   }
 };
 
-// P.u[i] for a runtime index i < D, without an indexed (local-memory) access
-template <int D>
-__device__ __forceinline__ float pick(const float (&u)[D], int i) {
-  float r = u[0];
+// u[i] for a runtime index i known to lie in [LO, HI], by HI - LO selects
+// (no indexed, local-memory access)
+template <int LO, int HI, int D>
+__device__ __forceinline__ float pick_in(const float (&u)[D], int i) {
+  static_assert(0 <= LO && LO <= HI && HI < D, "pick_in range");
+  float r = u[LO];
 #pragma unroll
-  for (int j = 1; j < D; ++j)
+  for (int j = LO + 1; j <= HI; ++j)
     if (j == i) r = u[j];
   return r;
 }
