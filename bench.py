@@ -108,14 +108,16 @@ def ring_bytes(precision):
 BYTES_PER_STEP_RECORDS = 336
 
 
-# DRAM traffic per particle-step of each batched kernel, from one ncu capture
-# of one launch of each (dram__bytes_read.sum + dram__bytes_write.sum, caches
-# as the run leaves them, divided by that wave's particle-steps); the capture
-# and its command are summarised in the named profile.  The bench scales it
-# to its own launches by the particle-steps they process.
+# DRAM traffic per particle-step of each batched kernel in a large wave, from
+# one ncu capture of every launch of the two kernels in a 2e4-primary step
+# (dram__bytes_read.sum + dram__bytes_write.sum over the step's
+# particle-steps, scaled to a large wave by the 20 longest launches' bytes
+# per executed thread-instruction); the capture and its command are
+# summarised in the named profile.  The bench scales it to its own launches
+# by the particle-steps they process.
 NCU_TRAFFIC = {
-    "propagate": {"bytes_per_step": 96.0, "profile": "profiles/batched_kernels_lead_20k.md"},
-    "sample": {"bytes_per_step": 138.0, "profile": "profiles/batched_kernels_lead_20k.md"},
+    "propagate": {"bytes_per_step": 98.0, "profile": "profiles/batched_kernels_lead_20k.md"},
+    "sample": {"bytes_per_step": 141.0, "profile": "profiles/batched_kernels_lead_20k.md"},
 }
 
 
@@ -126,10 +128,10 @@ NCU_TRAFFIC = {
 # active per executed instruction.  The bench divides the flop rates by the
 # FMA peaks it measures in the same run (pt_alu_peaks).
 NCU_ALU = {
-    "propagate": {"fp32_tflops": 3.88, "fp64_tflops": 0.0065, "issue_active": 0.523, "fp64_pipe": 0.181,
-                  "threads_per_inst": 19.6, "profile": "profiles/alu_batched_lead_20k.md"},
-    "sample": {"fp32_tflops": 3.54, "fp64_tflops": 0.0098, "issue_active": 0.455, "fp64_pipe": 0.101,
-               "threads_per_inst": 21.7, "profile": "profiles/alu_batched_lead_20k.md"},
+    "propagate": {"fp32_tflops": 2.74, "fp64_tflops": 0.0069, "issue_active": 0.580, "fp64_pipe": 0.039,
+                  "threads_per_inst": 19.7, "profile": "profiles/alu_batched_lead_20k.md"},
+    "sample": {"fp32_tflops": 3.21, "fp64_tflops": 0.0113, "issue_active": 0.486, "fp64_pipe": 0.092,
+               "threads_per_inst": 21.9, "profile": "profiles/alu_batched_lead_20k.md"},
 }
 
 
