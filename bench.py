@@ -78,6 +78,15 @@ WORKLOADS = {
                                      seed=3, masses=(0.1,), mode="batchdark", precision="mixed", tables="400GeV",
                                      dark_processes=("DarkBrem", "DarkAnn", "DarkComp", "DarkMuonBrem"),
                                      dark_precision="mixed"),
+    # detector acceptance (detector_cut, shower.py:825-865) of 10^8 dark-vector
+    # rows: E log-uniform on [0.1, 30] GeV, polar angle log-uniform on
+    # [1e-4, 0.3] rad, production points spread 1 cm transversely over 1 m
+    # of target, weights uniform on [0.1, 2]; disks at z = 5, 50, 100 m,
+    # radius 1 m around a 5 cm hole, energy window (1, 20) GeV
+    # (a step is 100 passes over the rows, so the timed region is long enough
+    # for the clock samples)
+    "detector_cut_1e8": dict(n=100_000_000, seed=0, z=(5.0, 50.0, 100.0), radius=1.0, inner=0.05,
+                             energy_cut=(1.0, 20.0), cpu_sample=20_000_000, passes=100, mode="detector"),
     # differentiable dark yield: 4096 (E, mV) pairs, E log-uniform on [0.05, 10] GeV,
     # mV log-uniform on [0.001, 0.3] GeV, 10^4 map samples each, graphite
     "dark_yield_4096": dict(target="graphite", n=4096, samples=10_000, seed=0, mode="yield"),
@@ -119,6 +128,22 @@ NCU_TRAFFIC = {
     "propagate": {"bytes_per_step": 98.0, "profile": "profiles/batched_kernels_lead_20k.md"},
     "sample": {"bytes_per_step": 141.0, "profile": "profiles/batched_kernels_lead_20k.md"},
 }
+
+
+# DRAM bytes per row of k_detector_cut with three detectors, from one ncu
+# capture of a 4e6-row launch (profiles/k_detector_cut_4e6_rows.md):
+# (256.04 + 11.25) MB / 4e6 rows; the traffic of a launch scales with its rows.
+NCU_DETECTOR_BYTES_PER_ROW = 66.8
+
+
+def measured_peak_hbm():
+    """The HBM copy bandwidth of MEASURED_PEAKS.json (GB/s), else the
+    fallback figure, with its source."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return {"value": float(peaks["hbm_gbs"]), "source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    except Exception:
+        return {"value": 6800.0, "source": "fallback 6.8 TB/s"}
 
 
 # Arithmetic and issue rates of the two mixed-form kernels while they run,
@@ -347,6 +372,21 @@ def run_reference(args, w, name):
                                      "masses_GeV": list(w["masses"])},
                           "cpu_baseline": {**cb, "value": v},
                           "e2e": {"value": v, "unit": "row-masses/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    if w["mode"] == "detector":
+        vals, cb = [], None
+        for _ in range(args.steps):
+            cb = detector_cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
+            vals.append(cb["value"])
+        v = float(np.median(vals))
+        print(json.dumps({"impl": "reference", "metric": "detector acceptance: rows x detectors per second "
+                          "(pt_detector_cut)", "value": v, "unit": "row-detectors/s", "n_gpus": args.gpus,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": name, "rows": args.cpu_sample or w["cpu_sample"]},
+                          "cpu_baseline": {**cb, "value": v},
+                          "e2e": {"value": v, "unit": "row-detectors/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
     if w["mode"] not in ("batch", "records"):
@@ -790,6 +830,131 @@ def bench_yield(args, w, name, dist, rank, ws):
         "grad_finite_fraction": float(torch.isfinite(g).float().mean().item()), "clocks": clk.summary()}))
 
 
+def detector_rows(w, n, seed):
+    """Synthetic dark-vector rows of the detector workload: p0 (n, 4), r0
+    (n, 3), w (n,)."""
+    rng = np.random.default_rng(seed)
+    E = 10 ** rng.uniform(-1.0, math.log10(30.0), n)
+    th = 10 ** rng.uniform(-4.0, math.log10(0.3), n)
+    ph = rng.uniform(0.0, 2.0 * math.pi, n)
+    p = np.sqrt(E * E - 0.01 ** 2)
+    p0 = np.empty((n, 4))
+    p0[:, 0] = E
+    p0[:, 1] = p * np.sin(th) * np.cos(ph)
+    p0[:, 2] = p * np.sin(th) * np.sin(ph)
+    p0[:, 3] = p * np.cos(th)
+    r0 = np.c_[rng.normal(0.0, 0.01, n), rng.normal(0.0, 0.01, n), rng.uniform(0.0, 1.0, n)]
+    return p0, r0, rng.uniform(0.1, 2.0, n)
+
+
+def detector_cpu_baseline(w, n_sample, chunk=5_000_000):
+    """The oracle's detector_cut (numpy, one thread) on a bounded sample,
+    in chunks of at most ``chunk`` rows (memory-bounded); the rows are drawn
+    outside the timed region."""
+    from oracle import detector as od
+    t, done, k = 0.0, 0, 0
+    while done < n_sample:
+        m = min(chunk, n_sample - done)
+        p0, r0, wt = detector_rows(w, m, w["seed"] + 99 + k)
+        t0 = time.perf_counter()
+        od.detector_cut(p0, r0, wt, list(w["z"]), w["radius"], method="TotalWeight", energy_cut=w["energy_cut"],
+                        inner=w["inner"])
+        t += time.perf_counter() - t0
+        done += m
+        k += 1
+    return {"value": n_sample * len(w["z"]) / t, "unit": "row-detectors/s", "cores": 1, "kind": "port",
+            "sample": f"{n_sample} rows x {len(w['z'])} detectors in {t:.1f} s: oracle/detector.py (numpy "
+                      "restatement of detector_cut), one thread"}
+
+
+def bench_detector(args, w, name, dist, rank, ws):
+    """detector_cut over 10^8 device rows (pt_detector_cut): pass mask and
+    weight sums for three disks; e2e through detector_cut_rows from pinned
+    host arrays with the efficiencies read back."""
+    import torch
+    from petite_gb300 import _lib
+    from petite_gb300.shower import detector_cut_rows
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    n = args.primaries or w["n"]
+    nd = len(w["z"])
+    p0, r0, wt = detector_rows(w, n, w["seed"] + 1000 * rank)
+    P4 = torch.as_tensor(np.ascontiguousarray(p0.T), device=dev)
+    R3 = torch.as_tensor(np.ascontiguousarray(r0.T), device=dev)
+    W = torch.as_tensor(wt, device=dev)
+    Z = torch.as_tensor(np.asarray(w["z"], np.float64), device=dev)
+    mask = torch.empty((nd, n), dtype=torch.uint8, device=dev)
+    sums = torch.empty(nd + 1, dtype=torch.float64, device=dev)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    lo, hi = w["energy_cut"]
+
+    def launch():
+        s = lib.pt_detector_cut(C.c_void_p(P4.data_ptr()), n, C.c_void_p(R3.data_ptr()), n, C.c_void_p(W.data_ptr()),
+                                n, C.c_void_p(Z.data_ptr()), nd, w["inner"], w["radius"], 1, lo, hi,
+                                C.c_void_p(mask.data_ptr()), C.c_void_p(sums.data_ptr()), C.c_void_p(stream.cuda_stream))
+        if s != 0:
+            raise RuntimeError(f"pt_detector_cut status {s}")
+
+    for _ in range(max(args.warmup, 3)):
+        launch()
+    torch.cuda.synchronize(dev)
+    times = []
+    with ClockSampler(dev.index or 0) as clk:
+        for _ in range(args.steps):
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(w["passes"]):
+                launch()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(sum(times))
+    if dist:
+        tt = torch.tensor([t], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    # e2e: pinned host rows in, efficiencies out, through the public function
+    p0h = torch.as_tensor(p0).pin_memory()
+    r0h = torch.as_tensor(r0).pin_memory()
+    wh = torch.as_tensor(wt).pin_memory()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    eff = detector_cut_rows(p0h, r0h, wh, list(w["z"]), w["radius"], method="Efficiency",
+                            energy_cut=w["energy_cut"], detector_inner_radius=w["inner"], device=dev)
+    torch.cuda.synchronize(dev)
+    te = time.perf_counter() - t0
+    if rank != 0:
+        return
+    per_launch = n * (64 + nd)          # rows read (8 doubles), mask bytes written
+    peak = measured_peak_hbm()
+    ach = per_launch / (float(np.mean(times)) / w["passes"]) / 1e9
+    cb = None if args.no_cpu_baseline else detector_cpu_baseline(w, args.cpu_sample or w["cpu_sample"])
+    print(json.dumps({
+        "metric": "detector acceptance: rows x detectors per second (pt_detector_cut)",
+        "value": args.steps * w["passes"] * n * nd * ws / t, "unit": "row-detectors/s", "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "rows": n, "passes_per_step": w["passes"], "detectors_z_m": list(w["z"]),
+                   "radius_m": w["radius"],
+                   "inner_radius_m": w["inner"], "energy_cut_GeV": list(w["energy_cut"]),
+                   "l2": "inputs (6.4 GB) larger than L2"},
+        "efficiency": [float(x) for x in eff],
+        "e2e": {"value": n * nd / te, "unit": "row-detectors/s", "h2d_bytes_per_step": n * 64,
+                "d2h_bytes_per_step": 8 * (nd + 1)},
+        "gpu_launches": args.steps * w["passes"],
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak["value"], "unit": "GB/s",
+                     "frac": ach / peak["value"], "traffic": NCU_DETECTOR_BYTES_PER_ROW * n, "kernel": "k_detector_cut",
+                     "algorithmic_bytes_per_launch": per_launch,
+                     "avg_launch_ms": 1e3 * float(np.mean(times)) / w["passes"],
+                     "peak_source": peak["source"]},
+        "cpu_baseline": cb, "clocks": clk.summary()}))
+
+
 def bench_batchdark(args, w, name, dist, rank, ws):
     """The batched engine with dark vectors on every wave for all masses at
     once (DarkShower.run_tallied, pt_run_batch_dark); a step is the batch of
@@ -899,6 +1064,8 @@ def main():
         bench_batchdark(args, w, args.workload, dist, rank, ws)
     elif w["mode"] == "yield":
         bench_yield(args, w, args.workload, dist, rank, ws)
+    elif w["mode"] == "detector":
+        bench_detector(args, w, args.workload, dist, rank, ws)
     else:
         bench_records(args, w, args.workload, dist, rank, ws)
 

@@ -500,6 +500,28 @@ pt_status pt_dark_yield_adjoint(pt_dark* d, int32_t process, const double* energ
                                 const int32_t* mass_index, int64_t n_pairs, int64_t n_samples, uint64_t seed,
                                 const double* g_yield, const double* g_moment, double* g_mV, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Detector acceptance: detector_cut (shower.py:825-865) with
+ * transverse_position (shower.py:815-823) over n device rows in SoA form,
+ * E/px/py/pz at p4 + {0,1,2,3} * p4_stride and x0/y0/z0 at
+ * r + {0,1,2} * r_stride (a pt_particles store's p0/r0 with the store's
+ * capacity as stride, or pt_dark_out's p4/r), weight[n] (null: weights 1).
+ * Row i passes disk detector d at z_det[d] (device, [n_det]) when its initial
+ * straight line crosses z_det[d] at a transverse radius in the open interval
+ * (r_inner, r_outer) and, with use_window, e_min < E < e_max; each operation
+ * rounded on its own as numpy evaluates the reference's expressions.
+ * Outputs (device, each may be null): pass[n_det][n], 1 where row i passes
+ * detector d; sums[n_det + 1], the weight passing each detector, then the
+ * weight of the rows in the energy window (all rows without one).  The sums
+ * add block totals atomically, so their last bits may vary from run to run.
+ * Needs no handle.  Replaces the reference's detector_cut over a Python list
+ * of Particle objects (methods "SampleW", "Sample", "Efficiency" and
+ * "TotalWeight" are read from these outputs). */
+pt_status pt_detector_cut(const double* p4, int64_t p4_stride, const double* r, int64_t r_stride,
+                          const double* weight, int64_t n, const double* z_det, int32_t n_det,
+                          double r_inner, double r_outer, int32_t use_window, double e_min, double e_max,
+                          uint8_t* pass, double* sums, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libpetite_gpu.so"
-SOURCES = ["pt_engine.cu", "pt_batch.cu", "pt_dark.cu", "pt_train.cu"]
+SOURCES = ["pt_engine.cu", "pt_batch.cu", "pt_dark.cu", "pt_train.cu", "pt_detector.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -23,7 +23,7 @@ EXPORTS = ("pt_create", "pt_destroy", "pt_strerror", "pt_last_error_info", "pt_l
            "pt_vegas_accumulate", "pt_vegas_adapt", "pt_find_maxes",
            "pt_dark_create", "pt_dark_destroy", "pt_dark_dsigma", "pt_dark_sample_only", "pt_run_dark",
            "pt_run_batch_dark", "pt_dark_screen32",
-           "pt_dark_yield", "pt_dark_yield_adjoint")
+           "pt_dark_yield", "pt_dark_yield_adjoint", "pt_detector_cut")
 
 # pt_run_sm_noalloc: largest particle-store capacity (its static scratch)
 NOALLOC_MAX_ROWS = 1 << 19
@@ -191,6 +191,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     lib.pt_sample_only.restype = C.c_int
     lib.pt_dsigma.argtypes = [vp, i32, vp, vp, i64, i32, vp, vp]
     lib.pt_dsigma.restype = C.c_int
+    lib.pt_detector_cut.argtypes = [vp, i64, vp, i64, vp, i64, vp, i32, C.c_double, C.c_double, i32, C.c_double,
+                                    C.c_double, vp, vp, vp]
+    lib.pt_detector_cut.restype = C.c_int
     lib.pt_moliere_inverse_cdf.argtypes = [vp, vp, i64, i32, vp, vp]
     lib.pt_moliere_inverse_cdf.restype = C.c_int
     i32p = C.POINTER(i32)                    # host arrays of increments per dimension

@@ -326,3 +326,81 @@ def detector_cut(particle_list, detector_positions, detector_radius, method="Sam
     if method == "TotalWeight":
         return [np.sum(w[passed[i]]) for i in range(nd)]
     return None
+
+
+def _soa_columns(t, ncomp, dev):
+    """(n, ncomp) float64 rows on ``dev`` as (base tensor, column stride,
+    first column): a column-major view (strides (1, S), e.g.
+    ``store.t["p0"][:, :n].T``) is used in place, anything else is copied
+    into SoA form."""
+    import torch
+    t = torch.as_tensor(t, dtype=torch.float64, device=dev)
+    if t.dim() != 2 or t.shape[1] != ncomp:
+        raise ValueError(f"expected an (n, {ncomp}) array, got shape {tuple(t.shape)}")
+    if t.shape[0] > 0 and t.stride(0) == 1 and t.stride(1) >= t.shape[0]:
+        return t, t.stride(1), t[:, 0]
+    s = t.T.contiguous()
+    return s, max(t.shape[0], 1), s[0]
+
+
+def detector_cut_rows(p0, r0, weight, detector_positions, detector_radius, method="Sample", energy_cut=None,
+                      detector_inner_radius=0.0, device=None, stream=None):
+    """detector_cut (shower.py:825-865) on particle rows held as arrays, on
+    the GPU (``pt_detector_cut``): p0 (n, 4) four-momenta, r0 (n, 3)
+    positions, weight (n,) or None (weights 1), as numpy arrays or torch
+    tensors; device tensors in SoA layout (``ParticleStore.t["p0"][:, :n].T``,
+    the dark run's ``p4`` buffer) are read in place.
+
+    Same arguments and acceptance as ``detector_cut``; the results index the
+    rows instead of holding Particle objects:
+      "SampleW": bool tensor (n_detectors, n) on the device, False for rows
+                 outside ``energy_cut`` (the list form keeps only the rows
+                 inside it);
+      "Sample": per detector, the int64 indices of the rows that pass;
+      "Efficiency": per detector, passing weight / weight in the window
+                    (0.0 when no row is in the window);
+      "TotalWeight": per detector, the passing weight."""
+    import ctypes as C
+    import torch
+    from . import _lib
+    dev = torch.device(device) if device is not None else (
+        p0.device if torch.is_tensor(p0) and p0.is_cuda else torch.device("cuda"))
+    P, ps, E = _soa_columns(p0, 4, dev)
+    R, rs, _ = _soa_columns(r0, 3, dev)
+    n = int(p0.shape[0])
+    if int(r0.shape[0]) != n:
+        raise ValueError("p0 and r0 must have the same number of rows")
+    W = None
+    if weight is not None:
+        W = torch.as_tensor(weight, dtype=torch.float64, device=dev).contiguous()
+        if W.shape != (n,):
+            raise ValueError(f"weight must have shape ({n},), got {tuple(W.shape)}")
+    zs = torch.as_tensor(np.asarray(detector_positions, dtype=np.float64).reshape(-1), device=dev)
+    nd = int(zs.numel())
+    want_mask = method in ("SampleW", "Sample")
+    mask = torch.zeros((nd, n), dtype=torch.uint8, device=dev) if want_mask else None
+    sums = torch.zeros(nd + 1, dtype=torch.float64, device=dev)
+    win = energy_cut is not None
+    lo, hi = (float(energy_cut[0]), float(energy_cut[1])) if win else (0.0, 0.0)
+    st = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    lib = _lib.load()
+    s = lib.pt_detector_cut(C.c_void_p(P.data_ptr()), ps, C.c_void_p(R.data_ptr()), rs,
+                            C.c_void_p(W.data_ptr()) if W is not None else None, n,
+                            C.c_void_p(zs.data_ptr()) if nd else None, nd, float(detector_inner_radius),
+                            float(detector_radius), int(win), lo, hi,
+                            C.c_void_p(mask.data_ptr()) if mask is not None else None, C.c_void_p(sums.data_ptr()),
+                            C.c_void_p(st))
+    _lib.check(s, "pt_detector_cut")
+    if method == "SampleW":
+        return mask.bool()
+    if method == "Sample":
+        return [torch.nonzero(mask[d], as_tuple=True)[0] for d in range(nd)]
+    if method not in ("Efficiency", "TotalWeight"):
+        return None
+    tot = sums.cpu().numpy()
+    if method == "TotalWeight":
+        return [float(v) for v in tot[:nd]]
+    in_window = bool(((E < hi) & (E > lo)).any()) if win else n > 0
+    if not in_window:
+        return [0.0] * nd
+    return [float(v / tot[nd]) for v in tot[:nd]]

@@ -90,6 +90,8 @@ def test_entry_points_refuse_missing_handles_without_a_device(lib):
     assert lib.pt_dark_screen32(None, 0, None, None, 1, 0.1, None, None, None) == _lib.PT_BAD_ARG
     assert lib.pt_set_batch_tuning(None, None) == _lib.PT_BAD_ARG
     assert lib.pt_vegas_adapt(0, 1, None, None, 2, None, None, 0.5, None) == _lib.PT_BAD_ARG
+    assert lib.pt_detector_cut(None, 0, None, 0, None, 5, None, 1, 0.0, 1.0, 0, 0.0, 0.0, None, None,
+                               None) == _lib.PT_BAD_ARG
 
 
 def test_staging_timeout_marks_the_handle_unusable():

@@ -19,3 +19,10 @@ def test_dark_cpu_sample_is_bounded_for_400gev_muons():
     import bench
     assert bench.dark_cpu_sample(bench.WORKLOADS["batchdark_mu400_lead_1e3"])["per_proc"] == 1
     assert bench.dark_cpu_sample(bench.WORKLOADS["dark_e10_graphite_1e5"])["per_proc"] > 1
+
+
+def test_detector_cpu_baseline_runs_bounded():
+    import bench
+    w = bench.WORKLOADS["detector_cut_1e8"]
+    cb = bench.detector_cpu_baseline(w, 20_000, chunk=7_000)
+    assert cb["unit"] == "row-detectors/s" and cb["value"] > 0 and cb["cores"] == 1 and cb["kind"] == "port"
