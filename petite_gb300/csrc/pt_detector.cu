@@ -57,7 +57,7 @@ __device__ __forceinline__ bool pass_exact(double z, double x0, double y0, doubl
 // annulus edges are clear of it.  Otherwise, whenever a value is not finite,
 // and for |pz| beyond 2^126 (where the approximate division returns 0), the
 // row takes the exact path.  The decisions are the exact ones.
-__global__ void __launch_bounds__(kThreads, 3) k_detector_cut(const double* __restrict__ p4, int64_t p4_stride,
+__global__ void __launch_bounds__(kThreads, 4) k_detector_cut(const double* __restrict__ p4, int64_t p4_stride,
                                                            const double* __restrict__ r, int64_t r_stride,
                                                            const double* __restrict__ weight, int64_t n,
                                                            const double* __restrict__ z_det, int d0, int nd,
@@ -137,11 +137,13 @@ extern "C" pt_status pt_detector_cut(const double* p4, int64_t p4_stride, const 
   const cudaStream_t st = (cudaStream_t)stream;
   if (sums && cudaMemsetAsync(sums, 0, (size_t)(n_det + 1) * sizeof(double), st) != cudaSuccess) return PT_CUDA_ERR;
   if (n == 0 || (n_det == 0 && !sums)) return cudaGetLastError() == cudaSuccess ? PT_OK : PT_CUDA_ERR;
-  int dev = 0, sms = 0;
+  int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_detector_cut, kThreads, 0);
   if (sms < 1) sms = 1;
-  const int64_t want = (n + kThreads - 1) / kThreads, cap = (int64_t)sms * 3;   // the resident blocks
+  if (per < 1) per = 1;
+  const int64_t want = (n + kThreads - 1) / kThreads, cap = (int64_t)sms * per;   // the resident blocks
   const int blocks = (int)(want < cap ? want : cap);
   // one pass over the rows per group of detectors; the first pass also
   // sums the window's total weight (a pass with no detector when n_det = 0)
