@@ -132,8 +132,8 @@ NCU_TRAFFIC = {
 
 # DRAM bytes per row of k_detector_cut with three detectors, from one ncu
 # capture of a 4e6-row launch (profiles/k_detector_cut_4e6_rows.md):
-# (256.04 + 11.25) MB / 4e6 rows; the traffic of a launch scales with its rows.
-NCU_DETECTOR_BYTES_PER_ROW = 66.8
+# (256.04 + 11.57) MB / 4e6 rows; the traffic of a launch scales with its rows.
+NCU_DETECTOR_BYTES_PER_ROW = 66.9
 
 
 def measured_peak_hbm():
