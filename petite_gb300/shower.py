@@ -187,11 +187,16 @@ class Shower:
         n = p0t.shape[0]
         pidt = torch.as_tensor(np.broadcast_to(np.asarray(pid, np.int32), (n,)).copy()) if not torch.is_tensor(pid) \
             else pid.to(torch.int32)
-        for q in torch.unique(pidt).tolist():
-            if int(q) not in SUPPORTED_PIDS:
-                raise ValueError(f"PID {int(q)} is not transported by the shower path")
+        # one comparison pass per supported PID (no sort of the batch)
+        known = torch.zeros(pidt.shape, dtype=torch.bool, device=pidt.device)
+        for q in SUPPORTED_PIDS:
+            known |= pidt == q
+        if not bool(known.all()):
+            raise ValueError(f"PID {int(pidt[~known].min())} is not transported by the shower path")
         if mass is None:
-            mass = torch.as_tensor([MASS[int(q)] for q in pidt.tolist()], dtype=torch.float64)
+            mass = torch.zeros(pidt.shape, dtype=torch.float64, device=pidt.device)
+            for q in SUPPORTED_PIDS:
+                mass[pidt == q] = MASS[q]
         mt = torch.as_tensor(mass, dtype=torch.float64)
         if mt.dim() == 0:                               # one mass for every primary
             mt = mt.expand(n).contiguous()
