@@ -92,6 +92,14 @@ def test_entry_points_refuse_missing_handles_without_a_device(lib):
     assert lib.pt_vegas_adapt(0, 1, None, None, 2, None, None, 0.5, None) == _lib.PT_BAD_ARG
     assert lib.pt_detector_cut(None, 0, None, 0, None, 5, None, 1, 0.0, 1.0, 0, 0.0, 0.0, None, None,
                                None) == _lib.PT_BAD_ARG
+    buf = (C.c_double * 64)()
+    # strides shorter than the rows, a negative count, detectors without positions
+    assert lib.pt_detector_cut(buf, 4, buf, 8, None, 8, buf, 1, 0.0, 1.0, 0, 0.0, 0.0, None, None,
+                               None) == _lib.PT_BAD_ARG
+    assert lib.pt_detector_cut(buf, 8, buf, 8, None, -1, buf, 1, 0.0, 1.0, 0, 0.0, 0.0, None, None,
+                               None) == _lib.PT_BAD_ARG
+    assert lib.pt_detector_cut(buf, 8, buf, 8, None, 8, None, 2, 0.0, 1.0, 0, 0.0, 0.0, None, None,
+                               None) == _lib.PT_BAD_ARG
 
 
 def test_staging_timeout_marks_the_handle_unusable():
